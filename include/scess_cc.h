@@ -1,0 +1,172 @@
+/*
+ * scess_cc.h - C ABI of the GB300-native closed-shell CCSD / CCSD(T) engine.
+ *
+ * Drop-in for SCESS's closed-shell coupled-cluster calls:
+ *   RCCSD_Wfn SolveRCCSD_DIIS(const TEITensor &eri, const VectorXd &orbitalEnergies,
+ *                             Index nOcc, const RCCSD_F12Coupling *f12,
+ *                             const DH::Thread *thread, std::stringstream *console)
+ *       declared src/Quantum/CC/CC.h:136-141, defined src/Quantum/CC/RCCSD.cpp:295-394
+ *   double RCCSD_TriplesCorrection(const TEITensor &eri, const VectorXd &orbitalEnergies,
+ *                                  Index nOcc, const T1Tensor &t1, const T2Tensor &t2,
+ *                                  const DH::Thread *thread)
+ *       declared src/Quantum/CC/CC.h:154-158, defined src/Quantum/CC/RCCSD_T.cpp:17-168
+ *
+ * Conventions (identical to the reference's Eigen tensors):
+ *   - every array is a caller-owned HOST buffer of doubles in COLUMN-MAJOR order
+ *     (first index fastest), exactly the memory of an Eigen::Tensor<double,k>;
+ *   - eri(p,q,r,s) = <pq|rs> = (pr|qs) over nmo spatial MOs, occupied first;
+ *   - t1(i,a) is o x v, t2(i,j,a,b) is o x o x v x v with t2(i,j,a,b) = t2(j,i,b,a);
+ *   - DF factors B(Q,p,q) are naux x nmo x nmo, symmetric in (p,q), with
+ *     (pq|rs) = sum_Q B(Q,p,q) B(Q,r,s).
+ *
+ * Every call is synchronous and returns an SCESS_* status.  A context owns one
+ * GPU's device memory and stream; use one context per calling thread.
+ * Non-convergence is not an error (result.converged = 0, as the reference).
+ */
+#ifndef SCESS_CC_H
+#define SCESS_CC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. The reference signals cancellation by returning an empty
+ * wavefunction / 0.0 (RCCSD.cpp:346-347, RCCSD_T.cpp:161-162); here it is
+ * SCESS_ERR_CANCELLED. */
+#define SCESS_OK 0
+#define SCESS_ERR_INVALID 1     /* bad shape, null pointer, NaN/Inf input      */
+#define SCESS_ERR_OOM 2         /* device (or pinned host) allocation failed   */
+#define SCESS_ERR_CUDA 3        /* CUDA runtime / launch failure               */
+#define SCESS_ERR_CANCELLED 4   /* cancel callback returned non-zero           */
+#define SCESS_ERR_TIMEOUT 5     /* options.time_limit_s exceeded               */
+#define SCESS_ERR_UNSUPPORTED 6 /* no sm_103a device / feature not available   */
+
+/* Arithmetic of the contractions. FP64 is the drop-in path (matches the
+ * reference to <= 1e-9 Eh); MIXED runs the contractions on BF16 tensor cores
+ * (tcgen05, split hi+lo operands, FP32 accumulation) with FP64 denominators,
+ * DIIS and energies, followed by FP64 refinement sweeps. */
+#define SCESS_PRECISION_FP64 0
+#define SCESS_PRECISION_MIXED 1
+
+typedef struct scess_ctx scess_ctx;
+
+/* Polled between phases; non-zero stops the call with SCESS_ERR_CANCELLED.
+ * Replaces DH::Thread::ShouldStop() (RCCSD.cpp:346, RCCSD_T.cpp:123). */
+typedef int (*scess_cancel_fn)(void *user);
+/* Receives the per-iteration console lines of RCCSD.cpp:312-392
+ * ("CCSD(n): E(corr) = ... dE = ... rms(dt) = ..."). */
+typedef void (*scess_log_fn)(int level, const char *message, void *user);
+
+/* Options of SolveRCCSD_DIIS. Defaults (scess_rccsd_default_options) are the
+ * reference's compile-time constants, RCCSD.cpp:302-307. */
+typedef struct {
+  double energy_convergence;    /* 1e-10 */
+  double amplitude_convergence; /* 1e-8  */
+  int32_t max_iterations;       /* 100   */
+  int32_t diis_start;           /* 2     */
+  int32_t max_diis_vectors;     /* 8     */
+  int32_t precision;            /* SCESS_PRECISION_FP64 */
+  /* MIXED only: after the mixed iterations meet the thresholds, this many
+   * further iterations run in FP64 (0 = none). Convergence is re-checked in
+   * FP64 and the returned energy comes from an FP64 iteration. */
+  int32_t refine_sweeps;        /* 2 */
+  /* MIXED only: the mixed phase ends once dE < mixed_energy_switch and
+   * rms(dt) < mixed_amplitude_switch; the FP64 phase then starts from the
+   * mixed amplitudes with a fresh DIIS subspace. */
+  double mixed_energy_switch;     /* 1e-8 */
+  double mixed_amplitude_switch;  /* 1e-6 */
+  /* 0: MP2 initial guess (RCCSD.cpp:333-339). 1: resume from the amplitudes
+   * passed in t1_out / t2_out (e.g. a checkpoint). */
+  int32_t resume;               /* 0 */
+  /* Optional per-iteration amplitude checkpoint ring on the host: iteration n
+   * writes slot n % capacity (o*v and o^2*v^2 doubles per slot). */
+  double *checkpoint_t1;
+  double *checkpoint_t2;
+  int32_t checkpoint_capacity;
+  /* Optional: 3 doubles per iteration (E, dE, rms) for max_iterations rows. */
+  double *history;
+  /* Wall-clock limit of the call in seconds (0 = none) -> SCESS_ERR_TIMEOUT. */
+  double time_limit_s;
+} scess_rccsd_options;
+
+/* RCCSD_Wfn (CC.h:105-115) minus the tensors, which go to t1_out / t2_out. */
+typedef struct {
+  double E_CCSD;          /* correlation energy incl. the F12 coupling energy */
+  double E_F12_Coupling;  /* CouplingEnergy(f12, t2) (RCCSD.cpp:91-98)         */
+  double E_T;             /* set by scess_rccsd_triples only                  */
+  int32_t converged;
+  int32_t iterations;     /* total iterations run (mixed + FP64)              */
+  int32_t mixed_iterations;
+  double last_dE;
+  double last_rms;
+} scess_rccsd_result;
+
+const char *scess_status_string(int status);
+
+/* Context on CUDA device `device` (must be sm_103a). */
+int scess_ctx_create(int device, scess_ctx **out);
+void scess_ctx_destroy(scess_ctx *ctx);
+/* Message of the last failing call on this context ("" if none). */
+const char *scess_ctx_last_error(const scess_ctx *ctx);
+int scess_ctx_set_callbacks(scess_ctx *ctx, scess_cancel_fn cancel, scess_log_fn log, void *user);
+
+void scess_rccsd_default_options(scess_rccsd_options *opts);
+
+/* SolveRCCSD_DIIS (CC.h:136-141, RCCSD.cpp:295-394).
+ *   eri          nmo^4, <pq|rs>
+ *   eps          nmo orbital energies
+ *   f12_residual RCCSD_F12Coupling::residual (o^2 v^2) or NULL  (CC.h:121-124)
+ *   f12_energy   RCCSD_F12Coupling::energy   (o^2 v^2) or NULL
+ *   t1_out       o*v   converged t1 (also the resume input when opts->resume)
+ *   t2_out       o^2 v^2 converged t2
+ * On non-convergence result->converged = 0, energies are 0 and t1/t2 are left
+ * unchanged, as RCCSD.cpp:376-380. opts may be NULL (defaults). */
+int scess_rccsd_solve(scess_ctx *ctx, const double *eri, const double *eps, int64_t nmo,
+                      int64_t nocc, const double *f12_residual, const double *f12_energy,
+                      const scess_rccsd_options *opts, double *t1_out, double *t2_out,
+                      scess_rccsd_result *result);
+
+/* Same as scess_rccsd_solve, from DF factors B (naux x nmo x nmo): the integral
+ * blocks are built on the GPU and the nmo^4 eri never crosses the bus. */
+int scess_rccsd_solve_df(scess_ctx *ctx, const double *B, int64_t naux, const double *eps,
+                         int64_t nmo, int64_t nocc, const double *f12_residual,
+                         const double *f12_energy, const scess_rccsd_options *opts,
+                         double *t1_out, double *t2_out, scess_rccsd_result *result);
+
+/* RCCSD_TriplesCorrection (CC.h:154-158, RCCSD_T.cpp:17-168): E_(T) into *e_t.
+ * precision: SCESS_PRECISION_FP64 (drop-in) or SCESS_PRECISION_MIXED. */
+int scess_rccsd_triples(scess_ctx *ctx, const double *eri, const double *eps, int64_t nmo,
+                        int64_t nocc, const double *t1, const double *t2, int32_t precision,
+                        double *e_t);
+
+/* (T) from DF factors (only the ovvv, ooov and oovv blocks are built). */
+int scess_rccsd_triples_df(scess_ctx *ctx, const double *B, int64_t naux, const double *eps,
+                           int64_t nmo, int64_t nocc, const double *t1, const double *t2,
+                           int32_t precision, double *e_t);
+
+/* One UpdateAmplitudes residual (RCCSD.cpp:101-233) without the final division
+ * by the denominators (:235-236): r1_out = t1new (o*v), r2_out = t2new
+ * (o^2 v^2), so that t1 <- r1/eia and t2 <- r2/eijab is the reference's
+ * update.  t2_driver is RCCSD_F12Coupling::residual or NULL. */
+int scess_rccsd_residual(scess_ctx *ctx, const double *eri, int64_t nmo, int64_t nocc,
+                         const double *t1, const double *t2, const double *t2_driver,
+                         int32_t precision, double *r1_out, double *r2_out);
+
+/* General binary contraction C = alpha * A.B + beta * C on the GPU, the
+ * runtime counterpart of the tensor layer's compile-time Einsum
+ * (src/Tensor/TensorEinsum.h:170-205): spec like "kcld,ilcd->ki", each
+ * operand a dense column-major host tensor of rank <= 6 with extents *_ext.
+ * Every label of C appears in exactly one of A, B; labels shared by A and B
+ * and absent from C are summed.  precision selects the FP64 (DFMA) backend
+ * or, for MIXED, the tcgen05 tensor-core backend for any shape. */
+int scess_einsum(scess_ctx *ctx, const char *spec, double alpha, const double *A, int32_t a_nd,
+                 const int64_t *a_ext, const double *B, int32_t b_nd, const int64_t *b_ext,
+                 double beta, double *C, int32_t c_nd, const int64_t *c_ext, int32_t precision);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SCESS_CC_H */

@@ -1,0 +1,341 @@
+"""Python mirror of SCESS's closed-shell CC interface over the C ABI (libscess_cc.so).
+
+``SolveRCCSD_DIIS`` and ``RCCSD_TriplesCorrection`` keep the names, argument
+meaning and error behaviour of ``src/Quantum/CC/CC.h:136-158``:
+
+* arrays are indexed like the reference's Eigen tensors (``eri[p,q,r,s] =
+  <pq|rs>``, ``t1[i,a]``, ``t2[i,j,a,b]``); they are handed to the library as
+  column-major (Fortran-order) buffers, exactly an Eigen tensor's memory;
+* ``thread`` is any object with ``ShouldStop()``; when it asks to stop,
+  ``SolveRCCSD_DIIS`` returns an empty ``RCCSD_Wfn`` and
+  ``RCCSD_TriplesCorrection`` returns 0.0 (RCCSD.cpp:346-347, RCCSD_T.cpp:161-162);
+* ``console`` is any object with ``write(str)``; it receives the reference's
+  per-iteration lines;
+* non-convergence gives ``converged = False`` with zero energies and no
+  amplitudes (RCCSD.cpp:376-380).
+
+Every other failure raises :class:`ScessError` carrying the C status.  The
+library is GPU-only: there is no CPU fallback, and loading fails loudly when
+``libscess_cc.so`` is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, 'libscess_cc.so')
+
+SCESS_OK = 0
+SCESS_ERR_INVALID = 1
+SCESS_ERR_OOM = 2
+SCESS_ERR_CUDA = 3
+SCESS_ERR_CANCELLED = 4
+SCESS_ERR_TIMEOUT = 5
+SCESS_ERR_UNSUPPORTED = 6
+PRECISION = {'fp64': 0, 'mixed': 1}
+
+
+class ScessError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f'{message} (status {status})')
+        self.status = status
+
+
+class Options(C.Structure):
+    """scess_rccsd_options (include/scess_cc.h)."""
+    _fields_ = [('energy_convergence', C.c_double), ('amplitude_convergence', C.c_double),
+                ('max_iterations', C.c_int32), ('diis_start', C.c_int32),
+                ('max_diis_vectors', C.c_int32), ('precision', C.c_int32),
+                ('refine_sweeps', C.c_int32),
+                ('mixed_energy_switch', C.c_double), ('mixed_amplitude_switch', C.c_double),
+                ('resume', C.c_int32),
+                ('checkpoint_t1', C.POINTER(C.c_double)), ('checkpoint_t2', C.POINTER(C.c_double)),
+                ('checkpoint_capacity', C.c_int32), ('history', C.POINTER(C.c_double)),
+                ('time_limit_s', C.c_double)]
+
+
+class Result(C.Structure):
+    """scess_rccsd_result (include/scess_cc.h)."""
+    _fields_ = [('E_CCSD', C.c_double), ('E_F12_Coupling', C.c_double), ('E_T', C.c_double),
+                ('converged', C.c_int32), ('iterations', C.c_int32),
+                ('mixed_iterations', C.c_int32), ('last_dE', C.c_double),
+                ('last_rms', C.c_double)]
+
+
+CANCEL_FN = C.CFUNCTYPE(C.c_int, C.c_void_p)
+LOG_FN = C.CFUNCTYPE(None, C.c_int, C.c_char_p, C.c_void_p)
+_dp = C.POINTER(C.c_double)
+_i64p = C.POINTER(C.c_int64)
+
+EXPORTS = {
+    'scess_status_string': (C.c_char_p, [C.c_int]),
+    'scess_ctx_create': (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
+    'scess_ctx_destroy': (None, [C.c_void_p]),
+    'scess_ctx_last_error': (C.c_char_p, [C.c_void_p]),
+    'scess_ctx_set_callbacks': (C.c_int, [C.c_void_p, CANCEL_FN, LOG_FN, C.c_void_p]),
+    'scess_rccsd_default_options': (None, [C.POINTER(Options)]),
+    'scess_rccsd_solve': (C.c_int, [C.c_void_p, _dp, _dp, C.c_int64, C.c_int64, _dp, _dp,
+                                    C.POINTER(Options), _dp, _dp, C.POINTER(Result)]),
+    'scess_rccsd_solve_df': (C.c_int, [C.c_void_p, _dp, C.c_int64, _dp, C.c_int64, C.c_int64,
+                                       _dp, _dp, C.POINTER(Options), _dp, _dp,
+                                       C.POINTER(Result)]),
+    'scess_rccsd_triples': (C.c_int, [C.c_void_p, _dp, _dp, C.c_int64, C.c_int64, _dp, _dp,
+                                      C.c_int32, _dp]),
+    'scess_rccsd_triples_df': (C.c_int, [C.c_void_p, _dp, C.c_int64, _dp, C.c_int64, C.c_int64,
+                                         _dp, _dp, C.c_int32, _dp]),
+    'scess_rccsd_residual': (C.c_int, [C.c_void_p, _dp, C.c_int64, C.c_int64, _dp, _dp, _dp,
+                                       C.c_int32, _dp, _dp]),
+    'scess_einsum': (C.c_int, [C.c_void_p, C.c_char_p, C.c_double, _dp, C.c_int32, _i64p, _dp,
+                               C.c_int32, _i64p, C.c_double, _dp, C.c_int32, _i64p, C.c_int32]),
+}
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Loads libscess_cc.so and declares every exported C symbol."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ScessError(SCESS_ERR_UNSUPPORTED,
+                         f'{path} is missing: build it with `python -m scess_gb300.build`')
+    lib = C.CDLL(path)
+    for name, (res, args) in EXPORTS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _f64(x, shape=None):
+    a = np.asfortranarray(np.asarray(x, dtype=np.float64))
+    if shape is not None and a.shape != tuple(shape):
+        raise ScessError(SCESS_ERR_INVALID, f'expected shape {tuple(shape)}, got {a.shape}')
+    return a
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(_dp)
+
+
+@dataclass
+class RCCSD_Wfn:
+    """RCCSD_Wfn, CC.h:105-115 (plus iteration bookkeeping)."""
+    E_CCSD: float = 0.0
+    E_F12_Coupling: float = 0.0
+    E_T: float = 0.0
+    converged: bool = False
+    t1: np.ndarray | None = None
+    t2: np.ndarray | None = None
+    iterations: int = 0
+    mixed_iterations: int = 0
+    history: np.ndarray | None = field(default=None, repr=False)
+
+
+@dataclass
+class RCCSD_F12Coupling:
+    """RCCSD_F12Coupling, CC.h:121-124: both indexed (i, j, a, b)."""
+    residual: np.ndarray
+    energy: np.ndarray
+
+
+class Context:
+    """One GPU context (scess_ctx): device memory, stream and callbacks."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = C.c_void_p()
+        st = self.lib.scess_ctx_create(device, C.byref(h))
+        if st != SCESS_OK:
+            raise ScessError(st, 'scess_ctx_create: ' + self.lib.scess_status_string(st).decode())
+        self.h = h
+        self._thread = None
+        self._console = None
+        self._cancel = CANCEL_FN(self._cancel_cb)
+        self._log = LOG_FN(self._log_cb)
+        self.lib.scess_ctx_set_callbacks(self.h, self._cancel, self._log, None)
+
+    def close(self):
+        if getattr(self, 'h', None):
+            self.lib.scess_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _cancel_cb(self, user):
+        t = self._thread
+        try:
+            return 1 if (t is not None and t.ShouldStop()) else 0
+        except Exception:
+            return 1
+
+    def _log_cb(self, level, msg, user):
+        if self._console is not None:
+            self._console.write(msg.decode() + '\n')
+
+    def _check(self, st, what):
+        if st != SCESS_OK:
+            msg = self.lib.scess_ctx_last_error(self.h).decode()
+            raise ScessError(st, f'{what}: {msg}')
+
+    # -- options ---------------------------------------------------------------------------
+    def default_options(self) -> Options:
+        o = Options()
+        self.lib.scess_rccsd_default_options(C.byref(o))
+        return o
+
+    # -- SolveRCCSD_DIIS ----------------------------------------------------------------------
+    def solve(self, eri=None, eps=None, nocc=None, f12: RCCSD_F12Coupling | None = None,
+              precision: str = 'fp64', B=None, thread=None, console=None, t1_init=None,
+              t2_init=None, checkpoint=0, **opts) -> RCCSD_Wfn:
+        eps = _f64(eps)
+        N = eps.shape[0]
+        o, v = int(nocc), N - int(nocc)
+        op = self.default_options()
+        op.precision = PRECISION[precision]
+        for k, val in opts.items():
+            setattr(op, k, val)
+        hist = np.zeros(3 * max(op.max_iterations, 1))
+        op.history = _ptr(hist)
+        t1 = np.zeros((o, v), order='F')
+        t2 = np.zeros((o, o, v, v), order='F')
+        if t1_init is not None:
+            t1[...] = t1_init
+            t2[...] = t2_init
+            op.resume = 1
+        ck1 = ck2 = None
+        if checkpoint:
+            ck1 = np.zeros((checkpoint, o * v))
+            ck2 = np.zeros((checkpoint, o * o * v * v))
+            op.checkpoint_t1, op.checkpoint_t2 = _ptr(ck1), _ptr(ck2)
+            op.checkpoint_capacity = checkpoint
+        fr = fe = None
+        if f12 is not None:
+            fr = _f64(f12.residual, (o, o, v, v))
+            fe = _f64(f12.energy, (o, o, v, v))
+        res = Result()
+        self._thread, self._console = thread, console
+        try:
+            if B is not None:
+                Bf = _f64(B)
+                st = self.lib.scess_rccsd_solve_df(self.h, _ptr(Bf), Bf.shape[0], _ptr(eps), N, o,
+                                                   _ptr(fr), _ptr(fe), C.byref(op), _ptr(t1),
+                                                   _ptr(t2), C.byref(res))
+            else:
+                ef = _f64(eri, (N, N, N, N))
+                st = self.lib.scess_rccsd_solve(self.h, _ptr(ef), _ptr(eps), N, o, _ptr(fr),
+                                                _ptr(fe), C.byref(op), _ptr(t1), _ptr(t2),
+                                                C.byref(res))
+        finally:
+            self._thread, self._console = None, None
+        if st == SCESS_ERR_CANCELLED:
+            return RCCSD_Wfn()
+        self._check(st, 'scess_rccsd_solve')
+        w = RCCSD_Wfn(iterations=res.iterations, mixed_iterations=res.mixed_iterations,
+                      history=hist[:3 * res.iterations].reshape(-1, 3))
+        if checkpoint:
+            w.checkpoints = (ck1, ck2)
+        if not res.converged:
+            return w
+        w.converged = True
+        w.E_CCSD = res.E_CCSD
+        w.E_F12_Coupling = res.E_F12_Coupling
+        w.t1, w.t2 = t1, t2
+        return w
+
+    # -- RCCSD_TriplesCorrection --------------------------------------------------------------
+    def triples(self, eri=None, eps=None, nocc=None, t1=None, t2=None, precision: str = 'fp64',
+                B=None, thread=None) -> float:
+        eps = _f64(eps)
+        N = eps.shape[0]
+        o, v = int(nocc), N - int(nocc)
+        t1f = _f64(t1, (o, v))
+        t2f = _f64(t2, (o, o, v, v))
+        et = C.c_double(0.0)
+        self._thread = thread
+        try:
+            if B is not None:
+                Bf = _f64(B)
+                st = self.lib.scess_rccsd_triples_df(self.h, _ptr(Bf), Bf.shape[0], _ptr(eps), N,
+                                                     o, _ptr(t1f), _ptr(t2f),
+                                                     PRECISION[precision], C.byref(et))
+            else:
+                ef = _f64(eri, (N, N, N, N))
+                st = self.lib.scess_rccsd_triples(self.h, _ptr(ef), _ptr(eps), N, o, _ptr(t1f),
+                                                  _ptr(t2f), PRECISION[precision], C.byref(et))
+        finally:
+            self._thread = None
+        if st == SCESS_ERR_CANCELLED:
+            return 0.0
+        self._check(st, 'scess_rccsd_triples')
+        return et.value
+
+    # -- one residual -------------------------------------------------------------------------
+    def residual(self, eri, nocc, t1, t2, t2_driver=None, precision: str = 'fp64'):
+        """(t1new, t2new) numerators of UpdateAmplitudes (before the division)."""
+        ef = _f64(eri)
+        N = ef.shape[0]
+        o, v = int(nocc), N - int(nocc)
+        t1f, t2f = _f64(t1, (o, v)), _f64(t2, (o, o, v, v))
+        drv = None if t2_driver is None else _f64(t2_driver, (o, o, v, v))
+        r1 = np.zeros((o, v), order='F')
+        r2 = np.zeros((o, o, v, v), order='F')
+        st = self.lib.scess_rccsd_residual(self.h, _ptr(ef), N, o, _ptr(t1f), _ptr(t2f),
+                                           _ptr(drv), PRECISION[precision], _ptr(r1), _ptr(r2))
+        self._check(st, 'scess_rccsd_residual')
+        return r1, r2
+
+    # -- generic contraction ------------------------------------------------------------------
+    def einsum(self, spec: str, A, B, C_init=None, alpha=1.0, beta=0.0, precision='fp64',
+               out_shape=None):
+        Af, Bf = _f64(A), _f64(B)
+        if C_init is None:
+            Cf = np.zeros(out_shape, order='F')
+        else:
+            Cf = _f64(C_init).copy(order='F')
+        ext = lambda a: (C.c_int64 * a.ndim)(*a.shape)  # noqa: E731
+        st = self.lib.scess_einsum(self.h, spec.encode(), alpha, _ptr(Af), Af.ndim, ext(Af),
+                                   _ptr(Bf), Bf.ndim, ext(Bf), beta, _ptr(Cf), Cf.ndim, ext(Cf),
+                                   PRECISION[precision])
+        self._check(st, 'scess_einsum')
+        return Cf
+
+
+_default_ctx = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+def SolveRCCSD_DIIS(eri, orbitalEnergies, nOcc, f12: RCCSD_F12Coupling | None = None,
+                    thread=None, console=None, precision: str = 'fp64') -> RCCSD_Wfn:
+    """CC::SolveRCCSD_DIIS (CC.h:136-141) on the GPU."""
+    return default_context().solve(eri, orbitalEnergies, nOcc, f12=f12, thread=thread,
+                                   console=console, precision=precision)
+
+
+def RCCSD_TriplesCorrection(eri, orbitalEnergies, nOcc, t1, t2, thread=None,
+                            precision: str = 'fp64') -> float:
+    """CC::RCCSD_TriplesCorrection (CC.h:154-158) on the GPU."""
+    return default_context().triples(eri, orbitalEnergies, nOcc, t1, t2, precision=precision,
+                                     thread=thread)

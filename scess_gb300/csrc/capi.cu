@@ -1,0 +1,327 @@
+// C ABI of the engine (include/scess_cc.h): argument checks, host<->device
+// transfers and exception-to-status translation around the C++ drivers.
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "gemm_tc.h"
+#include "rccsd.h"
+#include "triples.h"
+
+struct scess_ctx {
+  scess::Ctx *impl = nullptr;
+  std::string err;
+};
+
+namespace {
+
+using scess::Error;
+
+template <class F>
+int guard(scess_ctx *ctx, F &&f) {
+  if (!ctx || !ctx->impl) return SCESS_ERR_INVALID;
+  int code = SCESS_OK;
+  try {
+    SCESS_CUDA(cudaSetDevice(ctx->impl->device));
+    f(*ctx->impl);
+    ctx->err.clear();
+  } catch (const Error &e) {
+    ctx->err = e.what();
+    code = e.code;
+  } catch (const std::bad_alloc &) {
+    ctx->err = "host allocation failed";
+    code = SCESS_ERR_OOM;
+  } catch (const std::exception &e) {
+    ctx->err = e.what();
+    code = SCESS_ERR_CUDA;
+  }
+  // Packed-operand caches are keyed by device pointers of this call: drop them.
+  cudaStreamSynchronize(ctx->impl->stream);
+  if (ctx->impl->tc) ctx->impl->tc->clear_cache();
+  if (code != SCESS_OK) cudaGetLastError();
+  return code;
+}
+
+void check_shape(int64_t nmo, int64_t nocc) {
+  if (nmo <= 0 || nocc <= 0 || nocc >= nmo)
+    throw Error(SCESS_ERR_INVALID, "need 0 < nocc < nmo");
+  if (nmo > 4096) throw Error(SCESS_ERR_INVALID, "nmo too large");
+}
+
+void need(const void *p, const char *what) {
+  if (!p) throw Error(SCESS_ERR_INVALID, std::string("null pointer: ") + what);
+}
+
+void host_finite(const double *x, int64_t n, const char *what) {
+  for (int64_t i = 0; i < n; i++)
+    if (!std::isfinite(x[i])) throw Error(SCESS_ERR_INVALID, std::string("non-finite value in ") + what);
+}
+
+void device_finite(scess::Ctx &ctx, const double *x, int64_t n, const char *what) {
+  int *flag = reinterpret_cast<int *>(ctx.dscalars + 63);
+  SCESS_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), ctx.stream));
+  scess::check_finite(n, x, flag, ctx.stream);
+  int h = 0;
+  SCESS_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
+  ctx.sync();
+  if (h) throw Error(SCESS_ERR_INVALID, std::string("non-finite value in ") + what);
+}
+
+// eri (nmo^4) on the device, from the host eri or from DF factors (FP64 build).
+scess::DTensor device_eri(scess::Ctx &ctx, const double *eri, const double *B, int64_t naux,
+                          int64_t N) {
+  scess::DTensor d({N, N, N, N});
+  if (eri) {
+    scess::upload(ctx, d.p(), eri, N * N * N * N);
+    device_finite(ctx, d.p(), N * N * N * N, "eri");
+  } else {
+    scess::DTensor dB({naux, N, N});
+    scess::upload(ctx, dB.p(), B, naux * N * N);
+    device_finite(ctx, dB.p(), naux * N * N, "B");
+    // eri(p,q,r,s) = (pr|qs) = sum_Q B(Q,p,r) B(Q,q,s)
+    scess::einsum(ctx, "Qpr,Qqs->pqrs", 1.0, dB.v, dB.v, 0.0, d.v, scess::Backend::FP64);
+    ctx.sync();
+  }
+  return d;
+}
+
+int solve_common(scess_ctx *ctx, const double *eri, const double *B, int64_t naux,
+                 const double *eps, int64_t nmo, int64_t nocc, const double *f12_residual,
+                 const double *f12_energy, const scess_rccsd_options *opts, double *t1_out,
+                 double *t2_out, scess_rccsd_result *result) {
+  return guard(ctx, [&](scess::Ctx &c) {
+    check_shape(nmo, nocc);
+    need(eps, "eps");
+    need(t1_out, "t1_out");
+    need(t2_out, "t2_out");
+    need(result, "result");
+    host_finite(eps, nmo, "eps");
+    scess_rccsd_options o;
+    if (opts) o = *opts;
+    else scess_rccsd_default_options(&o);
+    if (o.max_iterations < 0 || o.max_diis_vectors < 1 || o.diis_start < 0 ||
+        (o.precision != SCESS_PRECISION_FP64 && o.precision != SCESS_PRECISION_MIXED))
+      throw Error(SCESS_ERR_INVALID, "bad options");
+    const int64_t v = nmo - nocc;
+    if (f12_residual) host_finite(f12_residual, nocc * nocc * v * v, "f12_residual");
+    if (f12_energy) host_finite(f12_energy, nocc * nocc * v * v, "f12_energy");
+    scess::Control ctl;
+    ctl.cancel = c.cancel;
+    ctl.user = c.user;
+    ctl.time_limit_s = o.time_limit_s;
+    scess::DTensor d_eri = device_eri(c, eri, B, naux, nmo);
+    ctl.poll();
+    scess::RccsdBlocks blocks;
+    blocks.build(c, d_eri.p(), nmo, nocc);
+    scess::SolveInput in;
+    in.eps_host = eps;
+    in.f12_residual = f12_residual;
+    in.f12_energy = f12_energy;
+    scess::rccsd_solve(c, blocks, in, o, ctl, t1_out, t2_out, result);
+  });
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *scess_status_string(int status) {
+  switch (status) {
+    case SCESS_OK: return "ok";
+    case SCESS_ERR_INVALID: return "invalid argument";
+    case SCESS_ERR_OOM: return "out of memory";
+    case SCESS_ERR_CUDA: return "CUDA error";
+    case SCESS_ERR_CANCELLED: return "cancelled";
+    case SCESS_ERR_TIMEOUT: return "time limit exceeded";
+    case SCESS_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+  }
+}
+
+int scess_ctx_create(int device, scess_ctx **out) {
+  if (!out) return SCESS_ERR_INVALID;
+  *out = nullptr;
+  try {
+    auto *c = new scess_ctx;
+    try {
+      c->impl = new scess::Ctx(device);
+    } catch (...) {
+      delete c;
+      throw;
+    }
+    *out = c;
+    return SCESS_OK;
+  } catch (const Error &e) {
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    return SCESS_ERR_OOM;
+  } catch (...) {
+    return SCESS_ERR_CUDA;
+  }
+}
+
+void scess_ctx_destroy(scess_ctx *ctx) {
+  if (!ctx) return;
+  if (ctx->impl) {
+    cudaSetDevice(ctx->impl->device);
+    delete ctx->impl;
+  }
+  delete ctx;
+}
+
+const char *scess_ctx_last_error(const scess_ctx *ctx) { return ctx ? ctx->err.c_str() : ""; }
+
+int scess_ctx_set_callbacks(scess_ctx *ctx, scess_cancel_fn cancel, scess_log_fn log, void *user) {
+  if (!ctx || !ctx->impl) return SCESS_ERR_INVALID;
+  ctx->impl->cancel = cancel;
+  ctx->impl->log = log;
+  ctx->impl->user = user;
+  return SCESS_OK;
+}
+
+void scess_rccsd_default_options(scess_rccsd_options *o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->energy_convergence = 1.0e-10;   // RCCSD.cpp:302
+  o->amplitude_convergence = 1.0e-8; // :303
+  o->max_iterations = 100;           // :304
+  o->diis_start = 2;                 // :306
+  o->max_diis_vectors = 8;           // :307
+  o->precision = SCESS_PRECISION_FP64;
+  o->refine_sweeps = 2;
+  o->mixed_energy_switch = 1.0e-8;
+  o->mixed_amplitude_switch = 1.0e-6;
+}
+
+int scess_rccsd_solve(scess_ctx *ctx, const double *eri, const double *eps, int64_t nmo,
+                      int64_t nocc, const double *f12_residual, const double *f12_energy,
+                      const scess_rccsd_options *opts, double *t1_out, double *t2_out,
+                      scess_rccsd_result *result) {
+  if (!eri) return SCESS_ERR_INVALID;
+  return solve_common(ctx, eri, nullptr, 0, eps, nmo, nocc, f12_residual, f12_energy, opts,
+                      t1_out, t2_out, result);
+}
+
+int scess_rccsd_solve_df(scess_ctx *ctx, const double *B, int64_t naux, const double *eps,
+                         int64_t nmo, int64_t nocc, const double *f12_residual,
+                         const double *f12_energy, const scess_rccsd_options *opts,
+                         double *t1_out, double *t2_out, scess_rccsd_result *result) {
+  if (!B || naux <= 0) return SCESS_ERR_INVALID;
+  return solve_common(ctx, nullptr, B, naux, eps, nmo, nocc, f12_residual, f12_energy, opts,
+                      t1_out, t2_out, result);
+}
+
+static int triples_common(scess_ctx *ctx, const double *eri, const double *B, int64_t naux,
+                          const double *eps, int64_t nmo, int64_t nocc, const double *t1,
+                          const double *t2, int32_t precision, double *e_t) {
+  return guard(ctx, [&](scess::Ctx &c) {
+    check_shape(nmo, nocc);
+    need(eps, "eps");
+    need(t1, "t1");
+    need(t2, "t2");
+    need(e_t, "e_t");
+    if (precision != SCESS_PRECISION_FP64 && precision != SCESS_PRECISION_MIXED)
+      throw Error(SCESS_ERR_INVALID, "bad precision");
+    const int64_t o = nocc, v = nmo - nocc;
+    host_finite(eps, nmo, "eps");
+    scess::Control ctl;
+    ctl.cancel = c.cancel;
+    ctl.user = c.user;
+    scess::DTensor d_eri = device_eri(c, eri, B, naux, nmo);
+    scess::DTensor d_eps({nmo}), d_t1({o, v}), d_t2({o, o, v, v});
+    scess::upload(c, d_eps.p(), eps, nmo);
+    scess::upload(c, d_t1.p(), t1, o * v);
+    scess::upload(c, d_t2.p(), t2, o * o * v * v);
+    device_finite(c, d_t1.p(), o * v, "t1");
+    device_finite(c, d_t2.p(), o * o * v * v, "t2");
+    ctl.poll();
+    *e_t = scess::rccsd_triples(c, d_eri.p(), nmo, nocc, d_eps.p(), d_t1.p(), d_t2.p(),
+                                precision == SCESS_PRECISION_MIXED, ctl);
+  });
+}
+
+int scess_rccsd_triples(scess_ctx *ctx, const double *eri, const double *eps, int64_t nmo,
+                        int64_t nocc, const double *t1, const double *t2, int32_t precision,
+                        double *e_t) {
+  if (!eri) return SCESS_ERR_INVALID;
+  return triples_common(ctx, eri, nullptr, 0, eps, nmo, nocc, t1, t2, precision, e_t);
+}
+
+int scess_rccsd_triples_df(scess_ctx *ctx, const double *B, int64_t naux, const double *eps,
+                           int64_t nmo, int64_t nocc, const double *t1, const double *t2,
+                           int32_t precision, double *e_t) {
+  if (!B || naux <= 0) return SCESS_ERR_INVALID;
+  return triples_common(ctx, nullptr, B, naux, eps, nmo, nocc, t1, t2, precision, e_t);
+}
+
+int scess_rccsd_residual(scess_ctx *ctx, const double *eri, int64_t nmo, int64_t nocc,
+                         const double *t1, const double *t2, const double *t2_driver,
+                         int32_t precision, double *r1_out, double *r2_out) {
+  if (!eri) return SCESS_ERR_INVALID;
+  return guard(ctx, [&](scess::Ctx &c) {
+    check_shape(nmo, nocc);
+    need(t1, "t1");
+    need(t2, "t2");
+    need(r1_out, "r1_out");
+    need(r2_out, "r2_out");
+    const int64_t o = nocc, v = nmo - nocc, n1 = o * v, n2 = o * o * v * v;
+    scess::DTensor d_eri = device_eri(c, eri, nullptr, 0, nmo);
+    scess::RccsdBlocks blocks;
+    blocks.build(c, d_eri.p(), nmo, nocc);
+    scess::DTensor amp({n1 + n2}), R({n1 + n2}), drv;
+    scess::upload(c, amp.p(), t1, n1);
+    scess::upload(c, amp.p() + n1, t2, n2);
+    if (t2_driver) {
+      drv = scess::DTensor({o, o, v, v});
+      scess::upload(c, drv.p(), t2_driver, n2);
+    }
+    const bool mixed = precision == SCESS_PRECISION_MIXED;
+    scess::RccsdWork w;
+    w.alloc(o, v, !mixed);
+    scess::rccsd_residual(c, blocks, amp.p(), drv.p(), mixed ? scess::Backend::MIXED : scess::Backend::FP64,
+                          w, R.p());
+    scess::download(c, r1_out, R.p(), n1);
+    scess::download(c, r2_out, R.p() + n1, n2);
+    if (mixed) c.tensor_cores().check_error();
+  });
+}
+
+int scess_einsum(scess_ctx *ctx, const char *spec, double alpha, const double *A, int32_t a_nd,
+                 const int64_t *a_ext, const double *B, int32_t b_nd, const int64_t *b_ext,
+                 double beta, double *C, int32_t c_nd, const int64_t *c_ext, int32_t precision) {
+  return guard(ctx, [&](scess::Ctx &c) {
+    need(spec, "spec");
+    need(A, "A");
+    need(B, "B");
+    need(C, "C");
+    auto mk = [&](int nd, const int64_t *ext, scess::DTensor &t) {
+      if (nd < 1 || nd > 6 || !ext) throw Error(SCESS_ERR_INVALID, "bad rank");
+      int64_t n = 1;
+      for (int d = 0; d < nd; d++) {
+        if (ext[d] <= 0) throw Error(SCESS_ERR_INVALID, "bad extent");
+        n *= ext[d];
+      }
+      t.mem.alloc((size_t)n * sizeof(double));
+      t.v.p = t.mem.d();
+      t.v.nd = nd;
+      int64_t s = 1;
+      for (int d = 0; d < nd; d++) {
+        t.v.ext[d] = ext[d];
+        t.v.str[d] = s;
+        s *= ext[d];
+      }
+      return n;
+    };
+    scess::DTensor dA, dB, dC;
+    const int64_t na = mk(a_nd, a_ext, dA), nbb = mk(b_nd, b_ext, dB), nc = mk(c_nd, c_ext, dC);
+    scess::upload(c, dA.p(), A, na);
+    scess::upload(c, dB.p(), B, nbb);
+    scess::upload(c, dC.p(), C, nc);
+    scess::einsum(c, spec, alpha, dA.v, dB.v, beta, dC.v,
+                  precision == SCESS_PRECISION_MIXED ? scess::Backend::TENSOR : scess::Backend::FP64);
+    scess::download(c, C, dC.p(), nc);
+    if (precision == SCESS_PRECISION_MIXED) c.tensor_cores().check_error();
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,331 @@
+// Host engine: device memory, context, einsum compiler (spec -> offset-table GEMM).
+#include <cstdarg>
+#include <cstring>
+
+#include "engine.h"
+#include "gemm_tc.h"
+
+namespace scess {
+
+void DevMem::alloc(size_t bytes) {
+  release();
+  if (bytes == 0) return;
+  cudaError_t e = cudaMalloc(&p_, bytes);
+  if (e != cudaSuccess) {
+    p_ = nullptr;
+    cudaGetLastError();
+    throw Error(e == cudaErrorMemoryAllocation ? SCESS_ERR_OOM : SCESS_ERR_CUDA,
+                "cudaMalloc(" + std::to_string(bytes) + " B): " + cudaGetErrorString(e));
+  }
+  bytes_ = bytes;
+}
+
+void DevMem::release() {
+  if (p_) cudaFree(p_);
+  p_ = nullptr;
+  bytes_ = 0;
+}
+
+TV cm(double *p, std::initializer_list<int64_t> ext) {
+  TV t;
+  t.p = p;
+  t.nd = (int)ext.size();
+  int64_t s = 1;
+  int d = 0;
+  for (int64_t e : ext) {
+    t.ext[d] = e;
+    t.str[d] = s;
+    s *= e;
+    d++;
+  }
+  return t;
+}
+
+DTensor::DTensor(std::initializer_list<int64_t> ext) {
+  int64_t n = 1;
+  for (int64_t e : ext) n *= e;
+  mem.alloc((size_t)std::max<int64_t>(n, 1) * sizeof(double));
+  v = cm(mem.d(), ext);
+}
+
+void Control::poll() const {
+  if (cancel && cancel(user)) throw Error(SCESS_ERR_CANCELLED, "cancelled by the caller");
+  if (time_limit_s > 0.0) {
+    const double el =
+        std::chrono::duration<double>(std::chrono::steady_clock::now() - start).count();
+    if (el > time_limit_s) throw Error(SCESS_ERR_TIMEOUT, "time limit exceeded");
+  }
+}
+
+Ctx::Ctx(int dev) : device(dev) {
+  int n = 0;
+  SCESS_CUDA(cudaGetDeviceCount(&n));
+  if (dev < 0 || dev >= n) throw Error(SCESS_ERR_INVALID, "no CUDA device " + std::to_string(dev));
+  cudaDeviceProp prop;
+  SCESS_CUDA(cudaGetDeviceProperties(&prop, dev));
+  if (prop.major != 10 || prop.minor != 3)
+    throw Error(SCESS_ERR_UNSUPPORTED, std::string("device is ") + prop.name + " (sm_" +
+                                           std::to_string(prop.major) + std::to_string(prop.minor) +
+                                           "); this library is built for sm_103a (GB300)");
+  SCESS_CUDA(cudaSetDevice(dev));
+  SCESS_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  scratch.alloc((kDotBlocks + 64) * sizeof(double));
+  partials = scratch.d();
+  dscalars = partials + kDotBlocks;
+  SCESS_CUDA(cudaMallocHost(&hscalars, 64 * sizeof(double)));
+}
+
+Ctx::~Ctx() {
+  if (stream) cudaStreamSynchronize(stream);
+  tc.reset();
+  plans.clear();
+  workspace.release();
+  scratch.release();
+  if (hscalars) cudaFreeHost(hscalars);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+double *Ctx::ensure_workspace(int64_t doubles) {
+  if (doubles <= 0) return workspace.d();
+  if ((size_t)doubles * sizeof(double) > workspace.bytes()) {
+    sync();
+    workspace.alloc((size_t)doubles * sizeof(double));
+  }
+  return workspace.d();
+}
+
+void Ctx::logf(int level, const char *fmt, ...) const {
+  if (!log) return;
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  log(level, buf, user);
+}
+
+TcEngine &Ctx::tensor_cores() {
+  if (!tc) tc = std::make_unique<TcEngine>(*this);
+  return *tc;
+}
+
+void upload(Ctx &ctx, double *dst, const double *src, int64_t n) {
+  if (n <= 0) return;
+  SCESS_CUDA(cudaMemcpyAsync(dst, src, (size_t)n * sizeof(double), cudaMemcpyHostToDevice,
+                             ctx.stream));
+  ctx.sync();
+}
+
+void download(Ctx &ctx, double *dst, const double *src, int64_t n) {
+  if (n <= 0) return;
+  SCESS_CUDA(cudaMemcpyAsync(dst, src, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost,
+                             ctx.stream));
+  ctx.sync();
+}
+
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+struct Spec {
+  std::string a, b, c;
+};
+
+Spec parse_spec(const char *spec, bool binary) {
+  std::string s(spec);
+  const size_t arrow = s.find("->");
+  if (arrow == std::string::npos) throw Error(SCESS_ERR_INVALID, std::string("bad spec ") + spec);
+  Spec r;
+  std::string lhs = s.substr(0, arrow);
+  r.c = s.substr(arrow + 2);
+  if (binary) {
+    const size_t comma = lhs.find(',');
+    if (comma == std::string::npos) throw Error(SCESS_ERR_INVALID, std::string("bad spec ") + spec);
+    r.a = lhs.substr(0, comma);
+    r.b = lhs.substr(comma + 1);
+  } else {
+    r.a = lhs;
+  }
+  return r;
+}
+
+void geom_key(std::string &k, const TV &t) {
+  k += '|';
+  for (int d = 0; d < t.nd; d++) {
+    k += std::to_string(t.ext[d]);
+    k += ':';
+    k += std::to_string(t.str[d]);
+    k += ',';
+  }
+}
+
+struct Lbl {
+  char c;
+  int64_t ext;
+  int64_t sa, sb, sc;
+};
+
+std::vector<int64_t> offsets(const std::vector<Lbl> &ls, int which) {
+  int64_t n = 1;
+  for (auto &l : ls) n *= l.ext;
+  std::vector<int64_t> out((size_t)n);
+  for (int64_t e = 0; e < n; e++) {
+    int64_t r = e, off = 0;
+    for (auto &l : ls) {
+      const int64_t i = r % l.ext;
+      r /= l.ext;
+      off += i * (which == 0 ? l.sa : which == 1 ? l.sb : l.sc);
+    }
+    out[(size_t)e] = off;
+  }
+  return out;
+}
+
+}  // namespace
+
+const EinsumPlan &plan_einsum(Ctx &ctx, const char *spec, const TV &A, const TV &B, const TV &C) {
+  std::string key(spec);
+  geom_key(key, A);
+  geom_key(key, B);
+  geom_key(key, C);
+  auto it = ctx.plans.find(key);
+  if (it != ctx.plans.end()) return *it->second;
+
+  const Spec s = parse_spec(spec, true);
+  if ((int)s.a.size() != A.nd || (int)s.b.size() != B.nd || (int)s.c.size() != C.nd)
+    throw Error(SCESS_ERR_INVALID, std::string("rank mismatch in ") + spec);
+  auto find = [](const std::string &l, char c) { return (int)l.find(c); };
+  std::vector<Lbl> M, N, K;
+  auto ext_of = [&](char c) -> int64_t {
+    int64_t e = -1;
+    int p;
+    if ((p = find(s.a, c)) >= 0) e = A.ext[p];
+    if ((p = find(s.b, c)) >= 0) {
+      if (e >= 0 && e != B.ext[p]) throw Error(SCESS_ERR_INVALID, std::string("extent mismatch in ") + spec);
+      e = B.ext[p];
+    }
+    if ((p = find(s.c, c)) >= 0) {
+      if (e >= 0 && e != C.ext[p]) throw Error(SCESS_ERR_INVALID, std::string("extent mismatch in ") + spec);
+      e = C.ext[p];
+    }
+    return e;
+  };
+  for (char c : s.c) {
+    const int pa = find(s.a, c), pb = find(s.b, c), pc = find(s.c, c);
+    if ((pa >= 0) == (pb >= 0))
+      throw Error(SCESS_ERR_INVALID, std::string("unsupported batch/free label in ") + spec);
+    Lbl l{c, ext_of(c), pa >= 0 ? A.str[pa] : 0, pb >= 0 ? B.str[pb] : 0, C.str[pc]};
+    (pa >= 0 ? M : N).push_back(l);
+  }
+  for (char c : s.a) {
+    if (find(s.c, c) >= 0) continue;
+    const int pa = find(s.a, c), pb = find(s.b, c);
+    if (pb < 0) throw Error(SCESS_ERR_INVALID, std::string("label only in A: ") + spec);
+    K.push_back(Lbl{c, ext_of(c), A.str[pa], B.str[pb], 0});
+  }
+  for (char c : s.b)
+    if (find(s.c, c) < 0 && find(s.a, c) < 0)
+      throw Error(SCESS_ERR_INVALID, std::string("label only in B: ") + spec);
+
+  auto pl = std::make_unique<EinsumPlan>();
+  pl->key = key;
+  pl->rowA = offsets(M, 0);
+  pl->rowC = offsets(M, 2);
+  pl->colB = offsets(N, 1);
+  pl->colC = offsets(N, 2);
+  pl->kA = offsets(K, 0);
+  pl->kB = offsets(K, 1);
+  pl->M = (int64_t)pl->rowA.size();
+  pl->N = (int64_t)pl->colB.size();
+  pl->K = (int64_t)pl->kA.size();
+  pl->aUnitM = !M.empty() && M[0].sa == 1;
+  pl->bUnitN = !N.empty() && N[0].sb == 1;
+  pl->aUnitK = !K.empty() && K[0].sa == 1;
+  pl->bUnitK = false;
+  for (auto &l : K)
+    if (l.sb == 1) pl->bUnitK = true;
+  const size_t tot = pl->rowA.size() + pl->kA.size() + pl->colB.size() + pl->kB.size() +
+                     pl->rowC.size() + pl->colC.size();
+  pl->dev = std::make_shared<DevMem>(tot * sizeof(int64_t));
+  int64_t *base = pl->dev->as<int64_t>();
+  size_t off = 0;
+  auto put = [&](const std::vector<int64_t> &v, const int64_t *&dptr) {
+    dptr = base + off;
+    if (!v.empty())
+      SCESS_CUDA(cudaMemcpy(base + off, v.data(), v.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
+    off += v.size();
+  };
+  put(pl->rowA, pl->d_rowA);
+  put(pl->kA, pl->d_kA);
+  put(pl->colB, pl->d_colB);
+  put(pl->kB, pl->d_kB);
+  put(pl->rowC, pl->d_rowC);
+  put(pl->colC, pl->d_colC);
+  auto &ref = *pl;
+  ctx.plans.emplace(key, std::move(pl));
+  return ref;
+}
+
+void einsum(Ctx &ctx, const char *spec, double alpha, const TV &A, const TV &B, double beta,
+            const TV &C, Backend be, bool constA, bool constB) {
+  const EinsumPlan &pl = plan_einsum(ctx, spec, A, B, C);
+  if ((be == Backend::MIXED && TcEngine::worth_it(pl)) || be == Backend::TENSOR) {
+    ctx.tensor_cores().contract(pl, alpha, A.p, B.p, beta, C.p, constA, constB);
+    return;
+  }
+  TableGemm g;
+  g.A = A.p;
+  g.B = B.p;
+  g.C = C.p;
+  g.rowA = pl.d_rowA;
+  g.kA = pl.d_kA;
+  g.colB = pl.d_colB;
+  g.kB = pl.d_kB;
+  g.rowC = pl.d_rowC;
+  g.colC = pl.d_colC;
+  g.M = pl.M;
+  g.N = pl.N;
+  g.K = pl.K;
+  g.alpha = alpha;
+  g.beta = beta;
+  g.aUnitM = pl.aUnitM;
+  g.bUnitN = pl.bUnitN;
+  if (pl.N == 1 && pl.K > 0) {
+    dgemv_table(g, ctx.stream);
+    return;
+  }
+  if (pl.M == 1 && pl.K > 0) {  // C^T = B^T A^T
+    TableGemm h = g;
+    h.A = B.p;
+    h.B = A.p;
+    h.rowA = pl.d_colB;
+    h.kA = pl.d_kB;
+    h.colB = pl.d_rowA;
+    h.kB = pl.d_kA;
+    h.rowC = pl.d_colC;
+    h.colC = pl.d_rowC;
+    h.M = pl.N;
+    h.N = 1;
+    dgemv_table(h, ctx.stream);
+    return;
+  }
+  double *ws = ctx.ensure_workspace(dgemm_table_workspace(g));
+  dgemm_table(g, ws, ctx.stream);
+}
+
+void permute(Ctx &ctx, const char *spec, double alpha, const TV &X, double beta, const TV &Y) {
+  const Spec s = parse_spec(spec, false);
+  if ((int)s.a.size() != X.nd || (int)s.c.size() != Y.nd)
+    throw Error(SCESS_ERR_INVALID, std::string("rank mismatch in ") + spec);
+  PermDesc d;
+  d.nd = Y.nd;
+  for (int k = 0; k < Y.nd; k++) {
+    const int p = (int)s.a.find(s.c[k]);
+    if (p < 0 || X.ext[p] != Y.ext[k]) throw Error(SCESS_ERR_INVALID, std::string("bad permute ") + spec);
+    d.ext[k] = Y.ext[k];
+    d.ys[k] = Y.str[k];
+    d.xs[k] = X.str[p];
+  }
+  permute_add(d, alpha, X.p, beta, Y.p, ctx.stream);
+}
+
+}  // namespace scess

@@ -1,0 +1,128 @@
+// Host-side engine: context, device memory, tensor views and the einsum compiler.
+#pragma once
+#include <chrono>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace scess {
+
+// Owning device allocation (freed on destruction).
+class DevMem {
+ public:
+  DevMem() = default;
+  explicit DevMem(size_t bytes) { alloc(bytes); }
+  ~DevMem() { release(); }
+  DevMem(const DevMem &) = delete;
+  DevMem &operator=(const DevMem &) = delete;
+  DevMem(DevMem &&o) noexcept : p_(o.p_), bytes_(o.bytes_) { o.p_ = nullptr; o.bytes_ = 0; }
+  DevMem &operator=(DevMem &&o) noexcept {
+    if (this != &o) { release(); p_ = o.p_; bytes_ = o.bytes_; o.p_ = nullptr; o.bytes_ = 0; }
+    return *this;
+  }
+  void alloc(size_t bytes);
+  void release();
+  template <class T> T *as() const { return static_cast<T *>(p_); }
+  double *d() const { return static_cast<double *>(p_); }
+  size_t bytes() const { return bytes_; }
+
+ private:
+  void *p_ = nullptr;
+  size_t bytes_ = 0;
+};
+
+// Strided view of an FP64 tensor in device memory: element (i_0, ..., i_{nd-1})
+// lives at p[sum_d i_d * str[d]].
+struct TV {
+  double *p = nullptr;
+  int nd = 0;
+  int64_t ext[6] = {1, 1, 1, 1, 1, 1};
+  int64_t str[6] = {0, 0, 0, 0, 0, 0};
+  int64_t size() const {
+    int64_t n = 1;
+    for (int d = 0; d < nd; d++) n *= ext[d];
+    return n;
+  }
+};
+// Column-major (first index fastest) dense view.
+TV cm(double *p, std::initializer_list<int64_t> ext);
+// A dense column-major tensor that owns its memory.
+struct DTensor {
+  DevMem mem;
+  TV v;
+  DTensor() = default;
+  DTensor(std::initializer_list<int64_t> ext);
+  double *p() const { return v.p; }
+  int64_t size() const { return v.size(); }
+};
+
+// Geometry of an einsum (label groups and offset tables), shared by backends.
+struct EinsumPlan {
+  int64_t M = 1, N = 1, K = 1;
+  std::vector<int64_t> rowA, kA, colB, kB, rowC, colC;  // host copies
+  std::shared_ptr<DevMem> dev;  // rowA | kA | colB | kB | rowC | colC on the device
+  const int64_t *d_rowA = nullptr, *d_kA = nullptr, *d_colB = nullptr, *d_kB = nullptr;
+  const int64_t *d_rowC = nullptr, *d_colC = nullptr;
+  bool aUnitM = false, bUnitN = false, aUnitK = false, bUnitK = false;
+  std::string key;
+};
+class TcEngine;  // tensor-core (mixed precision) backend, gemm_tc.cu
+
+// Per-call control: cancellation and the time limit.
+struct Control {
+  scess_cancel_fn cancel = nullptr;
+  void *user = nullptr;
+  double time_limit_s = 0.0;
+  std::chrono::steady_clock::time_point start = std::chrono::steady_clock::now();
+  void poll() const;
+};
+
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  scess_cancel_fn cancel = nullptr;
+  scess_log_fn log = nullptr;
+  void *user = nullptr;
+
+  // einsum plans (offset tables), keyed by spec + operand geometry
+  std::map<std::string, std::unique_ptr<EinsumPlan>> plans;
+  DevMem workspace;          // split-K partials
+  DevMem scratch;            // partial sums of reductions + device scalars
+  double *partials = nullptr;
+  double *dscalars = nullptr;  // 64 device doubles
+  double *hscalars = nullptr;  // 64 pinned host doubles
+  std::unique_ptr<TcEngine> tc;
+
+  explicit Ctx(int dev);
+  ~Ctx();
+  void sync() const { SCESS_CUDA(cudaStreamSynchronize(stream)); }
+  double *ensure_workspace(int64_t doubles);
+  void logf(int level, const char *fmt, ...) const;
+  TcEngine &tensor_cores();
+};
+
+// FP64: DFMA engine.  MIXED: tensor cores for contractions large enough to pay
+// for packing, FP64 for the rest.  TENSOR: tensor cores for every contraction.
+enum class Backend { FP64 = 0, MIXED = 1, TENSOR = 2 };
+
+// C[labels] = alpha * A[labels] B[labels] + beta * C   (spec "kcld,ilcd->ki").
+// Backend::MIXED routes large contractions to the tcgen05 engine and keeps
+// small ones in FP64.  `constA`/`constB` mark operands whose contents do not
+// change during the call so that their tensor-core packing can be reused.
+void einsum(Ctx &ctx, const char *spec, double alpha, const TV &A, const TV &B, double beta,
+            const TV &C, Backend be = Backend::FP64, bool constA = false, bool constB = false);
+// Y[out labels] = alpha * X[in labels] + beta * Y   (spec "kcai->akic").
+void permute(Ctx &ctx, const char *spec, double alpha, const TV &X, double beta, const TV &Y);
+
+const EinsumPlan &plan_einsum(Ctx &ctx, const char *spec, const TV &A, const TV &B, const TV &C);
+
+// Upload helpers (synchronous w.r.t. the host buffer).
+void upload(Ctx &ctx, double *dst, const double *src, int64_t n);
+void download(Ctx &ctx, double *dst, const double *src, int64_t n);
+
+}  // namespace scess

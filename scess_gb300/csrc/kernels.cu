@@ -1,0 +1,390 @@
+// FP64 contraction engine and bandwidth-bound kernels of the closed-shell CC path.
+//
+// GB300 runs FP64 at a small fraction of its tensor rate, so the FP64 GEMM is
+// DFMA-bound at any reasonable tile size: one 64x64 tile per 256-thread CTA with
+// 4x4 register blocking, operands gathered through offset tables (the einsum
+// permutation is fused into the tile loads), deterministic split-K when the
+// output has too few tiles to cover the 152 SMs.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace scess {
+
+namespace {
+
+constexpr int BM = 64, BN = 64, BK = 16;
+
+__global__ void __launch_bounds__(256) dgemm_table_kernel(TableGemm g, int64_t kChunk,
+                                                          double *partial) {
+  __shared__ double As[BK][BM];
+  __shared__ double Bs[BK][BN];
+  __shared__ int64_t sRowA[BM], sColB[BN], sKA[BK], sKB[BK];
+  const int t = threadIdx.x;
+  const int64_t m0 = (int64_t)blockIdx.x * BM, n0 = (int64_t)blockIdx.y * BN;
+  const int64_t kb = (int64_t)blockIdx.z * kChunk;
+  const int64_t ke = min(g.K, kb + kChunk);
+  if (t < BM) {
+    const int64_t m = m0 + t;
+    sRowA[t] = m < g.M ? g.baseA + g.rowA[m] : -1;
+  } else if (t < BM + BN) {
+    const int64_t n = n0 + (t - BM);
+    sColB[t - BM] = n < g.N ? g.baseB + g.colB[n] : -1;
+  }
+  double acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) acc[i][j] = 0.0;
+  const int tx = t & 15, ty = t >> 4;
+  for (int64_t k0 = kb; k0 < ke; k0 += BK) {
+    __syncthreads();
+    if (t < BK) {
+      const int64_t k = k0 + t;
+      sKA[t] = k < ke ? g.kA[k] : -1;
+    } else if (t >= 32 && t < 32 + BK) {
+      const int64_t k = k0 + (t - 32);
+      sKB[t - 32] = k < ke ? g.kB[k] : -1;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      const int idx = t + 256 * r;
+      int mm, kk;
+      if (g.aUnitM) { mm = idx & (BM - 1); kk = idx / BM; }
+      else { kk = idx & (BK - 1); mm = idx / BK; }
+      const int64_t ro = sRowA[mm], ko = sKA[kk];
+      As[kk][mm] = (ro >= 0 && ko >= 0) ? g.A[ro + ko] : 0.0;
+    }
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      const int idx = t + 256 * r;
+      int nn, kk;
+      if (g.bUnitN) { nn = idx & (BN - 1); kk = idx / BN; }
+      else { kk = idx & (BK - 1); nn = idx / BK; }
+      const int64_t co = sColB[nn], ko = sKB[kk];
+      Bs[kk][nn] = (co >= 0 && ko >= 0) ? g.B[co + ko] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; kk++) {
+      double a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; i++) a[i] = As[kk][tx + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; j++) b[j] = Bs[kk][ty + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const int64_t m = m0 + tx + 16 * i;
+    if (m >= g.M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int64_t n = n0 + ty + 16 * j;
+      if (n >= g.N) continue;
+      if (partial) {
+        partial[(int64_t)blockIdx.z * g.M * g.N + m + g.M * n] = acc[i][j];
+      } else {
+        const int64_t off = g.baseC + g.rowC[m] + g.colC[n];
+        double val = g.alpha * acc[i][j];
+        if (g.beta != 0.0) val += g.beta * g.C[off];
+        g.C[off] = val;
+      }
+    }
+  }
+}
+
+__global__ void splitk_reduce_kernel(TableGemm g, int splits, const double *partial) {
+  const int64_t MN = g.M * g.N;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < MN;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int z = 0; z < splits; z++) s += partial[(int64_t)z * MN + e];
+    const int64_t m = e % g.M, n = e / g.M;
+    const int64_t off = g.baseC + g.rowC[m] + g.colC[n];
+    double val = g.alpha * s;
+    if (g.beta != 0.0) val += g.beta * g.C[off];
+    g.C[off] = val;
+  }
+}
+
+int choose_splits(const TableGemm &g) {
+  const int64_t tiles = ceil_div(g.M, BM) * ceil_div(g.N, BN);
+  const int64_t target = 2 * kNumSMs;
+  if (tiles >= target || g.K <= 4 * BK) return 1;
+  int64_t s = ceil_div(target, tiles);
+  s = std::min<int64_t>(s, ceil_div(g.K, 4 * BK));
+  // keep the partial buffer below 64 Mi doubles
+  while (s > 1 && s * g.M * g.N > (int64_t(64) << 20)) s--;
+  return (int)std::max<int64_t>(s, 1);
+}
+
+}  // namespace
+
+namespace {
+__global__ void dgemv_table_kernel(TableGemm g) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const double *__restrict__ B = g.B + g.baseB + g.colB[0];
+  for (int64_t m = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; m < g.M; m += warps) {
+    const double *__restrict__ A = g.A + g.baseA + g.rowA[m];
+    double s = 0.0;
+    for (int64_t k = lane; k < g.K; k += 32) s = fma(A[g.kA[k]], B[g.kB[k]], s);
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    if (lane == 0) {
+      const int64_t off = g.baseC + g.rowC[m] + g.colC[0];
+      double val = g.alpha * s;
+      if (g.beta != 0.0) val += g.beta * g.C[off];
+      g.C[off] = val;
+    }
+  }
+}
+}  // namespace
+
+void dgemv_table(const TableGemm &g, cudaStream_t stream) {
+  if (g.M <= 0) return;
+  const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(g.M * 32, 256), 16 * kNumSMs);
+  dgemv_table_kernel<<<blocks, 256, 0, stream>>>(g);
+  SCESS_CHECK_LAUNCH();
+}
+
+int64_t dgemm_table_workspace(const TableGemm &g) {
+  const int s = choose_splits(g);
+  return s > 1 ? s * g.M * g.N : 0;
+}
+
+void dgemm_table(const TableGemm &g, double *workspace, cudaStream_t stream) {
+  if (g.M <= 0 || g.N <= 0) return;
+  if (g.K <= 0) {
+    // C = beta * C
+    TableGemm h = g;
+    h.alpha = 0.0;
+    splitk_reduce_kernel<<<(unsigned)std::min<int64_t>(ceil_div(g.M * g.N, 256), 4096), 256, 0,
+                           stream>>>(h, 0, nullptr);
+    SCESS_CHECK_LAUNCH();
+    return;
+  }
+  const int splits = choose_splits(g);
+  const int64_t kChunk = round_up(ceil_div(g.K, splits), BK);
+  const int nz = (int)ceil_div(g.K, kChunk);
+  dim3 grid((unsigned)ceil_div(g.M, BM), (unsigned)ceil_div(g.N, BN), (unsigned)nz);
+  if (nz > 1) {
+    if (!workspace) throw Error(SCESS_ERR_INVALID, "dgemm_table: split-K needs a workspace");
+    dgemm_table_kernel<<<grid, 256, 0, stream>>>(g, kChunk, workspace);
+    SCESS_CHECK_LAUNCH();
+    splitk_reduce_kernel<<<(unsigned)std::min<int64_t>(ceil_div(g.M * g.N, 256), 4096), 256, 0,
+                           stream>>>(g, nz, workspace);
+  } else {
+    dgemm_table_kernel<<<grid, 256, 0, stream>>>(g, kChunk, nullptr);
+  }
+  SCESS_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------------------------------------
+
+namespace {
+
+__global__ void permute_add_kernel(PermDesc d, double alpha, const double *__restrict__ X,
+                                   double beta, double *__restrict__ Y, int64_t n) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = e, xo = 0, yo = 0;
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+      if (k < d.nd) {
+        const int64_t i = r % d.ext[k];
+        r /= d.ext[k];
+        xo += i * d.xs[k];
+        yo += i * d.ys[k];
+      }
+    }
+    double val = alpha * X[xo];
+    if (beta != 0.0) val += beta * Y[yo];
+    Y[yo] = val;
+  }
+}
+
+unsigned grid_for(int64_t n, int threads = 256) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, threads), 16 * kNumSMs * 8));
+}
+
+__global__ void tau_kernel(int64_t o, int64_t v, const double *__restrict__ t1,
+                           const double *__restrict__ t2, double s, double *__restrict__ tau) {
+  const int64_t n = o * o * v * v;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e % o, j = (e / o) % o, a = (e / (o * o)) % v, b = e / (o * o * v);
+    tau[e] = t2[e] + s * t1[i + o * a] * t1[j + o * b];
+  }
+}
+
+__global__ void denom_kernel(int64_t o, int64_t v, const double *__restrict__ eps,
+                             const double *__restrict__ R1, const double *__restrict__ R2,
+                             double *__restrict__ t1, double *__restrict__ t2) {
+  const int64_t n1 = o * v, n2 = o * o * v * v;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n1 + n2;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    if (e < n1) {
+      const int64_t i = e % o, a = e / o;
+      t1[e] = R1[e] / (eps[i] - eps[o + a]);
+    } else {
+      const int64_t x = e - n1;
+      const int64_t i = x % o, j = (x / o) % o, a = (x / (o * o)) % v, b = x / (o * o * v);
+      // eijab = eia(i,a) + eia(j,b), the reference's association (RCCSD.cpp:331)
+      const double d = (eps[i] - eps[o + a]) + (eps[j] - eps[o + b]);
+      t2[x] = R2[x] / d;
+    }
+  }
+}
+
+__global__ void plus_transpose_kernel(int64_t o, int64_t v, double alpha,
+                                      const double *__restrict__ X, double *__restrict__ out) {
+  const int64_t n = o * o * v * v;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e % o, j = (e / o) % o, a = (e / (o * o)) % v, b = e / (o * o * v);
+    const int64_t et = j + o * i + o * o * b + o * o * v * a;
+    out[e] += alpha * (X[e] + X[et]);
+  }
+}
+
+__global__ void axpby_kernel(int64_t n, double a, const double *__restrict__ x, double b,
+                             double *__restrict__ y) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x)
+    y[e] = a * x[e] + (b == 0.0 ? 0.0 : b * y[e]);
+}
+
+__device__ double block_sum(double v) {
+  __shared__ double sh[32];
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (w == 0) {
+    r = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+    for (int off = 16; off > 0; off >>= 1) r += __shfl_down_sync(0xffffffffu, r, off);
+  }
+  __syncthreads();
+  return r;  // valid in thread 0
+}
+
+__global__ void dot_partial_kernel(int64_t n, const double *__restrict__ x,
+                                   const double *__restrict__ y, double *__restrict__ partials) {
+  double s = 0.0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x)
+    s = fma(x[e], y[e], s);
+  s = block_sum(s);
+  if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+__global__ void sum_partials_kernel(int np, const double *__restrict__ partials,
+                                    double *__restrict__ result) {
+  double s = 0.0;
+  for (int e = threadIdx.x; e < np; e += blockDim.x) s += partials[e];
+  s = block_sum(s);
+  if (threadIdx.x == 0) result[0] = s;
+}
+
+__global__ void tau_energy_partial_kernel(int64_t o, int64_t v, const double *__restrict__ L,
+                                          const double *__restrict__ t1,
+                                          const double *__restrict__ t2,
+                                          double *__restrict__ partials) {
+  const int64_t n = o * o * v * v;
+  double s = 0.0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e % o, j = (e / o) % o, a = (e / (o * o)) % v, b = e / (o * o * v);
+    const double tau = t2[e] + t1[i + o * a] * t1[j + o * b];
+    s = fma(L[e], tau, s);
+  }
+  s = block_sum(s);
+  if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+__global__ void lincomb_kernel(int64_t n, int nv, const double *const *__restrict__ vecs,
+                               const double *__restrict__ coef, double *__restrict__ out) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int c = 0; c < nv; c++) s += coef[c] * vecs[c][e];
+    out[e] = s;
+  }
+}
+
+__global__ void finite_kernel(int64_t n, const double *__restrict__ x, int *flag) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x)
+    if (!isfinite(x[e])) *flag = 1;
+}
+
+}  // namespace
+
+void permute_add(const PermDesc &d, double alpha, const double *X, double beta, double *Y,
+                 cudaStream_t stream) {
+  int64_t n = 1;
+  for (int k = 0; k < d.nd; k++) n *= d.ext[k];
+  if (n == 0) return;
+  permute_add_kernel<<<grid_for(n), 256, 0, stream>>>(d, alpha, X, beta, Y, n);
+  SCESS_CHECK_LAUNCH();
+}
+
+void make_tau(int64_t o, int64_t v, const double *t1, const double *t2, double s, double *tau,
+              cudaStream_t stream) {
+  tau_kernel<<<grid_for(o * o * v * v), 256, 0, stream>>>(o, v, t1, t2, s, tau);
+  SCESS_CHECK_LAUNCH();
+}
+
+void divide_denominators(int64_t o, int64_t v, const double *eps, const double *R1,
+                         const double *R2, double *t1, double *t2, cudaStream_t stream) {
+  denom_kernel<<<grid_for(o * v + o * o * v * v), 256, 0, stream>>>(o, v, eps, R1, R2, t1, t2);
+  SCESS_CHECK_LAUNCH();
+}
+
+void plus_transpose(int64_t o, int64_t v, double alpha, const double *X, double *out,
+                    cudaStream_t stream) {
+  plus_transpose_kernel<<<grid_for(o * o * v * v), 256, 0, stream>>>(o, v, alpha, X, out);
+  SCESS_CHECK_LAUNCH();
+}
+
+void axpby(int64_t n, double a, const double *x, double b, double *y, cudaStream_t stream) {
+  if (n == 0) return;
+  axpby_kernel<<<grid_for(n), 256, 0, stream>>>(n, a, x, b, y);
+  SCESS_CHECK_LAUNCH();
+}
+
+void dot(int64_t n, const double *x, const double *y, double *partials, double *result,
+         cudaStream_t stream) {
+  dot_partial_kernel<<<kDotBlocks, 256, 0, stream>>>(n, x, y, partials);
+  SCESS_CHECK_LAUNCH();
+  sum_partials_kernel<<<1, 1024, 0, stream>>>(kDotBlocks, partials, result);
+  SCESS_CHECK_LAUNCH();
+}
+
+void linear_combination(int64_t n, int nv, const double *const *vecs, const double *coef,
+                        double *out, cudaStream_t stream) {
+  lincomb_kernel<<<grid_for(n), 256, 0, stream>>>(n, nv, vecs, coef, out);
+  SCESS_CHECK_LAUNCH();
+}
+
+void tau_energy(int64_t o, int64_t v, const double *L, const double *t1, const double *t2,
+                double *partials, double *result, cudaStream_t stream) {
+  tau_energy_partial_kernel<<<kDotBlocks, 256, 0, stream>>>(o, v, L, t1, t2, partials);
+  SCESS_CHECK_LAUNCH();
+  sum_partials_kernel<<<1, 1024, 0, stream>>>(kDotBlocks, partials, result);
+  SCESS_CHECK_LAUNCH();
+}
+
+void check_finite(int64_t n, const double *x, int *flag, cudaStream_t stream) {
+  if (n == 0) return;
+  finite_kernel<<<grid_for(n), 256, 0, stream>>>(n, x, flag);
+  SCESS_CHECK_LAUNCH();
+}
+
+}  // namespace scess

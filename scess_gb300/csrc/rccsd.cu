@@ -1,0 +1,416 @@
+// Closed-shell CCSD: integral block views, residual op list, solver loop with DIIS.
+//
+// Follows SCESS src/Quantum/CC/RCCSD.cpp:
+//   MakeIntegralBlocks :47-72 -> RccsdBlocks::build (strided views, no copies)
+//   UpdateAmplitudes   :101-237 -> rccsd_residual + divide_denominators
+//   AmplitudeDIIS      :240-279 -> device vectors + host Gram/full-pivot LU
+//   SolveRCCSD_DIIS    :295-394 -> rccsd_solve
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+
+#include "gemm_tc.h"
+#include "rccsd.h"
+
+namespace scess {
+
+namespace {
+
+TV view(double *base, int64_t off, std::initializer_list<int64_t> ext,
+        std::initializer_list<int64_t> str) {
+  TV t;
+  t.p = base + off;
+  t.nd = (int)ext.size();
+  int d = 0;
+  for (int64_t e : ext) t.ext[d++] = e;
+  d = 0;
+  for (int64_t s : str) t.str[d++] = s;
+  return t;
+}
+
+}  // namespace
+
+void RccsdBlocks::build(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t nocc) {
+  o = nocc;
+  v = nmo - nocc;
+  N = nmo;
+  double *e = const_cast<double *>(d_eri);
+  const int64_t N1 = 1, N2 = N, N3 = N * N, N4 = N * N * N;  // strides of p, q, r, s
+  // eri(p,q,r,s) = <pq|rs> at p + N q + N^2 r + N^3 s
+  // ovov(k,c,l,d) = (kc|ld) = <kl|cd> = eri(k, l, o+c, o+d)                       :55
+  ovov = view(e, o * N3 + o * N4, {o, v, o, v}, {N1, N3, N2, N4});
+  // oovv(k,i,a,c) = (ki|ac) = <ka|ic> = eri(k, o+a, i, o+c)                       :57
+  oovv = view(e, o * N2 + o * N4, {o, o, v, v}, {N1, N3, N2, N4});
+  // ovvo(k,c,a,i) = (kc|ai) = <ka|ci> = eri(k, o+a, o+c, i)                       :59
+  ovvo = view(e, o * N2 + o * N3, {o, v, v, o}, {N1, N3, N2, N4});
+  // ovvv(k,d,a,c) = (kd|ac) = <ka|dc> = eri(k, o+a, o+d, o+c)                     :61
+  ovvv = view(e, o * N2 + o * N3 + o * N4, {o, v, v, v}, {N1, N3, N2, N4});
+  // ovoo(l,c,k,i) = (lc|ki) = <lk|ci> = eri(l, k, o+c, i)                         :63
+  ovoo = view(e, o * N3, {o, v, o, o}, {N1, N3, N2, N4});
+  // oooo_phys(k,l,i,j) = <kl|ij>                                                    :64
+  oooo = view(e, 0, {o, o, o, o}, {N1, N2, N3, N4});
+  // vvvv_phys(a,b,c,d) = <ab|cd>                                                    :65
+  vvvv = view(e, o * (N1 + N2 + N3 + N4), {v, v, v, v}, {N1, N2, N3, N4});
+  // oovv_phys(i,j,a,b) = <ij|ab>                                                    :66
+  oovv_phys = view(e, o * N3 + o * N4, {o, o, v, v}, {N1, N2, N3, N4});
+  // L_oovv = 2 <ij|ab> - <ij|ba>                                                   :68-69
+  L_oovv = DTensor({o, o, v, v});
+  permute(ctx, "ijab->ijab", 2.0, oovv_phys, 0.0, L_oovv.v);
+  permute(ctx, "ijba->ijab", -1.0, oovv_phys, 1.0, L_oovv.v);
+  // L_ovov = 2 (kc|ld) - (kd|lc)                                                   :70
+  L_ovov = DTensor({o, v, o, v});
+  permute(ctx, "kcld->kcld", 2.0, ovov, 0.0, L_ovov.v);
+  permute(ctx, "kdlc->kcld", -1.0, ovov, 1.0, L_ovov.v);
+}
+
+void RccsdWork::alloc(int64_t o, int64_t v, bool direct_vvvv) {
+  tau = DTensor({o, o, v, v});
+  Foo = DTensor({o, o});
+  Fvv = DTensor({v, v});
+  Fov = DTensor({o, v});
+  Fovt1 = DTensor({o, o});
+  Loo = DTensor({o, o});
+  Lvv = DTensor({v, v});
+  X = DTensor({o, o, v, v});
+  tmp_abic = DTensor({v, v, o, v});
+  tmp_akij = DTensor({v, o, o, o});
+  Woooo = DTensor({o, o, o, o});
+  Wvoov = DTensor({v, o, o, v});
+  Wvovo = DTensor({v, o, v, o});
+  tmp_lkci = DTensor({o, o, v, o});
+  tmp_lcki = DTensor({o, v, o, o});
+  Yd = DTensor({o, v, o, o});
+  if (direct_vvvv) Wvvvv = DTensor({v, v, v, v});
+}
+
+void rccsd_residual(Ctx &ctx, const RccsdBlocks &B, const double *amp, const double *t2driver,
+                    Backend be, RccsdWork &w, double *R) {
+  const int64_t o = B.o, v = B.v;
+  cudaStream_t s = ctx.stream;
+  double *a = const_cast<double *>(amp);
+  const TV t1 = cm(a, {o, v});
+  const TV t2 = cm(a + o * v, {o, o, v, v});
+  const TV R1 = cm(R, {o, v});
+  const TV R2 = cm(R + o * v, {o, o, v, v});
+  auto E = [&](const char *spec, double alpha, const TV &A, const TV &Bt, double beta,
+               const TV &C, bool cA = false, bool cB = false) {
+    einsum(ctx, spec, alpha, A, Bt, beta, C, be, cA, cB);
+  };
+  make_tau(o, v, t1.p, t2.p, 1.0, w.tau.p(), s);                                     // :107
+  const TV tau = w.tau.v;
+  E("kcld,ilcd->ki", 1.0, B.L_ovov.v, tau, 0.0, w.Foo.v, true);                      // :111
+  E("kcld,klad->ac", -1.0, B.L_ovov.v, tau, 0.0, w.Fvv.v, true);                     // :113
+  E("kcld,ld->kc", 1.0, B.L_ovov.v, t1, 0.0, w.Fov.v, true);                         // :115
+
+  E("ac,ic->ia", 1.0, w.Fvv.v, t1, 0.0, R1);                                         // :119
+  E("ki,ka->ia", -1.0, w.Foo.v, t1, 1.0, R1);                                        // :121
+  E("kc,kica->ia", 2.0, w.Fov.v, t2, 1.0, R1);                                       // :123
+  E("kc,ikca->ia", -1.0, w.Fov.v, t2, 1.0, R1);                                      // :124
+  E("kc,ic->ki", 1.0, w.Fov.v, t1, 0.0, w.Fovt1.v);                                  // :127
+  E("ki,ka->ia", 1.0, w.Fovt1.v, t1, 1.0, R1);                                       // :128
+  E("kcai,kc->ia", 2.0, B.ovvo, t1, 1.0, R1, true);                                  // :131
+  E("kiac,kc->ia", -1.0, B.oovv, t1, 1.0, R1, true);                                 // :132
+  E("kdac,ikcd->ia", 2.0, B.ovvv, tau, 1.0, R1, true);                               // :134
+  E("kcad,ikcd->ia", -1.0, B.ovvv, tau, 1.0, R1, true);                              // :135
+  E("lcki,klac->ia", -2.0, B.ovoo, tau, 1.0, R1, true);                              // :137
+  E("kcli,klac->ia", 1.0, B.ovoo, tau, 1.0, R1, true);                               // :138
+
+  // T2.  X collects every term the reference wraps in PlusTranspose.
+  E("kibc,ka->abic", -1.0, B.oovv, t1, 0.0, w.tmp_abic.v, true);                     // :144
+  permute(ctx, "iacb->abic", 1.0, B.ovvv, 1.0, w.tmp_abic.v);                        // :145
+  E("abic,jc->ijab", 1.0, w.tmp_abic.v, t1, 0.0, w.X.v);                             // :147
+  E("kcai,jc->akij", 1.0, B.ovvo, t1, 0.0, w.tmp_akij.v, true);                      // :152
+  permute(ctx, "iajk->akij", 1.0, B.ovoo, 1.0, w.tmp_akij.v);                        // :153
+  E("akij,kb->ijab", -1.0, w.tmp_akij.v, t1, 1.0, w.X.v);                            // :155
+  permute(ctx, "ijab->ijab", 1.0, B.oovv_phys, 0.0, R2);                             // :158
+  if (t2driver) axpby(o * o * v * v, 1.0, t2driver, 1.0, R2.p, s);                   // :159-160
+
+  permute(ctx, "ki->ki", 1.0, w.Foo.v, 0.0, w.Loo.v);                                // :163
+  E("lcki,lc->ki", 2.0, B.ovoo, t1, 1.0, w.Loo.v, true);                             // :164
+  E("kcli,lc->ki", -1.0, B.ovoo, t1, 1.0, w.Loo.v, true);                            // :165
+  permute(ctx, "ac->ac", 1.0, w.Fvv.v, 0.0, w.Lvv.v);                                // :167
+  E("kdac,kd->ac", 2.0, B.ovvv, t1, 1.0, w.Lvv.v, true);                             // :168
+  E("kcad,kd->ac", -1.0, B.ovvv, t1, 1.0, w.Lvv.v, true);                            // :169
+
+  permute(ctx, "klij->klij", 1.0, B.oooo, 0.0, w.Woooo.v);                           // :172
+  E("lcki,jc->klij", 1.0, B.ovoo, t1, 1.0, w.Woooo.v, true);                         // :173
+  E("kclj,ic->klij", 1.0, B.ovoo, t1, 1.0, w.Woooo.v, true);                         // :174
+  E("kcld,ijcd->klij", 1.0, B.ovov, tau, 1.0, w.Woooo.v, true);                      // :175
+
+  permute(ctx, "kcai->akic", 1.0, B.ovvo, 0.0, w.Wvoov.v);                           // :183
+  E("kcad,id->akic", 1.0, B.ovvv, t1, 1.0, w.Wvoov.v, true);                         // :185
+  E("kcli,la->akic", -1.0, B.ovoo, t1, 1.0, w.Wvoov.v, true);                        // :186
+  E("ldkc,ilda->akic", -0.5, B.ovov, t2, 1.0, w.Wvoov.v, true);                      // :188
+  E("lckd,ilad->akic", -0.5, B.ovov, t2, 1.0, w.Wvoov.v, true);                      // :190
+  E("ldkc,ilad->akic", 1.0, B.ovov, t2, 1.0, w.Wvoov.v, true);                       // :192
+  E("ldkc,id->lkci", 1.0, B.ovov, t1, 0.0, w.tmp_lkci.v, true);                      // :195
+  E("lkci,la->akic", -1.0, w.tmp_lkci.v, t1, 1.0, w.Wvoov.v);                        // :196
+
+  permute(ctx, "kiac->akci", 1.0, B.oovv, 0.0, w.Wvovo.v);                           // :200
+  E("kdac,id->akci", 1.0, B.ovvv, t1, 1.0, w.Wvovo.v, true);                         // :202
+  E("lcki,la->akci", -1.0, B.ovoo, t1, 1.0, w.Wvovo.v, true);                        // :203
+  E("lckd,ilda->akci", -0.5, B.ovov, t2, 1.0, w.Wvovo.v, true);                      // :205
+  E("lckd,id->lcki", 1.0, B.ovov, t1, 0.0, w.tmp_lcki.v, true);                      // :209
+  E("lcki,la->akci", -1.0, w.tmp_lcki.v, t1, 1.0, w.Wvovo.v);                        // :210
+
+  E("klij,klab->ijab", 1.0, w.Woooo.v, tau, 1.0, R2);                                // :214
+  if (be == Backend::FP64) {
+    permute(ctx, "abcd->abcd", 1.0, B.vvvv, 0.0, w.Wvvvv.v);                         // :178
+    E("kdac,kb->abcd", -1.0, B.ovvv, t1, 1.0, w.Wvvvv.v, true);                      // :179
+    E("kcbd,ka->abcd", -1.0, B.ovvv, t1, 1.0, w.Wvvvv.v, true);                      // :180
+    E("abcd,ijcd->ijab", 1.0, w.Wvvvv.v, tau, 1.0, R2);                              // :216
+  } else {
+    // sum_cd Wvvvv tau = vvvv tau - PlusTranspose(sum_k t1(k,a) Y(k,b,i,j)),
+    // Y(k,b,i,j) = sum_cd (kc|bd) tau(i,j,c,d), using tau(i,j,c,d) = tau(j,i,d,c).
+    E("abcd,ijcd->ijab", 1.0, B.vvvv, tau, 1.0, R2, true);                           // :216
+    E("kcbd,ijcd->kbij", 1.0, B.ovvv, tau, 0.0, w.Yd.v, true);                       // :179-180
+    E("ka,kbij->ijab", -1.0, t1, w.Yd.v, 1.0, w.X.v);
+  }
+  E("ac,ijcb->ijab", 1.0, w.Lvv.v, t2, 1.0, w.X.v);                                  // :218
+  E("ki,kjab->ijab", -1.0, w.Loo.v, t2, 1.0, w.X.v);                                 // :220
+  E("akic,kjcb->ijab", 2.0, w.Wvoov.v, t2, 1.0, w.X.v);                              // :223
+  E("akci,kjcb->ijab", -1.0, w.Wvovo.v, t2, 1.0, w.X.v);                             // :225
+  E("akic,kjbc->ijab", -1.0, w.Wvoov.v, t2, 1.0, w.X.v);                             // :228
+  E("bkci,kjac->ijab", -1.0, w.Wvovo.v, t2, 1.0, w.X.v);                             // :231
+  plus_transpose(o, v, 1.0, w.X.p(), R2.p, s);                                       // :147-232
+}
+
+// ---------------------------------------------------------------------------------------------
+
+std::vector<double> full_piv_lu_solve(std::vector<double> A, std::vector<double> b, int n) {
+  std::vector<int> rowp(n), colp(n);
+  for (int i = 0; i < n; i++) rowp[i] = colp[i] = i;
+  int nonzero = n;
+  auto at = [&](int i, int j) -> double & { return A[(size_t)i * n + j]; };
+  for (int k = 0; k < n; k++) {
+    double best = -1.0;
+    int bi = k, bj = k;
+    for (int i = k; i < n; i++)
+      for (int j = k; j < n; j++) {
+        const double x = std::fabs(at(i, j));
+        if (x > best) { best = x; bi = i; bj = j; }
+      }
+    if (best == 0.0) { nonzero = k; break; }
+    if (bi != k) {
+      for (int j = 0; j < n; j++) std::swap(at(k, j), at(bi, j));
+      std::swap(rowp[k], rowp[bi]);
+    }
+    if (bj != k) {
+      for (int i = 0; i < n; i++) std::swap(at(i, k), at(i, bj));
+      std::swap(colp[k], colp[bj]);
+    }
+    for (int i = k + 1; i < n; i++) {
+      at(i, k) /= at(k, k);
+      for (int j = k + 1; j < n; j++) at(i, j) -= at(i, k) * at(k, j);
+    }
+  }
+  double maxpiv = 0.0;
+  for (int i = 0; i < nonzero; i++) maxpiv = std::max(maxpiv, std::fabs(at(i, i)));
+  const double thresh = DBL_EPSILON * n;
+  int rank = 0;
+  for (int i = 0; i < nonzero; i++)
+    if (std::fabs(at(i, i)) > thresh * maxpiv) rank++;
+  std::vector<double> c(n), y(n, 0.0), x(n, 0.0);
+  for (int i = 0; i < n; i++) c[i] = b[rowp[i]];
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < std::min(i, rank); j++) c[i] -= at(i, j) * c[j];
+  for (int i = rank - 1; i >= 0; i--) {
+    double sum = c[i];
+    for (int j = i + 1; j < rank; j++) sum -= at(i, j) * y[j];
+    y[i] = sum / at(i, i);
+  }
+  for (int i = 0; i < n; i++) x[colp[i]] = y[i];
+  return x;
+}
+
+std::vector<double> diis_coefficients(const std::vector<std::vector<double>> &gram) {
+  const int n = (int)gram.size();
+  const int m = n + 1;
+  std::vector<double> B((size_t)m * m, -1.0);
+  B[(size_t)n * m + n] = 0.0;
+  double maxv = 0.0;
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) {
+      B[(size_t)i * m + j] = gram[i][j];
+      maxv = std::max(maxv, std::fabs(gram[i][j]));
+    }
+  if (maxv > 0.0)
+    for (int i = 0; i < n; i++)
+      for (int j = 0; j < n; j++) B[(size_t)i * m + j] /= maxv;
+  std::vector<double> rhs(m, 0.0);
+  rhs[n] = -1.0;
+  std::vector<double> c = full_piv_lu_solve(B, rhs, m);
+  c.resize(n);
+  return c;
+}
+
+// ---------------------------------------------------------------------------------------------
+
+void rccsd_solve(Ctx &ctx, const RccsdBlocks &B, const SolveInput &in,
+                 const scess_rccsd_options &opts, const Control &ctl, double *t1_out,
+                 double *t2_out, scess_rccsd_result *res) {
+  const int64_t o = B.o, v = B.v, N = B.N;
+  const int64_t n1 = o * v, n2 = o * o * v * v, n = n1 + n2;
+  cudaStream_t s = ctx.stream;
+  const bool mixed = opts.precision == SCESS_PRECISION_MIXED;
+  std::memset(res, 0, sizeof(*res));
+
+  ctx.logf(0, in.f12_residual
+                  ? "--- Closed-shell CCSD with F12 geminals (CCSD-F12b) with DIIS acceleration ---"
+                  : "--- Closed-shell Coupled Cluster Singles & Doubles (CCSD) with DIIS acceleration ---");
+
+  DTensor eps({N});
+  upload(ctx, eps.p(), in.eps_host, N);
+  DTensor amp({n}), prev({n}), R({n});
+  DTensor drv, Lf12;
+  if (in.f12_residual) {
+    drv = DTensor({o, o, v, v});
+    upload(ctx, drv.p(), in.f12_residual, n2);
+  }
+  if (in.f12_energy) {
+    DTensor e12({o, o, v, v});
+    upload(ctx, e12.p(), in.f12_energy, n2);
+    Lf12 = DTensor({o, o, v, v});
+    permute(ctx, "ijab->ijab", 2.0, e12.v, 0.0, Lf12.v);                             // :95-96
+    permute(ctx, "ijba->ijab", -1.0, e12.v, 1.0, Lf12.v);
+    ctx.sync();
+  }
+  const int maxv = std::max(1, opts.max_diis_vectors);
+  DevMem diis_amp((size_t)maxv * n * sizeof(double)), diis_err((size_t)maxv * n * sizeof(double));
+  DevMem vecptr((size_t)maxv * sizeof(double *)), coefd((size_t)(maxv + 1) * sizeof(double));
+  std::vector<const double *> hptr(maxv);
+  RccsdWork w;
+  w.alloc(o, v, !mixed);
+  bool have_wvvvv = !mixed;
+
+  double *t1 = amp.p(), *t2 = amp.p() + n1;
+  if (opts.resume) {
+    upload(ctx, t1, t1_out, n1);
+    upload(ctx, t2, t2_out, n2);
+  } else {
+    // MP2 guess: t1 = 0, t2 = (<ij|ab> + f12 residual) / eijab                       :334-339
+    SCESS_CUDA(cudaMemsetAsync(R.p(), 0, n1 * sizeof(double), s));
+    permute(ctx, "ijab->ijab", 1.0, B.oovv_phys, 0.0, cm(R.p() + n1, {o, o, v, v}));
+    if (drv.p()) axpby(n2, 1.0, drv.p(), 1.0, R.p() + n1, s);
+    divide_denominators(o, v, eps.p(), R.p(), R.p() + n1, t1, t2, s);
+  }
+
+  std::deque<int> order;  // DIIS slots, oldest first
+  std::vector<std::vector<double>> gram;
+  double E_last = DBL_MAX;
+  bool mixed_phase = mixed;
+  int phase_start = 0;
+  int fp64_iters = 0;
+  bool converged = false;
+  int it = 0;
+  double E = 0.0, dE = 0.0, rms = 0.0;
+  for (it = 0; it < opts.max_iterations; it++) {
+    ctl.poll();                                                                       // :346
+    SCESS_CUDA(cudaMemcpyAsync(prev.p(), amp.p(), n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    const Backend be = mixed_phase ? Backend::MIXED : Backend::FP64;
+    if (be == Backend::FP64 && !have_wvvvv) {
+      w.Wvvvv = DTensor({v, v, v, v});
+      have_wvvvv = true;
+    }
+    rccsd_residual(ctx, B, amp.p(), drv.p(), be, w, R.p());                           // :350
+    divide_denominators(o, v, eps.p(), R.p(), R.p() + n1, t1, t2, s);
+
+    // AmplitudeDIIS::Extrapolate(updated, change)                                    :246-274
+    int slot;
+    if ((int)order.size() < maxv) {
+      slot = (int)order.size();
+    } else {
+      slot = order.front();
+      order.pop_front();
+      gram.erase(gram.begin());
+      for (auto &row : gram) row.erase(row.begin());
+    }
+    double *va = diis_amp.d() + (size_t)slot * n;
+    double *ve = diis_err.d() + (size_t)slot * n;
+    SCESS_CUDA(cudaMemcpyAsync(va, amp.p(), n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    SCESS_CUDA(cudaMemcpyAsync(ve, amp.p(), n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    axpby(n, -1.0, prev.p(), 1.0, ve, s);                                             // :352
+    order.push_back(slot);
+    const int nv = (int)order.size();
+    for (int q = 0; q < nv; q++)
+      dot(n, diis_err.d() + (size_t)order[q] * n, ve, ctx.partials, ctx.dscalars + q, s);
+    SCESS_CUDA(cudaMemcpyAsync(ctx.hscalars, ctx.dscalars, nv * sizeof(double),
+                               cudaMemcpyDeviceToHost, s));
+    ctx.sync();
+    for (int q = 0; q < nv - 1; q++) gram[q].push_back(ctx.hscalars[q]);
+    gram.emplace_back(ctx.hscalars, ctx.hscalars + nv);
+    const double errdot = ctx.hscalars[nv - 1];
+    if (it - phase_start >= opts.diis_start) {                                         // :354-357
+      if (it - phase_start == opts.diis_start) ctx.logf(1, "Turning on DIIS");
+      std::vector<double> c = diis_coefficients(gram);
+      for (int q = 0; q < nv; q++) hptr[q] = diis_amp.d() + (size_t)order[q] * n;
+      SCESS_CUDA(cudaMemcpyAsync(vecptr.as<void>(), hptr.data(), nv * sizeof(double *),
+                                 cudaMemcpyHostToDevice, s));
+      SCESS_CUDA(cudaMemcpyAsync(coefd.d(), c.data(), nv * sizeof(double), cudaMemcpyHostToDevice, s));
+      linear_combination(n, nv, vecptr.as<const double *>(), coefd.d(), amp.p(), s);
+      ctx.sync();  // hptr / c are pageable host buffers reused next iteration
+    }
+    // E = CorrelationEnergy + CouplingEnergy                                         :361
+    tau_energy(o, v, B.L_oovv.p(), t1, t2, ctx.partials, ctx.dscalars, s);
+    if (Lf12.p()) dot(n2, Lf12.p(), t2, ctx.partials, ctx.dscalars + 1, s);
+    SCESS_CUDA(cudaMemcpyAsync(ctx.hscalars, ctx.dscalars, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    ctx.sync();
+    E = ctx.hscalars[0] + (Lf12.p() ? ctx.hscalars[1] : 0.0);
+    dE = std::fabs(E - E_last);                                                       // :362
+    rms = std::sqrt(errdot) / std::sqrt((double)n);                                   // :363
+    E_last = E;
+    if (!std::isfinite(E)) throw Error(SCESS_ERR_INVALID, "non-finite CCSD energy (diverging amplitudes)");
+    ctx.logf(1, "   CCSD(%d): E(corr) = %.12g      dE = %.12g      rms(dt) = %.12g%s", it, E, dE,
+             rms, mixed_phase ? "   [mixed]" : "");
+    if (opts.history && it < opts.max_iterations) {
+      opts.history[3 * it + 0] = E;
+      opts.history[3 * it + 1] = dE;
+      opts.history[3 * it + 2] = rms;
+    }
+    if (opts.checkpoint_capacity > 0 && opts.checkpoint_t1 && opts.checkpoint_t2) {
+      const int sl = it % opts.checkpoint_capacity;
+      download(ctx, opts.checkpoint_t1 + (size_t)sl * n1, t1, n1);
+      download(ctx, opts.checkpoint_t2 + (size_t)sl * n2, t2, n2);
+    }
+    if (!mixed_phase) fp64_iters++;
+    if (mixed_phase) {
+      res->mixed_iterations = it + 1;
+      if (dE < opts.mixed_energy_switch && rms < opts.mixed_amplitude_switch) {
+        // switch to FP64 refinement with a fresh DIIS subspace
+        mixed_phase = false;
+        phase_start = it + 1;
+        order.clear();
+        gram.clear();
+        ctx.logf(1, "Mixed-precision phase done; FP64 refinement");
+      }
+    } else if (dE < opts.energy_convergence && rms < opts.amplitude_convergence &&   // :370
+               (!mixed || fp64_iters >= std::max(1, opts.refine_sweeps))) {
+      converged = true;
+      it++;
+      break;
+    }
+  }
+  res->iterations = it;
+  res->last_dE = dE;
+  res->last_rms = rms;
+  if (mixed && ctx.tc) ctx.tc->check_error();
+  if (!converged) {                                                                   // :376-380
+    ctx.logf(0, "!!! CCSD procedure failed to converge !!!");
+    res->converged = 0;
+    return;
+  }
+  res->converged = 1;
+  res->E_CCSD = E_last;                                                               // :382
+  if (Lf12.p()) {                                                                     // :383
+    dot(n2, Lf12.p(), t2, ctx.partials, ctx.dscalars, s);
+    SCESS_CUDA(cudaMemcpyAsync(ctx.hscalars, ctx.dscalars, sizeof(double), cudaMemcpyDeviceToHost, s));
+    ctx.sync();
+    res->E_F12_Coupling = ctx.hscalars[0];
+  }
+  download(ctx, t1_out, t1, n1);
+  download(ctx, t2_out, t2, n2);
+  ctx.logf(0, "---- CCSD procedure converged! ----");
+  ctx.logf(0, "E(CCSD correlation) = %.12g hartrees", res->E_CCSD);
+}
+
+}  // namespace scess

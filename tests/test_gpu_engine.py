@@ -1,0 +1,65 @@
+"""Contraction engine on the GPU: FP64 (DFMA) and tensor-core (tcgen05, split BF16) backends
+against NumPy float64 einsum, including permuted operands, split-K and GEMV shapes."""
+import numpy as np
+import pytest
+
+from tests.gpu_common import gctx, rel_err  # noqa: F401
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    ('mk,nk->mn', (128, 64), (256, 64)),
+    ('mk,nk->mn', (300, 1000), (200, 1000)),
+    ('mk,nk->mn', (1000, 50), (20, 50)),
+    ('mk,nk->mn', (64, 7000), (500, 7000)),
+    ('kcld,ilcd->ki', (5, 19, 5, 19), (5, 5, 19, 19)),
+    ('kcld,klad->ac', (6, 33, 6, 33), (6, 6, 33, 33)),
+    ('akic,kjcb->ijab', (21, 7, 7, 21), (7, 7, 21, 21)),
+    ('abcd,ijcd->ijab', (30, 30, 30, 30), (9, 9, 30, 30)),
+    ('kdac,ikcd->ia', (8, 40, 40, 40), (8, 8, 40, 40)),
+    ('ka,kbij->ijab', (10, 90), (10, 90, 10, 10)),
+    ('kcld,ld->kc', (10, 90, 10, 90), (10, 90)),
+    ('kc,kica->ia', (10, 90), (10, 10, 90, 90)),
+    ('ia,jb->ijab', (7, 11), (7, 11)),
+]
+
+
+def _operands(spec, sa, sb, seed=0):
+    rng = np.random.default_rng(seed)
+    A = rng.standard_normal(sa)
+    B = rng.standard_normal(sb)
+    ref = np.einsum(spec, A, B)
+    return A, B, ref
+
+
+@pytest.mark.parametrize('spec,sa,sb', CASES)
+def test_einsum_fp64(gctx, spec, sa, sb):
+    A, B, ref = _operands(spec, sa, sb)
+    C0 = np.random.default_rng(1).standard_normal(ref.shape)
+    out = gctx.einsum(spec, A, B, C_init=C0, alpha=-0.5, beta=2.0, precision='fp64')
+    assert rel_err(out, -0.5 * ref + 2.0 * C0) < 1e-13
+
+
+@pytest.mark.parametrize('spec,sa,sb', CASES)
+def test_einsum_tensor_cores(gctx, spec, sa, sb):
+    # split BF16 hi+lo operands, FP32 accumulation: relative error below 1e-5 of max|C|
+    A, B, ref = _operands(spec, sa, sb)
+    C0 = np.random.default_rng(2).standard_normal(ref.shape)
+    out = gctx.einsum(spec, A, B, C_init=C0, alpha=1.5, beta=1.0, precision='mixed')
+    assert rel_err(out, 1.5 * ref + C0) < 1e-5
+
+
+def test_tensor_core_gemm_exact_on_bf16_values(gctx):
+    # integers representable in BF16 with small sums: the tensor-core result is exact
+    rng = np.random.default_rng(3)
+    A = rng.integers(-8, 9, (384, 256)).astype(np.float64)
+    B = rng.integers(-8, 9, (272, 256)).astype(np.float64)
+    out = gctx.einsum('mk,nk->mn', A, B, out_shape=(384, 272), precision='mixed')
+    assert np.array_equal(out, A @ B.T)
+
+
+def test_fp64_einsum_deterministic(gctx):
+    A, B, _ = _operands('kdac,ikcd->ia', (8, 40, 40, 40), (8, 8, 40, 40))
+    o1 = gctx.einsum('kdac,ikcd->ia', A, B, out_shape=(8, 40))
+    o2 = gctx.einsum('kdac,ikcd->ia', A, B, out_shape=(8, 40))
+    assert np.array_equal(o1, o2)

@@ -1,0 +1,41 @@
+"""(T) on the GPU against the FP64 oracle and the reference's pins."""
+import numpy as np
+import pytest
+
+import oracle
+from scess_gb300.synthetic import make_workload
+from tests.golden import PINS, load
+from tests.gpu_common import gctx  # noqa: F401
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize('tag', ['h2o_sto3g', 'h2o_ccpvdz'])
+def test_triples_reference_pins(gctx, tag):
+    d = load(tag)
+    ref = oracle.solve_rccsd_diis(d['eri'], d['eps'], d['nocc'])
+    et_ref = oracle.rccsd_triples_correction(d['eri'], d['eps'], d['nocc'], ref.t1, ref.t2)
+    et = gctx.triples(d['eri'], d['eps'], d['nocc'], ref.t1, ref.t2)
+    assert abs(et - et_ref) <= 1e-11
+    val, tol = PINS[tag]['E_T']
+    assert abs(et - val) <= tol
+    em = gctx.triples(d['eri'], d['eps'], d['nocc'], ref.t1, ref.t2, precision='mixed')
+    assert abs(em - et_ref) <= 1e-7
+
+
+@pytest.mark.parametrize('o,v', [(3, 7), (5, 19), (4, 41), (10, 90)])
+def test_triples_fixed_amplitudes(gctx, o, v):
+    w = make_workload(o, v, seed=0, with_amplitudes=True)
+    eri = w.eri()
+    ref = oracle.rccsd_triples_correction(eri, w.eps, o, w.t1, w.t2)
+    et = gctx.triples(eri, w.eps, o, w.t1, w.t2)
+    assert abs(et - ref) <= 1e-9 * max(1.0, abs(ref))
+    em = gctx.triples(eri, w.eps, o, w.t1, w.t2, precision='mixed')
+    assert abs(em - ref) <= 1e-6
+
+
+def test_triples_df_equals_eri(gctx):
+    w = make_workload(5, 19, seed=1, with_amplitudes=True)
+    a = gctx.triples(w.eri(), w.eps, 5, w.t1, w.t2)
+    b = gctx.triples(None, w.eps, 5, w.t1, w.t2, B=w.B)
+    assert abs(a - b) < 1e-12
