@@ -1,0 +1,382 @@
+"""Benchmark: one closed-shell CCSD iteration + (T), mixed precision vs FP64, on one GB300.
+
+Metric (lower is better): seconds for one CCSD iteration (residual, Jacobi
+update, DIIS, energy) plus the full (T) correction, mixed-precision form, at
+o=20, v=180 on seeded synthetic DF integrals (the convergent variant of the
+generator; see scess_gb300/synthetic.py), inputs resident in HBM.  Beside it:
+
+* the FP64 GPU path on the same workload (the drop-in form) and the ratio;
+* the energy differences mixed - FP64 on identical inputs;
+* ``e2e``: the same step through the public C ABI from pinned host buffers
+  (state create = nmo^4 eri upload + block build + MP2 guess, one iteration,
+  (T), amplitudes back), timed on the host around synchronous calls;
+* ``roofline`` of the dominant kernel (tcgen05 GEMM) from the library's
+  per-launch CUDA-event timers over the timed steps;
+* ``cpu_baseline``: the FP64 NumPy oracle on this host (one full CCSD
+  iteration + (T) extrapolated from the costliest leading-virtual slices).
+
+``--impl reference`` times only the CPU oracle on the same workload and prints
+the same JSON line with ``"impl": "reference"``.  Run ``python bench.py`` for
+the defaults (N=1).  Under torchrun every rank runs an independent replica
+(the path does not shard in this build: replicas only) and rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'CCSD iter + (T) seconds, mixed vs FP64 GPU at <=1uEh; % tensor-pipe peak'
+UNIT = 's'
+
+
+def peaks():
+    p = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get('hbm_gbs', 6800.0), d.get('bf16_tflops', 1900.0), 'measured'
+    return 6800.0, 1900.0, 'fallback'
+
+
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+    Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+         'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+         'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, dev):
+        self.dev = dev
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.dev), f'--query-gpu={self.Q}',
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(',')]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, val in zip(names, f[5:9]):
+                if val.lower() == 'active':
+                    reasons.add(n)
+        return {'sm_mhz': float(np.median(sm)) if sm else None, 'sm_max_mhz': mx,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+def build_eri_pinned(w, torch):
+    """eri(p,q,r,s) = (pr|qs), column-major, in pinned host memory (built on the GPU)."""
+    N = w.nmo
+    B = torch.from_numpy(w.B).cuda()
+    # T[s,r,q,p] (row-major) == eri(p,q,r,s) at p + N q + N^2 r + N^3 s
+    T = torch.einsum('Qpr,Qqs->srqp', B, B).contiguous()
+    host = torch.empty(N ** 4, dtype=torch.float64, pin_memory=True)
+    host.copy_(T.reshape(-1))
+    del T, B
+    torch.cuda.empty_cache()
+    return host, host.numpy().reshape((N, N, N, N), order='F')
+
+
+def fp64_peak_tflops(torch):
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device='cuda')
+    b = torch.randn(n, n, dtype=torch.float64, device='cuda')
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    del a, b
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def cpu_oracle_step(eri, eps, o, t1=None, t2=None, tslices=1, ints=None):
+    """One FP64 oracle CCSD iteration + (T) extrapolated from the costliest slices.
+
+    Returns (seconds, details).  The (T) cost of leading virtual a scales as
+    (a+1)^2, so the slices a = v-1, v-2, ... are timed and scaled by
+    sum_a (a+1)^2 / sum_sampled (a+1)^2.
+    """
+    import oracle
+    from oracle.rccsd_t import _repack
+    v = eri.shape[0] - o
+    if ints is None:
+        ints = oracle.make_integral_blocks(eri, o)
+    eia, eijab = oracle.rccsd.denominators(eps, o)
+    if t1 is None:
+        t1 = np.zeros((o, v))
+        t2 = ints.oovv_phys / eijab
+    t0 = time.perf_counter()
+    n1, n2 = oracle.update_amplitudes(ints, eia, eijab, None, t1, t2)
+    E = oracle.correlation_energy(ints, n1, n2)
+    t_ccsd = time.perf_counter() - t0
+    P, R, S, Q = _repack(eri, o, n2)
+    t0 = time.perf_counter()
+    sampled = 0.0
+    for a in range(v - 1, v - 1 - tslices, -1):
+        _triples_slice(P, R, S, Q, n1, n2, eps, o, a)
+        sampled += (a + 1) ** 2
+    t_slice = time.perf_counter() - t0
+    total = sum((a + 1) ** 2 for a in range(v))
+    t_T = t_slice * total / sampled
+    return t_ccsd + t_T, {'ccsd_iter_s': t_ccsd, 'triples_s_extrapolated': t_T,
+                          'triples_slices': tslices, 'E_iter': E}
+
+
+def _triples_slice(P, R, S, Q, t1, t2, eps, o, a):
+    """The work of one leading virtual a in the vectorised oracle (T) (energy discarded)."""
+    n = a + 1
+    A1 = np.einsum('ifb,fjkc->bcijk', P[:, :, a, :n], Q[:, :, :, :n], optimize=True)
+    A1 -= np.einsum('ijm,mkbc->bcijk', R[:, :, :, a], t2[:, :, :n, :n], optimize=True)
+    A2 = np.einsum('ifb,fjkc->bcijk', P[:, :, :n, a], Q[:, :, :, :n], optimize=True)
+    A2 -= np.einsum('ijmb,mkc->bcijk', R[:, :, :, :n], t2[:, :, a, :n], optimize=True)
+    A3 = np.einsum('ifbc,fjk->bcijk', P[:, :, :n, :n], Q[:, :, :, a], optimize=True)
+    A3 -= np.einsum('ijmb,mkc->bcijk', R[:, :, :, :n], t2[:, :, :n, a], optimize=True)
+    W = (A1 + A1.transpose(1, 0, 2, 4, 3) + A2.transpose(0, 1, 3, 2, 4)
+         + A3.transpose(0, 1, 4, 2, 3) + A2.transpose(1, 0, 3, 4, 2)
+         + A3.transpose(1, 0, 4, 3, 2))
+    from oracle.rccsd_t import _r3
+    return float(np.sum(W * _r3(W)))
+
+
+def rank_info():
+    return (int(os.environ.get('RANK', 0)), int(os.environ.get('WORLD_SIZE', 1)),
+            int(os.environ.get('LOCAL_RANK', 0)))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=3)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--o', type=int, default=20)
+    ap.add_argument('--v', type=int, default=180)
+    ap.add_argument('--seed', type=int, default=0)
+    ap.add_argument('--fp64-steps', type=int, default=1)
+    ap.add_argument('--e2e-steps', type=int, default=2)
+    ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--no-fp64', action='store_true')
+    args = ap.parse_args()
+    rank, world, local = rank_info()
+    o, v = args.o, args.v
+
+    from scess_gb300.synthetic import convergent_sigma, make_workload
+    import oracle
+    sigma = convergent_sigma(o, v)
+    wl = make_workload(o, v, seed=args.seed, sigma=sigma)
+    config = {'workload': f'closed-shell CCSD iteration + (T), o={o} v={v} (nmo={o + v}, '
+                          f'naux={wl.naux}), seeded synthetic DF integrals (sigma_B={sigma:.5f})',
+              'o': o, 'v': v, 'naux': wl.naux, 'seed': args.seed,
+              'ccsd_flops_per_iter': oracle.ccsd_flops(o, v),
+              'triples_flops': oracle.triples_flops(o, v),
+              'l2': 'inputs larger than L2 (nmo^4 eri 12.8 GB, packed vvvv 4.2 GB)',
+              'parallelism': 'replicas' if world > 1 else 'single GPU'}
+
+    if args.impl == 'reference':
+        if rank != 0:
+            return
+        import torch  # noqa: F401  (only for symmetry of the environment)
+        N = o + v
+        # eri on the host without a GPU: (pr|qs) from the DF factors
+        Bm = wl.B.reshape(wl.naux, N * N)
+        chem = (Bm.T @ Bm).reshape(N, N, N, N)
+        eri = np.ascontiguousarray(chem.transpose(0, 2, 1, 3))
+        del chem
+        ints = oracle.make_integral_blocks(eri, o)
+        for _ in range(min(args.warmup, 1)):
+            cpu_oracle_step(eri, wl.eps, o, ints=ints)
+        times = []
+        det = None
+        for _ in range(args.steps):
+            t, det = cpu_oracle_step(eri, wl.eps, o, ints=ints)
+            times.append(t)
+        val = float(np.mean(times))
+        print(json.dumps({
+            'impl': 'reference', 'metric': METRIC, 'value': val, 'unit': UNIT, 'n_gpus': args.gpus,
+            'steps': args.steps, 'warmup': min(args.warmup, 1), 'ms_per_step': val * 1e3,
+            'higher_is_better': False, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+            'data': 'synthetic', 'config': config,
+            'cpu_baseline': {'value': val, 'unit': UNIT, 'cores': os.cpu_count(), 'kind': 'port',
+                             'sample': 'one full FP64 NumPy-oracle CCSD iteration (MP2 guess) + '
+                                       '(T) extrapolated from the costliest leading-virtual '
+                                       'slice by sum_a (a+1)^2', 'details': det},
+            'e2e': {'value': val, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+        }))
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl')
+    from scess_gb300 import build as sbuild
+    sbuild.build()
+    import scess_gb300 as s
+    lib = s.load_library()
+    hbm, bf16_peak, peak_kind = peaks()
+
+    host_t, eri_h = build_eri_pinned(wl, torch)
+    N = wl.nmo
+    ctx = s.Context(local)
+
+    # ---- mixed form, inputs resident ----------------------------------------------------
+    st = ctx.state(eri_h, wl.eps, o, precision='mixed', max_iterations=1000)
+    for _ in range(args.warmup):
+        st.iterate(1)
+        st.triples('mixed')
+    torch.cuda.synchronize()
+    clk = Clocks(local)
+    clk.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ctx.profile(True)
+    n0 = lib.scess_launch_count()
+    it_ms, t_ms, ets = [], [], []
+    wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        r, ms1 = st.iterate(1)
+        et, ms2 = st.triples('mixed')
+        it_ms.append(ms1)
+        t_ms.append(ms2)
+        ets.append(et)
+    torch.cuda.synchronize()
+    wall = (time.perf_counter() - wall0) / args.steps
+    launches = int(lib.scess_launch_count() - n0)
+    prof = ctx.profile_report()
+    ctx.profile(False)
+    clocks = clk.stop()
+    step_s = (float(np.mean(it_ms)) + float(np.mean(t_ms))) / 1e3
+    if world > 1:
+        tt = torch.tensor([step_s], device='cuda')
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        step_s = float(tt.item())
+    hist_mixed = st.hist.reshape(-1, 3)
+    n_iter_mixed = args.warmup + args.steps
+    t1m, t2m = st.amplitudes()
+
+    # ---- roofline of the dominant kernel ----------------------------------------------------
+    tc = prof.get('tc_gemm', {'launches': 0, 'ms': 0.0, 'flops': 0.0})
+    top = max(prof.items(), key=lambda kv: kv[1]['ms'])[0] if prof else None
+    achieved = tc['flops'] / (tc['ms'] / 1e3) / 1e12 if tc['ms'] > 0 else 0.0
+    peak_alg = bf16_peak / 3.0
+    roofline = {'kernel': 'tc_gemm_kernel (tcgen05 split hi/lo, FP32 accumulate)', 'bound': 'tensor',
+                'achieved': achieved, 'peak': peak_alg, 'unit': 'TFLOP/s', 'frac': achieved / peak_alg,
+                'peak_basis': f'bf16 dense {bf16_peak} TFLOP/s ({peak_kind}) / 3 products per '
+                              'algorithmic FLOP; achieved = algorithmic 2MNK per launch / '
+                              'CUDA-event launch time',
+                'tensor_pipe_frac': 3.0 * achieved / bf16_peak,
+                'launches': tc['launches'], 'avg_launch_ms': tc['ms'] / max(tc['launches'], 1),
+                'traffic': None, 'top_kernel_by_time': top}
+    share = {k: round(v['ms'] / max(sum(x['ms'] for x in prof.values()), 1e-9), 4) for k, v in prof.items()}
+
+    # ---- FP64 form on the same workload -------------------------------------------------------
+    fp64 = None
+    if not args.no_fp64:
+        sf = ctx.state(eri_h, wl.eps, o, precision='fp64', max_iterations=1000)
+        for _ in range(args.fp64_steps):
+            sf.iterate(1)
+        rf, fms1 = sf.iterate(1)
+        etf, fms2 = sf.triples('fp64')
+        etm_same, _ = sf.triples('mixed')
+        hist_f = sf.hist.reshape(-1, 3)
+        nf = args.fp64_steps + 1
+        dE_iter = float(np.max(np.abs(hist_mixed[:nf, 0] - hist_f[:nf, 0])))
+        fp64 = {'ccsd_iter_s': fms1 / 1e3, 'triples_s': fms2 / 1e3,
+                'step_s': (fms1 + fms2) / 1e3,
+                'speedup_mixed_vs_fp64': (fms1 + fms2) / 1e3 / step_s,
+                'dE_ccsd_iter_mixed_vs_fp64_max': dE_iter,
+                'dE_T_mixed_vs_fp64_same_amplitudes': abs(etm_same - etf),
+                'E_T_fp64': etf, 'fp64_peak_tflops_cublas_dgemm': fp64_peak_tflops(torch),
+                'fp64_ccsd_tflops': oracle.ccsd_flops(o, v) / (fms1 / 1e3) / 1e12,
+                'fp64_triples_tflops': oracle.triples_flops(o, v) / (fms2 / 1e3) / 1e12}
+        sf.close()
+        del sf
+    st.close()
+    del st
+
+    # ---- e2e through the public API from pinned host buffers ----------------------------------
+    e2e_times = []
+    for _ in range(args.e2e_steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        se = ctx.state(eri_h, wl.eps, o, precision='mixed', max_iterations=1000)
+        se.iterate(1)
+        se.triples('mixed')
+        se.amplitudes()
+        se.close()
+        torch.cuda.synchronize()
+        e2e_times.append(time.perf_counter() - t0)
+    e2e = {'value': float(np.min(e2e_times)) if e2e_times else None, 'unit': UNIT,
+           'h2d_bytes_per_step': int(8 * (N ** 4 + N)),
+           'd2h_bytes_per_step': int(8 * (o * v + o * o * v * v) + 64),
+           'path': 'scess_rccsd_state_create (eri from pinned host) + state_iterate(1) + '
+                   'state_triples(MIXED) + state_amplitudes + destroy'}
+
+    # ---- CPU baseline (rank 0 only) -------------------------------------------------------------
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        t, det = cpu_oracle_step(np.asarray(eri_h), wl.eps, o)
+        cpu = {'value': t, 'unit': UNIT, 'cores': os.cpu_count(), 'kind': 'port',
+               'sample': 'one full FP64 NumPy-oracle CCSD iteration (MP2 guess) + (T) '
+                         'extrapolated from the costliest leading-virtual slice by sum_a (a+1)^2',
+               'details': det}
+
+    if rank == 0:
+        line = {'metric': METRIC, 'value': step_s, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
+                'warmup': args.warmup, 'ms_per_step': step_s * 1e3, 'higher_is_better': False,
+                'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f16x2-split (FP32 acc) + f64',
+                'data': 'synthetic', 'config': config,
+                'breakdown_ms': {'ccsd_iter': float(np.mean(it_ms)), 'triples': float(np.mean(t_ms)),
+                                 'wall_per_step': wall * 1e3},
+                'E_T_mixed': ets[-1], 'E_ccsd_iter_mixed': float(hist_mixed[n_iter_mixed - 1, 0]),
+                'fp64': fp64, 'roofline': roofline, 'kernel_share': share, 'kernel_timers': prof,
+                'cpu_baseline': cpu, 'e2e': e2e, 'gpu_launches': launches // max(args.steps, 1),
+                'gpu_launches_total': launches, 'clocks': clocks}
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

@@ -104,6 +104,8 @@ typedef struct {
 } scess_rccsd_result;
 
 const char *scess_status_string(int status);
+/* Number of CUDA kernels this library has launched in the process so far. */
+int64_t scess_launch_count(void);
 
 /* Context on CUDA device `device` (must be sm_103a). */
 int scess_ctx_create(int device, scess_ctx **out);
@@ -145,6 +147,41 @@ int scess_rccsd_triples(scess_ctx *ctx, const double *eri, const double *eps, in
 int scess_rccsd_triples_df(scess_ctx *ctx, const double *B, int64_t naux, const double *eps,
                            int64_t nmo, int64_t nocc, const double *t1, const double *t2,
                            int32_t precision, double *e_t);
+
+/* ---- Device-resident session (no counterpart call in the reference: SCESS
+ * keeps these objects inside SolveRCCSD_DIIS, RCCSD.cpp:318-344).  The
+ * integrals, orbital energies, amplitudes (MP2 guess, RCCSD.cpp:333-339) and
+ * the DIIS subspace stay in GPU memory between calls, so a caller can step the
+ * iteration, run (T) on the current amplitudes and read them back without
+ * re-sending the nmo^4 integrals. */
+typedef struct scess_rccsd_state scess_rccsd_state;
+
+int scess_rccsd_state_create(scess_ctx *ctx, const double *eri, const double *eps, int64_t nmo,
+                             int64_t nocc, const double *f12_residual, const double *f12_energy,
+                             const scess_rccsd_options *opts, scess_rccsd_state **out);
+int scess_rccsd_state_create_df(scess_ctx *ctx, const double *B, int64_t naux, const double *eps,
+                                int64_t nmo, int64_t nocc, const double *f12_residual,
+                                const double *f12_energy, const scess_rccsd_options *opts,
+                                scess_rccsd_state **out);
+void scess_rccsd_state_destroy(scess_rccsd_state *state);
+/* Runs up to n_iterations of the SolveRCCSD_DIIS loop (RCCSD.cpp:345-374),
+ * fewer once converged; *device_ms (optional) is the GPU time of the call
+ * measured with CUDA events on the context's stream. */
+int scess_rccsd_state_iterate(scess_rccsd_state *state, int32_t n_iterations,
+                              scess_rccsd_result *result, double *device_ms);
+/* E_(T) (RCCSD_T.cpp:17-168) from the state's current amplitudes. */
+int scess_rccsd_state_triples(scess_rccsd_state *state, int32_t precision, double *e_t,
+                              double *device_ms);
+int scess_rccsd_state_amplitudes(scess_rccsd_state *state, double *t1_out, double *t2_out);
+int scess_rccsd_state_set_amplitudes(scess_rccsd_state *state, const double *t1,
+                                     const double *t2);
+
+/* Kernel timing on the context's stream (CUDA events around each launch of
+ * the engine's GEMM, pack and (T) kernels).  enable != 0 clears and starts,
+ * 0 stops.  The report is a JSON object {kernel: {"launches", "ms", "flops",
+ * "bytes"}} written into buf (truncated to buflen). */
+int scess_ctx_profile(scess_ctx *ctx, int32_t enable);
+int scess_ctx_profile_report(scess_ctx *ctx, char *buf, int64_t buflen);
 
 /* One UpdateAmplitudes residual (RCCSD.cpp:101-233) without the final division
  * by the denominators (:235-236): r1_out = t1new (o*v), r2_out = t2new

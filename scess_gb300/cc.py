@@ -73,6 +73,7 @@ _i64p = C.POINTER(C.c_int64)
 
 EXPORTS = {
     'scess_status_string': (C.c_char_p, [C.c_int]),
+    'scess_launch_count': (C.c_int64, []),
     'scess_ctx_create': (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
     'scess_ctx_destroy': (None, [C.c_void_p]),
     'scess_ctx_last_error': (C.c_char_p, [C.c_void_p]),
@@ -87,6 +88,19 @@ EXPORTS = {
                                       C.c_int32, _dp]),
     'scess_rccsd_triples_df': (C.c_int, [C.c_void_p, _dp, C.c_int64, _dp, C.c_int64, C.c_int64,
                                          _dp, _dp, C.c_int32, _dp]),
+    'scess_rccsd_state_create': (C.c_int, [C.c_void_p, _dp, _dp, C.c_int64, C.c_int64, _dp, _dp,
+                                           C.POINTER(Options), C.POINTER(C.c_void_p)]),
+    'scess_rccsd_state_create_df': (C.c_int, [C.c_void_p, _dp, C.c_int64, _dp, C.c_int64,
+                                              C.c_int64, _dp, _dp, C.POINTER(Options),
+                                              C.POINTER(C.c_void_p)]),
+    'scess_rccsd_state_destroy': (None, [C.c_void_p]),
+    'scess_rccsd_state_iterate': (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(Result),
+                                            C.POINTER(C.c_double)]),
+    'scess_rccsd_state_triples': (C.c_int, [C.c_void_p, C.c_int32, _dp, C.POINTER(C.c_double)]),
+    'scess_rccsd_state_amplitudes': (C.c_int, [C.c_void_p, _dp, _dp]),
+    'scess_rccsd_state_set_amplitudes': (C.c_int, [C.c_void_p, _dp, _dp]),
+    'scess_ctx_profile': (C.c_int, [C.c_void_p, C.c_int32]),
+    'scess_ctx_profile_report': (C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),
     'scess_rccsd_residual': (C.c_int, [C.c_void_p, _dp, C.c_int64, C.c_int64, _dp, _dp, _dp,
                                        C.c_int32, _dp, _dp]),
     'scess_einsum': (C.c_int, [C.c_void_p, C.c_char_p, C.c_double, _dp, C.c_int32, _i64p, _dp,
@@ -286,6 +300,22 @@ class Context:
         self._check(st, 'scess_rccsd_triples')
         return et.value
 
+    # -- device-resident session -------------------------------------------------------------
+    def state(self, eri=None, eps=None, nocc=None, B=None, precision: str = 'fp64',
+              f12: RCCSD_F12Coupling | None = None, **opts) -> 'State':
+        return State(self, eri, eps, nocc, B=B, precision=precision, f12=f12, **opts)
+
+    # -- kernel timing ------------------------------------------------------------------------
+    def profile(self, enable: bool = True):
+        self._check(self.lib.scess_ctx_profile(self.h, 1 if enable else 0), 'scess_ctx_profile')
+
+    def profile_report(self) -> dict:
+        import json
+        buf = C.create_string_buffer(1 << 16)
+        self._check(self.lib.scess_ctx_profile_report(self.h, buf, len(buf)),
+                    'scess_ctx_profile_report')
+        return json.loads(buf.value.decode())
+
     # -- one residual -------------------------------------------------------------------------
     def residual(self, eri, nocc, t1, t2, t2_driver=None, precision: str = 'fp64'):
         """(t1new, t2new) numerators of UpdateAmplitudes (before the division)."""
@@ -315,6 +345,80 @@ class Context:
                                    PRECISION[precision])
         self._check(st, 'scess_einsum')
         return Cf
+
+
+class State:
+    """scess_rccsd_state: integrals, amplitudes and DIIS resident in GPU memory."""
+
+    def __init__(self, ctx: Context, eri, eps, nocc, B=None, precision='fp64', f12=None, **opts):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        self.eps = _f64(eps)
+        N = self.eps.shape[0]
+        self.o, self.v = int(nocc), N - int(nocc)
+        o, v = self.o, self.v
+        self.op = ctx.default_options()
+        self.op.precision = PRECISION[precision]
+        for k, val in opts.items():
+            setattr(self.op, k, val)
+        self.hist = np.zeros(3 * max(self.op.max_iterations, 1))
+        self.op.history = _ptr(self.hist)
+        fr = fe = None
+        if f12 is not None:
+            fr = _f64(f12.residual, (o, o, v, v))
+            fe = _f64(f12.energy, (o, o, v, v))
+        h = C.c_void_p()
+        if B is not None:
+            Bf = B if (isinstance(B, np.ndarray) and B.flags.f_contiguous) else _f64(B)
+            st = self.lib.scess_rccsd_state_create_df(ctx.h, _ptr(Bf), Bf.shape[0], _ptr(self.eps),
+                                                      N, o, _ptr(fr), _ptr(fe), C.byref(self.op),
+                                                      C.byref(h))
+        else:
+            ef = eri if (isinstance(eri, np.ndarray) and eri.flags.f_contiguous
+                         and eri.dtype == np.float64) else _f64(eri, (N, N, N, N))
+            st = self.lib.scess_rccsd_state_create(ctx.h, _ptr(ef), _ptr(self.eps), N, o, _ptr(fr),
+                                                   _ptr(fe), C.byref(self.op), C.byref(h))
+        ctx._check(st, 'scess_rccsd_state_create')
+        self.h = h
+
+    def iterate(self, n: int = 1):
+        res = Result()
+        ms = C.c_double(0.0)
+        self.ctx._check(self.lib.scess_rccsd_state_iterate(self.h, n, C.byref(res), C.byref(ms)),
+                        'scess_rccsd_state_iterate')
+        return res, ms.value
+
+    def triples(self, precision='fp64'):
+        et = C.c_double(0.0)
+        ms = C.c_double(0.0)
+        self.ctx._check(self.lib.scess_rccsd_state_triples(self.h, PRECISION[precision],
+                                                           C.byref(et), C.byref(ms)),
+                        'scess_rccsd_state_triples')
+        return et.value, ms.value
+
+    def amplitudes(self):
+        t1 = np.zeros((self.o, self.v), order='F')
+        t2 = np.zeros((self.o, self.o, self.v, self.v), order='F')
+        self.ctx._check(self.lib.scess_rccsd_state_amplitudes(self.h, _ptr(t1), _ptr(t2)),
+                        'scess_rccsd_state_amplitudes')
+        return t1, t2
+
+    def set_amplitudes(self, t1, t2):
+        t1f = _f64(t1, (self.o, self.v))
+        t2f = _f64(t2, (self.o, self.o, self.v, self.v))
+        self.ctx._check(self.lib.scess_rccsd_state_set_amplitudes(self.h, _ptr(t1f), _ptr(t2f)),
+                        'scess_rccsd_state_set_amplitudes')
+
+    def close(self):
+        if getattr(self, 'h', None):
+            self.lib.scess_rccsd_state_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 _default_ctx = None

@@ -13,6 +13,11 @@ struct scess_ctx {
   std::string err;
 };
 
+struct scess_rccsd_state {
+  scess_ctx *ctx = nullptr;
+  scess::RccsdState *impl = nullptr;
+};
+
 namespace {
 
 using scess::Error;
@@ -35,9 +40,9 @@ int guard(scess_ctx *ctx, F &&f) {
     ctx->err = e.what();
     code = SCESS_ERR_CUDA;
   }
-  // Packed-operand caches are keyed by device pointers of this call: drop them.
+  // Packings cached during a plain call are keyed by device pointers of that call.
   cudaStreamSynchronize(ctx->impl->stream);
-  if (ctx->impl->tc) ctx->impl->tc->clear_cache();
+  if (ctx->impl->tc) ctx->impl->tc->clear_cache(nullptr);
   if (code != SCESS_OK) cudaGetLastError();
   return code;
 }
@@ -85,6 +90,27 @@ scess::DTensor device_eri(scess::Ctx &ctx, const double *eri, const double *B, i
   return d;
 }
 
+scess::RccsdState *make_state(scess::Ctx &c, const double *eri, const double *B, int64_t naux,
+                              const double *eps, int64_t nmo, int64_t nocc,
+                              const double *f12_residual, const double *f12_energy,
+                              const scess_rccsd_options &o) {
+  check_shape(nmo, nocc);
+  need(eps, "eps");
+  host_finite(eps, nmo, "eps");
+  if (o.max_iterations < 0 || o.max_diis_vectors < 1 || o.diis_start < 0 ||
+      (o.precision != SCESS_PRECISION_FP64 && o.precision != SCESS_PRECISION_MIXED))
+    throw Error(SCESS_ERR_INVALID, "bad options");
+  const int64_t v = nmo - nocc;
+  if (f12_residual) host_finite(f12_residual, nocc * nocc * v * v, "f12_residual");
+  if (f12_energy) host_finite(f12_energy, nocc * nocc * v * v, "f12_energy");
+  scess::DTensor d_eri = device_eri(c, eri, B, naux, nmo);
+  scess::SolveInput in;
+  in.eps_host = eps;
+  in.f12_residual = f12_residual;
+  in.f12_energy = f12_energy;
+  return new scess::RccsdState(c, std::move(d_eri), nmo, nocc, in, o);
+}
+
 int solve_common(scess_ctx *ctx, const double *eri, const double *B, int64_t naux,
                  const double *eps, int64_t nmo, int64_t nocc, const double *f12_residual,
                  const double *f12_energy, const scess_rccsd_options *opts, double *t1_out,
@@ -111,19 +137,22 @@ int solve_common(scess_ctx *ctx, const double *eri, const double *B, int64_t nau
     ctl.time_limit_s = o.time_limit_s;
     scess::DTensor d_eri = device_eri(c, eri, B, naux, nmo);
     ctl.poll();
-    scess::RccsdBlocks blocks;
-    blocks.build(c, d_eri.p(), nmo, nocc);
     scess::SolveInput in;
     in.eps_host = eps;
     in.f12_residual = f12_residual;
     in.f12_energy = f12_energy;
-    scess::rccsd_solve(c, blocks, in, o, ctl, t1_out, t2_out, result);
+    scess::RccsdState st(c, std::move(d_eri), nmo, nocc, in, o);
+    if (o.resume) st.set_amplitudes(t1_out, t2_out);
+    else st.mp2_guess();
+    scess::rccsd_solve(c, st, ctl, t1_out, t2_out, result);
   });
 }
 
 }  // namespace
 
 extern "C" {
+
+int64_t scess_launch_count(void) { return (int64_t)scess::g_launches.load(); }
 
 const char *scess_status_string(int status) {
   switch (status) {
@@ -252,6 +281,138 @@ int scess_rccsd_triples_df(scess_ctx *ctx, const double *B, int64_t naux, const 
                            int32_t precision, double *e_t) {
   if (!B || naux <= 0) return SCESS_ERR_INVALID;
   return triples_common(ctx, nullptr, B, naux, eps, nmo, nocc, t1, t2, precision, e_t);
+}
+
+static int state_create(scess_ctx *ctx, const double *eri, const double *B, int64_t naux,
+                        const double *eps, int64_t nmo, int64_t nocc, const double *f12_residual,
+                        const double *f12_energy, const scess_rccsd_options *opts,
+                        scess_rccsd_state **out) {
+  if (!out) return SCESS_ERR_INVALID;
+  *out = nullptr;
+  return guard(ctx, [&](scess::Ctx &c) {
+    scess_rccsd_options o;
+    if (opts) o = *opts;
+    else scess_rccsd_default_options(&o);
+    std::unique_ptr<scess::RccsdState> st(
+        make_state(c, eri, B, naux, eps, nmo, nocc, f12_residual, f12_energy, o));
+    st->mp2_guess();
+    c.sync();
+    auto *h = new scess_rccsd_state;
+    h->ctx = ctx;
+    h->impl = st.release();
+    *out = h;
+  });
+}
+
+int scess_rccsd_state_create(scess_ctx *ctx, const double *eri, const double *eps, int64_t nmo,
+                             int64_t nocc, const double *f12_residual, const double *f12_energy,
+                             const scess_rccsd_options *opts, scess_rccsd_state **out) {
+  if (!eri) return SCESS_ERR_INVALID;
+  return state_create(ctx, eri, nullptr, 0, eps, nmo, nocc, f12_residual, f12_energy, opts, out);
+}
+
+int scess_rccsd_state_create_df(scess_ctx *ctx, const double *B, int64_t naux, const double *eps,
+                                int64_t nmo, int64_t nocc, const double *f12_residual,
+                                const double *f12_energy, const scess_rccsd_options *opts,
+                                scess_rccsd_state **out) {
+  if (!B || naux <= 0) return SCESS_ERR_INVALID;
+  return state_create(ctx, nullptr, B, naux, eps, nmo, nocc, f12_residual, f12_energy, opts, out);
+}
+
+void scess_rccsd_state_destroy(scess_rccsd_state *state) {
+  if (!state) return;
+  if (state->impl) {
+    cudaSetDevice(state->ctx->impl->device);
+    cudaStreamSynchronize(state->ctx->impl->stream);
+    if (state->ctx->impl->tc) state->ctx->impl->tc->clear_cache(state->impl);
+    delete state->impl;
+  }
+  delete state;
+}
+
+int scess_rccsd_state_iterate(scess_rccsd_state *state, int32_t n_iterations,
+                              scess_rccsd_result *result, double *device_ms) {
+  if (!state || !state->impl || n_iterations < 0) return SCESS_ERR_INVALID;
+  return guard(state->ctx, [&](scess::Ctx &c) {
+    scess::Control ctl;
+    ctl.cancel = c.cancel;
+    ctl.user = c.user;
+    ctl.time_limit_s = state->impl->options().time_limit_s;
+    if (c.tc) c.tc->set_cache_owner(state->impl);
+    struct Reset {
+      scess::Ctx &c;
+      ~Reset() { if (c.tc) c.tc->set_cache_owner(nullptr); }
+    } reset{c};
+    c.tensor_cores().set_cache_owner(state->impl);
+    state->impl->iterate(n_iterations, ctl);
+    if (result) *result = state->impl->result();
+    if (device_ms) *device_ms = state->impl->last_device_ms();
+  });
+}
+
+int scess_rccsd_state_triples(scess_rccsd_state *state, int32_t precision, double *e_t,
+                              double *device_ms) {
+  if (!state || !state->impl || !e_t) return SCESS_ERR_INVALID;
+  if (precision != SCESS_PRECISION_FP64 && precision != SCESS_PRECISION_MIXED)
+    return SCESS_ERR_INVALID;
+  return guard(state->ctx, [&](scess::Ctx &c) {
+    scess::Control ctl;
+    ctl.cancel = c.cancel;
+    ctl.user = c.user;
+    cudaEvent_t a, b;
+    SCESS_CUDA(cudaEventCreate(&a));
+    SCESS_CUDA(cudaEventCreate(&b));
+    SCESS_CUDA(cudaEventRecord(a, c.stream));
+    auto *st = state->impl;
+    *e_t = scess::rccsd_triples(c, st->d_eri(), st->nmo(), st->nocc(), st->d_eps(), st->d_t1(),
+                                st->d_t2(), precision == SCESS_PRECISION_MIXED, ctl);
+    SCESS_CUDA(cudaEventRecord(b, c.stream));
+    SCESS_CUDA(cudaEventSynchronize(b));
+    float ms = 0.0f;
+    SCESS_CUDA(cudaEventElapsedTime(&ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (device_ms) *device_ms = ms;
+  });
+}
+
+int scess_rccsd_state_amplitudes(scess_rccsd_state *state, double *t1_out, double *t2_out) {
+  if (!state || !state->impl) return SCESS_ERR_INVALID;
+  return guard(state->ctx, [&](scess::Ctx &) { state->impl->get_amplitudes(t1_out, t2_out); });
+}
+
+int scess_rccsd_state_set_amplitudes(scess_rccsd_state *state, const double *t1,
+                                     const double *t2) {
+  if (!state || !state->impl || !t1 || !t2) return SCESS_ERR_INVALID;
+  return guard(state->ctx, [&](scess::Ctx &) { state->impl->set_amplitudes(t1, t2); });
+}
+
+int scess_ctx_profile(scess_ctx *ctx, int32_t enable) {
+  return guard(ctx, [&](scess::Ctx &c) {
+    c.timer.collect();
+    if (enable) c.timer.agg.clear();
+    c.timer.on = enable != 0;
+  });
+}
+
+int scess_ctx_profile_report(scess_ctx *ctx, char *buf, int64_t buflen) {
+  if (!buf || buflen <= 0) return SCESS_ERR_INVALID;
+  return guard(ctx, [&](scess::Ctx &c) {
+    c.timer.collect();
+    std::string js = "{";
+    bool first = true;
+    for (auto &kv : c.timer.agg) {
+      char tmp[512];
+      snprintf(tmp, sizeof(tmp), "%s\"%s\": {\"launches\": %lld, \"ms\": %.6f, \"flops\": %.6e, \"bytes\": %.6e}",
+               first ? "" : ", ", kv.first.c_str(), (long long)kv.second.launches, kv.second.ms,
+               kv.second.flops, kv.second.bytes);
+      js += tmp;
+      first = false;
+    }
+    js += "}";
+    std::strncpy(buf, js.c_str(), (size_t)buflen - 1);
+    buf[buflen - 1] = 0;
+  });
 }
 
 int scess_rccsd_residual(scess_ctx *ctx, const double *eri, int64_t nmo, int64_t nocc,

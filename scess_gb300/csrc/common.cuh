@@ -1,6 +1,7 @@
 // Shared definitions of the GB300 closed-shell CC engine (device + host).
 #pragma once
 #include <cuda_runtime.h>
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <stdexcept>
@@ -28,7 +29,14 @@ struct Error : std::runtime_error {
     }                                                                                 \
   } while (0)
 
-#define SCESS_CHECK_LAUNCH() SCESS_CUDA(cudaGetLastError())
+// Every kernel launch of the engine is followed by SCESS_CHECK_LAUNCH(), which
+// also counts it (scess_launch_count()).
+extern std::atomic<long long> g_launches;
+#define SCESS_CHECK_LAUNCH()                                   \
+  do {                                                         \
+    ::scess::g_launches.fetch_add(1, std::memory_order_relaxed); \
+    SCESS_CUDA(cudaGetLastError());                            \
+  } while (0)
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 inline int64_t round_up(int64_t a, int64_t b) { return ceil_div(a, b) * b; }

@@ -7,6 +7,8 @@
 
 namespace scess {
 
+std::atomic<long long> g_launches{0};
+
 void DevMem::alloc(size_t bytes) {
   release();
   if (bytes == 0) return;
@@ -123,6 +125,57 @@ void download(Ctx &ctx, double *dst, const double *src, int64_t n) {
   ctx.sync();
 }
 
+KernelTimer::~KernelTimer() {
+  for (auto &r : recs_) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  for (auto e : pool_) cudaEventDestroy(e);
+}
+
+cudaEvent_t KernelTimer::get() {
+  if (!pool_.empty()) {
+    cudaEvent_t e = pool_.back();
+    pool_.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  SCESS_CUDA(cudaEventCreate(&e));
+  return e;
+}
+
+void KernelTimer::begin(const char *name, double flops, double bytes, cudaStream_t s) {
+  Rec r{name, get(), get(), flops, bytes};
+  SCESS_CUDA(cudaEventRecord(r.a, s));
+  recs_.push_back(r);
+}
+
+void KernelTimer::end(cudaStream_t s) {
+  SCESS_CUDA(cudaEventRecord(recs_.back().b, s));
+  if (recs_.size() >= 4096) collect();
+}
+
+void KernelTimer::collect() {
+  for (auto &r : recs_) {
+    SCESS_CUDA(cudaEventSynchronize(r.b));
+    float ms = 0.0f;
+    SCESS_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
+    Agg &g = agg[r.name];
+    g.launches++;
+    g.ms += ms;
+    g.flops += r.flops;
+    g.bytes += r.bytes;
+    pool_.push_back(r.a);
+    pool_.push_back(r.b);
+  }
+  recs_.clear();
+}
+
+void KernelTimer::reset() {
+  collect();
+  agg.clear();
+}
+
 // ---------------------------------------------------------------------------------------------
 namespace {
 
@@ -228,6 +281,7 @@ const EinsumPlan &plan_einsum(Ctx &ctx, const char *spec, const TV &A, const TV 
 
   auto pl = std::make_unique<EinsumPlan>();
   pl->key = key;
+  pl->spec = spec;
   pl->rowA = offsets(M, 0);
   pl->rowC = offsets(M, 2);
   pl->colB = offsets(N, 1);
@@ -240,6 +294,8 @@ const EinsumPlan &plan_einsum(Ctx &ctx, const char *spec, const TV &A, const TV 
   pl->aUnitM = !M.empty() && M[0].sa == 1;
   pl->bUnitN = !N.empty() && N[0].sb == 1;
   pl->aUnitK = !K.empty() && K[0].sa == 1;
+  pl->cUnitM = !M.empty() && M[0].sc == 1;
+  pl->cUnitN = !N.empty() && N[0].sc == 1;
   pl->bUnitK = false;
   for (auto &l : K)
     if (l.sb == 1) pl->bUnitK = true;
@@ -289,6 +345,8 @@ void einsum(Ctx &ctx, const char *spec, double alpha, const TV &A, const TV &B, 
   g.beta = beta;
   g.aUnitM = pl.aUnitM;
   g.bUnitN = pl.bUnitN;
+  TimedScope ts(ctx.timer, (pl.N == 1 || pl.M == 1) ? "dgemv_table" : "dgemm_table",
+                2.0 * pl.M * pl.N * pl.K, 0.0, ctx.stream);
   if (pl.N == 1 && pl.K > 0) {
     dgemv_table(g, ctx.stream);
     return;

@@ -68,7 +68,9 @@ struct EinsumPlan {
   const int64_t *d_rowA = nullptr, *d_kA = nullptr, *d_colB = nullptr, *d_kB = nullptr;
   const int64_t *d_rowC = nullptr, *d_colC = nullptr;
   bool aUnitM = false, bUnitN = false, aUnitK = false, bUnitK = false;
+  bool cUnitM = false, cUnitN = false;  // C's unit-stride label leads the M / N group
   std::string key;
+  std::string spec;
 };
 class TcEngine;  // tensor-core (mixed precision) backend, gemm_tc.cu
 
@@ -79,6 +81,48 @@ struct Control {
   double time_limit_s = 0.0;
   std::chrono::steady_clock::time_point start = std::chrono::steady_clock::now();
   void poll() const;
+};
+
+// Optional per-kernel timing: CUDA events recorded on the launching stream
+// around each instrumented launch, aggregated per kernel name (launches,
+// device milliseconds, algorithmic FLOPs and bytes).
+class KernelTimer {
+ public:
+  struct Agg {
+    int64_t launches = 0;
+    double ms = 0.0, flops = 0.0, bytes = 0.0;
+  };
+  bool on = false;
+  ~KernelTimer();
+  void begin(const char *name, double flops, double bytes, cudaStream_t s);
+  void end(cudaStream_t s);
+  void collect();  // waits for the recorded events and folds them into agg
+  void reset();
+  std::map<std::string, Agg> agg;
+
+ private:
+  struct Rec {
+    std::string name;
+    cudaEvent_t a, b;
+    double flops, bytes;
+  };
+  cudaEvent_t get();
+  std::vector<Rec> recs_;
+  std::vector<cudaEvent_t> pool_;
+};
+
+// RAII helper: times the launches issued in its scope when the timer is on.
+struct TimedScope {
+  KernelTimer &t;
+  cudaStream_t s;
+  bool active;
+  TimedScope(KernelTimer &tm, const char *name, double flops, double bytes, cudaStream_t st)
+      : t(tm), s(st), active(tm.on) {
+    if (active) t.begin(name, flops, bytes, s);
+  }
+  ~TimedScope() {
+    if (active) t.end(s);
+  }
 };
 
 struct Ctx {
@@ -97,6 +141,7 @@ struct Ctx {
   double *dscalars = nullptr;  // 64 device doubles
   double *hscalars = nullptr;  // 64 pinned host doubles
   std::unique_ptr<TcEngine> tc;
+  KernelTimer timer;
 
   explicit Ctx(int dev);
   ~Ctx();

@@ -13,6 +13,9 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <cuda_fp16.h>
+
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 
@@ -115,9 +118,10 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
   return d;
 }
 
-// Instruction descriptor of tcgen05.mma kind::f16: D=F32, A=B=BF16, both K-major.
-__device__ __forceinline__ uint32_t idesc_bf16(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+// Instruction descriptor of tcgen05.mma kind::f16: D=F32, A=B=BF16 (fmt 1) or
+// F16 (fmt 0), both K-major; N>>3 at bits 17-22, M>>4 at bits 24-28.
+__device__ __forceinline__ uint32_t idesc_f16kind(int M, int N, uint32_t ab_fmt) {
+  return (1u << 4) | (ab_fmt << 7) | (ab_fmt << 10) | ((uint32_t)(N >> 3) << 17) |
          ((uint32_t)(M >> 4) << 24);
 }
 
@@ -154,150 +158,247 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
 struct TcArgs {
   int rowA0, rowB0, M, N;
   int nkb;           // K blocks (of 64) per segment
-  int nseg;          // 1 or 3
-  int kb_per_split;  // K blocks per split (blockIdx.z)
-  int bn;            // tile width, multiple of 16, <= 256
+  int nseg;          // 1 (hi only) or 3 (lo*hi, hi*lo, hi*hi)
+  int kb_per_split;  // K blocks per work unit along K
+  int tiles_m, tiles_n, splits;
   int Kpad;          // lo offset in the packed rows
+  int f16;           // operands are FP16 (else BF16)
   float *partial;    // split-K partials (nullptr: direct epilogue)
   int64_t part_stride;
   unsigned *err;
 };
+
+// Persistent tcgen05 GEMM, one 128 x 128 output tile per work unit.
+//   warp 0     TMA producer: per 64-wide K block one smem stage holding A_hi,
+//              A_lo, B_hi, B_lo (128 rows x 128 B each, 128B swizzle);
+//   warp 1     TMEM owner + MMA issuer: the block's products lo*hi, hi*lo,
+//              hi*hi (4 x K=16 each) go into one of two 128-column TMEM
+//              buffers, starting from zero, then tcgen05.commit;
+//   warps 2-5  drain each buffer into an FP32 register accumulator (one row
+//              per thread, round-to-nearest adds) and, after the last K block
+//              of the unit, scatter alpha*acc + beta*C through the tables.
+// Draining every K block bounds the truncating accumulation inside TMEM to
+// the 12 products of one block, so the result's error does not grow with K.
+constexpr int V2_BN = 128;
+constexpr int V2_STAGES = 3;
+constexpr uint32_t V2_TILE_BYTES = 128 * TC_BK * 2;  // 16 KiB: 128 rows x 128 B
+constexpr uint32_t V2_STAGE_BYTES = 4 * V2_TILE_BYTES;
+constexpr uint32_t V2_TMEM_COLS = 2 * V2_BN;
+constexpr size_t V2_SMEM_BYTES = 1024 + V2_STAGES * V2_STAGE_BYTES + (2 * V2_STAGES + 5) * 8 + 8 +
+                                 V2_BN * 8;
 
 __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    TcOut out, TcArgs a) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint8_t *As = smem;
-  uint8_t *Bs = smem + TC_STAGES * A_STAGE_BYTES;
-  uint64_t *full = (uint64_t *)(Bs + TC_STAGES * B_STAGE_BYTES);
-  uint64_t *empty = full + TC_STAGES;
-  uint64_t *accum = empty + TC_STAGES;
-  uint32_t *tmem_slot = (uint32_t *)(accum + 1);
+  uint64_t *full = (uint64_t *)(smem + V2_STAGES * V2_STAGE_BYTES);
+  uint64_t *empty = full + V2_STAGES;
+  uint64_t *tfull = empty + V2_STAGES;   // [2]
+  uint64_t *tempty = tfull + 2;          // [2]
+  uint64_t *done = tempty + 2;           // [1]
+  uint32_t *tmem_slot = (uint32_t *)(done + 1);
   int64_t *colOff = (int64_t *)(tmem_slot + 2);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * a.bn;
-  const int kb0 = blockIdx.z * a.kb_per_split;
-  const int kb1 = min(a.nkb, kb0 + a.kb_per_split);
-  const int nk = kb1 - kb0;
-  const int iters = a.nseg * nk;
+  const int units = a.tiles_m * a.tiles_n * a.splits;
+  const bool split3 = a.nseg == 3;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < TC_STAGES; s++) {
+    for (int s = 0; s < V2_STAGES; s++) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(accum, 1);
+    for (int b = 0; b < 2; b++) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], 4);  // one arrival per epilogue warp
+    }
+    mbar_init(done, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
-                 "r"(TMEM_COLS)
+                 "r"(V2_TMEM_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-  }
-  if (warp >= 2 && !a.partial) {
-    for (int c = threadIdx.x - 64; c < a.bn; c += 128) {
-      const int n = n0 + c;
-      colOff[c] = n < a.N ? out.baseC + out.colC[n] : -1;
-    }
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
+  auto unit_coords = [&](int u, int &tm, int &tn, int &kb0, int &kb1) {
+    const int tile = u % (a.tiles_m * a.tiles_n);
+    const int sp = u / (a.tiles_m * a.tiles_n);
+    tn = tile % a.tiles_n;
+    tm = tile / a.tiles_n;
+    kb0 = sp * a.kb_per_split;
+    kb1 = min(a.nkb, kb0 + a.kb_per_split);
+  };
+
   if (warp == 0) {
-    if (lane == 0 && iters > 0) {
+    if (lane == 0) {
       asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmA) : "memory");
       asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmB) : "memory");
-      int last[TC_STAGES];
-      for (int s = 0; s < TC_STAGES; s++) last[s] = -1;
-      const uint32_t bytes = A_STAGE_BYTES + (uint32_t)a.bn * TC_BK * 2;
-      for (int it = 0; it < iters; it++) {
-        const int s = it % TC_STAGES;
-        const uint32_t ph = (uint32_t)(it / TC_STAGES) & 1u;
-        if (!mbar_wait(&empty[s], ph ^ 1u, a.err, ERR_EMPTY_WAIT)) break;
-        const int seg = it / nk;
-        const int kb = kb0 + it % nk;
-        const int xa = (seg == 2 ? a.Kpad : 0) + kb * TC_BK;
-        const int xb = (seg == 1 ? a.Kpad : 0) + kb * TC_BK;
-        mbar_expect_tx(&full[s], bytes);
-        tma_load_2d(As + s * A_STAGE_BYTES, &tmA, xa, a.rowA0 + m0, &full[s]);
-        tma_load_2d(Bs + s * B_STAGE_BYTES, &tmB, xb, a.rowB0 + n0, &full[s]);
-        last[s] = it;
+      const uint32_t bytes = split3 ? V2_STAGE_BYTES : 2 * V2_TILE_BYTES;
+      int g = 0;
+      int last[V2_STAGES];
+      for (int s = 0; s < V2_STAGES; s++) last[s] = -1;
+      bool ok = true;
+      for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
+        int tm, tn, kb0, kb1;
+        unit_coords(u, tm, tn, kb0, kb1);
+        const int ya = a.rowA0 + tm * TC_BM, yb = a.rowB0 + tn * V2_BN;
+        for (int kb = kb0; kb < kb1; kb++, g++) {
+          const int s = g % V2_STAGES;
+          const uint32_t ph = (uint32_t)(g / V2_STAGES) & 1u;
+          if (!mbar_wait(&empty[s], ph ^ 1u, a.err, ERR_EMPTY_WAIT)) { ok = false; break; }
+          uint8_t *st = smem + s * V2_STAGE_BYTES;
+          mbar_expect_tx(&full[s], bytes);
+          const int x = kb * TC_BK;
+          tma_load_2d(st, &tmA, x, ya, &full[s]);                          // A hi
+          tma_load_2d(st + V2_TILE_BYTES, &tmB, x, yb, &full[s]);          // B hi
+          if (split3) {
+            tma_load_2d(st + 2 * V2_TILE_BYTES, &tmA, a.Kpad + x, ya, &full[s]);  // A lo
+            tma_load_2d(st + 3 * V2_TILE_BYTES, &tmB, a.Kpad + x, yb, &full[s]);  // B lo
+          }
+          last[s] = g;
+        }
       }
-      // Let every issued copy land before the CTA may exit.
-      for (int s = 0; s < TC_STAGES; s++)
-        if (last[s] >= 0) mbar_drain(&full[s], (uint32_t)(last[s] / TC_STAGES) & 1u);
+      for (int s = 0; s < V2_STAGES; s++)
+        if (last[s] >= 0) mbar_drain(&full[s], (uint32_t)(last[s] / V2_STAGES) & 1u);
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      const uint32_t idesc = idesc_bf16(TC_BM, a.bn);
-      for (int it = 0; it < iters; it++) {
-        const int s = it % TC_STAGES;
-        const uint32_t ph = (uint32_t)(it / TC_STAGES) & 1u;
-        if (!mbar_wait(&full[s], ph, a.err, ERR_FULL_WAIT)) break;
-        tc_fence_after();
-        const uint32_t abase = smem_u32(As + s * A_STAGE_BYTES);
-        const uint32_t bbase = smem_u32(Bs + s * B_STAGE_BYTES);
+      const uint32_t idesc = idesc_f16kind(TC_BM, V2_BN, a.f16 ? 0u : 1u);
+      int g = 0, c = 0;
+      bool ok = true;
+      for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
+        int tm, tn, kb0, kb1;
+        unit_coords(u, tm, tn, kb0, kb1);
+        for (int kb = kb0; kb < kb1; kb++, g++, c++) {
+          const int s = g % V2_STAGES;
+          const uint32_t ph = (uint32_t)(g / V2_STAGES) & 1u;
+          const int b = c & 1;
+          const uint32_t bph = (uint32_t)(c >> 1) & 1u;
+          if (!mbar_wait(&tempty[b], bph ^ 1u, a.err, ERR_EMPTY_WAIT)) { ok = false; break; }
+          if (!mbar_wait(&full[s], ph, a.err, ERR_FULL_WAIT)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t st = smem_u32(smem + s * V2_STAGE_BYTES);
+          const uint32_t ahi = st, bhi = st + V2_TILE_BYTES;
+          const uint32_t alo = st + 2 * V2_TILE_BYTES, blo = st + 3 * V2_TILE_BYTES;
+          const uint32_t d = tmem + (uint32_t)(b * V2_BN);
+          uint32_t acc = 0;
+          if (split3) {
 #pragma unroll
-        for (int k = 0; k < TC_BK / 16; k++) {
-          mma_bf16(tmem, sw128_desc(abase + 32 * k), sw128_desc(bbase + 32 * k), idesc,
-                   (it > 0 || k > 0) ? 1u : 0u);
+            for (int k = 0; k < TC_BK / 16; k++, acc = 1)
+              mma_bf16(d, sw128_desc(alo + 32 * k), sw128_desc(bhi + 32 * k), idesc, acc);
+#pragma unroll
+            for (int k = 0; k < TC_BK / 16; k++)
+              mma_bf16(d, sw128_desc(ahi + 32 * k), sw128_desc(blo + 32 * k), idesc, 1u);
+          }
+#pragma unroll
+          for (int k = 0; k < TC_BK / 16; k++, acc = 1)
+            mma_bf16(d, sw128_desc(ahi + 32 * k), sw128_desc(bhi + 32 * k), idesc, acc);
+          mma_commit(&empty[s]);
+          mma_commit(&tfull[b]);
         }
-        mma_commit(&empty[s]);
       }
-      mma_commit(accum);
+      // every MMA issued above has completed once `done` fires
+      mma_commit(done);
+      mbar_drain(done, 0);
     }
   } else {
     const int q = warp & 3;
     const int row = 32 * q + lane;
-    const int m = m0 + row;
-    const bool ok = mbar_wait(accum, 0, a.err, ERR_ACCUM_WAIT);
-    tc_fence_after();
-    const bool good = ok && (*(volatile unsigned *)a.err == 0) && iters > 0;
-    if (good) {
-      int64_t rowOff = 0;
-      if (!a.partial && m < a.M) rowOff = out.rowC[m];
-      for (int c = 0; c < a.bn; c += 16) {
-        float v[16];
-        tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c, v);
-        if (m < a.M) {
-          if (a.partial) {
-            float *P = a.partial + (int64_t)blockIdx.z * a.part_stride;
+    const int et = threadIdx.x - 64;  // 0..127
+    int c = 0;
+    bool ok = true;
+    for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
+      int tm, tn, kb0, kb1;
+      unit_coords(u, tm, tn, kb0, kb1);
+      const int m = tm * TC_BM + row;
+      const int n0 = tn * V2_BN;
+      asm volatile("bar.sync 1, 128;" ::: "memory");  // previous unit's colOff reads done
+      if (!a.partial) {
+        const int nn = n0 + et;
+        colOff[et] = nn < a.N ? out.baseC + out.colC[nn] : -1;
+      }
+      float acc[V2_BN];
 #pragma unroll
-            for (int j = 0; j < 16; j++) {
-              const int n = n0 + c + j;
-              if (n < a.N) P[(int64_t)m + (int64_t)a.M * n] = v[j];
-            }
-          } else if (out.fp32) {
-            float *C = (float *)out.C;
+      for (int j = 0; j < V2_BN; j++) acc[j] = 0.0f;
+      for (int kb = kb0; kb < kb1; kb++, c++) {
+        const int b = c & 1;
+        const uint32_t bph = (uint32_t)(c >> 1) & 1u;
+        if (!mbar_wait(&tfull[b], bph, a.err, ERR_ACCUM_WAIT)) { ok = false; break; }
+        tc_fence_after();
+        const uint32_t t0 = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * V2_BN);
 #pragma unroll
-            for (int j = 0; j < 16; j++) {
-              const int64_t co = colOff[c + j];
-              if (co >= 0) {
-                const int64_t off = rowOff + co;
-                float val = (float)out.alpha * v[j];
-                if (out.beta != 0.0) val += (float)out.beta * C[off];
-                C[off] = val;
-              }
-            }
-          } else {
-            double *C = (double *)out.C;
+        for (int j = 0; j < V2_BN; j += 16) {
+          float v[16];
+          tmem_ld16(t0 + (uint32_t)j, v);
 #pragma unroll
-            for (int j = 0; j < 16; j++) {
-              const int64_t co = colOff[c + j];
-              if (co >= 0) {
-                const int64_t off = rowOff + co;
-                double val = out.alpha * (double)v[j];
-                if (out.beta != 0.0) val += out.beta * C[off];
-                C[off] = val;
-              }
+          for (int i = 0; i < 16; i++) acc[j + i] += v[i];
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[b])) : "memory");
+      }
+      asm volatile("bar.sync 1, 128;" ::: "memory");  // colOff of this unit written
+      if (!ok || *(volatile unsigned *)a.err) break;
+      if (m >= a.M) continue;
+      if (a.partial) {
+        const int sp = u / (a.tiles_m * a.tiles_n);
+        float *P = a.partial + (int64_t)sp * a.part_stride;
+#pragma unroll
+        for (int j = 0; j < V2_BN; j++) {
+          const int n = n0 + j;
+          if (n < a.N) P[(int64_t)m + (int64_t)a.M * n] = acc[j];
+        }
+        continue;
+      }
+      double alpha = out.alpha;
+      if (out.scaleA) alpha /= *out.scaleA;
+      if (out.scaleB) alpha /= *out.scaleB;
+      const int64_t rowOff = out.rowC[m];
+      if (out.fp32) {
+        float *C = (float *)out.C;
+        const float fa = (float)alpha, fb = (float)out.beta;
+#pragma unroll
+        for (int j = 0; j < V2_BN; j += 16) {
+          float old[16];
+          if (fb != 0.0f) {
+#pragma unroll
+            for (int i = 0; i < 16; i++) {
+              const int64_t co = colOff[j + i];
+              old[i] = co >= 0 ? C[rowOff + co] : 0.0f;
             }
+          }
+#pragma unroll
+          for (int i = 0; i < 16; i++) {
+            const int64_t co = colOff[j + i];
+            if (co >= 0) C[rowOff + co] = fa * acc[j + i] + (fb != 0.0f ? fb * old[i] : 0.0f);
+          }
+        }
+      } else {
+        double *C = (double *)out.C;
+#pragma unroll
+        for (int j = 0; j < V2_BN; j += 16) {
+          double old[16];
+          if (out.beta != 0.0) {
+#pragma unroll
+            for (int i = 0; i < 16; i++) {
+              const int64_t co = colOff[j + i];
+              old[i] = co >= 0 ? C[rowOff + co] : 0.0;
+            }
+          }
+#pragma unroll
+          for (int i = 0; i < 16; i++) {
+            const int64_t co = colOff[j + i];
+            if (co >= 0)
+              C[rowOff + co] = alpha * (double)acc[j + i] + (out.beta != 0.0 ? out.beta * old[i] : 0.0);
           }
         }
       }
@@ -308,7 +409,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   if (warp == 1) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                 "r"(TMEM_COLS)
+                 "r"(V2_TMEM_COLS)
                  : "memory");
   }
 }
@@ -316,6 +417,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 __global__ void tc_reduce_kernel(TcOut out, int64_t M, int64_t N, int splits,
                                  const float *__restrict__ partial) {
   const int64_t MN = M * N;
+  double alpha = out.alpha;
+  if (out.scaleA) alpha /= *out.scaleA;
+  if (out.scaleB) alpha /= *out.scaleB;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < MN;
        e += (int64_t)gridDim.x * blockDim.x) {
     double s = 0.0;
@@ -324,29 +428,68 @@ __global__ void tc_reduce_kernel(TcOut out, int64_t M, int64_t N, int splits,
     const int64_t off = out.baseC + out.rowC[m] + out.colC[n];
     if (out.fp32) {
       float *C = (float *)out.C;
-      double val = out.alpha * s;
+      double val = alpha * s;
       if (out.beta != 0.0) val += out.beta * (double)C[off];
       C[off] = (float)val;
     } else {
       double *C = (double *)out.C;
-      double val = out.alpha * s;
+      double val = alpha * s;
       if (out.beta != 0.0) val += out.beta * C[off];
       C[off] = val;
     }
   }
 }
 
-// Gathers rows x K FP64 values through offset tables into BF16 hi/lo rows.
+// max|x| over the gathered operand, as float bits (positive floats order like
+// unsigned integers).
+__global__ void maxabs_kernel(const double *__restrict__ src, const int64_t *__restrict__ rowOff,
+                              int64_t rows, const int64_t *__restrict__ kOff, int64_t K, int unitK,
+                              unsigned *__restrict__ maxbits) {
+  float m = 0.0f;
+  const int64_t n = rows * K;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r, k;
+    if (unitK) { k = e % K; r = e / K; }
+    else { r = e % rows; k = e / rows; }
+    m = fmaxf(m, (float)fabs(src[rowOff[r] + kOff[k]]));
+  }
+  for (int off = 16; off > 0; off >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, off));
+  if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(maxbits, __float_as_uint(m));
+}
+
+struct HalfPair {
+  __device__ static void split(double x, double s, __half &hi, __half &lo) {
+    const double xs = x * s;
+    hi = __double2half(xs);
+    lo = __double2half(xs - (double)__half2float(hi));
+  }
+};
+
+// Gathers rows x K FP64 values through offset tables into 16-bit hi/lo rows.
+// FP16 format: values are scaled by s = 2^(15 - e), max|x| = f 2^e, f in [0.5, 1),
+// which block (0,0) also stores for the epilogue.
+template <bool F16>
 __global__ void __launch_bounds__(256) pack_split_kernel(
     const double *__restrict__ src, const int64_t *__restrict__ rowOff, int64_t rows,
-    const int64_t *__restrict__ kOff, int64_t K, int unitK, __nv_bfloat16 *__restrict__ dst,
-    int64_t Kpad) {
+    const int64_t *__restrict__ kOff, int64_t K, int unitK, uint16_t *__restrict__ dst,
+    int64_t Kpad, const unsigned *__restrict__ maxbits, double *__restrict__ scale_out) {
   __shared__ double tile[32][65];
   __shared__ int64_t sr[32], sk[64];
   const int t = threadIdx.x;
   const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 64;
   if (t < 32) sr[t] = (r0 + t < rows) ? rowOff[r0 + t] : -1;
   else if (t < 96) sk[t - 32] = (k0 + t - 32 < K) ? kOff[k0 + t - 32] : -1;
+  double s = 1.0;
+  if (F16) {
+    const float mx = __uint_as_float(*maxbits);
+    if (mx > 0.0f) {
+      int e;
+      frexpf(mx, &e);
+      s = ldexp(1.0, 15 - e);
+    }
+    if (blockIdx.x == 0 && blockIdx.y == 0 && t == 0) *scale_out = s;
+  }
   __syncthreads();
 #pragma unroll
   for (int p = 0; p < 8; p++) {
@@ -358,14 +501,21 @@ __global__ void __launch_bounds__(256) pack_split_kernel(
   }
   __syncthreads();
   const int rr = t >> 3, ch = t & 7;
-  __align__(16) __nv_bfloat16 hi[8];
-  __align__(16) __nv_bfloat16 lo[8];
+  __align__(16) uint16_t hi[8];
+  __align__(16) uint16_t lo[8];
 #pragma unroll
   for (int j = 0; j < 8; j++) {
     const double x = tile[rr][ch * 8 + j];
-    const __nv_bfloat16 h = __double2bfloat16(x);
-    hi[j] = h;
-    lo[j] = __double2bfloat16(x - (double)__bfloat162float(h));
+    if (F16) {
+      __half h, l;
+      HalfPair::split(x, s, h, l);
+      hi[j] = __half_as_ushort(h);
+      lo[j] = __half_as_ushort(l);
+    } else {
+      const __nv_bfloat16 h = __double2bfloat16(x);
+      hi[j] = __bfloat16_as_ushort(h);
+      lo[j] = __bfloat16_as_ushort(__double2bfloat16(x - (double)__bfloat162float(h)));
+    }
   }
   const int64_t base = (r0 + rr) * 2 * Kpad + k0 + ch * 8;
   *reinterpret_cast<uint4 *>(dst + base) = *reinterpret_cast<const uint4 *>(hi);
@@ -387,14 +537,16 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
   return fn;
 }
 
-CUtensorMap make_map(const __nv_bfloat16 *base, int64_t rows_pad, int64_t Kpad, int box_rows) {
+CUtensorMap make_map(const void *base, int64_t rows_pad, int64_t Kpad, int box_rows, TcFormat fmt) {
   CUtensorMap m;
   std::memset(&m, 0, sizeof(m));
   cuuint64_t dims[2] = {(cuuint64_t)(2 * Kpad), (cuuint64_t)rows_pad};
   cuuint64_t strides[1] = {(cuuint64_t)(2 * Kpad * 2)};
   cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
-  CUresult r = get_encode()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)base, dims, strides,
+  CUresult r = get_encode()(&m, fmt == TcFormat::FP16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                                      : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
+                            2, const_cast<void *>(base), dims, strides,
                             box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS)
@@ -404,29 +556,28 @@ CUtensorMap make_map(const __nv_bfloat16 *base, int64_t rows_pad, int64_t Kpad, 
 
 }  // namespace
 
-int TcEngine::tile_n(int64_t N) {
-  const int64_t ntn = ceil_div(N, TC_MAX_BN);
-  return (int)round_up(ceil_div(N, ntn), 16);
-}
+int TcEngine::tile_n(int64_t) { return V2_BN; }
 
 CUtensorMap TcEngine::map_of(const Packed &p, int box_rows) {
-  return make_map(p.p(), p.rows_pad, p.Kpad, box_rows);
+  return make_map(p.p(), p.rows_pad, p.Kpad, box_rows, p.fmt);
 }
 
 void tc_gemm_launch_maps(const CUtensorMap &ma, const CUtensorMap &mb, int64_t Kpad, int64_t rowA0,
-                         int64_t M, int64_t rowB0, int64_t N, int bn, const TcOut &out, int nseg,
-                         int splits, float *partial, unsigned *err, cudaStream_t stream) {
+                         int64_t M, int64_t rowB0, int64_t N, int bn, TcFormat fmt,
+                         const TcOut &out, int nseg, int splits, float *partial, unsigned *err,
+                         cudaStream_t stream) {
+  (void)bn;
   static std::once_flag once;
   std::call_once(once, [] {
     cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)TC_SMEM_BYTES);
+                         (int)V2_SMEM_BYTES);
   });
   if (M <= 0 || N <= 0) return;
   if (Kpad % TC_BK != 0 || Kpad <= 0) throw Error(SCESS_ERR_INVALID, "tc_gemm: Kpad % 64");
   if (M > INT32_MAX || N > INT32_MAX || rowA0 + M > INT32_MAX || rowB0 + N > INT32_MAX ||
       2 * Kpad > INT32_MAX)
     throw Error(SCESS_ERR_INVALID, "tc_gemm: dimension too large");
-  if (bn % 16 != 0 || bn < 16 || bn > TC_MAX_BN) throw Error(SCESS_ERR_INVALID, "tc_gemm: bad bn");
+  if (nseg != 1 && nseg != 3) throw Error(SCESS_ERR_INVALID, "tc_gemm: nseg");
   const int nkb = (int)(Kpad / TC_BK);
   if (splits < 1) splits = 1;
   if (splits > nkb) splits = nkb;
@@ -440,14 +591,18 @@ void tc_gemm_launch_maps(const CUtensorMap &ma, const CUtensorMap &mb, int64_t K
   a.nkb = nkb;
   a.nseg = nseg;
   a.kb_per_split = kbs;
-  a.bn = bn;
+  a.tiles_m = (int)ceil_div(M, TC_BM);
+  a.tiles_n = (int)ceil_div(N, V2_BN);
+  a.splits = splits;
   a.Kpad = (int)Kpad;
+  a.f16 = fmt == TcFormat::FP16 ? 1 : 0;
   a.partial = splits > 1 ? partial : nullptr;
   a.part_stride = M * N;
   a.err = err;
   if (splits > 1 && !partial) throw Error(SCESS_ERR_INVALID, "tc_gemm: split-K needs partials");
-  dim3 grid((unsigned)ceil_div(N, bn), (unsigned)ceil_div(M, TC_BM), (unsigned)splits);
-  tc_gemm_kernel<<<grid, TC_THREADS, TC_SMEM_BYTES, stream>>>(ma, mb, out, a);
+  const int64_t units = (int64_t)a.tiles_m * a.tiles_n * splits;
+  const unsigned grid = (unsigned)std::min<int64_t>(units, kNumSMs);
+  tc_gemm_kernel<<<grid, TC_THREADS, V2_SMEM_BYTES, stream>>>(ma, mb, out, a);
   SCESS_CHECK_LAUNCH();
   if (splits > 1) {
     const int64_t MN = M * N;
@@ -457,27 +612,20 @@ void tc_gemm_launch_maps(const CUtensorMap &ma, const CUtensorMap &mb, int64_t K
   }
 }
 
-void tc_gemm_launch(const __nv_bfloat16 *A, int64_t a_rows_pad, const __nv_bfloat16 *B,
-                    int64_t b_rows_pad, int64_t Kpad, int64_t rowA0, int64_t M, int64_t rowB0,
-                    int64_t N, const TcOut &out, int nseg, int splits, float *partial,
-                    unsigned *err, cudaStream_t stream) {
-  if (M <= 0 || N <= 0) return;
-  const int bn = TcEngine::tile_n(N);
-  const CUtensorMap ma = make_map(A, a_rows_pad, Kpad, TC_BM);
-  const CUtensorMap mb = make_map(B, b_rows_pad, Kpad, bn);
-  tc_gemm_launch_maps(ma, mb, Kpad, rowA0, M, rowB0, N, bn, out, nseg, splits, partial, err, stream);
-}
-
-void TcEngine::gemm_maps(const CUtensorMap &ma, const CUtensorMap &mb, int64_t Kpad, int64_t rowA0,
-                         int64_t M, int64_t rowB0, int64_t N, const TcOut &out, int nseg,
-                         cudaStream_t stream) {
-  tc_gemm_launch_maps(ma, mb, Kpad, rowA0, M, rowB0, N, tile_n(N), out, nseg, 1, nullptr,
+void TcEngine::gemm_maps(const CUtensorMap &ma, const CUtensorMap &mb, int64_t Kpad, int64_t Kreal,
+                         int64_t rowA0, int64_t M, int64_t rowB0, int64_t N, const TcOut &out,
+                         int nseg, cudaStream_t stream) {
+  TimedScope ts(ctx_.timer, "tc_gemm", 2.0 * M * N * Kreal, 0.0, stream ? stream : ctx_.stream);
+  tc_gemm_launch_maps(ma, mb, Kpad, rowA0, M, rowB0, N, tile_n(N), fmt_, out, nseg, 1, nullptr,
                       err_.as<unsigned>(), stream ? stream : ctx_.stream);
 }
 
 // ---------------------------------------------------------------------------------------------
 
 TcEngine::TcEngine(Ctx &ctx) : ctx_(ctx) {
+  // SCESS_TC_FORMAT=bf16 selects the unscaled BF16 split (default: scaled FP16).
+  const char *f = std::getenv("SCESS_TC_FORMAT");
+  if (f && std::strcmp(f, "bf16") == 0) fmt_ = TcFormat::BF16;
   err_.alloc(sizeof(unsigned) * 4);
   SCESS_CUDA(cudaMemsetAsync(err_.as<void>(), 0, sizeof(unsigned) * 4, ctx_.stream));
 }
@@ -493,18 +641,36 @@ void TcEngine::pack(const double *src, const int64_t *rowOff, int64_t rows, cons
                     int64_t K, bool unitK, int64_t row_align, Packed &out) {
   const int64_t Kpad = round_up(std::max<int64_t>(K, 1), TC_BK);
   const int64_t rows_pad = round_up(std::max<int64_t>(rows, 1), std::max<int64_t>(row_align, 32));
-  const size_t bytes = (size_t)rows_pad * 2 * Kpad * sizeof(__nv_bfloat16);
-  if (out.mem.bytes() < bytes) {
+  const size_t bytes = (size_t)rows_pad * 2 * Kpad * sizeof(uint16_t);
+  if (out.mem.bytes() < bytes || !out.aux.bytes()) {
     ctx_.sync();
-    out.mem.alloc(bytes);
+    if (out.mem.bytes() < bytes) out.mem.alloc(bytes);
+    if (!out.aux.bytes()) out.aux.alloc(16);
   }
   out.rows = rows;
   out.rows_pad = rows_pad;
   out.K = K;
   out.Kpad = Kpad;
+  out.fmt = fmt_;
+  TimedScope ts(ctx_.timer, "pack_split", 0.0,
+                (double)rows * K * 8 + (double)rows_pad * Kpad * 4, ctx_.stream);
+  unsigned *maxbits = out.aux.as<unsigned>();
+  double *scale = reinterpret_cast<double *>(out.aux.as<char>() + 8);
   dim3 grid((unsigned)(Kpad / 64), (unsigned)(rows_pad / 32));
-  pack_split_kernel<<<grid, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, unitK ? 1 : 0,
-                                                   out.p(), Kpad);
+  if (fmt_ == TcFormat::FP16) {
+    SCESS_CUDA(cudaMemsetAsync(maxbits, 0, sizeof(unsigned), ctx_.stream));
+    const int64_t n = rows * K;
+    const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), 4 * kNumSMs));
+    maxabs_kernel<<<blocks, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, unitK ? 1 : 0, maxbits);
+    SCESS_CHECK_LAUNCH();
+    pack_split_kernel<true><<<grid, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, unitK ? 1 : 0,
+                                                           out.mem.as<uint16_t>(), Kpad, maxbits, scale);
+  } else {
+    const double one = 1.0;
+    SCESS_CUDA(cudaMemcpyAsync(scale, &one, sizeof(double), cudaMemcpyHostToDevice, ctx_.stream));
+    pack_split_kernel<false><<<grid, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, unitK ? 1 : 0,
+                                                            out.mem.as<uint16_t>(), Kpad, maxbits, scale);
+  }
   SCESS_CHECK_LAUNCH();
 }
 
@@ -514,8 +680,7 @@ void TcEngine::gemm(const Packed &A, int64_t rowA0, int64_t M, const Packed &B, 
   const int nkb = (int)(A.Kpad / TC_BK);
   int splits = force_splits;
   if (splits <= 0) {
-    const int64_t ntn = ceil_div(N, TC_MAX_BN);
-    const int64_t tiles = ceil_div(M, TC_BM) * ntn;
+    const int64_t tiles = ceil_div(M, TC_BM) * ceil_div(N, V2_BN);
     splits = 1;
     if (tiles < kNumSMs) {
       splits = (int)std::min<int64_t>(ceil_div(kNumSMs, tiles), std::max(1, nkb / 4));
@@ -531,8 +696,21 @@ void TcEngine::gemm(const Packed &A, int64_t rowA0, int64_t M, const Packed &B, 
     }
     partial = partial_.as<float>();
   }
-  tc_gemm_launch(A.p(), A.rows_pad, B.p(), B.rows_pad, A.Kpad, rowA0, M, rowB0, N, out, nseg,
-                 splits, partial, err_.as<unsigned>(), ctx_.stream);
+  TimedScope ts(ctx_.timer, timer_name_ ? timer_name_ : "tc_gemm", 2.0 * M * N * A.K, 0.0,
+                ctx_.stream);
+  TcOut o = out;
+  set_scales(o, A, B);
+  const int bn = tile_n(N);
+  const CUtensorMap ma = map_of(A, TC_BM), mb = map_of(B, bn);
+  tc_gemm_launch_maps(ma, mb, A.Kpad, rowA0, M, rowB0, N, bn, fmt_, o, nseg, splits, partial,
+                      err_.as<unsigned>(), ctx_.stream);
+}
+
+void TcEngine::clear_cache(const void *owner) {
+  for (auto it = cache_.begin(); it != cache_.end();) {
+    if (it->second.first == owner) it = cache_.erase(it);
+    else ++it;
+  }
 }
 
 void TcEngine::check_error() {
@@ -548,8 +726,8 @@ void TcEngine::check_error() {
 
 void TcEngine::contract(const EinsumPlan &pl, double alpha, const double *A, const double *B,
                         double beta, double *C, bool constA, bool constB) {
-  // Put the longer output side on the 128-row MMA dimension.
-  const bool swap = pl.M < 64 && pl.N >= 64;
+  // Epilogue lanes walk the GEMM rows: put C's unit-stride index there.
+  const bool swap = pl.cUnitM ? false : (pl.cUnitN ? true : (pl.M < 64 && pl.N >= 64));
   const int64_t *rowX = swap ? pl.d_colB : pl.d_rowA, *kX = swap ? pl.d_kB : pl.d_kA;
   const int64_t *rowY = swap ? pl.d_rowA : pl.d_colB, *kY = swap ? pl.d_kA : pl.d_kB;
   const double *X = swap ? B : A, *Y = swap ? A : B;
@@ -565,13 +743,15 @@ void TcEngine::contract(const EinsumPlan &pl, double alpha, const double *A, con
     }
     std::string key = pl.key + tag + std::to_string((uintptr_t)src);
     auto it = cache_.find(key);
-    if (it != cache_.end()) return *it->second;
+    if (it != cache_.end() && it->second.first == owner_) return *it->second.second;
     auto pk = std::make_unique<Packed>();
     pack(src, rows, nrows, ks, pl.K, unitK, TC_BM, *pk);
     auto &ref = *pk;
-    cache_.emplace(key, std::move(pk));
+    cache_[key] = std::make_pair(owner_, std::move(pk));
     return ref;
   };
+  const std::string tname = "tc_gemm[" + pl.spec + "]";
+  timer_name_ = tname.c_str();
   const Packed &PX = get(X, rowX, MX, kX, uX, cX, swap ? "#B" : "#A", tmpA_);
   const Packed &PY = get(Y, rowY, NY, kY, uY, cY, swap ? "#A" : "#B", tmpB_);
   TcOut o;
@@ -582,6 +762,7 @@ void TcEngine::contract(const EinsumPlan &pl, double alpha, const double *A, con
   o.alpha = alpha;
   o.beta = beta;
   gemm(PX, 0, MX, PY, 0, NY, o, 3);
+  timer_name_ = nullptr;
 }
 
 }  // namespace scess

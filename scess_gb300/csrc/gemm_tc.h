@@ -1,12 +1,16 @@
 // Tensor-core (tcgen05 / TMEM / TMA) backend of the mixed-precision form.
 //
 // Operands are FP64 in HBM.  A pack kernel gathers them through offset tables
-// (fusing the einsum permutation) and splits every value x into BF16 hi + lo
-// (hi = bf16(x), lo = bf16(x - hi)); a packed operand is a row-major
-// [rows_pad][2*Kpad] BF16 array holding hi in columns [0, Kpad) and lo in
-// [Kpad, 2 Kpad).  The GEMM kernel runs three K segments hi*hi + hi*lo + lo*hi
-// into one FP32 TMEM accumulator (the lo*lo term is below FP32 resolution) and
-// its epilogue scatters alpha*acc + beta*C into the FP64 (or FP32) output.
+// (fusing the einsum permutation) and splits every value into a 16-bit hi + lo
+// pair; a packed operand is a row-major [rows_pad][2*Kpad] array holding hi in
+// columns [0, Kpad) and lo in [Kpad, 2 Kpad).  Two operand formats:
+//   FP16 (default): x is first scaled by a power of two s chosen on the device
+//     from max|x| so that max|x| s lies in [2^14, 2^15); hi = fp16(x s),
+//     lo = fp16(x s - hi).  11 significant bits each: |x s - hi - lo| <= 2^-22 |x s|.
+//   BF16: hi = bf16(x), lo = bf16(x - hi), no scaling (|x - hi - lo| <= 2^-16 |x|).
+// The GEMM kernel runs three K segments hi*hi + hi*lo + lo*hi into one FP32
+// TMEM accumulator (lo*lo is dropped) and its epilogue scatters
+// alpha/(sA sB) * acc + beta*C into the FP64 (or FP32) output.
 #pragma once
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -19,10 +23,15 @@
 
 namespace scess {
 
+enum class TcFormat { BF16 = 0, FP16 = 1 };
+
 struct Packed {
   DevMem mem;
+  DevMem aux;  // [0]: max|x| as float bits (uint32), [8]: scale s (double)
   int64_t rows = 0, rows_pad = 0, K = 0, Kpad = 0;
+  TcFormat fmt = TcFormat::FP16;
   __nv_bfloat16 *p() const { return mem.as<__nv_bfloat16>(); }
+  const double *scale() const { return aux.bytes() ? reinterpret_cast<const double *>(aux.as<char>() + 8) : nullptr; }
 };
 
 // Output of a tensor-core GEMM: element (m, n) of the product goes to
@@ -33,6 +42,9 @@ struct TcOut {
   const int64_t *rowC = nullptr, *colC = nullptr;
   int64_t baseC = 0;
   double alpha = 1.0, beta = 0.0;
+  // Scales of the packed operands (device doubles, null = 1): the product is
+  // divided by scaleA * scaleB.
+  const double *scaleA = nullptr, *scaleB = nullptr;
 };
 
 class TcEngine {
@@ -49,6 +61,7 @@ class TcEngine {
   // contiguous along k (load-coalescing hint).
   void pack(const double *src, const int64_t *rowOff, int64_t rows, const int64_t *kOff,
             int64_t K, bool unitK, int64_t row_align, Packed &out);
+  TcFormat format() const { return fmt_; }
   // D(m, n) = sum_k A(rowA0 + m, k) B(rowB0 + n, k) for m < M, n < N, written
   // through `out`.  nseg = 3 (split hi/lo) or 1 (hi only, BF16 accuracy).
   void gemm(const Packed &A, int64_t rowA0, int64_t M, const Packed &B, int64_t rowB0, int64_t N,
@@ -57,31 +70,40 @@ class TcEngine {
   static int tile_n(int64_t N);
   // TMA descriptor of a packed operand with boxes of box_rows x 64.
   static CUtensorMap map_of(const Packed &p, int box_rows);
+  // TcOut scale pointers of a product of two packed operands.
+  static void set_scales(TcOut &out, const Packed &A, const Packed &B) {
+    out.scaleA = A.scale();
+    out.scaleB = B.scale();
+  }
   // gemm() with prebuilt descriptors (mb must use box_rows == tile_n(N)); no split-K.
-  void gemm_maps(const CUtensorMap &ma, const CUtensorMap &mb, int64_t Kpad, int64_t rowA0,
-                 int64_t M, int64_t rowB0, int64_t N, const TcOut &out, int nseg = 3,
-                 cudaStream_t stream = nullptr);
+  // Kreal: the unpadded K (algorithmic FLOPs for the kernel timer).
+  void gemm_maps(const CUtensorMap &ma, const CUtensorMap &mb, int64_t Kpad, int64_t Kreal,
+                 int64_t rowA0, int64_t M, int64_t rowB0, int64_t N, const TcOut &out,
+                 int nseg = 3, cudaStream_t stream = nullptr);
   // Device error word set by bounded waits inside the kernels (0 = fine).
   void check_error();
-  // Drops cached packings of constant operands (called at the end of every
-  // top-level call: the cache is keyed by device pointer).
-  void clear_cache() { cache_.clear(); }
+  // Cached packings of constant operands are keyed by device pointer and
+  // tagged with the owner that keeps those pointers alive: a resident
+  // RccsdState (its address) or 0 for a single C-ABI call.  clear_cache(owner)
+  // drops the owner's entries; owner changes with set_cache_owner().
+  void set_cache_owner(const void *owner) { owner_ = owner; }
+  void clear_cache(const void *owner);
 
  private:
   Ctx &ctx_;
-  std::map<std::string, std::unique_ptr<Packed>> cache_;
+  TcFormat fmt_ = TcFormat::FP16;
+  std::map<std::string, std::pair<const void *, std::unique_ptr<Packed>>> cache_;
+  const void *owner_ = nullptr;
+  const char *timer_name_ = nullptr;
   Packed tmpA_, tmpB_;
   DevMem partial_;
   DevMem err_;
 };
 
 // Raw launchers.
-void tc_gemm_launch(const __nv_bfloat16 *A, int64_t a_rows_pad, const __nv_bfloat16 *B,
-                    int64_t b_rows_pad, int64_t Kpad, int64_t rowA0, int64_t M, int64_t rowB0,
-                    int64_t N, const TcOut &out, int nseg, int splits, float *partial,
-                    unsigned *err, cudaStream_t stream);
 void tc_gemm_launch_maps(const CUtensorMap &ma, const CUtensorMap &mb, int64_t Kpad, int64_t rowA0,
-                         int64_t M, int64_t rowB0, int64_t N, int bn, const TcOut &out, int nseg,
-                         int splits, float *partial, unsigned *err, cudaStream_t stream);
+                         int64_t M, int64_t rowB0, int64_t N, int bn, TcFormat fmt,
+                         const TcOut &out, int nseg, int splits, float *partial, unsigned *err,
+                         cudaStream_t stream);
 
 }  // namespace scess

@@ -246,169 +246,219 @@ std::vector<double> diis_coefficients(const std::vector<std::vector<double>> &gr
 
 // ---------------------------------------------------------------------------------------------
 
-void rccsd_solve(Ctx &ctx, const RccsdBlocks &B, const SolveInput &in,
-                 const scess_rccsd_options &opts, const Control &ctl, double *t1_out,
-                 double *t2_out, scess_rccsd_result *res) {
-  const int64_t o = B.o, v = B.v, N = B.N;
-  const int64_t n1 = o * v, n2 = o * o * v * v, n = n1 + n2;
-  cudaStream_t s = ctx.stream;
-  const bool mixed = opts.precision == SCESS_PRECISION_MIXED;
-  std::memset(res, 0, sizeof(*res));
-
-  ctx.logf(0, in.f12_residual
-                  ? "--- Closed-shell CCSD with F12 geminals (CCSD-F12b) with DIIS acceleration ---"
-                  : "--- Closed-shell Coupled Cluster Singles & Doubles (CCSD) with DIIS acceleration ---");
-
-  DTensor eps({N});
-  upload(ctx, eps.p(), in.eps_host, N);
-  DTensor amp({n}), prev({n}), R({n});
-  DTensor drv, Lf12;
+RccsdState::RccsdState(Ctx &ctx, DTensor &&eri, int64_t nmo, int64_t nocc, const SolveInput &in,
+                       const scess_rccsd_options &opts)
+    : ctx_(ctx), eri_(std::move(eri)), opts_(opts) {
+  B_.build(ctx, eri_.p(), nmo, nocc);
+  const int64_t o = B_.o, v = B_.v, N = B_.N;
+  n1_ = o * v;
+  n2_ = o * o * v * v;
+  n_ = n1_ + n2_;
+  mixed_ = opts.precision == SCESS_PRECISION_MIXED;
+  have_f12_ = in.f12_residual != nullptr;
+  eps_ = DTensor({N});
+  upload(ctx, eps_.p(), in.eps_host, N);
+  amp_ = DTensor({n_});
+  prev_ = DTensor({n_});
+  R_ = DTensor({n_});
   if (in.f12_residual) {
-    drv = DTensor({o, o, v, v});
-    upload(ctx, drv.p(), in.f12_residual, n2);
+    drv_ = DTensor({o, o, v, v});
+    upload(ctx, drv_.p(), in.f12_residual, n2_);
   }
   if (in.f12_energy) {
     DTensor e12({o, o, v, v});
-    upload(ctx, e12.p(), in.f12_energy, n2);
-    Lf12 = DTensor({o, o, v, v});
-    permute(ctx, "ijab->ijab", 2.0, e12.v, 0.0, Lf12.v);                             // :95-96
-    permute(ctx, "ijba->ijab", -1.0, e12.v, 1.0, Lf12.v);
+    upload(ctx, e12.p(), in.f12_energy, n2_);
+    Lf12_ = DTensor({o, o, v, v});
+    permute(ctx, "ijab->ijab", 2.0, e12.v, 0.0, Lf12_.v);                            // :95-96
+    permute(ctx, "ijba->ijab", -1.0, e12.v, 1.0, Lf12_.v);
     ctx.sync();
   }
-  const int maxv = std::max(1, opts.max_diis_vectors);
-  DevMem diis_amp((size_t)maxv * n * sizeof(double)), diis_err((size_t)maxv * n * sizeof(double));
-  DevMem vecptr((size_t)maxv * sizeof(double *)), coefd((size_t)(maxv + 1) * sizeof(double));
-  std::vector<const double *> hptr(maxv);
-  RccsdWork w;
-  w.alloc(o, v, !mixed);
-  bool have_wvvvv = !mixed;
+  maxv_ = std::max(1, opts.max_diis_vectors);
+  diis_amp_.alloc((size_t)maxv_ * n_ * sizeof(double));
+  diis_err_.alloc((size_t)maxv_ * n_ * sizeof(double));
+  vecptr_.alloc((size_t)maxv_ * sizeof(double *));
+  coefd_.alloc((size_t)(maxv_ + 1) * sizeof(double));
+  w_.alloc(o, v, !mixed_);
+  have_wvvvv_ = !mixed_;
+  mixed_phase_ = mixed_;
+  std::memset(&res_, 0, sizeof(res_));
+  SCESS_CUDA(cudaEventCreate(&ev0_));
+  SCESS_CUDA(cudaEventCreate(&ev1_));
+}
 
-  double *t1 = amp.p(), *t2 = amp.p() + n1;
-  if (opts.resume) {
-    upload(ctx, t1, t1_out, n1);
-    upload(ctx, t2, t2_out, n2);
-  } else {
-    // MP2 guess: t1 = 0, t2 = (<ij|ab> + f12 residual) / eijab                       :334-339
-    SCESS_CUDA(cudaMemsetAsync(R.p(), 0, n1 * sizeof(double), s));
-    permute(ctx, "ijab->ijab", 1.0, B.oovv_phys, 0.0, cm(R.p() + n1, {o, o, v, v}));
-    if (drv.p()) axpby(n2, 1.0, drv.p(), 1.0, R.p() + n1, s);
-    divide_denominators(o, v, eps.p(), R.p(), R.p() + n1, t1, t2, s);
-  }
+RccsdState::~RccsdState() {
+  cudaEventDestroy(ev0_);
+  cudaEventDestroy(ev1_);
+}
 
-  std::deque<int> order;  // DIIS slots, oldest first
-  std::vector<std::vector<double>> gram;
-  double E_last = DBL_MAX;
-  bool mixed_phase = mixed;
-  int phase_start = 0;
-  int fp64_iters = 0;
-  bool converged = false;
-  int it = 0;
-  double E = 0.0, dE = 0.0, rms = 0.0;
-  for (it = 0; it < opts.max_iterations; it++) {
+void RccsdState::mp2_guess() {
+  // t1 = 0, t2 = (<ij|ab> + f12 residual) / eijab                                    :334-339
+  const int64_t o = B_.o, v = B_.v;
+  cudaStream_t s = ctx_.stream;
+  SCESS_CUDA(cudaMemsetAsync(R_.p(), 0, n1_ * sizeof(double), s));
+  permute(ctx_, "ijab->ijab", 1.0, B_.oovv_phys, 0.0, cm(R_.p() + n1_, {o, o, v, v}));
+  if (drv_.p()) axpby(n2_, 1.0, drv_.p(), 1.0, R_.p() + n1_, s);
+  divide_denominators(o, v, eps_.p(), R_.p(), R_.p() + n1_, amp_.p(), amp_.p() + n1_, s);
+  reset_history();
+}
+
+void RccsdState::set_amplitudes(const double *t1, const double *t2) {
+  upload(ctx_, amp_.p(), t1, n1_);
+  upload(ctx_, amp_.p() + n1_, t2, n2_);
+  reset_history();
+}
+
+void RccsdState::get_amplitudes(double *t1, double *t2) {
+  if (t1) download(ctx_, t1, amp_.p(), n1_);
+  if (t2) download(ctx_, t2, amp_.p() + n1_, n2_);
+}
+
+void RccsdState::reset_history() {
+  order_.clear();
+  gram_.clear();
+  E_last_ = DBL_MAX;
+  it_ = 0;
+  phase_start_ = 0;
+  fp64_iters_ = 0;
+  mixed_phase_ = mixed_;
+  converged_ = false;
+  std::memset(&res_, 0, sizeof(res_));
+}
+
+double RccsdState::energy_of_amplitudes() {
+  const int64_t o = B_.o, v = B_.v;
+  cudaStream_t s = ctx_.stream;
+  tau_energy(o, v, B_.L_oovv.p(), amp_.p(), amp_.p() + n1_, ctx_.partials, ctx_.dscalars, s);
+  if (Lf12_.p()) dot(n2_, Lf12_.p(), amp_.p() + n1_, ctx_.partials, ctx_.dscalars + 1, s);
+  SCESS_CUDA(cudaMemcpyAsync(ctx_.hscalars, ctx_.dscalars, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  ctx_.sync();
+  return ctx_.hscalars[0] + (Lf12_.p() ? ctx_.hscalars[1] : 0.0);
+}
+
+bool RccsdState::iterate(int max_steps, const Control &ctl) {
+  const int64_t o = B_.o, v = B_.v;
+  cudaStream_t s = ctx_.stream;
+  double *t1 = amp_.p(), *t2 = amp_.p() + n1_;
+  SCESS_CUDA(cudaEventRecord(ev0_, s));
+  int steps = 0;
+  while (steps < max_steps && it_ < opts_.max_iterations && !converged_) {
     ctl.poll();                                                                       // :346
-    SCESS_CUDA(cudaMemcpyAsync(prev.p(), amp.p(), n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    const Backend be = mixed_phase ? Backend::MIXED : Backend::FP64;
-    if (be == Backend::FP64 && !have_wvvvv) {
-      w.Wvvvv = DTensor({v, v, v, v});
-      have_wvvvv = true;
+    SCESS_CUDA(cudaMemcpyAsync(prev_.p(), amp_.p(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    const Backend be = mixed_phase_ ? Backend::MIXED : Backend::FP64;
+    if (be == Backend::FP64 && !have_wvvvv_) {
+      w_.Wvvvv = DTensor({v, v, v, v});
+      have_wvvvv_ = true;
     }
-    rccsd_residual(ctx, B, amp.p(), drv.p(), be, w, R.p());                           // :350
-    divide_denominators(o, v, eps.p(), R.p(), R.p() + n1, t1, t2, s);
+    rccsd_residual(ctx_, B_, amp_.p(), drv_.p(), be, w_, R_.p());                     // :350
+    divide_denominators(o, v, eps_.p(), R_.p(), R_.p() + n1_, t1, t2, s);
 
     // AmplitudeDIIS::Extrapolate(updated, change)                                    :246-274
     int slot;
-    if ((int)order.size() < maxv) {
-      slot = (int)order.size();
+    if ((int)order_.size() < maxv_) {
+      slot = (int)order_.size();
     } else {
-      slot = order.front();
-      order.pop_front();
-      gram.erase(gram.begin());
-      for (auto &row : gram) row.erase(row.begin());
+      slot = order_.front();
+      order_.pop_front();
+      gram_.erase(gram_.begin());
+      for (auto &row : gram_) row.erase(row.begin());
     }
-    double *va = diis_amp.d() + (size_t)slot * n;
-    double *ve = diis_err.d() + (size_t)slot * n;
-    SCESS_CUDA(cudaMemcpyAsync(va, amp.p(), n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    SCESS_CUDA(cudaMemcpyAsync(ve, amp.p(), n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    axpby(n, -1.0, prev.p(), 1.0, ve, s);                                             // :352
-    order.push_back(slot);
-    const int nv = (int)order.size();
+    double *va = diis_amp_.d() + (size_t)slot * n_;
+    double *ve = diis_err_.d() + (size_t)slot * n_;
+    SCESS_CUDA(cudaMemcpyAsync(va, amp_.p(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    SCESS_CUDA(cudaMemcpyAsync(ve, amp_.p(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    axpby(n_, -1.0, prev_.p(), 1.0, ve, s);                                           // :352
+    order_.push_back(slot);
+    const int nv = (int)order_.size();
     for (int q = 0; q < nv; q++)
-      dot(n, diis_err.d() + (size_t)order[q] * n, ve, ctx.partials, ctx.dscalars + q, s);
-    SCESS_CUDA(cudaMemcpyAsync(ctx.hscalars, ctx.dscalars, nv * sizeof(double),
+      dot(n_, diis_err_.d() + (size_t)order_[q] * n_, ve, ctx_.partials, ctx_.dscalars + q, s);
+    SCESS_CUDA(cudaMemcpyAsync(ctx_.hscalars, ctx_.dscalars, nv * sizeof(double),
                                cudaMemcpyDeviceToHost, s));
-    ctx.sync();
-    for (int q = 0; q < nv - 1; q++) gram[q].push_back(ctx.hscalars[q]);
-    gram.emplace_back(ctx.hscalars, ctx.hscalars + nv);
-    const double errdot = ctx.hscalars[nv - 1];
-    if (it - phase_start >= opts.diis_start) {                                         // :354-357
-      if (it - phase_start == opts.diis_start) ctx.logf(1, "Turning on DIIS");
-      std::vector<double> c = diis_coefficients(gram);
-      for (int q = 0; q < nv; q++) hptr[q] = diis_amp.d() + (size_t)order[q] * n;
-      SCESS_CUDA(cudaMemcpyAsync(vecptr.as<void>(), hptr.data(), nv * sizeof(double *),
+    ctx_.sync();
+    for (int q = 0; q < nv - 1; q++) gram_[q].push_back(ctx_.hscalars[q]);
+    gram_.emplace_back(ctx_.hscalars, ctx_.hscalars + nv);
+    const double errdot = ctx_.hscalars[nv - 1];
+    if (it_ - phase_start_ >= opts_.diis_start) {                                    // :354-357
+      if (it_ - phase_start_ == opts_.diis_start) ctx_.logf(1, "Turning on DIIS");
+      std::vector<double> c = diis_coefficients(gram_);
+      std::vector<const double *> hptr(nv);
+      for (int q = 0; q < nv; q++) hptr[q] = diis_amp_.d() + (size_t)order_[q] * n_;
+      SCESS_CUDA(cudaMemcpyAsync(vecptr_.as<void>(), hptr.data(), nv * sizeof(double *),
                                  cudaMemcpyHostToDevice, s));
-      SCESS_CUDA(cudaMemcpyAsync(coefd.d(), c.data(), nv * sizeof(double), cudaMemcpyHostToDevice, s));
-      linear_combination(n, nv, vecptr.as<const double *>(), coefd.d(), amp.p(), s);
-      ctx.sync();  // hptr / c are pageable host buffers reused next iteration
+      SCESS_CUDA(cudaMemcpyAsync(coefd_.d(), c.data(), nv * sizeof(double), cudaMemcpyHostToDevice, s));
+      linear_combination(n_, nv, vecptr_.as<const double *>(), coefd_.d(), amp_.p(), s);
+      ctx_.sync();  // hptr / c are host buffers of this scope
     }
-    // E = CorrelationEnergy + CouplingEnergy                                         :361
-    tau_energy(o, v, B.L_oovv.p(), t1, t2, ctx.partials, ctx.dscalars, s);
-    if (Lf12.p()) dot(n2, Lf12.p(), t2, ctx.partials, ctx.dscalars + 1, s);
-    SCESS_CUDA(cudaMemcpyAsync(ctx.hscalars, ctx.dscalars, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
-    ctx.sync();
-    E = ctx.hscalars[0] + (Lf12.p() ? ctx.hscalars[1] : 0.0);
-    dE = std::fabs(E - E_last);                                                       // :362
-    rms = std::sqrt(errdot) / std::sqrt((double)n);                                   // :363
-    E_last = E;
+    const double E = energy_of_amplitudes();                                          // :361
+    const double dE = std::fabs(E - E_last_);                                         // :362
+    const double rms = std::sqrt(errdot) / std::sqrt((double)n_);                     // :363
+    E_last_ = E;
     if (!std::isfinite(E)) throw Error(SCESS_ERR_INVALID, "non-finite CCSD energy (diverging amplitudes)");
-    ctx.logf(1, "   CCSD(%d): E(corr) = %.12g      dE = %.12g      rms(dt) = %.12g%s", it, E, dE,
-             rms, mixed_phase ? "   [mixed]" : "");
-    if (opts.history && it < opts.max_iterations) {
-      opts.history[3 * it + 0] = E;
-      opts.history[3 * it + 1] = dE;
-      opts.history[3 * it + 2] = rms;
+    ctx_.logf(1, "   CCSD(%d): E(corr) = %.12g      dE = %.12g      rms(dt) = %.12g%s", it_, E,
+              dE, rms, mixed_phase_ ? "   [mixed]" : "");
+    if (opts_.history) {
+      opts_.history[3 * it_ + 0] = E;
+      opts_.history[3 * it_ + 1] = dE;
+      opts_.history[3 * it_ + 2] = rms;
     }
-    if (opts.checkpoint_capacity > 0 && opts.checkpoint_t1 && opts.checkpoint_t2) {
-      const int sl = it % opts.checkpoint_capacity;
-      download(ctx, opts.checkpoint_t1 + (size_t)sl * n1, t1, n1);
-      download(ctx, opts.checkpoint_t2 + (size_t)sl * n2, t2, n2);
+    if (opts_.checkpoint_capacity > 0 && opts_.checkpoint_t1 && opts_.checkpoint_t2) {
+      const int sl = it_ % opts_.checkpoint_capacity;
+      download(ctx_, opts_.checkpoint_t1 + (size_t)sl * n1_, t1, n1_);
+      download(ctx_, opts_.checkpoint_t2 + (size_t)sl * n2_, t2, n2_);
     }
-    if (!mixed_phase) fp64_iters++;
-    if (mixed_phase) {
-      res->mixed_iterations = it + 1;
-      if (dE < opts.mixed_energy_switch && rms < opts.mixed_amplitude_switch) {
-        // switch to FP64 refinement with a fresh DIIS subspace
-        mixed_phase = false;
-        phase_start = it + 1;
-        order.clear();
-        gram.clear();
-        ctx.logf(1, "Mixed-precision phase done; FP64 refinement");
+    res_.last_dE = dE;
+    res_.last_rms = rms;
+    if (!mixed_phase_) fp64_iters_++;
+    it_++;
+    steps++;
+    res_.iterations = it_;
+    if (mixed_phase_) {
+      res_.mixed_iterations = it_;
+      if (dE < opts_.mixed_energy_switch && rms < opts_.mixed_amplitude_switch) {
+        // FP64 refinement from the mixed amplitudes with a fresh DIIS subspace
+        mixed_phase_ = false;
+        phase_start_ = it_;
+        order_.clear();
+        gram_.clear();
+        ctx_.logf(1, "Mixed-precision phase done; FP64 refinement");
       }
-    } else if (dE < opts.energy_convergence && rms < opts.amplitude_convergence &&   // :370
-               (!mixed || fp64_iters >= std::max(1, opts.refine_sweeps))) {
-      converged = true;
-      it++;
-      break;
+    } else if (dE < opts_.energy_convergence && rms < opts_.amplitude_convergence &&  // :370
+               (!mixed_ || fp64_iters_ >= std::max(1, opts_.refine_sweeps))) {
+      converged_ = true;
     }
   }
-  res->iterations = it;
-  res->last_dE = dE;
-  res->last_rms = rms;
-  if (mixed && ctx.tc) ctx.tc->check_error();
-  if (!converged) {                                                                   // :376-380
+  SCESS_CUDA(cudaEventRecord(ev1_, s));
+  SCESS_CUDA(cudaEventSynchronize(ev1_));
+  float ms = 0.0f;
+  SCESS_CUDA(cudaEventElapsedTime(&ms, ev0_, ev1_));
+  last_device_ms_ = ms;
+  if (mixed_ && ctx_.tc) ctx_.tc->check_error();
+  res_.converged = converged_ ? 1 : 0;
+  res_.E_CCSD = converged_ ? E_last_ : 0.0;
+  return converged_;
+}
+
+double RccsdState::coupling_energy() {
+  if (!Lf12_.p()) return 0.0;
+  dot(n2_, Lf12_.p(), amp_.p() + n1_, ctx_.partials, ctx_.dscalars, ctx_.stream);
+  SCESS_CUDA(cudaMemcpyAsync(ctx_.hscalars, ctx_.dscalars, sizeof(double), cudaMemcpyDeviceToHost, ctx_.stream));
+  ctx_.sync();
+  return ctx_.hscalars[0];
+}
+
+void rccsd_solve(Ctx &ctx, RccsdState &st, const Control &ctl, double *t1_out, double *t2_out,
+                 scess_rccsd_result *res) {
+  ctx.logf(0, st.has_f12()
+                  ? "--- Closed-shell CCSD with F12 geminals (CCSD-F12b) with DIIS acceleration ---"
+                  : "--- Closed-shell Coupled Cluster Singles & Doubles (CCSD) with DIIS acceleration ---");
+  const bool conv = st.iterate(st.options().max_iterations, ctl);
+  *res = st.result();
+  if (!conv) {                                                                        // :376-380
     ctx.logf(0, "!!! CCSD procedure failed to converge !!!");
-    res->converged = 0;
+    res->E_CCSD = 0.0;
     return;
   }
-  res->converged = 1;
-  res->E_CCSD = E_last;                                                               // :382
-  if (Lf12.p()) {                                                                     // :383
-    dot(n2, Lf12.p(), t2, ctx.partials, ctx.dscalars, s);
-    SCESS_CUDA(cudaMemcpyAsync(ctx.hscalars, ctx.dscalars, sizeof(double), cudaMemcpyDeviceToHost, s));
-    ctx.sync();
-    res->E_F12_Coupling = ctx.hscalars[0];
-  }
-  download(ctx, t1_out, t1, n1);
-  download(ctx, t2_out, t2, n2);
+  res->E_F12_Coupling = st.coupling_energy();                                         // :383
+  st.get_amplitudes(t1_out, t2_out);
   ctx.logf(0, "---- CCSD procedure converged! ----");
   ctx.logf(0, "E(CCSD correlation) = %.12g hartrees", res->E_CCSD);
 }

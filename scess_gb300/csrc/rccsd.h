@@ -32,15 +32,64 @@ struct RccsdWork {
 void rccsd_residual(Ctx &ctx, const RccsdBlocks &B, const double *amp, const double *t2driver,
                     Backend be, RccsdWork &w, double *R);
 
-// Full solver (SolveRCCSD_DIIS, RCCSD.cpp:295-394) on device-resident blocks.
 struct SolveInput {
   const double *eps_host = nullptr;     // nmo
   const double *f12_residual = nullptr; // host o^2v^2 or null
   const double *f12_energy = nullptr;   // host o^2v^2 or null
 };
-void rccsd_solve(Ctx &ctx, const RccsdBlocks &B, const SolveInput &in,
-                 const scess_rccsd_options &opts, const Control &ctl, double *t1_out,
-                 double *t2_out, scess_rccsd_result *res);
+
+// Device-resident CCSD problem: integrals (eri + block views), orbital
+// energies, amplitudes and the DIIS subspace stay in HBM between calls.
+// iterate() runs the loop body of SolveRCCSD_DIIS (RCCSD.cpp:345-374).
+class RccsdState {
+ public:
+  RccsdState(Ctx &ctx, DTensor &&eri, int64_t nmo, int64_t nocc, const SolveInput &in,
+             const scess_rccsd_options &opts);
+  ~RccsdState();
+  void mp2_guess();
+  void set_amplitudes(const double *t1, const double *t2);
+  void get_amplitudes(double *t1, double *t2);
+  // Up to max_steps iterations (fewer once converged); returns converged.
+  bool iterate(int max_steps, const Control &ctl);
+  double coupling_energy();
+  double energy_of_amplitudes();
+  const scess_rccsd_result &result() const { return res_; }
+  const scess_rccsd_options &options() const { return opts_; }
+  bool has_f12() const { return have_f12_; }
+  float last_device_ms() const { return last_device_ms_; }
+  const RccsdBlocks &blocks() const { return B_; }
+  const double *d_eri() const { return eri_.p(); }
+  const double *d_eps() const { return eps_.p(); }
+  const double *d_t1() const { return amp_.p(); }
+  const double *d_t2() const { return amp_.p() + n1_; }
+  int64_t nocc() const { return B_.o; }
+  int64_t nmo() const { return B_.N; }
+
+ private:
+  void reset_history();
+  Ctx &ctx_;
+  DTensor eri_;
+  RccsdBlocks B_;
+  scess_rccsd_options opts_;
+  int64_t n1_ = 0, n2_ = 0, n_ = 0;
+  bool mixed_ = false, have_f12_ = false, have_wvvvv_ = false;
+  DTensor eps_, amp_, prev_, R_, drv_, Lf12_;
+  int maxv_ = 8;
+  DevMem diis_amp_, diis_err_, vecptr_, coefd_;
+  RccsdWork w_;
+  std::deque<int> order_;  // DIIS slots, oldest first
+  std::vector<std::vector<double>> gram_;
+  double E_last_ = 0.0;
+  int it_ = 0, phase_start_ = 0, fp64_iters_ = 0;
+  bool mixed_phase_ = false, converged_ = false;
+  scess_rccsd_result res_{};
+  cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+  float last_device_ms_ = 0.0f;
+};
+
+// SolveRCCSD_DIIS (RCCSD.cpp:295-394) on a prepared state.
+void rccsd_solve(Ctx &ctx, RccsdState &st, const Control &ctl, double *t1_out, double *t2_out,
+                 scess_rccsd_result *res);
 
 // Host-side DIIS solve with the reference's semantics (RCCSD.cpp:246-274):
 // bordered Gram matrix scaled by max|B|, full-pivoting LU.

@@ -45,41 +45,59 @@ __global__ void __launch_bounds__(256) triples_energy_kernel(
   if (a >= v || b >= v || c >= v || b > a || c > b) return;
   extern __shared__ __align__(16) unsigned char sm_raw[];
   __shared__ double red[32];
-  const int64_t o2 = o * o, o3 = o2 * o;
+  const int oo = (int)o, o2 = oo * oo, o3 = o2 * oo;
+  // Y(i,j,k) at i + p1 j + p2 k with odd p1, p2: the six permuted reads of r3
+  // walk consecutive i with strides 1, p1 or p2, all free of bank conflicts.
+  const int p1 = oo | 1, p2 = (p1 * oo) | 1;
   CT *Y = reinterpret_cast<CT *>(sm_raw);
-  CT *Sbc = Y + o3, *Sac = Sbc + o2, *Sab = Sac + o2;
-  CT *ta = Sab + o2, *tb = ta + o, *tc = tb + o, *eo = tc + o;
-  const WT *Wt = W + ((al * nb + bl) * nb + cl) * o3;
+  CT *Sbc = Y + p2 * oo, *Sac = Sbc + o2, *Sab = Sac + o2;
+  CT *ta = Sab + o2, *tb = ta + oo, *tc = tb + oo, *eo = tc + oo;
+  const WT *Wt = W + ((al * nb + bl) * nb + cl) * (int64_t)o3;
   // S(i,j,a,b) = (ia|jb) = eri(i, j, o+a, o+b)
   const int64_t N2 = N * N, N3 = N2 * N;
-  for (int64_t e = threadIdx.x; e < o2; e += blockDim.x) {
-    const int64_t i = e % o, j = e / o;
+  for (int e = threadIdx.x; e < o2; e += blockDim.x) {
+    const int i = e % oo, j = e / oo;
     Sbc[e] = (CT)eri[i + N * j + (o + b) * N2 + (o + c) * N3];
     Sac[e] = (CT)eri[i + N * j + (o + a) * N2 + (o + c) * N3];
     Sab[e] = (CT)eri[i + N * j + (o + a) * N2 + (o + b) * N3];
   }
-  for (int64_t i = threadIdx.x; i < o; i += blockDim.x) {
+  for (int i = threadIdx.x; i < oo; i += blockDim.x) {
     ta[i] = (CT)t1[i + o * a];
     tb[i] = (CT)t1[i + o * b];
     tc[i] = (CT)t1[i + o * c];
     eo[i] = (CT)eps[i];
   }
   __syncthreads();
-  for (int64_t e = threadIdx.x; e < o3; e += blockDim.x) {
-    const int64_t i = e % o, j = (e / o) % o, k = e / o2;
-    // V_ijk = t1_ia (jb|kc) + t1_jb (ia|kc) + t1_kc (ia|jb)   (GetV + Symmetrise)
-    Y[e] = (CT)Wt[e] + ta[i] * Sbc[j + o * k] + tb[j] * Sac[i + o * k] + tc[k] * Sab[i + o * j];
+  // element e = i + o j + o^2 k; thread t visits e = t, t + 256, ... with
+  // incrementally maintained (i, j, k)
+  const int di = 256 % oo, dj = (256 / oo) % oo, dk = 256 / o2;
+  const int i0 = (int)threadIdx.x % oo, j0 = ((int)threadIdx.x / oo) % oo, k0 = (int)threadIdx.x / o2;
+  {
+    int i = i0, j = j0, k = k0;
+    for (int e = threadIdx.x; e < o3; e += 256) {
+      // V_ijk = t1_ia (jb|kc) + t1_jb (ia|kc) + t1_kc (ia|jb)   (GetV + Symmetrise)
+      Y[i + p1 * j + p2 * k] =
+          (CT)Wt[e] + ta[i] * Sbc[j + oo * k] + tb[j] * Sac[i + oo * k] + tc[k] * Sab[i + oo * j];
+      i += di;
+      int cj = 0;
+      if (i >= oo) { i -= oo; cj = 1; }
+      j += dj + cj;
+      int ck = 0;
+      if (j >= oo) { j -= oo; ck = 1; }
+      k += dk + ck;
+    }
   }
   __syncthreads();
   const CT evirt = (CT)(eps[o + a] + eps[o + b] + eps[o + c]);
   double acc = 0.0;
   CT part = 0;
   int cnt = 0;
-  for (int64_t e = threadIdx.x; e < o3; e += blockDim.x) {
-    const int64_t i = e % o, j = (e / o) % o, k = e / o2;
+  int i = i0, j = j0, k = k0;
+  for (int e = threadIdx.x; e < o3; e += 256) {
     // r3(Y) = 4 Y_ijk + Y_kij + Y_jki - 2 Y_kji - 2 Y_ikj - 2 Y_jik               :152-154
-    const CT r3 = (CT)4 * Y[e] + Y[k + o * i + o2 * j] + Y[j + o * k + o2 * i] -
-                  (CT)2 * (Y[k + o * j + o2 * i] + Y[i + o * k + o2 * j] + Y[j + o * i + o2 * k]);
+    const CT r3 = (CT)4 * Y[i + p1 * j + p2 * k] + Y[k + p1 * i + p2 * j] +
+                  Y[j + p1 * k + p2 * i] -
+                  (CT)2 * (Y[k + p1 * j + p2 * i] + Y[i + p1 * k + p2 * j] + Y[j + p1 * i + p2 * k]);
     const CT d = ((eo[i] + eo[j]) + eo[k]) - evirt;                              // :155
     part += (CT)Wt[e] * r3 / d;                                                    // :156
     if (++cnt == 16) {
@@ -87,6 +105,13 @@ __global__ void __launch_bounds__(256) triples_energy_kernel(
       part = 0;
       cnt = 0;
     }
+    i += di;
+    int cj = 0;
+    if (i >= oo) { i -= oo; cj = 1; }
+    j += dj + cj;
+    int ck = 0;
+    if (j >= oo) { j -= oo; ck = 1; }
+    k += dk + ck;
   }
   acc += (double)part;
   for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
@@ -219,25 +244,39 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   // Output positions in W[(a_l,b_l,c_l)][i,j,k]: strides of (a_l,b_l,c_l) and (i,j,k).
   const int64_t su[3] = {o3 * nb * nb, o3 * nb, o3};
   const int64_t sw[3] = {1, o, o2};
-  // Tables per permutation: PQ rows/cols and R rows/cols in W, and the shared operand tables.
+  // Tables per permutation: PQ rows/cols and R rows/cols in W.  W's unit-stride
+  // index i is kept first on the lane side (GEMM rows) or on the per-thread side
+  // (GEMM columns) of every epilogue: when i is the k' of a permutation the Q
+  // operand is taken in (k', j', z) column order, when it is the j' of an R
+  // product the R operand is taken in (j', i', x) row order.
+  auto q_swapped = [](const int *pi) { return pi[2] == 0; };
+  auto r_swapped = [](const int *pi) { return pi[1] == 0; };
   std::vector<std::vector<int64_t>> ts;
   for (int p = 0; p < 6; p++) {
     const int *pi = kPerm[p];
-    ts.push_back(table({{o, sw[pi[0]]}, {nb, su[pi[0]]}, {nb, su[pi[1]]}}));   // PQ rows (i',x,y)
-    ts.push_back(table({{o, sw[pi[1]]}, {o, sw[pi[2]]}, {nb, su[pi[2]]}}));    // PQ cols (j',k',z)
-    ts.push_back(table({{o, sw[pi[0]]}, {o, sw[pi[1]]}, {nb, su[pi[0]]}}));    // R rows (i',j',x)
-    ts.push_back(table({{o, sw[pi[2]]}, {nb, su[pi[1]]}, {nb, su[pi[2]]}}));   // R cols (k',y,z)
+    ts.push_back(table({{o, sw[pi[0]]}, {nb, su[pi[0]]}, {nb, su[pi[1]]}}));      // PQ rows (i',x,y)
+    if (q_swapped(pi))
+      ts.push_back(table({{o, sw[pi[2]]}, {o, sw[pi[1]]}, {nb, su[pi[2]]}}));     // PQ cols (k',j',z)
+    else
+      ts.push_back(table({{o, sw[pi[1]]}, {o, sw[pi[2]]}, {nb, su[pi[2]]}}));     // PQ cols (j',k',z)
+    if (r_swapped(pi))
+      ts.push_back(table({{o, sw[pi[1]]}, {o, sw[pi[0]]}, {nb, su[pi[0]]}}));     // R rows (j',i',x)
+    else
+      ts.push_back(table({{o, sw[pi[0]]}, {o, sw[pi[1]]}, {nb, su[pi[0]]}}));     // R rows (i',j',x)
+    ts.push_back(table({{o, sw[pi[2]]}, {nb, su[pi[1]]}, {nb, su[pi[2]]}}));      // R cols (k',y,z)
   }
   const size_t kOperand = ts.size();
   // operand tables (FP64 path): P rows (i',x,y), f; Q cols (j',k',z), f; R rows, m; t2 cols, m
-  ts.push_back(table({{o, 1}, {nb, o * v}, {nb, o * v * vp}}));                  // 24: P rows
-  ts.push_back(table({{v, o}}));                                                 // 25: P k (f)
-  ts.push_back(table({{o, v}, {o, v * o}, {nb, v * o2}}));                       // 26: Q cols
-  ts.push_back(table({{v, 1}}));                                                 // 27: Q k (f)
-  ts.push_back(table({{o, 1}, {o, o}, {nb, o3}}));                               // 28: R rows
-  ts.push_back(table({{o, o2}}));                                                // 29: R k (m)
-  ts.push_back(table({{o, o}, {nb, o2}, {nb, o2 * vp}}));                        // 30: t2 cols
-  ts.push_back(table({{o, 1}}));                                                 // 31: t2 k (m)
+  ts.push_back(table({{o, 1}, {nb, o * v}, {nb, o * v * vp}}));                  // +0: P rows
+  ts.push_back(table({{v, o}}));                                                 // +1: P k (f)
+  ts.push_back(table({{o, v}, {o, v * o}, {nb, v * o2}}));                       // +2: Q cols (j,k,z)
+  ts.push_back(table({{v, 1}}));                                                 // +3: Q k (f)
+  ts.push_back(table({{o, 1}, {o, o}, {nb, o3}}));                               // +4: R rows (i,j,x)
+  ts.push_back(table({{o, o2}}));                                                // +5: R k (m)
+  ts.push_back(table({{o, o}, {nb, o2}, {nb, o2 * vp}}));                        // +6: t2 cols
+  ts.push_back(table({{o, 1}}));                                                 // +7: t2 k (m)
+  ts.push_back(table({{o, v * o}, {o, v}, {nb, v * o2}}));                       // +8: Q cols (k,j,z)
+  ts.push_back(table({{o, o}, {o, 1}, {nb, o3}}));                               // +9: R rows (j,i,x)
   DevTables dt;
   dt.build(ts);
 
@@ -246,7 +285,8 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   SCESS_CUDA(cudaMemsetAsync(energies.p(), 0, energies.size() * sizeof(double), s));
   const size_t wbytes = (size_t)o3 * nb * nb * nb * (mixed ? 4 : 8);
   DevMem W(wbytes);
-  const size_t ysmem = (size_t)(o3 + 3 * o2 + 4 * o) * (mixed ? 4 : 8);
+  const int64_t p1 = o | 1, p2 = (p1 * o) | 1;
+  const size_t ysmem = (size_t)(p2 * o + 3 * o2 + 4 * o) * (mixed ? 4 : 8);
   if (ysmem > 200 * 1024) throw Error(SCESS_ERR_UNSUPPORTED, "(T): o^3 too large for one CTA");
   if (mixed) {
     SCESS_CUDA(cudaFuncSetAttribute(triples_energy_kernel<float, float>,
@@ -257,8 +297,8 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   }
 
   // MIXED: pack the operands once into block-grouped BF16 hi/lo rows.
-  Packed pP, pQ, pR, pT;
-  CUtensorMap mP{}, mQ{}, mR{}, mT{};
+  Packed pP, pQ, pQ2, pR, pR2, pT;
+  CUtensorMap mP{}, mQ{}, mQ2{}, mR{}, mR2{}, mT{};
   const int64_t Mpq = o * nb * nb, Npq = o2 * nb, Mr = o2 * nb, Nr = o * nb * nb;
   if (mixed) {
     TcEngine &tc = ctx.tensor_cores();
@@ -271,16 +311,24 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
     pt.push_back(table({{o, 1}, {o, o}, {nb, o3}, {NB, o3 * nb}}));
     // t2 rows r = k + o(y + nb(z + nb(Z + NB Y)))
     pt.push_back(table({{o, o}, {nb, o2}, {nb, o2 * vp}, {NB, o2 * vp * nb}, {NB, o2 * nb}}));
+    // Q rows in (k, j) order: r = k + o(j + o(z + nb Z))
+    pt.push_back(table({{o, v * o}, {o, v}, {nb, v * o2}, {NB, v * o2 * nb}}));
+    // R rows in (j, i) order: r = j + o(i + o(x + nb X))
+    pt.push_back(table({{o, o}, {o, 1}, {nb, o3}, {NB, o3 * nb}}));
     DevTables pdt;
     pdt.build(pt);
-    tc.pack(P.p(), pdt.ptr[0], o * vp * vp, dt.ptr[25], v, false, 128, pP);
-    tc.pack(Qt.p(), pdt.ptr[1], o2 * vp, dt.ptr[27], v, true, 128, pQ);
-    tc.pack(Rt.p(), pdt.ptr[2], o2 * vp, dt.ptr[29], o, false, 128, pR);
-    tc.pack(T2p.p(), pdt.ptr[3], o * vp * vp, dt.ptr[31], o, true, 128, pT);
+    tc.pack(P.p(), pdt.ptr[0], o * vp * vp, dt.ptr[kOperand + 1], v, false, 128, pP);
+    tc.pack(Qt.p(), pdt.ptr[1], o2 * vp, dt.ptr[kOperand + 3], v, true, 128, pQ);
+    tc.pack(Qt.p(), pdt.ptr[4], o2 * vp, dt.ptr[kOperand + 3], v, true, 128, pQ2);
+    tc.pack(Rt.p(), pdt.ptr[2], o2 * vp, dt.ptr[kOperand + 5], o, false, 128, pR);
+    tc.pack(Rt.p(), pdt.ptr[5], o2 * vp, dt.ptr[kOperand + 5], o, false, 128, pR2);
+    tc.pack(T2p.p(), pdt.ptr[3], o * vp * vp, dt.ptr[kOperand + 7], o, true, 128, pT);
     ctx.sync();
     mP = TcEngine::map_of(pP, 128);
     mQ = TcEngine::map_of(pQ, TcEngine::tile_n(Npq));
+    mQ2 = TcEngine::map_of(pQ2, TcEngine::tile_n(Npq));
     mR = TcEngine::map_of(pR, 128);
+    mR2 = TcEngine::map_of(pR2, 128);
     mT = TcEngine::map_of(pT, TcEngine::tile_n(Nr));
   }
   double *ws = nullptr;
@@ -316,12 +364,35 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
             out.colC = colPQ;
             out.alpha = 1.0;
             out.beta = p == 0 ? 0.0 : 1.0;
-            tc.gemm_maps(mP, mQ, pP.Kpad, Mpq * (X * NB + Yb), Mpq, Npq * Z, Npq, out);
-            out.rowC = rowR;
-            out.colC = colR;
+            const bool qs = q_swapped(pi), rs = r_swapped(pi);
+            // Lane side (GEMM rows) = the operand whose first index is W's i:
+            // P rows (i',x,y) when i' is i, else the Q columns (j'/k' first).
+            const Packed &pq = qs ? pQ2 : pQ;
+            const CUtensorMap &mq = qs ? mQ2 : mQ;
+            if (pi[0] == 0) {
+              TcEngine::set_scales(out, pP, pq);
+              tc.gemm_maps(mP, mq, pP.Kpad, v, Mpq * (X * NB + Yb), Mpq, Npq * Z, Npq, out);
+            } else {
+              out.rowC = colPQ;
+              out.colC = rowPQ;
+              TcEngine::set_scales(out, pq, pP);
+              tc.gemm_maps(mq, mP, pP.Kpad, v, Npq * Z, Npq, Mpq * (X * NB + Yb), Mpq, out);
+            }
             out.alpha = -1.0;
             out.beta = 1.0;
-            tc.gemm_maps(mR, mT, pR.Kpad, Mr * X, Mr, Nr * (Yb * NB + Z), Nr, out);
+            const Packed &pr = rs ? pR2 : pR;
+            const CUtensorMap &mr = rs ? mR2 : mR;
+            if (pi[2] != 0) {  // R rows (i',j',x) / (j',i',x) start with W's i
+              out.rowC = rowR;
+              out.colC = colR;
+              TcEngine::set_scales(out, pr, pT);
+              tc.gemm_maps(mr, mT, pR.Kpad, o, Mr * X, Mr, Nr * (Yb * NB + Z), Nr, out);
+            } else {           // k' is W's i: t2 rows (k',y,z) on the lane side
+              out.rowC = colR;
+              out.colC = rowR;
+              TcEngine::set_scales(out, pT, pr);
+              tc.gemm_maps(mT, mr, pR.Kpad, o, Nr * (Yb * NB + Z), Nr, Mr * X, Mr, out);
+            }
           } else {
             TableGemm g;
             g.A = P.p();
@@ -329,7 +400,7 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
             g.C = W.d();
             g.rowA = dt.ptr[kOperand + 0];
             g.kA = dt.ptr[kOperand + 1];
-            g.colB = dt.ptr[kOperand + 2];
+            g.colB = dt.ptr[kOperand + (q_swapped(pi) ? 8 : 2)];
             g.kB = dt.ptr[kOperand + 3];
             g.rowC = rowPQ;
             g.colC = colPQ;
@@ -342,12 +413,15 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
             g.beta = p == 0 ? 0.0 : 1.0;
             g.aUnitM = 1;
             g.bUnitN = 0;
-            dgemm_table(g, ws, s);
+            {
+              TimedScope ts(ctx.timer, "dgemm_table", 2.0 * g.M * g.N * g.K, 0.0, s);
+              dgemm_table(g, ws, s);
+            }
             TableGemm h;
             h.A = Rt.p();
             h.B = T2p.p();
             h.C = W.d();
-            h.rowA = dt.ptr[kOperand + 4];
+            h.rowA = dt.ptr[kOperand + (r_swapped(pi) ? 9 : 4)];
             h.kA = dt.ptr[kOperand + 5];
             h.colB = dt.ptr[kOperand + 6];
             h.kB = dt.ptr[kOperand + 7];
@@ -360,12 +434,14 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
             h.K = o;
             h.alpha = -1.0;
             h.beta = 1.0;
-            h.aUnitM = 1;
+            h.aUnitM = r_swapped(pi) ? 0 : 1;
             h.bUnitN = 0;
+            TimedScope ts(ctx.timer, "dgemm_table", 2.0 * h.M * h.N * h.K, 0.0, s);
             dgemm_table(h, ws, s);
           }
         }
         const unsigned nblk = (unsigned)(nb * nb * nb);
+        TimedScope ts(ctx.timer, "triples_energy", 0.0, (double)nblk * o3 * (mixed ? 4 : 8), s);
         if (mixed)
           triples_energy_kernel<float, float><<<nblk, 256, ysmem, s>>>(
               W.as<float>(), o, v, nb, A, Bk, C, d_eps, d_t1, d_eri, N, energies.p());

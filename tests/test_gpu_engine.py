@@ -42,11 +42,11 @@ def test_einsum_fp64(gctx, spec, sa, sb):
 
 @pytest.mark.parametrize('spec,sa,sb', CASES)
 def test_einsum_tensor_cores(gctx, spec, sa, sb):
-    # split BF16 hi+lo operands, FP32 accumulation: relative error below 1e-5 of max|C|
+    # scaled FP16 hi+lo operands, FP32 accumulation: below 5e-6 of max|C| (measured ~2e-6)
     A, B, ref = _operands(spec, sa, sb)
     C0 = np.random.default_rng(2).standard_normal(ref.shape)
     out = gctx.einsum(spec, A, B, C_init=C0, alpha=1.5, beta=1.0, precision='mixed')
-    assert rel_err(out, 1.5 * ref + C0) < 1e-5
+    assert rel_err(out, 1.5 * ref + C0) < 5e-6
 
 
 def test_tensor_core_gemm_exact_on_bf16_values(gctx):

@@ -30,8 +30,10 @@ def test_triples_fixed_amplitudes(gctx, o, v):
     ref = oracle.rccsd_triples_correction(eri, w.eps, o, w.t1, w.t2)
     et = gctx.triples(eri, w.eps, o, w.t1, w.t2)
     assert abs(et - ref) <= 1e-9 * max(1.0, abs(ref))
+    # mixed: FP32 tensor-core accumulation, relative error ~1e-6 of |E_T| (these fixed
+    # amplitudes give unphysically large |E_T|, up to 1e4 Eh)
     em = gctx.triples(eri, w.eps, o, w.t1, w.t2, precision='mixed')
-    assert abs(em - ref) <= 1e-6
+    assert abs(em - ref) <= 2e-6 * max(1.0, abs(ref))
 
 
 def test_triples_df_equals_eri(gctx):
