@@ -191,6 +191,23 @@ int scess_rccsd_residual(scess_ctx *ctx, const double *eri, int64_t nmo, int64_t
                          const double *t1, const double *t2, const double *t2_driver,
                          int32_t precision, double *r1_out, double *r2_out);
 
+/* Vector-Jacobian product of the residual numerators R(t1, t2; eri) of
+ * scess_rccsd_residual (UpdateAmplitudes, RCCSD.cpp:101-233; the reference has
+ * no derivative code).  Given cotangents g_r1 (o*v) and g_r2 (o^2 v^2):
+ *   g_t1 = (dR/dt1)^T g_r, g_t2 = (dR/dt2)^T g_r, g_eri = (dR/deri)^T g_r
+ * (g_eri nmo^4, may be NULL).  Hand-written reverse sweep over the forward's
+ * recorded contractions, on the GPU.  precision FP64 or MIXED (the
+ * contractions of forward and adjoint on tensor cores, FP32 accumulation). */
+int scess_rccsd_residual_vjp(scess_ctx *ctx, const double *eri, int64_t nmo, int64_t nocc,
+                             const double *t1, const double *t2, const double *g_r1,
+                             const double *g_r2, int32_t precision, double *g_t1, double *g_t2,
+                             double *g_eri);
+/* Same from DF factors; g_B (naux x nmo x nmo, may be NULL) = (dR/dB)^T g_r. */
+int scess_rccsd_residual_vjp_df(scess_ctx *ctx, const double *B, int64_t naux, int64_t nmo,
+                                int64_t nocc, const double *t1, const double *t2,
+                                const double *g_r1, const double *g_r2, int32_t precision,
+                                double *g_t1, double *g_t2, double *g_B);
+
 /* General binary contraction C = alpha * A.B + beta * C on the GPU, the
  * runtime counterpart of the tensor layer's compile-time Einsum
  * (src/Tensor/TensorEinsum.h:170-205): spec like "kcld,ilcd->ki", each

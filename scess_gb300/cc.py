@@ -103,6 +103,10 @@ EXPORTS = {
     'scess_ctx_profile_report': (C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),
     'scess_rccsd_residual': (C.c_int, [C.c_void_p, _dp, C.c_int64, C.c_int64, _dp, _dp, _dp,
                                        C.c_int32, _dp, _dp]),
+    'scess_rccsd_residual_vjp': (C.c_int, [C.c_void_p, _dp, C.c_int64, C.c_int64, _dp, _dp, _dp,
+                                           _dp, C.c_int32, _dp, _dp, _dp]),
+    'scess_rccsd_residual_vjp_df': (C.c_int, [C.c_void_p, _dp, C.c_int64, C.c_int64, C.c_int64,
+                                              _dp, _dp, _dp, _dp, C.c_int32, _dp, _dp, _dp]),
     'scess_einsum': (C.c_int, [C.c_void_p, C.c_char_p, C.c_double, _dp, C.c_int32, _i64p, _dp,
                                C.c_int32, _i64p, C.c_double, _dp, C.c_int32, _i64p, C.c_int32]),
 }
@@ -330,6 +334,35 @@ class Context:
                                            _ptr(drv), PRECISION[precision], _ptr(r1), _ptr(r2))
         self._check(st, 'scess_rccsd_residual')
         return r1, r2
+
+    # -- residual VJP -------------------------------------------------------------------------
+    def residual_vjp(self, eri, nocc, t1, t2, g_r1, g_r2, precision='fp64', B=None,
+                     want_integrals=False):
+        """(g_t1, g_t2, g_eri or g_B) = VJP of the residual numerators."""
+        o = int(nocc)
+        if B is not None:
+            Bf = _f64(B)
+            N = Bf.shape[1]
+        else:
+            ef = _f64(eri)
+            N = ef.shape[0]
+        v = N - o
+        args = [_f64(t1, (o, v)), _f64(t2, (o, o, v, v)), _f64(g_r1, (o, v)), _f64(g_r2, (o, o, v, v))]
+        gt1 = np.zeros((o, v), order='F')
+        gt2 = np.zeros((o, o, v, v), order='F')
+        if B is not None:
+            gI = np.zeros(Bf.shape, order='F') if want_integrals else None
+            st = self.lib.scess_rccsd_residual_vjp_df(self.h, _ptr(Bf), Bf.shape[0], N, o,
+                                                      *[_ptr(a) for a in args],
+                                                      PRECISION[precision], _ptr(gt1), _ptr(gt2),
+                                                      _ptr(gI))
+        else:
+            gI = np.zeros((N, N, N, N), order='F') if want_integrals else None
+            st = self.lib.scess_rccsd_residual_vjp(self.h, _ptr(ef), N, o, *[_ptr(a) for a in args],
+                                                   PRECISION[precision], _ptr(gt1), _ptr(gt2),
+                                                   _ptr(gI))
+        self._check(st, 'scess_rccsd_residual_vjp')
+        return gt1, gt2, gI
 
     # -- generic contraction ------------------------------------------------------------------
     def einsum(self, spec: str, A, B, C_init=None, alpha=1.0, beta=0.0, precision='fp64',

@@ -4,6 +4,7 @@
 #include <cstring>
 #include <new>
 
+#include "adjoint.h"
 #include "gemm_tc.h"
 #include "rccsd.h"
 #include "triples.h"
@@ -445,6 +446,80 @@ int scess_rccsd_residual(scess_ctx *ctx, const double *eri, int64_t nmo, int64_t
     scess::download(c, r2_out, R.p() + n1, n2);
     if (mixed) c.tensor_cores().check_error();
   });
+}
+
+static int residual_vjp_common(scess_ctx *ctx, const double *eri, const double *B, int64_t naux,
+                               int64_t nmo, int64_t nocc, const double *t1, const double *t2,
+                               const double *g_r1, const double *g_r2, int32_t precision,
+                               double *g_t1, double *g_t2, double *g_eri, double *g_B) {
+  return guard(ctx, [&](scess::Ctx &c) {
+    check_shape(nmo, nocc);
+    need(t1, "t1");
+    need(t2, "t2");
+    need(g_r1, "g_r1");
+    need(g_r2, "g_r2");
+    need(g_t1, "g_t1");
+    need(g_t2, "g_t2");
+    if (precision != SCESS_PRECISION_FP64 && precision != SCESS_PRECISION_MIXED)
+      throw Error(SCESS_ERR_INVALID, "bad precision");
+    const int64_t o = nocc, v = nmo - nocc, N = nmo, n1 = o * v, n2 = o * o * v * v;
+    const int64_t N4 = N * N * N * N;
+    scess::DTensor d_eri({N, N, N, N}), dB;
+    scess::Tape dfTape;
+    if (eri) {
+      scess::upload(c, d_eri.p(), eri, N4);
+      device_finite(c, d_eri.p(), N4, "eri");
+    } else {
+      dB = scess::DTensor({naux, N, N});
+      scess::upload(c, dB.p(), B, naux * N * N);
+      device_finite(c, dB.p(), naux * N * N, "B");
+      c.tape = &dfTape;  // eri(p,q,r,s) = sum_Q B(Q,p,r) B(Q,q,s), recorded for g_B
+      scess::einsum(c, "Qpr,Qqs->pqrs", 1.0, dB.v, dB.v, 0.0, d_eri.v, scess::Backend::FP64);
+      c.tape = nullptr;
+    }
+    scess::DTensor amp({n1 + n2}), gR({n1 + n2}), gAmp({n1 + n2}), geri;
+    scess::upload(c, amp.p(), t1, n1);
+    scess::upload(c, amp.p() + n1, t2, n2);
+    scess::upload(c, gR.p(), g_r1, n1);
+    scess::upload(c, gR.p() + n1, g_r2, n2);
+    const bool need_eri = g_eri || g_B;
+    if (need_eri) geri = scess::DTensor({N, N, N, N});
+    const scess::Backend be =
+        precision == SCESS_PRECISION_MIXED ? scess::Backend::MIXED : scess::Backend::FP64;
+    scess::rccsd_residual_vjp(c, d_eri.p(), nmo, nocc, amp.p(), gR.p(), be, be, gAmp.p(),
+                              need_eri ? geri.p() : nullptr);
+    scess::download(c, g_t1, gAmp.p(), n1);
+    scess::download(c, g_t2, gAmp.p() + n1, n2);
+    if (g_eri) scess::download(c, g_eri, geri.p(), N4);
+    if (g_B) {
+      scess::DTensor gB({naux, N, N});
+      SCESS_CUDA(cudaMemsetAsync(gB.p(), 0, (size_t)naux * N * N * sizeof(double), c.stream));
+      scess::GradMap gm;
+      gm.add(d_eri.p(), N4, geri.p());
+      gm.add(dB.p(), naux * N * N, gB.p());
+      scess::reverse_sweep(c, dfTape, gm, scess::Backend::FP64);
+      scess::download(c, g_B, gB.p(), naux * N * N);
+    }
+    if (precision == SCESS_PRECISION_MIXED) c.tensor_cores().check_error();
+  });
+}
+
+int scess_rccsd_residual_vjp(scess_ctx *ctx, const double *eri, int64_t nmo, int64_t nocc,
+                             const double *t1, const double *t2, const double *g_r1,
+                             const double *g_r2, int32_t precision, double *g_t1, double *g_t2,
+                             double *g_eri) {
+  if (!eri) return SCESS_ERR_INVALID;
+  return residual_vjp_common(ctx, eri, nullptr, 0, nmo, nocc, t1, t2, g_r1, g_r2, precision, g_t1,
+                             g_t2, g_eri, nullptr);
+}
+
+int scess_rccsd_residual_vjp_df(scess_ctx *ctx, const double *B, int64_t naux, int64_t nmo,
+                                int64_t nocc, const double *t1, const double *t2,
+                                const double *g_r1, const double *g_r2, int32_t precision,
+                                double *g_t1, double *g_t2, double *g_B) {
+  if (!B || naux <= 0) return SCESS_ERR_INVALID;
+  return residual_vjp_common(ctx, nullptr, B, naux, nmo, nocc, t1, t2, g_r1, g_r2, precision, g_t1,
+                             g_t2, nullptr, g_B);
 }
 
 int scess_einsum(scess_ctx *ctx, const char *spec, double alpha, const double *A, int32_t a_nd,

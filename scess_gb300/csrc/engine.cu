@@ -323,6 +323,17 @@ const EinsumPlan &plan_einsum(Ctx &ctx, const char *spec, const TV &A, const TV 
 
 void einsum(Ctx &ctx, const char *spec, double alpha, const TV &A, const TV &B, double beta,
             const TV &C, Backend be, bool constA, bool constB) {
+  if (ctx.tape) {
+    TapeOp op;
+    op.kind = TapeOp::EINSUM;
+    op.spec = spec;
+    op.alpha = alpha;
+    op.beta = beta;
+    op.A = A;
+    op.B = B;
+    op.C = C;
+    ctx.tape->ops.push_back(op);
+  }
   const EinsumPlan &pl = plan_einsum(ctx, spec, A, B, C);
   if ((be == Backend::MIXED && TcEngine::worth_it(pl)) || be == Backend::TENSOR) {
     ctx.tensor_cores().contract(pl, alpha, A.p, B.p, beta, C.p, constA, constB);
@@ -371,6 +382,16 @@ void einsum(Ctx &ctx, const char *spec, double alpha, const TV &A, const TV &B, 
 }
 
 void permute(Ctx &ctx, const char *spec, double alpha, const TV &X, double beta, const TV &Y) {
+  if (ctx.tape) {
+    TapeOp op;
+    op.kind = TapeOp::PERMUTE;
+    op.spec = spec;
+    op.alpha = alpha;
+    op.beta = beta;
+    op.A = X;
+    op.C = Y;
+    ctx.tape->ops.push_back(op);
+  }
   const Spec s = parse_spec(spec, false);
   if ((int)s.a.size() != X.nd || (int)s.c.size() != Y.nd)
     throw Error(SCESS_ERR_INVALID, std::string("rank mismatch in ") + spec);

@@ -74,6 +74,20 @@ struct EinsumPlan {
 };
 class TcEngine;  // tensor-core (mixed precision) backend, gemm_tc.cu
 
+// Forward-op record for the hand-written adjoint: every einsum / permute (and
+// the residual's tau and PlusTranspose steps) issued while Ctx::tape is set is
+// appended with its operand views; adjoint.cu sweeps the list in reverse.
+struct TapeOp {
+  enum Kind { EINSUM = 0, PERMUTE = 1, TAU = 2, PLUS_T = 3 } kind = EINSUM;
+  std::string spec;
+  double alpha = 1.0, beta = 0.0;
+  TV A, B, C;
+  int64_t o = 0, v = 0;
+};
+struct Tape {
+  std::vector<TapeOp> ops;
+};
+
 // Per-call control: cancellation and the time limit.
 struct Control {
   scess_cancel_fn cancel = nullptr;
@@ -142,6 +156,7 @@ struct Ctx {
   double *hscalars = nullptr;  // 64 pinned host doubles
   std::unique_ptr<TcEngine> tc;
   KernelTimer timer;
+  Tape *tape = nullptr;  // recording target while an adjoint forward pass runs
 
   explicit Ctx(int dev);
   ~Ctx();

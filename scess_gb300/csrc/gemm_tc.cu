@@ -363,42 +363,68 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       if (out.scaleA) alpha /= *out.scaleA;
       if (out.scaleB) alpha /= *out.scaleB;
       const int64_t rowOff = out.rowC[m];
+      // beta == 1: fire-and-forget reductions (each element receives exactly one
+      // per launch, so the result is deterministic); beta == 0: plain stores;
+      // otherwise a batched read-modify-write.
       if (out.fp32) {
         float *C = (float *)out.C;
         const float fa = (float)alpha, fb = (float)out.beta;
+        if (out.beta == 1.0) {
 #pragma unroll
-        for (int j = 0; j < V2_BN; j += 16) {
-          float old[16];
-          if (fb != 0.0f) {
+          for (int j = 0; j < V2_BN; j++) {
+            const int64_t co = colOff[j];
+            if (co >= 0) atomicAdd(C + rowOff + co, fa * acc[j]);
+          }
+        } else if (out.beta == 0.0) {
+#pragma unroll
+          for (int j = 0; j < V2_BN; j++) {
+            const int64_t co = colOff[j];
+            if (co >= 0) C[rowOff + co] = fa * acc[j];
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < V2_BN; j += 16) {
+            float old[16];
 #pragma unroll
             for (int i = 0; i < 16; i++) {
               const int64_t co = colOff[j + i];
               old[i] = co >= 0 ? C[rowOff + co] : 0.0f;
             }
-          }
 #pragma unroll
-          for (int i = 0; i < 16; i++) {
-            const int64_t co = colOff[j + i];
-            if (co >= 0) C[rowOff + co] = fa * acc[j + i] + (fb != 0.0f ? fb * old[i] : 0.0f);
+            for (int i = 0; i < 16; i++) {
+              const int64_t co = colOff[j + i];
+              if (co >= 0) C[rowOff + co] = fa * acc[j + i] + fb * old[i];
+            }
           }
         }
       } else {
         double *C = (double *)out.C;
+        if (out.beta == 1.0) {
 #pragma unroll
-        for (int j = 0; j < V2_BN; j += 16) {
-          double old[16];
-          if (out.beta != 0.0) {
+          for (int j = 0; j < V2_BN; j++) {
+            const int64_t co = colOff[j];
+            if (co >= 0) atomicAdd(C + rowOff + co, alpha * (double)acc[j]);
+          }
+        } else if (out.beta == 0.0) {
+#pragma unroll
+          for (int j = 0; j < V2_BN; j++) {
+            const int64_t co = colOff[j];
+            if (co >= 0) C[rowOff + co] = alpha * (double)acc[j];
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < V2_BN; j += 16) {
+            double old[16];
 #pragma unroll
             for (int i = 0; i < 16; i++) {
               const int64_t co = colOff[j + i];
               old[i] = co >= 0 ? C[rowOff + co] : 0.0;
             }
-          }
 #pragma unroll
-          for (int i = 0; i < 16; i++) {
-            const int64_t co = colOff[j + i];
-            if (co >= 0)
-              C[rowOff + co] = alpha * (double)acc[j + i] + (out.beta != 0.0 ? out.beta * old[i] : 0.0);
+            for (int i = 0; i < 16; i++) {
+              const int64_t co = colOff[j + i];
+              if (co >= 0) C[rowOff + co] = alpha * (double)acc[j + i] + out.beta * old[i];
+            }
           }
         }
       }

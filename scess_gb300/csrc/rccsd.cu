@@ -98,6 +98,16 @@ void rccsd_residual(Ctx &ctx, const RccsdBlocks &B, const double *amp, const dou
   };
   make_tau(o, v, t1.p, t2.p, 1.0, w.tau.p(), s);                                     // :107
   const TV tau = w.tau.v;
+  if (ctx.tape) {
+    TapeOp op;
+    op.kind = TapeOp::TAU;
+    op.A = t1;
+    op.B = t2;
+    op.C = tau;
+    op.o = o;
+    op.v = v;
+    ctx.tape->ops.push_back(op);
+  }
   E("kcld,ilcd->ki", 1.0, B.L_ovov.v, tau, 0.0, w.Foo.v, true);                      // :111
   E("kcld,klad->ac", -1.0, B.L_ovov.v, tau, 0.0, w.Fvv.v, true);                     // :113
   E("kcld,ld->kc", 1.0, B.L_ovov.v, t1, 0.0, w.Fov.v, true);                         // :115
@@ -173,6 +183,15 @@ void rccsd_residual(Ctx &ctx, const RccsdBlocks &B, const double *amp, const dou
   E("akic,kjbc->ijab", -1.0, w.Wvoov.v, t2, 1.0, w.X.v);                             // :228
   E("bkci,kjac->ijab", -1.0, w.Wvovo.v, t2, 1.0, w.X.v);                             // :231
   plus_transpose(o, v, 1.0, w.X.p(), R2.p, s);                                       // :147-232
+  if (ctx.tape) {
+    TapeOp op;
+    op.kind = TapeOp::PLUS_T;
+    op.A = w.X.v;
+    op.C = R2;
+    op.o = o;
+    op.v = v;
+    ctx.tape->ops.push_back(op);
+  }
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -32,6 +32,10 @@ __host__ __device__ inline int64_t triple_id(int64_t a, int64_t b, int64_t c) {
   return a * (a + 1) * (a + 2) / 6 + b * (b + 1) / 2 + c;
 }
 
+// x / y: fast FP32 division in the mixed form (2 ulp), IEEE division in FP64.
+__device__ __forceinline__ float div_fast(float x, float y) { return __fdividef(x, y); }
+__device__ __forceinline__ double div_fast(double x, double y) { return x / y; }
+
 // One CTA per local triple (a_l, b_l, c_l) of the block triple (A, B, C).
 // Shared memory: Y (o^3) then Sbc, Sac, Sab (o^2 each) then t1 columns and the
 // occupied orbital energies (o each), all in the arithmetic type CT.
@@ -99,7 +103,7 @@ __global__ void __launch_bounds__(256) triples_energy_kernel(
                   Y[j + p1 * k + p2 * i] -
                   (CT)2 * (Y[k + p1 * j + p2 * i] + Y[i + p1 * k + p2 * j] + Y[j + p1 * i + p2 * k]);
     const CT d = ((eo[i] + eo[j]) + eo[k]) - evirt;                              // :155
-    part += (CT)Wt[e] * r3 / d;                                                    // :156
+    part += div_fast((CT)Wt[e] * r3, d);                                           // :156
     if (++cnt == 16) {
       acc += (double)part;
       part = 0;

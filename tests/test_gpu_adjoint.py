@@ -1,0 +1,80 @@
+"""Hand-written GPU adjoint of the CCSD residual: against torch autograd of the
+restated contractions and against central finite differences (step 1e-5)."""
+import numpy as np
+import pytest
+
+from oracle import autodiff
+from scess_gb300.synthetic import convergent_sigma, make_workload
+from tests.gpu_common import gctx, rel_err  # noqa: F401
+
+pytestmark = pytest.mark.gpu
+
+
+def _point(o, v, seed=7):
+    w = make_workload(o, v, seed=seed, sigma=convergent_sigma(o, v))
+    rng = np.random.default_rng(seed)
+    t1 = 0.02 * rng.standard_normal((o, v))
+    t2 = 0.02 * rng.standard_normal((o, o, v, v))
+    g1 = rng.standard_normal((o, v))
+    g2 = rng.standard_normal((o, o, v, v))
+    return w, t1, t2, g1, g2
+
+
+@pytest.mark.parametrize('o,v', [(3, 7), (5, 19)])
+def test_vjp_matches_autograd(gctx, o, v):
+    w, t1, t2, g1, g2 = _point(o, v)
+    eri = w.eri()
+    rt1, rt2, re = autodiff.residual_vjp(eri, o, t1, t2, g1, g2)
+    gt1, gt2, ge = gctx.residual_vjp(eri, o, t1, t2, g1, g2, want_integrals=True)
+    assert rel_err(gt1, rt1) < 1e-11
+    assert rel_err(gt2, rt2) < 1e-11
+    assert rel_err(ge, re) < 1e-11
+
+
+def test_vjp_central_differences_64_directions(gctx):
+    o, v = 6, 30
+    w, t1, t2, g1, g2 = _point(o, v)
+    eri = w.eri()
+    gt1, gt2, ge = gctx.residual_vjp(eri, o, t1, t2, g1, g2, want_integrals=True)
+    rng = np.random.default_rng(11)
+    h = 1e-5
+    worst = 0.0
+    for _ in range(64):
+        d1, d2, de = (rng.standard_normal(x.shape) for x in (t1, t2, eri))
+
+        def f(s):
+            r1, r2 = gctx.residual(eri + s * de, o, t1 + s * d1, t2 + s * d2)
+            return float((r1 * g1).sum() + (r2 * g2).sum())
+        fd = (f(h) - f(-h)) / (2 * h)
+        an = float((gt1 * d1).sum() + (gt2 * d2).sum() + (ge * de).sum())
+        worst = max(worst, abs(fd - an) / max(abs(an), 1e-30))
+    assert worst <= 1e-6, worst
+
+
+def test_vjp_df_factors_central_differences(gctx):
+    o, v = 4, 12
+    w, t1, t2, g1, g2 = _point(o, v)
+    gt1, gt2, gB = gctx.residual_vjp(None, o, t1, t2, g1, g2, B=w.B, want_integrals=True)
+    rng = np.random.default_rng(5)
+    h = 1e-5
+    for _ in range(8):
+        dB = rng.standard_normal(w.B.shape)
+
+        def f(s):
+            from scess_gb300.synthetic import Workload
+            ws = Workload(w.o, w.v, w.naux, w.eps, w.B + s * dB)
+            r1, r2 = gctx.residual(ws.eri(), o, t1, t2)
+            return float((r1 * g1).sum() + (r2 * g2).sum())
+        fd = (f(h) - f(-h)) / (2 * h)
+        an = float((gB * dB).sum())
+        assert abs(fd - an) <= 1e-6 * max(abs(an), 1e-12)
+
+
+def test_vjp_mixed_close_to_fp64(gctx):
+    o, v = 10, 90
+    w, t1, t2, g1, g2 = _point(o, v)
+    eri = w.eri()
+    f1, f2, _ = gctx.residual_vjp(eri, o, t1, t2, g1, g2, precision='fp64')
+    m1, m2, _ = gctx.residual_vjp(eri, o, t1, t2, g1, g2, precision='mixed')
+    assert rel_err(m1, f1) < 1e-5
+    assert rel_err(m2, f2) < 1e-5
