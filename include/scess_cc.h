@@ -208,6 +208,27 @@ int scess_rccsd_residual_vjp_df(scess_ctx *ctx, const double *B, int64_t naux, i
                                 const double *g_r1, const double *g_r2, int32_t precision,
                                 double *g_t1, double *g_t2, double *g_B);
 
+/* CCSD Lambda (left-hand) equations at converged t1/t2 (no counterpart in the
+ * reference).  Omega(t; f) is the closed-shell residual with the Fock terms that
+ * UpdateAmplitudes drops for canonical orbitals (RCCSD.cpp:13-15, :109), the
+ * energy is E = 2 sum f_ia t_ia + sum L_oovv tau, and lambda solves
+ * dE/dt + (dOmega/dt)^T lambda = 0 on the closed-shell subspace
+ * t2(ijab) = t2(jiba) (l1: o*v, l2: o^2 v^2, l2 symmetric likewise).  Each iteration is
+ * one reverse sweep of the recorded residual on the GPU, with DIIS as in
+ * AmplitudeDIIS; convergence: rms(dlambda) < opts->amplitude_convergence.
+ * result->converged / iterations / last_rms are set. */
+int scess_rccsd_lambda(scess_ctx *ctx, const double *eri, const double *eps, int64_t nmo,
+                       int64_t nocc, const double *t1, const double *t2,
+                       const scess_rccsd_options *opts, double *l1_out, double *l2_out,
+                       scess_rccsd_result *result);
+/* Unrelaxed one-particle density (correlation part, spin-summed, MO basis,
+ * nmo x nmo symmetric, column-major): gamma_pq = dL/df_pq of the Lagrangian
+ * above, so that dE_CCSD = sum_pq gamma_pq df_pq for a symmetric change of the
+ * Fock matrix at fixed orbitals. */
+int scess_rccsd_rdm1(scess_ctx *ctx, const double *eri, const double *eps, int64_t nmo,
+                     int64_t nocc, const double *t1, const double *t2, const double *l1,
+                     const double *l2, int32_t precision, double *dm1_out);
+
 /* General binary contraction C = alpha * A.B + beta * C on the GPU, the
  * runtime counterpart of the tensor layer's compile-time Einsum
  * (src/Tensor/TensorEinsum.h:170-205): spec like "kcld,ilcd->ki", each

@@ -9,7 +9,8 @@ Hirata 2004 / PySCF ``rccsd.update_amps`` before it drops f_ov and the
 off-diagonal Fock).  At f = diag(eps) they reduce to R(t) - D t.
 
 * E(t; f) = 2 sum_ia f_ia t_ia + sum L_oovv tau
-* Lagrangian L = E + lambda . Omega(t; f); Lambda equations dL/dt = 0
+* Lagrangian L = E + lambda . Omega(t; f); Lambda equations dL/dt = 0 on the
+  closed-shell subspace t2(ijab) = t2(jiba) (lambda2 likewise symmetric)
 * unrelaxed one-particle density (correlation part, spin-summed, orbitals
   fixed): gamma_pq = dL/df_pq = dE_CCSD/df_pq
 """
@@ -92,6 +93,9 @@ def solve_lambda(eri, f, o, t1, t2, tol=1e-11, maxit=300):
     l1, l2 = gE1 / d1, gE2 / d2
     for _ in range(maxit):
         j1, j2 = torch.autograd.grad((r1, r2), (T1, T2), (l1, l2), retain_graph=True)
+        # t2 is constrained to t2(ijab) = t2(jiba): the stationarity condition is the
+        # symmetric part of the gradient (the antisymmetric subspace is unstable)
+        j2 = 0.5 * (j2 + j2.permute(1, 0, 3, 2))
         n1 = l1 + (gE1 + j1) / d1
         n2 = l2 + (gE2 + j2) / d2
         ch = float(torch.sqrt(((n1 - l1) ** 2).sum() + ((n2 - l2) ** 2).sum()))

@@ -107,6 +107,10 @@ EXPORTS = {
                                            _dp, C.c_int32, _dp, _dp, _dp]),
     'scess_rccsd_residual_vjp_df': (C.c_int, [C.c_void_p, _dp, C.c_int64, C.c_int64, C.c_int64,
                                               _dp, _dp, _dp, _dp, C.c_int32, _dp, _dp, _dp]),
+    'scess_rccsd_lambda': (C.c_int, [C.c_void_p, _dp, _dp, C.c_int64, C.c_int64, _dp, _dp,
+                                     C.POINTER(Options), _dp, _dp, C.POINTER(Result)]),
+    'scess_rccsd_rdm1': (C.c_int, [C.c_void_p, _dp, _dp, C.c_int64, C.c_int64, _dp, _dp, _dp, _dp,
+                                   C.c_int32, _dp]),
     'scess_einsum': (C.c_int, [C.c_void_p, C.c_char_p, C.c_double, _dp, C.c_int32, _i64p, _dp,
                                C.c_int32, _i64p, C.c_double, _dp, C.c_int32, _i64p, C.c_int32]),
 }
@@ -363,6 +367,36 @@ class Context:
                                                    _ptr(gI))
         self._check(st, 'scess_rccsd_residual_vjp')
         return gt1, gt2, gI
+
+    # -- Lambda equations and the one-particle density ---------------------------------------
+    def lambda_solve(self, eri, eps, nocc, t1, t2, precision='fp64', **opts):
+        eps = _f64(eps)
+        N = eps.shape[0]
+        o, v = int(nocc), N - int(nocc)
+        op = self.default_options()
+        op.precision = PRECISION[precision]
+        for k, val in opts.items():
+            setattr(op, k, val)
+        l1 = np.zeros((o, v), order='F')
+        l2 = np.zeros((o, o, v, v), order='F')
+        res = Result()
+        st = self.lib.scess_rccsd_lambda(self.h, _ptr(_f64(eri, (N, N, N, N))), _ptr(eps), N, o,
+                                         _ptr(_f64(t1, (o, v))), _ptr(_f64(t2, (o, o, v, v))),
+                                         C.byref(op), _ptr(l1), _ptr(l2), C.byref(res))
+        self._check(st, 'scess_rccsd_lambda')
+        return l1, l2, res
+
+    def rdm1(self, eri, eps, nocc, t1, t2, l1, l2, precision='fp64'):
+        eps = _f64(eps)
+        N = eps.shape[0]
+        o, v = int(nocc), N - int(nocc)
+        dm = np.zeros((N, N), order='F')
+        st = self.lib.scess_rccsd_rdm1(self.h, _ptr(_f64(eri, (N, N, N, N))), _ptr(eps), N, o,
+                                       _ptr(_f64(t1, (o, v))), _ptr(_f64(t2, (o, o, v, v))),
+                                       _ptr(_f64(l1, (o, v))), _ptr(_f64(l2, (o, o, v, v))),
+                                       PRECISION[precision], _ptr(dm))
+        self._check(st, 'scess_rccsd_rdm1')
+        return dm
 
     # -- generic contraction ------------------------------------------------------------------
     def einsum(self, spec: str, A, B, C_init=None, alpha=1.0, beta=0.0, precision='fp64',

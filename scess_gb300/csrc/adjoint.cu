@@ -172,7 +172,10 @@ namespace scess {
 
 namespace {
 
-// l_out = l + (dE + g) / D with D_ia = e_i - e_a, D_ijab = D_ia + D_jb.
+// l_out = l + (dE + g) / D with D_ia = e_i - e_a, D_ijab = D_ia + D_jb.  The
+// closed-shell doubles are constrained to t2(ijab) = t2(jiba), so only the
+// symmetric part of the t2 gradient enters (its antisymmetric part is not a
+// stationarity condition and the iteration is unstable on it).
 __global__ void lambda_step_kernel(int64_t o, int64_t v, const double *__restrict__ eps,
                                    const double *__restrict__ l, const double *__restrict__ dE,
                                    const double *__restrict__ g, double *__restrict__ out) {
@@ -187,6 +190,9 @@ __global__ void lambda_step_kernel(int64_t o, int64_t v, const double *__restric
       const int64_t x = e - n1;
       const int64_t i = x % o, j = (x / o) % o, a = (x / (o * o)) % v, b = x / (o * o * v);
       d = (eps[i] - eps[o + a]) + (eps[j] - eps[o + b]);
+      const int64_t xt = j + o * i + o * o * b + o * o * v * a;
+      out[e] = l[e] + (dE[e] + 0.5 * (g[e] + g[n1 + xt])) / d;
+      continue;
     }
     out[e] = l[e] + (dE[e] + g[e]) / d;
   }

@@ -49,8 +49,9 @@ namespace scess {
 // drops for canonical orbitals (RCCSD.cpp:13-15, :109); at f = diag(eps) they
 // equal -D t.  With E(t; f) = 2 sum f_ia t_ia + sum L_oovv tau and the
 // Lagrangian L = E + lambda . Omega, the Lambda equations are
-// dE/dt + (dOmega/dt)^T lambda = 0 (solved by lambda += (dE/dt + J^T lambda)/D
-// with DIIS), and gamma_pq = dL/df_pq.
+// dE/dt + (dOmega/dt)^T lambda = 0 on the closed-shell subspace
+// t2(ijab) = t2(jiba) (solved by lambda += (dE/dt + J^T lambda)/D with the t2
+// part of J^T lambda symmetrised, plus DIIS), and gamma_pq = dL/df_pq.
 struct LambdaResult {
   int converged = 0, iterations = 0;
   double last_rms = 0.0;

@@ -522,6 +522,73 @@ int scess_rccsd_residual_vjp_df(scess_ctx *ctx, const double *B, int64_t naux, i
                              g_t2, nullptr, g_B);
 }
 
+int scess_rccsd_lambda(scess_ctx *ctx, const double *eri, const double *eps, int64_t nmo,
+                       int64_t nocc, const double *t1, const double *t2,
+                       const scess_rccsd_options *opts, double *l1_out, double *l2_out,
+                       scess_rccsd_result *result) {
+  if (!eri) return SCESS_ERR_INVALID;
+  return guard(ctx, [&](scess::Ctx &c) {
+    check_shape(nmo, nocc);
+    need(eps, "eps");
+    need(t1, "t1");
+    need(t2, "t2");
+    need(l1_out, "l1_out");
+    need(l2_out, "l2_out");
+    host_finite(eps, nmo, "eps");
+    scess_rccsd_options o;
+    if (opts) o = *opts;
+    else scess_rccsd_default_options(&o);
+    const int64_t oc = nocc, v = nmo - nocc, n1 = oc * v, n2 = oc * oc * v * v;
+    scess::Control ctl;
+    ctl.cancel = c.cancel;
+    ctl.user = c.user;
+    ctl.time_limit_s = o.time_limit_s;
+    scess::DTensor d_eri = device_eri(c, eri, nullptr, 0, nmo);
+    scess::DTensor amp({n1 + n2}), lam({n1 + n2});
+    scess::upload(c, amp.p(), t1, n1);
+    scess::upload(c, amp.p() + n1, t2, n2);
+    const scess::Backend be =
+        o.precision == SCESS_PRECISION_MIXED ? scess::Backend::MIXED : scess::Backend::FP64;
+    const scess::LambdaResult r =
+        scess::rccsd_lambda(c, d_eri.p(), eps, nmo, nocc, amp.p(), o, be, ctl, lam.p());
+    scess::download(c, l1_out, lam.p(), n1);
+    scess::download(c, l2_out, lam.p() + n1, n2);
+    if (result) {
+      std::memset(result, 0, sizeof(*result));
+      result->converged = r.converged;
+      result->iterations = r.iterations;
+      result->last_rms = r.last_rms;
+    }
+  });
+}
+
+int scess_rccsd_rdm1(scess_ctx *ctx, const double *eri, const double *eps, int64_t nmo,
+                     int64_t nocc, const double *t1, const double *t2, const double *l1,
+                     const double *l2, int32_t precision, double *dm1_out) {
+  if (!eri) return SCESS_ERR_INVALID;
+  return guard(ctx, [&](scess::Ctx &c) {
+    check_shape(nmo, nocc);
+    need(eps, "eps");
+    need(t1, "t1");
+    need(t2, "t2");
+    need(l1, "l1");
+    need(l2, "l2");
+    need(dm1_out, "dm1_out");
+    const int64_t oc = nocc, v = nmo - nocc, n1 = oc * v, n2 = oc * oc * v * v;
+    scess::DTensor d_eri = device_eri(c, eri, nullptr, 0, nmo);
+    scess::DTensor amp({n1 + n2}), lam({n1 + n2}), dm({nmo, nmo});
+    scess::upload(c, amp.p(), t1, n1);
+    scess::upload(c, amp.p() + n1, t2, n2);
+    scess::upload(c, lam.p(), l1, n1);
+    scess::upload(c, lam.p() + n1, l2, n2);
+    scess::rccsd_rdm1(c, d_eri.p(), eps, nmo, nocc, amp.p(), lam.p(),
+                      precision == SCESS_PRECISION_MIXED ? scess::Backend::MIXED
+                                                         : scess::Backend::FP64,
+                      dm.p());
+    scess::download(c, dm1_out, dm.p(), nmo * nmo);
+  });
+}
+
 int scess_einsum(scess_ctx *ctx, const char *spec, double alpha, const double *A, int32_t a_nd,
                  const int64_t *a_ext, const double *B, int32_t b_nd, const int64_t *b_ext,
                  double beta, double *C, int32_t c_nd, const int64_t *c_ext, int32_t precision) {

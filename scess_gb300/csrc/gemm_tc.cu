@@ -155,30 +155,50 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
   for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// K segment of a tensor-core problem: operand maps, K blocks, lo offset and the
+// first A/B row of problem (y, z): row0 + y * row_y + z * row_z.
+struct TcSegArgs {
+  int mapA, mapB;
+  int nkb;   // K blocks of 64
+  int kpad;  // lo offset in the packed rows (elements)
+  int negA;  // negate this segment's products
+  int64_t rowA0, rowAy, rowAz, rowB0, rowBy, rowBz;
+};
+
+struct TcMaps {
+  CUtensorMap m[6];
+};
+
 struct TcArgs {
-  int rowA0, rowB0, M, N;
-  int nkb;           // K blocks (of 64) per segment
-  int nseg;          // 1 (hi only) or 3 (lo*hi, hi*lo, hi*hi)
-  int kb_per_split;  // K blocks per work unit along K
-  int tiles_m, tiles_n, splits;
-  int Kpad;          // lo offset in the packed rows
+  int M, N;
+  int tiles_m, tiles_n;
+  int ny, nz;        // problems: (y, z) in [0, ny) x [0, nz)
+  int nseg;          // K segments (<= 4)
+  int kb_total;      // sum of the segments' K blocks
+  int kb_per_split;  // K blocks per work unit (split-K when < kb_total)
+  int splits;
   int f16;           // operands are FP16 (else BF16)
+  int split3;        // three hi/lo products (else hi*hi only)
+  TcSegArgs seg[4];
+  int64_t cy, cz;    // output offset of problem (y, z): y * cy + z * cz
   float *partial;    // split-K partials (nullptr: direct epilogue)
   int64_t part_stride;
   unsigned *err;
 };
 
-// Persistent tcgen05 GEMM, one 128 x 128 output tile per work unit.
+// Persistent tcgen05 GEMM over work units (problem, 128 x 128 output tile, K range).
 //   warp 0     TMA producer: per 64-wide K block one smem stage holding A_hi,
 //              A_lo, B_hi, B_lo (128 rows x 128 B each, 128B swizzle);
 //   warp 1     TMEM owner + MMA issuer: the block's products lo*hi, hi*lo,
 //              hi*hi (4 x K=16 each) go into one of two 128-column TMEM
 //              buffers, starting from zero, then tcgen05.commit;
 //   warps 2-5  drain each buffer into an FP32 register accumulator (one row
-//              per thread, round-to-nearest adds) and, after the last K block
-//              of the unit, scatter alpha*acc + beta*C through the tables.
+//              per thread, round-to-nearest adds) and, after the unit's last K
+//              block, scatter alpha*acc + beta*C through the offset tables.
 // Draining every K block bounds the truncating accumulation inside TMEM to
 // the 12 products of one block, so the result's error does not grow with K.
+// A problem's K range may span several segments with different operands
+// (up to 4), each optionally negated through the instruction descriptor.
 constexpr int V2_BN = 128;
 constexpr int V2_STAGES = 3;
 constexpr uint32_t V2_TILE_BYTES = 128 * TC_BK * 2;  // 16 KiB: 128 rows x 128 B
@@ -187,9 +207,17 @@ constexpr uint32_t V2_TMEM_COLS = 2 * V2_BN;
 constexpr size_t V2_SMEM_BYTES = 1024 + V2_STAGES * V2_STAGE_BYTES + (2 * V2_STAGES + 5) * 8 + 8 +
                                  V2_BN * 8;
 
+__device__ __forceinline__ void seg_of(const TcArgs &a, int kb, int &s, int &lkb) {
+  s = 0;
+  lkb = kb;
+  while (s < a.nseg - 1 && lkb >= a.seg[s].nkb) {
+    lkb -= a.seg[s].nkb;
+    s++;
+  }
+}
+
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                   TcOut out, TcArgs a) {
+    tc_gemm_kernel(const __grid_constant__ TcMaps maps, TcOut out, TcArgs a) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t *full = (uint64_t *)(smem + V2_STAGES * V2_STAGE_BYTES);
@@ -201,8 +229,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   int64_t *colOff = (int64_t *)(tmem_slot + 2);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int units = a.tiles_m * a.tiles_n * a.splits;
-  const bool split3 = a.nseg == 3;
+  const int tiles = a.tiles_m * a.tiles_n;
+  const int nprob = a.ny * a.nz;
+  const int units = tiles * nprob * a.splits;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < V2_STAGES; s++) {
@@ -229,40 +258,50 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  auto unit_coords = [&](int u, int &tm, int &tn, int &kb0, int &kb1) {
-    const int tile = u % (a.tiles_m * a.tiles_n);
-    const int sp = u / (a.tiles_m * a.tiles_n);
+  // unit -> (tile m, tile n, problem y, z, K-block range)
+  auto unit_coords = [&](int u, int &tm, int &tn, int &py, int &pz, int &kb0, int &kb1) {
+    const int tile = u % tiles;
+    const int rest = u / tiles;
+    const int q = rest % nprob;
+    const int sp = rest / nprob;
     tn = tile % a.tiles_n;
     tm = tile / a.tiles_n;
+    py = q % a.ny;
+    pz = q / a.ny;
     kb0 = sp * a.kb_per_split;
-    kb1 = min(a.nkb, kb0 + a.kb_per_split);
+    kb1 = min(a.kb_total, kb0 + a.kb_per_split);
   };
 
   if (warp == 0) {
     if (lane == 0) {
-      asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmA) : "memory");
-      asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmB) : "memory");
-      const uint32_t bytes = split3 ? V2_STAGE_BYTES : 2 * V2_TILE_BYTES;
+      for (int i = 0; i < 6; i++)
+        asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&maps.m[i]) : "memory");
+      const uint32_t bytes = a.split3 ? V2_STAGE_BYTES : 2 * V2_TILE_BYTES;
       int g = 0;
       int last[V2_STAGES];
       for (int s = 0; s < V2_STAGES; s++) last[s] = -1;
       bool ok = true;
       for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
-        int tm, tn, kb0, kb1;
-        unit_coords(u, tm, tn, kb0, kb1);
-        const int ya = a.rowA0 + tm * TC_BM, yb = a.rowB0 + tn * V2_BN;
+        int tm, tn, py, pz, kb0, kb1;
+        unit_coords(u, tm, tn, py, pz, kb0, kb1);
         for (int kb = kb0; kb < kb1; kb++, g++) {
+          int sg, lkb;
+          seg_of(a, kb, sg, lkb);
+          const TcSegArgs &S = a.seg[sg];
+          const int ya = (int)(S.rowA0 + py * S.rowAy + pz * S.rowAz) + tm * TC_BM;
+          const int yb = (int)(S.rowB0 + py * S.rowBy + pz * S.rowBz) + tn * V2_BN;
           const int s = g % V2_STAGES;
           const uint32_t ph = (uint32_t)(g / V2_STAGES) & 1u;
           if (!mbar_wait(&empty[s], ph ^ 1u, a.err, ERR_EMPTY_WAIT)) { ok = false; break; }
           uint8_t *st = smem + s * V2_STAGE_BYTES;
+          const CUtensorMap *mA = &maps.m[S.mapA], *mB = &maps.m[S.mapB];
           mbar_expect_tx(&full[s], bytes);
-          const int x = kb * TC_BK;
-          tma_load_2d(st, &tmA, x, ya, &full[s]);                          // A hi
-          tma_load_2d(st + V2_TILE_BYTES, &tmB, x, yb, &full[s]);          // B hi
-          if (split3) {
-            tma_load_2d(st + 2 * V2_TILE_BYTES, &tmA, a.Kpad + x, ya, &full[s]);  // A lo
-            tma_load_2d(st + 3 * V2_TILE_BYTES, &tmB, a.Kpad + x, yb, &full[s]);  // B lo
+          const int x = lkb * TC_BK;
+          tma_load_2d(st, mA, x, ya, &full[s]);                          // A hi
+          tma_load_2d(st + V2_TILE_BYTES, mB, x, yb, &full[s]);          // B hi
+          if (a.split3) {
+            tma_load_2d(st + 2 * V2_TILE_BYTES, mA, S.kpad + x, ya, &full[s]);  // A lo
+            tma_load_2d(st + 3 * V2_TILE_BYTES, mB, S.kpad + x, yb, &full[s]);  // B lo
           }
           last[s] = g;
         }
@@ -276,9 +315,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       int g = 0, c = 0;
       bool ok = true;
       for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
-        int tm, tn, kb0, kb1;
-        unit_coords(u, tm, tn, kb0, kb1);
+        int tm, tn, py, pz, kb0, kb1;
+        unit_coords(u, tm, tn, py, pz, kb0, kb1);
         for (int kb = kb0; kb < kb1; kb++, g++, c++) {
+          int sg, lkb;
+          seg_of(a, kb, sg, lkb);
+          const uint32_t id = idesc | (a.seg[sg].negA ? (1u << 13) : 0u);  // negate A
           const int s = g % V2_STAGES;
           const uint32_t ph = (uint32_t)(g / V2_STAGES) & 1u;
           const int b = c & 1;
@@ -291,17 +333,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           const uint32_t alo = st + 2 * V2_TILE_BYTES, blo = st + 3 * V2_TILE_BYTES;
           const uint32_t d = tmem + (uint32_t)(b * V2_BN);
           uint32_t acc = 0;
-          if (split3) {
+          if (a.split3) {
 #pragma unroll
             for (int k = 0; k < TC_BK / 16; k++, acc = 1)
-              mma_bf16(d, sw128_desc(alo + 32 * k), sw128_desc(bhi + 32 * k), idesc, acc);
+              mma_bf16(d, sw128_desc(alo + 32 * k), sw128_desc(bhi + 32 * k), id, acc);
 #pragma unroll
             for (int k = 0; k < TC_BK / 16; k++)
-              mma_bf16(d, sw128_desc(ahi + 32 * k), sw128_desc(blo + 32 * k), idesc, 1u);
+              mma_bf16(d, sw128_desc(ahi + 32 * k), sw128_desc(blo + 32 * k), id, 1u);
           }
 #pragma unroll
           for (int k = 0; k < TC_BK / 16; k++, acc = 1)
-            mma_bf16(d, sw128_desc(ahi + 32 * k), sw128_desc(bhi + 32 * k), idesc, acc);
+            mma_bf16(d, sw128_desc(ahi + 32 * k), sw128_desc(bhi + 32 * k), id, acc);
           mma_commit(&empty[s]);
           mma_commit(&tfull[b]);
         }
@@ -317,14 +359,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     int c = 0;
     bool ok = true;
     for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
-      int tm, tn, kb0, kb1;
-      unit_coords(u, tm, tn, kb0, kb1);
+      int tm, tn, py, pz, kb0, kb1;
+      unit_coords(u, tm, tn, py, pz, kb0, kb1);
       const int m = tm * TC_BM + row;
       const int n0 = tn * V2_BN;
       asm volatile("bar.sync 1, 128;" ::: "memory");  // previous unit's colOff reads done
       if (!a.partial) {
         const int nn = n0 + et;
-        colOff[et] = nn < a.N ? out.baseC + out.colC[nn] : -1;
+        colOff[et] = nn < a.N ? out.baseC + py * a.cy + pz * a.cz + out.colC[nn] : -1;
       }
       float acc[V2_BN];
 #pragma unroll
@@ -350,7 +392,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       if (!ok || *(volatile unsigned *)a.err) break;
       if (m >= a.M) continue;
       if (a.partial) {
-        const int sp = u / (a.tiles_m * a.tiles_n);
+        const int sp = u / (tiles * nprob);
         float *P = a.partial + (int64_t)sp * a.part_stride;
 #pragma unroll
         for (int j = 0; j < V2_BN; j++) {
@@ -588,54 +630,98 @@ CUtensorMap TcEngine::map_of(const Packed &p, int box_rows) {
   return make_map(p.p(), p.rows_pad, p.Kpad, box_rows, p.fmt);
 }
 
-void tc_gemm_launch_maps(const CUtensorMap &ma, const CUtensorMap &mb, int64_t Kpad, int64_t rowA0,
-                         int64_t M, int64_t rowB0, int64_t N, int bn, TcFormat fmt,
-                         const TcOut &out, int nseg, int splits, float *partial, unsigned *err,
-                         cudaStream_t stream) {
-  (void)bn;
+void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &out, int nseg,
+                            int splits, float *partial, unsigned *err, cudaStream_t stream) {
   static std::once_flag once;
   std::call_once(once, [] {
     cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)V2_SMEM_BYTES);
   });
-  if (M <= 0 || N <= 0) return;
-  if (Kpad % TC_BK != 0 || Kpad <= 0) throw Error(SCESS_ERR_INVALID, "tc_gemm: Kpad % 64");
-  if (M > INT32_MAX || N > INT32_MAX || rowA0 + M > INT32_MAX || rowB0 + N > INT32_MAX ||
-      2 * Kpad > INT32_MAX)
-    throw Error(SCESS_ERR_INVALID, "tc_gemm: dimension too large");
+  if (ps.M <= 0 || ps.N <= 0 || ps.ny <= 0 || ps.nz <= 0) return;
   if (nseg != 1 && nseg != 3) throw Error(SCESS_ERR_INVALID, "tc_gemm: nseg");
-  const int nkb = (int)(Kpad / TC_BK);
-  if (splits < 1) splits = 1;
-  if (splits > nkb) splits = nkb;
-  const int kbs = (int)ceil_div(nkb, splits);
-  splits = (int)ceil_div(nkb, kbs);
+  if (ps.nseg < 1 || ps.nseg > 4) throw Error(SCESS_ERR_INVALID, "tc_gemm: segments");
+  if (ps.M > INT32_MAX || ps.N > INT32_MAX) throw Error(SCESS_ERR_INVALID, "tc_gemm: dimension too large");
   TcArgs a;
-  a.rowA0 = (int)rowA0;
-  a.rowB0 = (int)rowB0;
-  a.M = (int)M;
-  a.N = (int)N;
-  a.nkb = nkb;
-  a.nseg = nseg;
+  std::memset(&a, 0, sizeof(a));
+  a.M = (int)ps.M;
+  a.N = (int)ps.N;
+  a.tiles_m = (int)ceil_div(ps.M, TC_BM);
+  a.tiles_n = (int)ceil_div(ps.N, V2_BN);
+  a.ny = ps.ny;
+  a.nz = ps.nz;
+  a.nseg = ps.nseg;
+  int kbt = 0;
+  for (int s = 0; s < ps.nseg; s++) {
+    const TcSegment &g = ps.seg[s];
+    if (g.Kpad % TC_BK != 0 || g.Kpad <= 0 || 2 * g.Kpad > INT32_MAX)
+      throw Error(SCESS_ERR_INVALID, "tc_gemm: Kpad % 64");
+    const int64_t maxA = g.rowA0 + (int64_t)(ps.ny - 1) * g.rowAy + (int64_t)(ps.nz - 1) * g.rowAz +
+                         a.tiles_m * TC_BM;
+    const int64_t maxB = g.rowB0 + (int64_t)(ps.ny - 1) * g.rowBy + (int64_t)(ps.nz - 1) * g.rowBz +
+                         a.tiles_n * V2_BN;
+    if (maxA > INT32_MAX || maxB > INT32_MAX || g.rowA0 < 0 || g.rowB0 < 0)
+      throw Error(SCESS_ERR_INVALID, "tc_gemm: row coordinates");
+    a.seg[s].mapA = g.mapA;
+    a.seg[s].mapB = g.mapB;
+    a.seg[s].nkb = (int)(g.Kpad / TC_BK);
+    a.seg[s].kpad = (int)g.Kpad;
+    a.seg[s].negA = g.negate ? 1 : 0;
+    a.seg[s].rowA0 = g.rowA0;
+    a.seg[s].rowAy = g.rowAy;
+    a.seg[s].rowAz = g.rowAz;
+    a.seg[s].rowB0 = g.rowB0;
+    a.seg[s].rowBy = g.rowBy;
+    a.seg[s].rowBz = g.rowBz;
+    kbt += a.seg[s].nkb;
+  }
+  a.kb_total = kbt;
+  if (splits < 1) splits = 1;
+  if (ps.ny * ps.nz > 1) splits = 1;
+  if (splits > kbt) splits = kbt;
+  const int kbs = (int)ceil_div(kbt, splits);
+  splits = (int)ceil_div(kbt, kbs);
   a.kb_per_split = kbs;
-  a.tiles_m = (int)ceil_div(M, TC_BM);
-  a.tiles_n = (int)ceil_div(N, V2_BN);
   a.splits = splits;
-  a.Kpad = (int)Kpad;
   a.f16 = fmt == TcFormat::FP16 ? 1 : 0;
+  a.split3 = nseg == 3 ? 1 : 0;
+  a.cy = ps.cy;
+  a.cz = ps.cz;
   a.partial = splits > 1 ? partial : nullptr;
-  a.part_stride = M * N;
+  a.part_stride = ps.M * ps.N;
   a.err = err;
   if (splits > 1 && !partial) throw Error(SCESS_ERR_INVALID, "tc_gemm: split-K needs partials");
-  const int64_t units = (int64_t)a.tiles_m * a.tiles_n * splits;
+  TcMaps maps;
+  for (int i = 0; i < 6; i++) maps.m[i] = ps.maps[std::min(i, ps.nmaps - 1)];
+  const int64_t units = (int64_t)a.tiles_m * a.tiles_n * ps.ny * ps.nz * splits;
   const unsigned grid = (unsigned)std::min<int64_t>(units, kNumSMs);
-  tc_gemm_kernel<<<grid, TC_THREADS, V2_SMEM_BYTES, stream>>>(ma, mb, out, a);
+  tc_gemm_kernel<<<grid, TC_THREADS, V2_SMEM_BYTES, stream>>>(maps, out, a);
   SCESS_CHECK_LAUNCH();
   if (splits > 1) {
-    const int64_t MN = M * N;
+    const int64_t MN = ps.M * ps.N;
     tc_reduce_kernel<<<(unsigned)std::min<int64_t>(ceil_div(MN, 256), 8192), 256, 0, stream>>>(
-        out, M, N, splits, partial);
+        out, ps.M, ps.N, splits, partial);
     SCESS_CHECK_LAUNCH();
   }
+}
+
+void tc_gemm_launch_maps(const CUtensorMap &ma, const CUtensorMap &mb, int64_t Kpad, int64_t rowA0,
+                         int64_t M, int64_t rowB0, int64_t N, int bn, TcFormat fmt,
+                         const TcOut &out, int nseg, int splits, float *partial, unsigned *err,
+                         cudaStream_t stream) {
+  (void)bn;
+  TcProblemSet ps;
+  ps.maps[0] = ma;
+  ps.maps[1] = mb;
+  ps.nmaps = 2;
+  ps.M = M;
+  ps.N = N;
+  ps.nseg = 1;
+  ps.seg[0].mapA = 0;
+  ps.seg[0].mapB = 1;
+  ps.seg[0].Kpad = Kpad;
+  ps.seg[0].rowA0 = rowA0;
+  ps.seg[0].rowB0 = rowB0;
+  tc_gemm_launch_grouped(ps, fmt, out, nseg, splits, partial, err, stream);
 }
 
 void TcEngine::gemm_maps(const CUtensorMap &ma, const CUtensorMap &mb, int64_t Kpad, int64_t Kreal,
@@ -657,6 +743,13 @@ TcEngine::TcEngine(Ctx &ctx) : ctx_(ctx) {
 }
 
 TcEngine::~TcEngine() = default;
+
+void TcEngine::gemm_grouped(const TcProblemSet &ps, const TcOut &out, double flops,
+                            const char *name, cudaStream_t stream) {
+  TimedScope ts(ctx_.timer, name, flops, 0.0, stream ? stream : ctx_.stream);
+  tc_gemm_launch_grouped(ps, fmt_, out, 3, 1, nullptr, err_.as<unsigned>(),
+                         stream ? stream : ctx_.stream);
+}
 
 bool TcEngine::worth_it(const EinsumPlan &pl) {
   const int64_t mx = std::max(pl.M, pl.N), mn = std::min(pl.M, pl.N);

@@ -47,6 +47,28 @@ struct TcOut {
   const double *scaleA = nullptr, *scaleB = nullptr;
 };
 
+// A launch of several same-shaped GEMMs ("problems" (y, z) in [0,ny) x [0,nz)),
+// each summing up to four K segments whose operands are rows of packed
+// tensors: segment s of problem (y, z) multiplies rows
+// rowA0 + y rowAy + z rowAz (+ m) of maps[mapA] with rows
+// rowB0 + y rowBy + z rowBz (+ n) of maps[mapB] over Kpad columns, negated
+// when `negate`.  Problem (y, z) writes at offset y cy + z cz (plus the tables).
+struct TcSegment {
+  int mapA = 0, mapB = 1;
+  int64_t Kpad = 0;
+  bool negate = false;
+  int64_t rowA0 = 0, rowAy = 0, rowAz = 0, rowB0 = 0, rowBy = 0, rowBz = 0;
+};
+struct TcProblemSet {
+  CUtensorMap maps[6];
+  int nmaps = 0;
+  int64_t M = 0, N = 0;
+  int ny = 1, nz = 1;
+  int nseg = 1;
+  TcSegment seg[4];
+  int64_t cy = 0, cz = 0;
+};
+
 class TcEngine {
  public:
   explicit TcEngine(Ctx &ctx);
@@ -76,6 +98,9 @@ class TcEngine {
     out.scaleB = B.scale();
   }
   // gemm() with prebuilt descriptors (mb must use box_rows == tile_n(N)); no split-K.
+  // Grouped launch (see TcProblemSet); flops: algorithmic FLOPs for the timer.
+  void gemm_grouped(const TcProblemSet &ps, const TcOut &out, double flops, const char *name,
+                    cudaStream_t stream = nullptr);
   // Kreal: the unpadded K (algorithmic FLOPs for the kernel timer).
   void gemm_maps(const CUtensorMap &ma, const CUtensorMap &mb, int64_t Kpad, int64_t Kreal,
                  int64_t rowA0, int64_t M, int64_t rowB0, int64_t N, const TcOut &out,
@@ -101,6 +126,8 @@ class TcEngine {
 };
 
 // Raw launchers.
+void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &out, int nseg,
+                            int splits, float *partial, unsigned *err, cudaStream_t stream);
 void tc_gemm_launch_maps(const CUtensorMap &ma, const CUtensorMap &mb, int64_t Kpad, int64_t rowA0,
                          int64_t M, int64_t rowB0, int64_t N, int bn, TcFormat fmt,
                          const TcOut &out, int nseg, int splits, float *partial, unsigned *err,
