@@ -42,6 +42,7 @@ extern "C" {
 #define SCESS_ERR_CANCELLED 4   /* cancel callback returned non-zero           */
 #define SCESS_ERR_TIMEOUT 5     /* options.time_limit_s exceeded               */
 #define SCESS_ERR_UNSUPPORTED 6 /* no sm_103a device / feature not available   */
+#define SCESS_ERR_TOO_LARGE 7   /* scess_einsum_static: beyond its fixed scratch */
 
 /* Arithmetic of the contractions. FP64 is the drop-in path (matches the
  * reference to <= 1e-9 Eh); MIXED runs the contractions on BF16 tensor cores
@@ -239,6 +240,38 @@ int scess_rccsd_rdm1(scess_ctx *ctx, const double *eri, const double *eps, int64
 int scess_einsum(scess_ctx *ctx, const char *spec, double alpha, const double *A, int32_t a_nd,
                  const int64_t *a_ext, const double *B, int32_t b_nd, const int64_t *b_ext,
                  double beta, double *C, int32_t c_nd, const int64_t *c_ext, int32_t precision);
+
+/* scess_einsum's FP64 contraction for callers that cannot allocate device
+ * memory.  No counterpart in the reference.  Some host programs own every byte
+ * of the GPU: a framework whose caching allocator has reserved the device's
+ * memory, or an application that hands out a fixed arena at start-up and
+ * forbids allocations later, because cudaMalloc and cudaFree can synchronise
+ * the device and fail once that memory is spoken for.  This entry point
+ * allocates nothing and needs no context: A, B and C are the caller's DEVICE
+ * buffers (dense, column-major, extents as for scess_einsum), and the work is
+ * queued on `stream` (a cudaStream_t; NULL is the default stream) of the
+ * current device.  It returns once the work is queued; C is ready when the
+ * stream reaches that point.
+ *
+ * Its scratch (the contraction's offset tables and split-K partial sums) is
+ * one 16 MiB array inside this library, which every GPU that loads the
+ * library holds until the process exits.  The tables need 16 (M + N + K)
+ * bytes, M, N and K being the products of the extents of A's free labels, B's
+ * free labels and the summed labels; a contraction with M + N + K above
+ * 1,048,576 returns SCESS_ERR_TOO_LARGE and queues nothing.  Split-K uses what
+ * the tables leave, with fewer splits (down to none) when that is too small.
+ * Every call uses the same array and leaves its contents behind: calls whose
+ * work overlaps on the GPU (other streams, other host threads) race on it, so
+ * order them on one stream.  No part of it needs to start at zero: a call
+ * writes all the scratch it reads before reading it.  The first call on a
+ * device looks up the array's device address on that device (the CUDA runtime
+ * loads the library's device code there); make that first call before any
+ * stream capture.  Returns SCESS_ERR_INVALID for a bad spec, extents or null
+ * pointers, SCESS_ERR_CUDA for a failed launch. */
+int scess_einsum_static(const char *spec, double alpha, const double *A, int32_t a_nd,
+                        const int64_t *a_ext, const double *B, int32_t b_nd,
+                        const int64_t *b_ext, double beta, double *C, int32_t c_nd,
+                        const int64_t *c_ext, void *stream);
 
 #ifdef __cplusplus
 }

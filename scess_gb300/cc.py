@@ -36,6 +36,7 @@ SCESS_ERR_CUDA = 3
 SCESS_ERR_CANCELLED = 4
 SCESS_ERR_TIMEOUT = 5
 SCESS_ERR_UNSUPPORTED = 6
+SCESS_ERR_TOO_LARGE = 7
 PRECISION = {'fp64': 0, 'mixed': 1}
 
 
@@ -113,6 +114,9 @@ EXPORTS = {
                                    C.c_int32, _dp]),
     'scess_einsum': (C.c_int, [C.c_void_p, C.c_char_p, C.c_double, _dp, C.c_int32, _i64p, _dp,
                                C.c_int32, _i64p, C.c_double, _dp, C.c_int32, _i64p, C.c_int32]),
+    'scess_einsum_static': (C.c_int, [C.c_char_p, C.c_double, C.c_void_p, C.c_int32, _i64p,
+                                      C.c_void_p, C.c_int32, _i64p, C.c_double, C.c_void_p,
+                                      C.c_int32, _i64p, C.c_void_p]),
 }
 
 _lib = None
@@ -412,6 +416,20 @@ class Context:
                                    PRECISION[precision])
         self._check(st, 'scess_einsum')
         return Cf
+
+
+def einsum_static(spec: str, A_ptr: int, a_ext, B_ptr: int, b_ext, C_ptr: int, c_ext,
+                  alpha: float = 1.0, beta: float = 0.0, stream: int = 0) -> int:
+    """scess_einsum_static on device buffers given by address (column-major
+    extents as for Context.einsum), queued on `stream` (a cudaStream_t as int).
+    For callers that cannot allocate device memory: the library allocates
+    nothing here; its scratch is a fixed 16 MiB array.  Returns the status."""
+    lib = load_library()
+    ext = lambda e: (C.c_int64 * len(e))(*[int(x) for x in e])  # noqa: E731
+    return lib.scess_einsum_static(spec.encode(), float(alpha), C.c_void_p(A_ptr), len(a_ext),
+                                   ext(a_ext), C.c_void_p(B_ptr), len(b_ext), ext(b_ext),
+                                   float(beta), C.c_void_p(C_ptr), len(c_ext), ext(c_ext),
+                                   C.c_void_p(stream))
 
 
 class State:

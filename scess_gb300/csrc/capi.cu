@@ -164,6 +164,7 @@ const char *scess_status_string(int status) {
     case SCESS_ERR_CANCELLED: return "cancelled";
     case SCESS_ERR_TIMEOUT: return "time limit exceeded";
     case SCESS_ERR_UNSUPPORTED: return "unsupported";
+    case SCESS_ERR_TOO_LARGE: return "too large for the fixed scratch";
     default: return "unknown status";
   }
 }

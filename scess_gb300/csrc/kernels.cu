@@ -184,6 +184,32 @@ void dgemm_table(const TableGemm &g, double *workspace, cudaStream_t stream) {
   SCESS_CHECK_LAUNCH();
 }
 
+void dgemm_table_bounded(const TableGemm &g, double *workspace, int64_t ws_doubles,
+                         cudaStream_t stream) {
+  if (g.M <= 0 || g.N <= 0) return;
+  const unsigned rblocks = (unsigned)std::min<int64_t>(ceil_div(g.M * g.N, 256), 4096);
+  if (g.K <= 0) {
+    TableGemm h = g;
+    h.alpha = 0.0;
+    splitk_reduce_kernel<<<rblocks, 256, 0, stream>>>(h, 0, nullptr);
+    SCESS_CHECK_LAUNCH();
+    return;
+  }
+  int splits = choose_splits(g);
+  while (splits > 1 && (int64_t)splits * g.M * g.N > ws_doubles) splits--;
+  const int64_t kChunk = round_up(ceil_div(g.K, splits), BK);
+  const int nz = (int)ceil_div(g.K, kChunk);
+  dim3 grid((unsigned)ceil_div(g.M, BM), (unsigned)ceil_div(g.N, BN), (unsigned)nz);
+  if (nz > 1) {
+    dgemm_table_kernel<<<grid, 256, 0, stream>>>(g, kChunk, workspace);
+    SCESS_CHECK_LAUNCH();
+    splitk_reduce_kernel<<<rblocks, 256, 0, stream>>>(g, nz, workspace);
+  } else {
+    dgemm_table_kernel<<<grid, 256, 0, stream>>>(g, kChunk, nullptr);
+  }
+  SCESS_CHECK_LAUNCH();
+}
+
 // ---------------------------------------------------------------------------------------------
 
 namespace {

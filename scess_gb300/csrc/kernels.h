@@ -30,6 +30,10 @@ void dgemv_table(const TableGemm &g, cudaStream_t stream);
 // workspace == nullptr and query == true.
 int64_t dgemm_table_workspace(const TableGemm &g);
 void dgemm_table(const TableGemm &g, double *workspace, cudaStream_t stream);
+// dgemm_table with its split-K partials held to `ws_doubles` doubles of
+// `workspace` (fewer splits, down to none, when the usual count does not fit).
+void dgemm_table_bounded(const TableGemm &g, double *workspace, int64_t ws_doubles,
+                         cudaStream_t stream);
 
 // Y[perm] = alpha * X + beta * Y over an up-to-6-d index space `ext` (column
 // major linear order); xs/ys are the element strides of X/Y per index.
