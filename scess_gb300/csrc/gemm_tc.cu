@@ -155,14 +155,39 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
   for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// Asynchronous form: the 16 registers are valid after tmem_wait16 on them
+// (the wait takes them as operands, so no use can be scheduled before it).
+__device__ __forceinline__ void tmem_ld16_async(uint32_t taddr, uint32_t *r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait16(uint32_t *r) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]),
+                 "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]),
+                 "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15])
+               :
+               : "memory");
+}
+
+// TMEM loads (16 columns each) issued per wait in the drain.
+#ifndef SCESS_TC_LDB
+#define SCESS_TC_LDB 1
+#endif
+
 // K segment of a tensor-core problem: operand maps, K blocks, lo offset and the
-// first A/B row of problem (y, z): row0 + y * row_y + z * row_z.
+// first A/B row of problem (y, z) of group g: row0[g] + y * row_y[g] + z * row_z[g].
 struct TcSegArgs {
   int mapA, mapB;
   int nkb;   // K blocks of 64
   int kpad;  // lo offset in the packed rows (elements)
   int negA;  // negate this segment's products
-  int64_t rowA0, rowAy, rowAz, rowB0, rowBy, rowBz;
+  int64_t rowA0[3], rowAy[3], rowAz[3], rowB0[3], rowBy[3], rowBz[3];
 };
 
 struct TcMaps {
@@ -172,15 +197,17 @@ struct TcMaps {
 struct TcArgs {
   int M, N;
   int tiles_m, tiles_n;
-  int ny, nz;        // problems: (y, z) in [0, ny) x [0, nz)
+  int ny, nz, ng;    // problems: (y, z, g) in [0, ny) x [0, nz) x [0, ng)
   int nseg;          // K segments (<= 4)
   int kb_total;      // sum of the segments' K blocks
   int kb_per_split;  // K blocks per work unit (split-K when < kb_total)
   int splits;
   int f16;           // operands are FP16 (else BF16)
   int split3;        // three hi/lo products (else hi*hi only)
+  int kbd;           // K blocks accumulated in one TMEM buffer per drain (1 or 2)
   TcSegArgs seg[4];
-  int64_t cy, cz;    // output offset of problem (y, z): y * cy + z * cz
+  int64_t cy, cz;    // output offset of problem (y, z, g): y * cy + z * cz + cg[g]
+  int64_t cg[3];
   float *partial;    // split-K partials (nullptr: direct epilogue)
   int64_t part_stride;
   unsigned *err;
@@ -190,22 +217,27 @@ struct TcArgs {
 //   warp 0     TMA producer: per 64-wide K block one smem stage holding A_hi,
 //              A_lo, B_hi, B_lo (128 rows x 128 B each, 128B swizzle);
 //   warp 1     TMEM owner + MMA issuer: the block's products lo*hi, hi*lo,
-//              hi*hi (4 x K=16 each) go into one of two 128-column TMEM
+//              hi*hi (4 x K=16 each) go into one of four 128-column TMEM
 //              buffers, starting from zero, then tcgen05.commit;
 //   warps 2-5  drain each buffer into an FP32 register accumulator (one row
 //              per thread, round-to-nearest adds) and, after the unit's last K
 //              block, scatter alpha*acc + beta*C through the offset tables.
-// Draining every K block bounds the truncating accumulation inside TMEM to
-// the 12 products of one block, so the result's error does not grow with K.
+// Draining every K block (kbd = 1) bounds the truncating accumulation inside
+// TMEM to the 12 products of one block, so the result's error does not grow
+// with K; kbd = 2 drains every second block (half the drains, about twice the
+// per-element rounding error, still K-independent).
 // A problem's K range may span several segments with different operands
 // (up to 4), each optionally negated through the instruction descriptor.
 constexpr int V2_BN = 128;
 constexpr int V2_STAGES = 3;
 constexpr uint32_t V2_TILE_BYTES = 128 * TC_BK * 2;  // 16 KiB: 128 rows x 128 B
 constexpr uint32_t V2_STAGE_BYTES = 4 * V2_TILE_BYTES;
-constexpr uint32_t V2_TMEM_COLS = 2 * V2_BN;
-constexpr size_t V2_SMEM_BYTES = 1024 + V2_STAGES * V2_STAGE_BYTES + (2 * V2_STAGES + 5) * 8 + 8 +
-                                 V2_BN * 8;
+// TMEM accumulator buffers: all 512 columns as four 128-column buffers, so the
+// MMA warp can run four K blocks ahead while the epilogue scatters a unit.
+constexpr int V2_NBUF = 4;
+constexpr uint32_t V2_TMEM_COLS = V2_NBUF * V2_BN;
+constexpr size_t V2_SMEM_BYTES = 1024 + V2_STAGES * V2_STAGE_BYTES +
+                                 (2 * V2_STAGES + 2 * V2_NBUF + 1) * 8 + 8;
 
 __device__ __forceinline__ void seg_of(const TcArgs &a, int kb, int &s, int &lkb) {
   s = 0;
@@ -222,15 +254,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t *full = (uint64_t *)(smem + V2_STAGES * V2_STAGE_BYTES);
   uint64_t *empty = full + V2_STAGES;
-  uint64_t *tfull = empty + V2_STAGES;   // [2]
-  uint64_t *tempty = tfull + 2;          // [2]
-  uint64_t *done = tempty + 2;           // [1]
+  uint64_t *tfull = empty + V2_STAGES;   // [V2_NBUF]
+  uint64_t *tempty = tfull + V2_NBUF;    // [V2_NBUF]
+  uint64_t *done = tempty + V2_NBUF;     // [1]
   uint32_t *tmem_slot = (uint32_t *)(done + 1);
-  int64_t *colOff = (int64_t *)(tmem_slot + 2);
+  // Column offsets of the current unit.  A statically declared shared array:
+  // the compiler then knows these loads cannot alias the global stores of the
+  // scatter and batches them (through a generic pointer every load would wait
+  // for the previous store).
+  __shared__ int64_t colOff[V2_BN];
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tiles = a.tiles_m * a.tiles_n;
-  const int nprob = a.ny * a.nz;
+  const int nprob = a.ny * a.nz * a.ng;
   const int units = tiles * nprob * a.splits;
 
   if (threadIdx.x == 0) {
@@ -238,7 +274,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    for (int b = 0; b < 2; b++) {
+    for (int b = 0; b < V2_NBUF; b++) {
       mbar_init(&tfull[b], 1);
       mbar_init(&tempty[b], 4);  // one arrival per epilogue warp
     }
@@ -258,8 +294,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  // unit -> (tile m, tile n, problem y, z, K-block range)
-  auto unit_coords = [&](int u, int &tm, int &tn, int &py, int &pz, int &kb0, int &kb1) {
+  // unit -> (tile m, tile n, problem y, z, g, K-block range)
+  auto unit_coords = [&](int u, int &tm, int &tn, int &py, int &pz, int &pg, int &kb0, int &kb1) {
     const int tile = u % tiles;
     const int rest = u / tiles;
     const int q = rest % nprob;
@@ -267,7 +303,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     tn = tile % a.tiles_n;
     tm = tile / a.tiles_n;
     py = q % a.ny;
-    pz = q / a.ny;
+    pz = (q / a.ny) % a.nz;
+    pg = q / (a.ny * a.nz);
     kb0 = sp * a.kb_per_split;
     kb1 = min(a.kb_total, kb0 + a.kb_per_split);
   };
@@ -282,14 +319,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       for (int s = 0; s < V2_STAGES; s++) last[s] = -1;
       bool ok = true;
       for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
-        int tm, tn, py, pz, kb0, kb1;
-        unit_coords(u, tm, tn, py, pz, kb0, kb1);
+        int tm, tn, py, pz, pg, kb0, kb1;
+        unit_coords(u, tm, tn, py, pz, pg, kb0, kb1);
         for (int kb = kb0; kb < kb1; kb++, g++) {
           int sg, lkb;
           seg_of(a, kb, sg, lkb);
           const TcSegArgs &S = a.seg[sg];
-          const int ya = (int)(S.rowA0 + py * S.rowAy + pz * S.rowAz) + tm * TC_BM;
-          const int yb = (int)(S.rowB0 + py * S.rowBy + pz * S.rowBz) + tn * V2_BN;
+          const int ya = (int)(S.rowA0[pg] + py * S.rowAy[pg] + pz * S.rowAz[pg]) + tm * TC_BM;
+          const int yb = (int)(S.rowB0[pg] + py * S.rowBy[pg] + pz * S.rowBz[pg]) + tn * V2_BN;
           const int s = g % V2_STAGES;
           const uint32_t ph = (uint32_t)(g / V2_STAGES) & 1u;
           if (!mbar_wait(&empty[s], ph ^ 1u, a.err, ERR_EMPTY_WAIT)) { ok = false; break; }
@@ -315,24 +352,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       int g = 0, c = 0;
       bool ok = true;
       for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
-        int tm, tn, py, pz, kb0, kb1;
-        unit_coords(u, tm, tn, py, pz, kb0, kb1);
-        for (int kb = kb0; kb < kb1; kb++, g++, c++) {
+        int tm, tn, py, pz, pg, kb0, kb1;
+        unit_coords(u, tm, tn, py, pz, pg, kb0, kb1);
+        for (int kb = kb0; kb < kb1; kb++, g++) {
           int sg, lkb;
           seg_of(a, kb, sg, lkb);
           const uint32_t id = idesc | (a.seg[sg].negA ? (1u << 13) : 0u);  // negate A
           const int s = g % V2_STAGES;
           const uint32_t ph = (uint32_t)(g / V2_STAGES) & 1u;
-          const int b = c & 1;
-          const uint32_t bph = (uint32_t)(c >> 1) & 1u;
-          if (!mbar_wait(&tempty[b], bph ^ 1u, a.err, ERR_EMPTY_WAIT)) { ok = false; break; }
+          const int b = c % V2_NBUF;
+          const uint32_t bph = (uint32_t)(c / V2_NBUF) & 1u;
+          const bool first = (kb - kb0) % a.kbd == 0;
+          const bool last = (kb - kb0) % a.kbd == a.kbd - 1 || kb == kb1 - 1;
+          if (first && !mbar_wait(&tempty[b], bph ^ 1u, a.err, ERR_EMPTY_WAIT)) { ok = false; break; }
           if (!mbar_wait(&full[s], ph, a.err, ERR_FULL_WAIT)) { ok = false; break; }
           tc_fence_after();
           const uint32_t st = smem_u32(smem + s * V2_STAGE_BYTES);
           const uint32_t ahi = st, bhi = st + V2_TILE_BYTES;
           const uint32_t alo = st + 2 * V2_TILE_BYTES, blo = st + 3 * V2_TILE_BYTES;
           const uint32_t d = tmem + (uint32_t)(b * V2_BN);
-          uint32_t acc = 0;
+          uint32_t acc = first ? 0u : 1u;
           if (a.split3) {
 #pragma unroll
             for (int k = 0; k < TC_BK / 16; k++, acc = 1)
@@ -345,7 +384,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           for (int k = 0; k < TC_BK / 16; k++, acc = 1)
             mma_bf16(d, sw128_desc(ahi + 32 * k), sw128_desc(bhi + 32 * k), id, acc);
           mma_commit(&empty[s]);
-          mma_commit(&tfull[b]);
+          if (last) {
+            mma_commit(&tfull[b]);
+            c++;
+          }
         }
       }
       // every MMA issued above has completed once `done` fires
@@ -356,40 +398,65 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int q = warp & 3;
     const int row = 32 * q + lane;
     const int et = threadIdx.x - 64;  // 0..127
+    // Output scaling, once per CTA: alpha / (sA sB) with power-of-two pack
+    // scales sA, sB.  FP32 outputs multiply by it in FP32; FP64 outputs multiply
+    // by the user's alpha in FP32 and apply 2^-log2(sA sB) to the exponent field
+    // (exact, no FP64 arithmetic per element).
+    __shared__ double s_alpha;
+    __shared__ float s_falpha, s_fuser;
+    __shared__ int s_shift, s_shift_ok;
+    if (et == 0) {
+      double sc = 1.0;
+      if (out.scaleA) sc *= *out.scaleA;
+      if (out.scaleB) sc *= *out.scaleB;
+      s_alpha = out.alpha / sc;
+      s_falpha = (float)(out.alpha / sc);
+      s_fuser = (float)out.alpha;
+      int e = 0;
+      const double f = frexp(sc, &e);  // sc = 0.5 * 2^e exactly for a power of two
+      s_shift = 1 - e;
+      s_shift_ok = (f == 0.5 && e > -400 && e < 400) ? 1 : 0;
+    }
     int c = 0;
     bool ok = true;
     for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
-      int tm, tn, py, pz, kb0, kb1;
-      unit_coords(u, tm, tn, py, pz, kb0, kb1);
+      int tm, tn, py, pz, pg, kb0, kb1;
+      unit_coords(u, tm, tn, py, pz, pg, kb0, kb1);
       const int m = tm * TC_BM + row;
       const int n0 = tn * V2_BN;
       asm volatile("bar.sync 1, 128;" ::: "memory");  // previous unit's colOff reads done
       if (!a.partial) {
         const int nn = n0 + et;
-        colOff[et] = nn < a.N ? out.baseC + py * a.cy + pz * a.cz + out.colC[nn] : -1;
+        colOff[et] = nn < a.N ? out.baseC + py * a.cy + pz * a.cz + a.cg[pg] + out.colC[nn] : -1;
       }
+      // issued now, used after the K loop: their latency hides behind the MMAs
+      const int64_t rowOff = (!a.partial && m < a.M) ? out.rowC[m] : 0;
+      const unsigned errv = *(volatile unsigned *)a.err;
       float acc[V2_BN];
 #pragma unroll
       for (int j = 0; j < V2_BN; j++) acc[j] = 0.0f;
-      for (int kb = kb0; kb < kb1; kb++, c++) {
-        const int b = c & 1;
-        const uint32_t bph = (uint32_t)(c >> 1) & 1u;
+      for (int kb = kb0; kb < kb1; kb += a.kbd, c++) {
+        const int b = c % V2_NBUF;
+        const uint32_t bph = (uint32_t)(c / V2_NBUF) & 1u;
         if (!mbar_wait(&tfull[b], bph, a.err, ERR_ACCUM_WAIT)) { ok = false; break; }
         tc_fence_after();
         const uint32_t t0 = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * V2_BN);
 #pragma unroll
-        for (int j = 0; j < V2_BN; j += 16) {
-          float v[16];
-          tmem_ld16(t0 + (uint32_t)j, v);
+        for (int j = 0; j < V2_BN; j += 16 * SCESS_TC_LDB) {
+          uint32_t r[16 * SCESS_TC_LDB];
 #pragma unroll
-          for (int i = 0; i < 16; i++) acc[j + i] += v[i];
+          for (int h = 0; h < SCESS_TC_LDB; h++) tmem_ld16_async(t0 + (uint32_t)(j + 16 * h), r + 16 * h);
+#pragma unroll
+          for (int h = 0; h < SCESS_TC_LDB; h++) tmem_wait16(r + 16 * h);
+#pragma unroll
+          for (int i = 0; i < 16 * SCESS_TC_LDB; i++) acc[j + i] += __uint_as_float(r[i]);
         }
         tc_fence_before();
         __syncwarp();
         if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[b])) : "memory");
       }
       asm volatile("bar.sync 1, 128;" ::: "memory");  // colOff of this unit written
-      if (!ok || *(volatile unsigned *)a.err) break;
+      if (!ok || errv) break;
       if (m >= a.M) continue;
       if (a.partial) {
         const int sp = u / (tiles * nprob);
@@ -401,16 +468,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
         continue;
       }
-      double alpha = out.alpha;
-      if (out.scaleA) alpha /= *out.scaleA;
-      if (out.scaleB) alpha /= *out.scaleB;
-      const int64_t rowOff = out.rowC[m];
+      const double alpha = s_alpha;
       // beta == 1: fire-and-forget reductions (each element receives exactly one
       // per launch, so the result is deterministic); beta == 0: plain stores;
       // otherwise a batched read-modify-write.
       if (out.fp32) {
         float *C = (float *)out.C;
-        const float fa = (float)alpha, fb = (float)out.beta;
+        const float fa = s_falpha, fb = (float)out.beta;
         if (out.beta == 1.0) {
 #pragma unroll
           for (int j = 0; j < V2_BN; j++) {
@@ -441,7 +505,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
       } else {
         double *C = (double *)out.C;
-        if (out.beta == 1.0) {
+        const float fu = s_fuser;
+        const long long sh = (long long)s_shift << 52;
+        // alpha * acc as (double)(fu * acc) * 2^shift via the exponent field
+        auto scaled = [&](float x) -> double {
+          const float p = fu * x;
+          return p == 0.0f ? 0.0 : __longlong_as_double(__double_as_longlong((double)p) + sh);
+        };
+        if (s_shift_ok && out.beta == 1.0) {
+#pragma unroll
+          for (int j = 0; j < V2_BN; j++) {
+            const int64_t co = colOff[j];
+            if (co >= 0) atomicAdd(C + rowOff + co, scaled(acc[j]));
+          }
+        } else if (s_shift_ok && out.beta == 0.0) {
+#pragma unroll
+          for (int j = 0; j < V2_BN; j++) {
+            const int64_t co = colOff[j];
+            if (co >= 0) C[rowOff + co] = scaled(acc[j]);
+          }
+        } else if (out.beta == 1.0) {
 #pragma unroll
           for (int j = 0; j < V2_BN; j++) {
             const int64_t co = colOff[j];
@@ -541,7 +624,8 @@ template <bool F16>
 __global__ void __launch_bounds__(256) pack_split_kernel(
     const double *__restrict__ src, const int64_t *__restrict__ rowOff, int64_t rows,
     const int64_t *__restrict__ kOff, int64_t K, int unitK, uint16_t *__restrict__ dst,
-    int64_t Kpad, const unsigned *__restrict__ maxbits, double *__restrict__ scale_out) {
+    int64_t Kpad, const unsigned *__restrict__ maxbits, double *__restrict__ scale_out,
+    int negate) {
   __shared__ double tile[32][65];
   __shared__ int64_t sr[32], sk[64];
   const int t = threadIdx.x;
@@ -565,7 +649,11 @@ __global__ void __launch_bounds__(256) pack_split_kernel(
     if (unitK) { kk = t & 63; rr = (t >> 6) + 4 * p; }
     else { rr = t & 31; kk = (t >> 5) + 8 * p; }
     const int64_t ro = sr[rr], ko = sk[kk];
-    tile[rr][kk] = (ro >= 0 && ko >= 0) ? src[ro + ko] : 0.0;
+    // negation as a sign-bit flip (exact, no FP64 arithmetic)
+    tile[rr][kk] = (ro >= 0 && ko >= 0)
+                       ? __longlong_as_double(__double_as_longlong(src[ro + ko]) ^
+                                              ((long long)negate << 63))
+                       : 0.0;
   }
   __syncthreads();
   const int rr = t >> 3, ch = t & 7;
@@ -637,7 +725,8 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
     cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)V2_SMEM_BYTES);
   });
-  if (ps.M <= 0 || ps.N <= 0 || ps.ny <= 0 || ps.nz <= 0) return;
+  if (ps.M <= 0 || ps.N <= 0 || ps.ny <= 0 || ps.nz <= 0 || ps.ng <= 0) return;
+  if (ps.ng > 3) throw Error(SCESS_ERR_INVALID, "tc_gemm: groups");
   if (nseg != 1 && nseg != 3) throw Error(SCESS_ERR_INVALID, "tc_gemm: nseg");
   if (ps.nseg < 1 || ps.nseg > 4) throw Error(SCESS_ERR_INVALID, "tc_gemm: segments");
   if (ps.M > INT32_MAX || ps.N > INT32_MAX) throw Error(SCESS_ERR_INVALID, "tc_gemm: dimension too large");
@@ -649,34 +738,40 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
   a.tiles_n = (int)ceil_div(ps.N, V2_BN);
   a.ny = ps.ny;
   a.nz = ps.nz;
+  a.ng = ps.ng;
   a.nseg = ps.nseg;
   int kbt = 0;
   for (int s = 0; s < ps.nseg; s++) {
     const TcSegment &g = ps.seg[s];
     if (g.Kpad % TC_BK != 0 || g.Kpad <= 0 || 2 * g.Kpad > INT32_MAX)
       throw Error(SCESS_ERR_INVALID, "tc_gemm: Kpad % 64");
-    const int64_t maxA = g.rowA0 + (int64_t)(ps.ny - 1) * g.rowAy + (int64_t)(ps.nz - 1) * g.rowAz +
-                         a.tiles_m * TC_BM;
-    const int64_t maxB = g.rowB0 + (int64_t)(ps.ny - 1) * g.rowBy + (int64_t)(ps.nz - 1) * g.rowBz +
-                         a.tiles_n * V2_BN;
-    if (maxA > INT32_MAX || maxB > INT32_MAX || g.rowA0 < 0 || g.rowB0 < 0)
-      throw Error(SCESS_ERR_INVALID, "tc_gemm: row coordinates");
+    for (int q = 0; q < ps.ng; q++) {
+      const int64_t maxA = g.rowA0[q] + (int64_t)(ps.ny - 1) * g.rowAy[q] +
+                           (int64_t)(ps.nz - 1) * g.rowAz[q] + a.tiles_m * TC_BM;
+      const int64_t maxB = g.rowB0[q] + (int64_t)(ps.ny - 1) * g.rowBy[q] +
+                           (int64_t)(ps.nz - 1) * g.rowBz[q] + a.tiles_n * V2_BN;
+      if (maxA > INT32_MAX || maxB > INT32_MAX || g.rowA0[q] < 0 || g.rowB0[q] < 0 ||
+          g.rowAy[q] < 0 || g.rowAz[q] < 0 || g.rowBy[q] < 0 || g.rowBz[q] < 0)
+        throw Error(SCESS_ERR_INVALID, "tc_gemm: row coordinates");
+    }
     a.seg[s].mapA = g.mapA;
     a.seg[s].mapB = g.mapB;
     a.seg[s].nkb = (int)(g.Kpad / TC_BK);
     a.seg[s].kpad = (int)g.Kpad;
     a.seg[s].negA = g.negate ? 1 : 0;
-    a.seg[s].rowA0 = g.rowA0;
-    a.seg[s].rowAy = g.rowAy;
-    a.seg[s].rowAz = g.rowAz;
-    a.seg[s].rowB0 = g.rowB0;
-    a.seg[s].rowBy = g.rowBy;
-    a.seg[s].rowBz = g.rowBz;
+    for (int q = 0; q < 3; q++) {
+      a.seg[s].rowA0[q] = g.rowA0[q];
+      a.seg[s].rowAy[q] = g.rowAy[q];
+      a.seg[s].rowAz[q] = g.rowAz[q];
+      a.seg[s].rowB0[q] = g.rowB0[q];
+      a.seg[s].rowBy[q] = g.rowBy[q];
+      a.seg[s].rowBz[q] = g.rowBz[q];
+    }
     kbt += a.seg[s].nkb;
   }
   a.kb_total = kbt;
   if (splits < 1) splits = 1;
-  if (ps.ny * ps.nz > 1) splits = 1;
+  if (ps.ny * ps.nz * ps.ng > 1) splits = 1;
   if (splits > kbt) splits = kbt;
   const int kbs = (int)ceil_div(kbt, splits);
   splits = (int)ceil_div(kbt, kbs);
@@ -684,15 +779,18 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
   a.splits = splits;
   a.f16 = fmt == TcFormat::FP16 ? 1 : 0;
   a.split3 = nseg == 3 ? 1 : 0;
+  a.kbd = ps.kbd == 2 ? 2 : 1;
   a.cy = ps.cy;
   a.cz = ps.cz;
+  for (int q = 0; q < 3; q++) a.cg[q] = ps.cg[q];
   a.partial = splits > 1 ? partial : nullptr;
   a.part_stride = ps.M * ps.N;
   a.err = err;
   if (splits > 1 && !partial) throw Error(SCESS_ERR_INVALID, "tc_gemm: split-K needs partials");
   TcMaps maps;
   for (int i = 0; i < 6; i++) maps.m[i] = ps.maps[std::min(i, ps.nmaps - 1)];
-  const int64_t units = (int64_t)a.tiles_m * a.tiles_n * ps.ny * ps.nz * splits;
+  const int64_t units = (int64_t)a.tiles_m * a.tiles_n * ps.ny * ps.nz * ps.ng * splits;
+  if (units > INT32_MAX) throw Error(SCESS_ERR_INVALID, "tc_gemm: too many work units");
   const unsigned grid = (unsigned)std::min<int64_t>(units, kNumSMs);
   tc_gemm_kernel<<<grid, TC_THREADS, V2_SMEM_BYTES, stream>>>(maps, out, a);
   SCESS_CHECK_LAUNCH();
@@ -719,8 +817,8 @@ void tc_gemm_launch_maps(const CUtensorMap &ma, const CUtensorMap &mb, int64_t K
   ps.seg[0].mapA = 0;
   ps.seg[0].mapB = 1;
   ps.seg[0].Kpad = Kpad;
-  ps.seg[0].rowA0 = rowA0;
-  ps.seg[0].rowB0 = rowB0;
+  ps.seg[0].rowA0[0] = rowA0;
+  ps.seg[0].rowB0[0] = rowB0;
   tc_gemm_launch_grouped(ps, fmt, out, nseg, splits, partial, err, stream);
 }
 
@@ -783,12 +881,55 @@ void TcEngine::pack(const double *src, const int64_t *rowOff, int64_t rows, cons
     maxabs_kernel<<<blocks, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, unitK ? 1 : 0, maxbits);
     SCESS_CHECK_LAUNCH();
     pack_split_kernel<true><<<grid, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, unitK ? 1 : 0,
-                                                           out.mem.as<uint16_t>(), Kpad, maxbits, scale);
+                                                           out.mem.as<uint16_t>(), Kpad, maxbits, scale, 0);
   } else {
     const double one = 1.0;
     SCESS_CUDA(cudaMemcpyAsync(scale, &one, sizeof(double), cudaMemcpyHostToDevice, ctx_.stream));
     pack_split_kernel<false><<<grid, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, unitK ? 1 : 0,
-                                                            out.mem.as<uint16_t>(), Kpad, maxbits, scale);
+                                                            out.mem.as<uint16_t>(), Kpad, maxbits, scale, 0);
+  }
+  SCESS_CHECK_LAUNCH();
+}
+
+void TcEngine::maxabs_into(const double *src, const int64_t *rowOff, int64_t rows,
+                           const int64_t *kOff, int64_t K, bool unitK, unsigned *maxbits) {
+  const int64_t n = rows * K;
+  if (n <= 0) return;
+  const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), 4 * kNumSMs));
+  maxabs_kernel<<<blocks, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, unitK ? 1 : 0, maxbits);
+  SCESS_CHECK_LAUNCH();
+}
+
+void TcEngine::pack_with_max(const double *src, const int64_t *rowOff, int64_t rows,
+                             const int64_t *kOff, int64_t K, bool unitK, int64_t row_align,
+                             const unsigned *maxbits, bool negate, Packed &out) {
+  const int64_t Kpad = round_up(std::max<int64_t>(K, 1), TC_BK);
+  const int64_t rows_pad = round_up(std::max<int64_t>(rows, 1), std::max<int64_t>(row_align, 32));
+  const size_t bytes = (size_t)rows_pad * 2 * Kpad * sizeof(uint16_t);
+  if (out.mem.bytes() < bytes || !out.aux.bytes()) {
+    ctx_.sync();
+    if (out.mem.bytes() < bytes) out.mem.alloc(bytes);
+    if (!out.aux.bytes()) out.aux.alloc(16);
+  }
+  out.rows = rows;
+  out.rows_pad = rows_pad;
+  out.K = K;
+  out.Kpad = Kpad;
+  out.fmt = fmt_;
+  TimedScope ts(ctx_.timer, "pack_split", 0.0,
+                (double)rows * K * 8 + (double)rows_pad * Kpad * 4, ctx_.stream);
+  double *scale = reinterpret_cast<double *>(out.aux.as<char>() + 8);
+  dim3 grid((unsigned)(Kpad / 64), (unsigned)(rows_pad / 32));
+  if (fmt_ == TcFormat::FP16) {
+    pack_split_kernel<true><<<grid, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, unitK ? 1 : 0,
+                                                           out.mem.as<uint16_t>(), Kpad, maxbits,
+                                                           scale, negate ? 1 : 0);
+  } else {
+    const double one = 1.0;
+    SCESS_CUDA(cudaMemcpyAsync(scale, &one, sizeof(double), cudaMemcpyHostToDevice, ctx_.stream));
+    pack_split_kernel<false><<<grid, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, unitK ? 1 : 0,
+                                                            out.mem.as<uint16_t>(), Kpad, maxbits,
+                                                            scale, negate ? 1 : 0);
   }
   SCESS_CHECK_LAUNCH();
 }

@@ -47,26 +47,31 @@ struct TcOut {
   const double *scaleA = nullptr, *scaleB = nullptr;
 };
 
-// A launch of several same-shaped GEMMs ("problems" (y, z) in [0,ny) x [0,nz)),
-// each summing up to four K segments whose operands are rows of packed
-// tensors: segment s of problem (y, z) multiplies rows
-// rowA0 + y rowAy + z rowAz (+ m) of maps[mapA] with rows
-// rowB0 + y rowBy + z rowBz (+ n) of maps[mapB] over Kpad columns, negated
-// when `negate`.  Problem (y, z) writes at offset y cy + z cz (plus the tables).
+// A launch of several same-shaped GEMMs ("problems" (y, z, g) in
+// [0,ny) x [0,nz) x [0,ng), ng <= 3), each summing up to four K segments whose
+// operands are rows of packed tensors: segment s of problem (y, z, g)
+// multiplies rows rowA0[g] + y rowAy[g] + z rowAz[g] (+ m) of maps[mapA] with
+// rows rowB0[g] + y rowBy[g] + z rowBz[g] (+ n) of maps[mapB] over Kpad
+// columns, negated when `negate`.  Problem (y, z, g) writes at offset
+// y cy + z cz + cg[g] (plus the tables).  All segments' operand pairs must
+// carry the same scale product (the epilogue unscales once).
 struct TcSegment {
   int mapA = 0, mapB = 1;
   int64_t Kpad = 0;
   bool negate = false;
-  int64_t rowA0 = 0, rowAy = 0, rowAz = 0, rowB0 = 0, rowBy = 0, rowBz = 0;
+  int64_t rowA0[3] = {0, 0, 0}, rowAy[3] = {0, 0, 0}, rowAz[3] = {0, 0, 0};
+  int64_t rowB0[3] = {0, 0, 0}, rowBy[3] = {0, 0, 0}, rowBz[3] = {0, 0, 0};
 };
 struct TcProblemSet {
   CUtensorMap maps[6];
   int nmaps = 0;
   int64_t M = 0, N = 0;
-  int ny = 1, nz = 1;
+  int ny = 1, nz = 1, ng = 1;
   int nseg = 1;
   TcSegment seg[4];
   int64_t cy = 0, cz = 0;
+  int64_t cg[3] = {0, 0, 0};
+  int kbd = 1;  // K blocks per TMEM drain: 1, or 2 (fewer drains, ~2x rounding)
 };
 
 class TcEngine {
@@ -83,6 +88,15 @@ class TcEngine {
   // contiguous along k (load-coalescing hint).
   void pack(const double *src, const int64_t *rowOff, int64_t rows, const int64_t *kOff,
             int64_t K, bool unitK, int64_t row_align, Packed &out);
+  // max|x| over the same gather, folded into *maxbits (float bits, atomic max:
+  // several calls into one word give the max over all their tensors).
+  void maxabs_into(const double *src, const int64_t *rowOff, int64_t rows, const int64_t *kOff,
+                   int64_t K, bool unitK, unsigned *maxbits);
+  // pack() with the FP16 scale taken from a given max word (so that several
+  // packs share one scale), optionally negating the values (exact).
+  void pack_with_max(const double *src, const int64_t *rowOff, int64_t rows, const int64_t *kOff,
+                     int64_t K, bool unitK, int64_t row_align, const unsigned *maxbits,
+                     bool negate, Packed &out);
   TcFormat format() const { return fmt_; }
   // D(m, n) = sum_k A(rowA0 + m, k) B(rowB0 + n, k) for m < M, n < N, written
   // through `out`.  nseg = 3 (split hi/lo) or 1 (hi only, BF16 accuracy).

@@ -13,11 +13,14 @@
 // one partial energy per triple; a fixed-order reduction gives 2 * sum (:167).
 //
 // FP64 form: DFMA GEMMs straight from the padded FP64 repacks, FP64 W and
-// FP64 energy arithmetic.  MIXED form: the operands are packed once per call
-// into BF16 hi/lo rows grouped by block, the GEMMs run on tcgen05 tensor
-// cores into an FP32 W, and the energy kernel works in FP32 per element with
-// FP64 accumulation per triple.
+// FP64 energy arithmetic.  MIXED form: the same 12 products regroup into three
+// sets of four K segments that each write their own FP32 buffer once (one
+// grouped tcgen05 launch per block triple, plain stores, no reductions); the
+// operands are packed once per call into FP16 hi/lo rows grouped by block, and
+// the energy kernel sums the three buffers in shared memory, working in FP32
+// per element with FP64 accumulation per triple.
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -33,7 +36,6 @@ __host__ __device__ inline int64_t triple_id(int64_t a, int64_t b, int64_t c) {
 }
 
 // x / y: fast FP32 division in the mixed form (2 ulp), IEEE division in FP64.
-__device__ __forceinline__ float div_fast(float x, float y) { return __fdividef(x, y); }
 __device__ __forceinline__ double div_fast(double x, double y) { return x / y; }
 
 // One CTA per local triple (a_l, b_l, c_l) of the block triple (A, B, C).
@@ -132,6 +134,120 @@ __global__ void __launch_bounds__(256) triples_energy_kernel(
   }
 }
 
+// S(i, j, a, b) = (ia|jb) = eri(i, j, o+a, o+b) as FP32 at i + o j + o^2 (a + v b):
+// the integral slices of the tensor-core energy kernel, read contiguously.
+__global__ void ovov_f32_kernel(const double *__restrict__ eri, int64_t N, int64_t o, int64_t v,
+                                float *__restrict__ out) {
+  const int64_t o2 = o * o, n = o2 * v * v, N2 = N * N, N3 = N2 * N;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ij = e % o2, ab = e / o2;
+    const int64_t i = ij % o, j = ij / o, a = ab % v, b = ab / v;
+    out[e] = (float)eri[i + N * j + (o + a) * N2 + (o + b) * N3];
+  }
+}
+
+// Energy of one block triple from the three grouped W buffers of the
+// tensor-core form.  W^{abc}_{ijk} = W0[b,c][a][i + o j + o^2 k]
+//   + W1[a,c][b][j + o i + o^2 k] + W2[a,b][c][k + o i + o^2 j]
+// (buffer g holds [y_l][z_l][x_l][o^3] for its roles (x, y, z)).  Each thread
+// owns index pairs and walks the third index with fixed strides: every buffer
+// is read along its own unit-stride index (coalesced across the threads) and
+// added into Y in shared memory; W is recovered as Y - V in the energy loop.
+// Otherwise as triples_energy_kernel (FP32 per element, FP64 per thread sum).
+__global__ void __launch_bounds__(512) triples_energy3_kernel(
+    const float *__restrict__ W, int64_t o, int64_t v, int64_t nb, int64_t A, int64_t Bk,
+    int64_t C, const double *__restrict__ eps, const double *__restrict__ t1,
+    const float *__restrict__ S, double *__restrict__ energies) {
+  const int64_t al = blockIdx.x / (nb * nb), bl = (blockIdx.x / nb) % nb, cl = blockIdx.x % nb;
+  const int64_t a = A * nb + al, b = Bk * nb + bl, c = C * nb + cl;
+  if (a >= v || b >= v || c >= v || b > a || c > b) return;
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  __shared__ double red[32];
+  const int oo = (int)o, o2 = oo * oo, o3 = o2 * oo;
+  // Y(i,j,k) at i + p1 j + p2 k with odd p1, p2 (conflict-free permuted reads)
+  const int p1 = oo | 1, p2 = (p1 * oo) | 1;
+  float *Y = reinterpret_cast<float *>(sm_raw);
+  float *Sbc = Y + p2 * oo, *Sac = Sbc + o2, *Sab = Sac + o2;
+  float *ta = Sab + o2, *tb = ta + oo, *tc = tb + oo, *eo = tc + oo;
+  const int64_t nb3o3 = nb * nb * nb * (int64_t)o3;
+  const float *W0 = W + ((bl * nb + cl) * nb + al) * (int64_t)o3;
+  const float *W1 = W + nb3o3 + ((al * nb + cl) * nb + bl) * (int64_t)o3;
+  const float *W2 = W + 2 * nb3o3 + ((al * nb + bl) * nb + cl) * (int64_t)o3;
+  const float *S_bc = S + (b + v * c) * o2, *S_ac = S + (a + v * c) * o2, *S_ab = S + (a + v * b) * o2;
+  for (int e = threadIdx.x; e < o2; e += blockDim.x) {
+    Sbc[e] = S_bc[e];
+    Sac[e] = S_ac[e];
+    Sab[e] = S_ab[e];
+  }
+  for (int i = threadIdx.x; i < oo; i += blockDim.x) {
+    ta[i] = (float)t1[i + o * a];
+    tb[i] = (float)t1[i + o * b];
+    tc[i] = (float)t1[i + o * c];
+    eo[i] = (float)eps[i];
+  }
+  __syncthreads();
+  // Y = V + W0: pairs (i, j), k walks; V_ijk = t1_ia (jb|kc) + t1_jb (ia|kc) + t1_kc (ia|jb)
+  for (int pr = threadIdx.x; pr < o2; pr += blockDim.x) {
+    const int i = pr % oo, j = pr / oo;
+    const float tai = ta[i], tbj = tb[j], sab = Sab[pr];
+    const float *w = W0 + pr;
+    float *y = Y + i + p1 * j;
+#pragma unroll 4
+    for (int k = 0; k < oo; k++)
+      y[p2 * k] = w[o2 * k] + tai * Sbc[j + oo * k] + tbj * Sac[i + oo * k] + tc[k] * sab;
+  }
+  __syncthreads();
+  // Y += W1 (layout j + o i + o^2 k): pairs (j, i), k walks
+  for (int pr = threadIdx.x; pr < o2; pr += blockDim.x) {
+    const int j = pr % oo, i = pr / oo;
+    const float *w = W1 + pr;
+    float *y = Y + i + p1 * j;
+#pragma unroll 4
+    for (int k = 0; k < oo; k++) y[p2 * k] += w[o2 * k];
+  }
+  __syncthreads();
+  // Y += W2 (layout k + o i + o^2 j): pairs (k, i), j walks
+  for (int pr = threadIdx.x; pr < o2; pr += blockDim.x) {
+    const int k = pr % oo, i = pr / oo;
+    const float *w = W2 + pr;
+    float *y = Y + i + p2 * k;
+#pragma unroll 4
+    for (int j = 0; j < oo; j++) y[p1 * j] += w[o2 * j];
+  }
+  __syncthreads();
+  const float evirt = (float)(eps[o + a] + eps[o + b] + eps[o + c]);
+  double acc = 0.0;
+  for (int pr = threadIdx.x; pr < o2; pr += blockDim.x) {
+    const int i = pr % oo, j = pr / oo;
+    const float tai = ta[i], tbj = tb[j], sab = Sab[pr], eij = eo[i] + eo[j];
+    float part = 0.0f;
+#pragma unroll 2
+    for (int k = 0; k < oo; k++) {
+      const float y = Y[i + p1 * j + p2 * k];
+      // r3(Y) = 4 Y_ijk + Y_kij + Y_jki - 2 Y_kji - 2 Y_ikj - 2 Y_jik           :152-154
+      const float r3 = 4.0f * y + Y[k + p1 * i + p2 * j] + Y[j + p1 * k + p2 * i] -
+                       2.0f * (Y[k + p1 * j + p2 * i] + Y[i + p1 * k + p2 * j] + Y[j + p1 * i + p2 * k]);
+      const float wv = y - (tai * Sbc[j + oo * k] + tbj * Sac[i + oo * k] + tc[k] * sab);
+      const float d = (eij + eo[k]) - evirt;                                       // :155
+      part += __fdividef(wv * r3, d);                                               // :156
+    }
+    acc += (double)part;
+  }
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+  const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+  if (lane == 0) red[wi] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sum = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) sum += red[q];
+    double deg = 1.0;                                                               // :135-139
+    if (a == c) deg = 6.0;
+    else if (a == b || b == c) deg = 2.0;
+    energies[triple_id(a, b, c)] = sum / deg;
+  }
+}
+
 __global__ void sum_energies_kernel(int64_t n, const double *__restrict__ e, double *out) {
   __shared__ double red[32];
   double s = 0.0;
@@ -194,6 +310,33 @@ int choose_nb(int64_t o, int64_t v, size_t welem_bytes, size_t budget) {
   return nb;
 }
 
+// Block size of the grouped tensor-core form: GEMM rows (u, x_l) = o nb fill
+// the 128-row tiles well, the padded virtual range vp = NB nb stays close to v,
+// and the three W buffers (3 nb^3 o^3 floats) stay within 256 MiB; ties go to
+// the larger block (fewer, larger launches).  SCESS_T_NB overrides it.
+int choose_nb_grouped(int64_t o, int64_t v) {
+  if (const char *env = std::getenv("SCESS_T_NB")) {
+    const int nb = std::atoi(env);
+    if (nb >= 1) return (int)std::min<int64_t>(nb, v);
+  }
+  int best = 1;
+  double best_score = -1.0;
+  const double o3 = (double)o * o * o;
+  for (int nb = 1; nb <= std::min<int64_t>(v, 64); nb++) {
+    if (nb > 1 && 3.0 * nb * nb * nb * o3 * 4.0 > double(256 << 20)) break;
+    const double rows = (double)o * nb;
+    const double effM = rows / (128.0 * std::ceil(rows / 128.0));
+    const double vp = (double)ceil_div(v, nb) * nb;
+    const double effV = std::pow((double)v / vp, 3.0);
+    const double score = effM * effV;
+    if (score >= best_score * (1.0 - 1e-9)) {
+      best = nb;
+      best_score = std::max(score, best_score);
+    }
+  }
+  return best;
+}
+
 }  // namespace
 
 double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, const double *d_eps,
@@ -201,7 +344,7 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
                      TriplesStats *stats) {
   const int64_t v = nmo - o, N = nmo;
   cudaStream_t s = ctx.stream;
-  const int nb = mixed ? choose_nb(o, v, 4, size_t(64) << 20) : choose_nb(o, v, 8, size_t(128) << 20);
+  const int nb = mixed ? choose_nb_grouped(o, v) : choose_nb(o, v, 8, size_t(128) << 20);
   const int64_t NB = ceil_div(v, nb), vp = NB * nb;
   const int64_t o2 = o * o, o3 = o2 * o;
   const int64_t N2 = N * N, N3 = N2 * N;
@@ -287,54 +430,83 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   const int64_t ntrip = v * (v + 1) * (v + 2) / 6;
   DTensor energies({std::max<int64_t>(ntrip, 1)});
   SCESS_CUDA(cudaMemsetAsync(energies.p(), 0, energies.size() * sizeof(double), s));
-  const size_t wbytes = (size_t)o3 * nb * nb * nb * (mixed ? 4 : 8);
+  // FP64: one W; MIXED: the three grouped buffers W0 | W1 | W2
+  const size_t wbytes = (size_t)o3 * nb * nb * nb * (mixed ? 3 * 4 : 8);
   DevMem W(wbytes);
   const int64_t p1 = o | 1, p2 = (p1 * o) | 1;
   const size_t ysmem = (size_t)(p2 * o + 3 * o2 + 4 * o) * (mixed ? 4 : 8);
   if (ysmem > 200 * 1024) throw Error(SCESS_ERR_UNSUPPORTED, "(T): o^3 too large for one CTA");
   if (mixed) {
-    SCESS_CUDA(cudaFuncSetAttribute(triples_energy_kernel<float, float>,
+    SCESS_CUDA(cudaFuncSetAttribute(triples_energy3_kernel,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ysmem));
   } else {
     SCESS_CUDA(cudaFuncSetAttribute(triples_energy_kernel<double, double>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ysmem));
   }
 
-  // MIXED: pack the operands once into block-grouped BF16 hi/lo rows.
-  Packed pP, pQ, pQ2, pR, pR2, pT;
-  CUtensorMap mP{}, mQ{}, mQ2{}, mR{}, mR2{}, mT{};
-  const int64_t Mpq = o * nb * nb, Npq = o2 * nb, Mr = o2 * nb, Nr = o * nb * nb;
+  // MIXED: the 12 GEMMs of a block triple regroup into three problems sets that
+  // write disjoint buffers.  Group g has the roles (x, y, z) = (a, b, c),
+  // (b, a, c), (c, a, b) and, for each (y_l, z_l), the GEMM
+  //   W_g[(u, x_l), (s, t)] =   sum_f P(u,f,x,y) Q(f,s,t,z) + sum_f P(u,f,x,z) Q(f,t,s,y)
+  //                           - sum_m t2(m,u,z,x) R(s,t,m,y) - sum_m t2(m,u,y,x) R(t,s,m,z)
+  // where u is x's occupied partner (i, j or k for x = a, b, c) and (s, t) the
+  // other two occupied indices in order: the P.Q terms of the permutations
+  // that put x's pair on the rows and the R.t2 terms whose t2 carries it (four
+  // K segments of one accumulation).  The operands are packed once per call
+  // into block-grouped FP16 hi/lo rows; the t2 rows are packed negated, and
+  // the A side (P, t2) and the B side (Q, R) each share one scale so that all
+  // segments carry the same scale product.
+  Packed pP, pQ, pQ2, pR, pR2, pTx;
+  CUtensorMap mP{}, mQ{}, mQ2{}, mR{}, mR2{}, mTx{};
+  DevTables gdt;  // W_g row / column tables
+  DevMem Sf;      // (ia|jb) as FP32 for the energy kernel
+  const int64_t Mg = o * nb, Ng = o2;
+  const int64_t Mpq = o * nb * nb, Npq = o2 * nb, Mr = o2 * nb, Nr = o * nb * nb;  // FP64 GEMMs
   if (mixed) {
     TcEngine &tc = ctx.tensor_cores();
     std::vector<std::vector<int64_t>> pt;
-    // P rows r = i + o(x + nb(y + nb(Y + NB X)))
+    // P rows r = i + o(x + nb(y + nb(Y + NB X))):  P(i, f, X nb + x, Y nb + y)
     pt.push_back(table({{o, 1}, {nb, o * v}, {nb, o * v * vp}, {NB, o * v * vp * nb}, {NB, o * v * nb}}));
-    // Q rows r = j + o(k + o(z + nb Z))
+    // Q rows r = j + o(k + o(z + nb Z)):  Q(f, j, k, Z nb + z)
     pt.push_back(table({{o, v}, {o, v * o}, {nb, v * o2}, {NB, v * o2 * nb}}));
-    // R rows r = i + o(j + o(x + nb X))
+    // R rows r = i + o(j + o(x + nb X)):  R(i, j, m, X nb + x)
     pt.push_back(table({{o, 1}, {o, o}, {nb, o3}, {NB, o3 * nb}}));
-    // t2 rows r = k + o(y + nb(z + nb(Z + NB Y)))
-    pt.push_back(table({{o, o}, {nb, o2}, {nb, o2 * vp}, {NB, o2 * vp * nb}, {NB, o2 * nb}}));
+    // t2 rows r = u + o(x + nb(z + nb(X + NB Z))):  t2(m, u, Z nb + z, X nb + x)
+    pt.push_back(table({{o, o}, {nb, o2 * vp}, {nb, o2}, {NB, o2 * vp * nb}, {NB, o2 * nb}}));
     // Q rows in (k, j) order: r = k + o(j + o(z + nb Z))
     pt.push_back(table({{o, v * o}, {o, v}, {nb, v * o2}, {NB, v * o2 * nb}}));
     // R rows in (j, i) order: r = j + o(i + o(x + nb X))
     pt.push_back(table({{o, o}, {o, 1}, {nb, o3}, {NB, o3 * nb}}));
     DevTables pdt;
     pdt.build(pt);
-    tc.pack(P.p(), pdt.ptr[0], o * vp * vp, dt.ptr[kOperand + 1], v, false, 128, pP);
-    tc.pack(Qt.p(), pdt.ptr[1], o2 * vp, dt.ptr[kOperand + 3], v, true, 128, pQ);
-    tc.pack(Qt.p(), pdt.ptr[4], o2 * vp, dt.ptr[kOperand + 3], v, true, 128, pQ2);
-    tc.pack(Rt.p(), pdt.ptr[2], o2 * vp, dt.ptr[kOperand + 5], o, false, 128, pR);
-    tc.pack(Rt.p(), pdt.ptr[5], o2 * vp, dt.ptr[kOperand + 5], o, false, 128, pR2);
-    tc.pack(T2p.p(), pdt.ptr[3], o * vp * vp, dt.ptr[kOperand + 7], o, true, 128, pT);
+    DevMem maxw(2 * sizeof(unsigned));
+    unsigned *mx = maxw.as<unsigned>();
+    SCESS_CUDA(cudaMemsetAsync(mx, 0, 2 * sizeof(unsigned), s));
+    tc.maxabs_into(P.p(), pdt.ptr[0], o * vp * vp, dt.ptr[kOperand + 1], v, false, mx);
+    tc.maxabs_into(T2p.p(), pdt.ptr[3], o * vp * vp, dt.ptr[kOperand + 7], o, true, mx);
+    tc.maxabs_into(Qt.p(), pdt.ptr[1], o2 * vp, dt.ptr[kOperand + 3], v, true, mx + 1);
+    tc.maxabs_into(Rt.p(), pdt.ptr[2], o2 * vp, dt.ptr[kOperand + 5], o, false, mx + 1);
+    tc.pack_with_max(P.p(), pdt.ptr[0], o * vp * vp, dt.ptr[kOperand + 1], v, false, 128, mx, false, pP);
+    tc.pack_with_max(T2p.p(), pdt.ptr[3], o * vp * vp, dt.ptr[kOperand + 7], o, true, 128, mx, true, pTx);
+    tc.pack_with_max(Qt.p(), pdt.ptr[1], o2 * vp, dt.ptr[kOperand + 3], v, true, 128, mx + 1, false, pQ);
+    tc.pack_with_max(Qt.p(), pdt.ptr[4], o2 * vp, dt.ptr[kOperand + 3], v, true, 128, mx + 1, false, pQ2);
+    tc.pack_with_max(Rt.p(), pdt.ptr[2], o2 * vp, dt.ptr[kOperand + 5], o, false, 128, mx + 1, false, pR);
+    tc.pack_with_max(Rt.p(), pdt.ptr[5], o2 * vp, dt.ptr[kOperand + 5], o, false, 128, mx + 1, false, pR2);
     ctx.sync();
     mP = TcEngine::map_of(pP, 128);
-    mQ = TcEngine::map_of(pQ, TcEngine::tile_n(Npq));
-    mQ2 = TcEngine::map_of(pQ2, TcEngine::tile_n(Npq));
+    mQ = TcEngine::map_of(pQ, 128);
+    mQ2 = TcEngine::map_of(pQ2, 128);
     mR = TcEngine::map_of(pR, 128);
     mR2 = TcEngine::map_of(pR2, 128);
-    mT = TcEngine::map_of(pT, TcEngine::tile_n(Nr));
+    mTx = TcEngine::map_of(pTx, 128);
+    // W_g[(y_l nb + z_l) nb + x_l][u + o s + o^2 t]: rows (u, x_l), columns (s, t)
+    gdt.build({table({{o, 1}, {nb, o3}}), table({{o, o}, {o, o2}})});
+    Sf.alloc((size_t)o2 * v * v * sizeof(float));
+    ovov_f32_kernel<<<(unsigned)std::min<int64_t>(ceil_div(o2 * v * v, 256), 16 * kNumSMs), 256, 0, s>>>(
+        d_eri, N, o, v, Sf.as<float>());
+    SCESS_CHECK_LAUNCH();
   }
+  const unsigned e3threads = (unsigned)std::min<int64_t>(round_up(o2, 32), 512);
   double *ws = nullptr;
   if (!mixed) {
     TableGemm probe;
@@ -354,50 +526,60 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
       for (int64_t C = 0; C <= Bk; C++) {
         if ((blocks_done & 15) == 0) ctl.poll();                                   // :123
         const int64_t U[3] = {A, Bk, C};
-        for (int p = 0; p < 6; p++) {
-          const int *pi = kPerm[p];
-          const int64_t X = U[pi[0]], Yb = U[pi[1]], Z = U[pi[2]];
-          const int64_t *rowPQ = dt.ptr[4 * p + 0], *colPQ = dt.ptr[4 * p + 1];
-          const int64_t *rowR = dt.ptr[4 * p + 2], *colR = dt.ptr[4 * p + 3];
-          if (mixed) {
-            TcEngine &tc = ctx.tensor_cores();
-            TcOut out;
-            out.C = W.as<float>();
-            out.fp32 = 1;
-            out.rowC = rowPQ;
-            out.colC = colPQ;
-            out.alpha = 1.0;
-            out.beta = p == 0 ? 0.0 : 1.0;
-            const bool qs = q_swapped(pi), rs = r_swapped(pi);
-            // Lane side (GEMM rows) = the operand whose first index is W's i:
-            // P rows (i',x,y) when i' is i, else the Q columns (j'/k' first).
-            const Packed &pq = qs ? pQ2 : pQ;
-            const CUtensorMap &mq = qs ? mQ2 : mQ;
-            if (pi[0] == 0) {
-              TcEngine::set_scales(out, pP, pq);
-              tc.gemm_maps(mP, mq, pP.Kpad, v, Mpq * (X * NB + Yb), Mpq, Npq * Z, Npq, out);
-            } else {
-              out.rowC = colPQ;
-              out.colC = rowPQ;
-              TcEngine::set_scales(out, pq, pP);
-              tc.gemm_maps(mq, mP, pP.Kpad, v, Npq * Z, Npq, Mpq * (X * NB + Yb), Mpq, out);
-            }
-            out.alpha = -1.0;
-            out.beta = 1.0;
-            const Packed &pr = rs ? pR2 : pR;
-            const CUtensorMap &mr = rs ? mR2 : mR;
-            if (pi[2] != 0) {  // R rows (i',j',x) / (j',i',x) start with W's i
-              out.rowC = rowR;
-              out.colC = colR;
-              TcEngine::set_scales(out, pr, pT);
-              tc.gemm_maps(mr, mT, pR.Kpad, o, Mr * X, Mr, Nr * (Yb * NB + Z), Nr, out);
-            } else {           // k' is W's i: t2 rows (k',y,z) on the lane side
-              out.rowC = colR;
-              out.colC = rowR;
-              TcEngine::set_scales(out, pT, pr);
-              tc.gemm_maps(mT, mr, pR.Kpad, o, Nr * (Yb * NB + Z), Nr, Mr * X, Mr, out);
-            }
-          } else {
+        if (mixed) {
+          TcEngine &tc = ctx.tensor_cores();
+          TcProblemSet ps;
+          ps.maps[0] = mP;
+          ps.maps[1] = mQ;
+          ps.maps[2] = mQ2;
+          ps.maps[3] = mR;
+          ps.maps[4] = mR2;
+          ps.maps[5] = mTx;
+          ps.nmaps = 6;
+          ps.M = Mg;
+          ps.N = Ng;
+          ps.ny = nb;
+          ps.nz = nb;
+          ps.ng = 3;
+          ps.nseg = 4;
+          ps.kbd = 2;  // E_T within ~5e-7 relative of FP64 (1.8e-7 with kbd = 1)
+          ps.cy = nb * nb * o3;
+          ps.cz = nb * o3;
+          const int kRoles[3][3] = {{0, 1, 2}, {1, 0, 2}, {2, 0, 1}};  // (x, y, z) of group g
+          const int64_t rp = o * nb * nb, rq = o2 * nb;                 // block strides of the packs
+          TcSegment &s0 = ps.seg[0], &s1 = ps.seg[1], &s2 = ps.seg[2], &s3 = ps.seg[3];
+          s0.mapA = 0; s0.mapB = 1; s0.Kpad = pP.Kpad;   // P(u,f,x,y) Q(f,s,t,z)
+          s1.mapA = 0; s1.mapB = 2; s1.Kpad = pP.Kpad;   // P(u,f,x,z) Q(f,t,s,y)
+          s2.mapA = 5; s2.mapB = 3; s2.Kpad = pTx.Kpad;  // -t2(m,u,z,x) R(s,t,m,y)
+          s3.mapA = 5; s3.mapB = 4; s3.Kpad = pTx.Kpad;  // -t2(m,u,y,x) R(t,s,m,z)
+          for (int g = 0; g < 3; g++) {
+            const int64_t X = U[kRoles[g][0]], Yb = U[kRoles[g][1]], Z = U[kRoles[g][2]];
+            ps.cg[g] = g * nb * nb * nb * o3;
+            s0.rowA0[g] = rp * (Yb + NB * X); s0.rowAy[g] = o * nb;
+            s0.rowB0[g] = rq * Z;             s0.rowBz[g] = o2;
+            s1.rowA0[g] = rp * (Z + NB * X);  s1.rowAz[g] = o * nb;
+            s1.rowB0[g] = rq * Yb;            s1.rowBy[g] = o2;
+            s2.rowA0[g] = rp * (X + NB * Z);  s2.rowAz[g] = o * nb;
+            s2.rowB0[g] = rq * Yb;            s2.rowBy[g] = o2;
+            s3.rowA0[g] = rp * (X + NB * Yb); s3.rowAy[g] = o * nb;
+            s3.rowB0[g] = rq * Z;             s3.rowBz[g] = o2;
+          }
+          TcOut out;
+          out.C = W.as<float>();
+          out.fp32 = 1;
+          out.rowC = gdt.ptr[0];
+          out.colC = gdt.ptr[1];
+          out.alpha = 1.0;
+          out.beta = 0.0;
+          TcEngine::set_scales(out, pP, pQ);
+          const double flops = 3.0 * nb * nb * 2.0 * (double)Mg * Ng * (2.0 * v + 2.0 * o);
+          tc.gemm_grouped(ps, out, flops, "tc_gemm[triples]");
+        } else {
+          for (int p = 0; p < 6; p++) {
+            const int *pi = kPerm[p];
+            const int64_t X = U[pi[0]], Yb = U[pi[1]], Z = U[pi[2]];
+            const int64_t *rowPQ = dt.ptr[4 * p + 0], *colPQ = dt.ptr[4 * p + 1];
+            const int64_t *rowR = dt.ptr[4 * p + 2], *colR = dt.ptr[4 * p + 3];
             TableGemm g;
             g.A = P.p();
             g.B = Qt.p();
@@ -445,10 +627,10 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
           }
         }
         const unsigned nblk = (unsigned)(nb * nb * nb);
-        TimedScope ts(ctx.timer, "triples_energy", 0.0, (double)nblk * o3 * (mixed ? 4 : 8), s);
+        TimedScope ts(ctx.timer, "triples_energy", 0.0, (double)nblk * o3 * (mixed ? 3 * 4 : 8), s);
         if (mixed)
-          triples_energy_kernel<float, float><<<nblk, 256, ysmem, s>>>(
-              W.as<float>(), o, v, nb, A, Bk, C, d_eps, d_t1, d_eri, N, energies.p());
+          triples_energy3_kernel<<<nblk, e3threads, ysmem, s>>>(
+              W.as<float>(), o, v, nb, A, Bk, C, d_eps, d_t1, Sf.as<float>(), energies.p());
         else
           triples_energy_kernel<double, double><<<nblk, 256, ysmem, s>>>(
               W.d(), o, v, nb, A, Bk, C, d_eps, d_t1, d_eri, N, energies.p());
