@@ -43,6 +43,12 @@ CPU_SAMPLE = ('one full FP64 CCSD iteration of the NumPy oracle (MP2 guess, BLAS
               'o=10, v=90 lands within 16% of this estimate)')
 
 
+# DRAM bytes (read + write) of one grouped (T) GEMM launch at o=20, nb=12,
+# measured with ncu: the three W buffers (166 MB) are written once, 109 MB of
+# them reach DRAM, operands are read mostly from L2.
+TRIPLES_LAUNCH_TRAFFIC = 138.9e6
+
+
 def peaks():
     p = os.path.join(ROOT, 'MEASURED_PEAKS.json')
     if os.path.exists(p):
@@ -307,7 +313,11 @@ def main():
                 'tensor_pipe_frac': 3.0 * issued / bf16_peak,
                 'launches': tc['launches'], 'avg_launch_ms': avg_ms,
                 'algorithmic_flops_per_launch': per_launch_alg,
-                'traffic': None, 'top_kernel_by_time': top}
+                'traffic': TRIPLES_LAUNCH_TRAFFIC if (o, v) == (20, 180) else None,
+                'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of one grouped '
+                                  '(T) launch at o=20 v=96, which has the same launch shape '
+                                  '(nb=12, 3456 work units) as o=20 v=180',
+                'top_kernel_by_time': top}
     share = {k: round(v['ms'] / max(sum(x['ms'] for x in prof.values()), 1e-9), 4) for k, v in prof.items()}
 
     # ---- FP64 form on the same workload -------------------------------------------------------

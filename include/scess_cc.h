@@ -209,6 +209,21 @@ int scess_rccsd_residual_vjp_df(scess_ctx *ctx, const double *B, int64_t naux, i
                                 const double *g_r1, const double *g_r2, int32_t precision,
                                 double *g_t1, double *g_t2, double *g_B);
 
+/* Vector-Jacobian product of E_(T) (RCCSD_TriplesCorrection, RCCSD_T.cpp:17-168;
+ * the reference has no derivative code), FP64: for a cotangent g_e, writes
+ * g_e dE_T/dt1 (o*v), g_e dE_T/dt2 (o^2 v^2) and, when g_eri is not NULL,
+ * g_e dE_T/deri (nmo^4, eri layout; nonzero only on the (ov|vv), (oo|vo) and
+ * (ov|ov) blocks E_T reads).  e_t (may be NULL) receives E_T.  The forward
+ * W is recomputed block by block, so the memory use is that of the FP64 (T). */
+int scess_rccsd_triples_vjp(scess_ctx *ctx, const double *eri, const double *eps, int64_t nmo,
+                            int64_t nocc, const double *t1, const double *t2, double g_e,
+                            double *e_t, double *g_t1, double *g_t2, double *g_eri);
+/* Same from DF factors; g_B (naux x nmo x nmo, may be NULL) = g_e dE_T/dB. */
+int scess_rccsd_triples_vjp_df(scess_ctx *ctx, const double *B, int64_t naux, const double *eps,
+                               int64_t nmo, int64_t nocc, const double *t1, const double *t2,
+                               double g_e, double *e_t, double *g_t1, double *g_t2,
+                               double *g_B);
+
 /* CCSD Lambda (left-hand) equations at converged t1/t2 (no counterpart in the
  * reference).  Omega(t; f) is the closed-shell residual with the Fock terms that
  * UpdateAmplitudes drops for canonical orbitals (RCCSD.cpp:13-15, :109), the

@@ -82,3 +82,61 @@ def residual_vjp(eri, o, t1, t2, g1, g2):
     loss = (r1 * torch.tensor(g1)).sum() + (r2 * torch.tensor(g2)).sum()
     loss.backward()
     return T1.grad.numpy(), T2.grad.numpy(), E.grad.numpy()
+
+
+def _r3_torch(Y):
+    """r3(Y)_ijk = 4Y_ijk + Y_kij + Y_jki - 2Y_kji - 2Y_ikj - 2Y_jik on the last three axes."""
+    def tp(p):
+        return Y.permute(0, 1, 2 + p[0], 2 + p[1], 2 + p[2])
+    return (4.0 * Y + tp((1, 2, 0)) + tp((2, 0, 1)) - 2.0 * tp((2, 1, 0))
+            - 2.0 * tp((0, 2, 1)) - 2.0 * tp((1, 0, 2)))
+
+
+def triples_energy(eri, eps, o, t1, t2):
+    """E_(T) of RCCSD_TriplesCorrection (RCCSD_T.cpp:17-168) as a torch function of
+    (eri, t1, t2), in the batched per-``a`` form of ``oracle.rccsd_t.rccsd_triples_correction``
+    (P/R/S/Q repack :29-56, raw w :62-68, the six terms of Symmetrise :78-106,
+    V :70-75, r3 :152-154, degeneracy :135-139, denominators :155, factor 2 :167)."""
+    O, V = slice(0, o), slice(o, None)
+    P = eri[O, V, V, V].permute(0, 3, 2, 1)      # P(i,f,a,b) = eri(i, o+b, o+a, o+f)
+    R = eri[O, O, V, O].permute(0, 3, 1, 2)      # R(i,j,m,a) = eri(i, m, o+a, j)
+    S = eri[O, O, V, V]                          # S(i,j,a,b) = eri(i, j, o+a, o+b)
+    Q = t2.permute(3, 1, 0, 2)                   # Q(f,j,k,c) = t2(k,j,c,f)
+    v = P.shape[1]
+    e = torch.as_tensor(np.asarray(eps), dtype=torch.float64)
+    eo, ev = e[:o], e[o:]
+    Dijk = eo[:, None, None] + eo[None, :, None] + eo[None, None, :]
+    energy = torch.zeros((), dtype=torch.float64)
+    for a in range(v):
+        n = a + 1
+        A1 = _es('ifb,fjkc->bcijk', P[:, :, a, :n], Q[:, :, :, :n])
+        A1 = A1 - _es('ijm,mkbc->bcijk', R[:, :, :, a], t2[:, :, :n, :n])
+        A2 = _es('ifb,fjkc->bcijk', P[:, :, :n, a], Q[:, :, :, :n])
+        A2 = A2 - _es('ijmb,mkc->bcijk', R[:, :, :, :n], t2[:, :, a, :n])
+        A3 = _es('ifbc,fjk->bcijk', P[:, :, :n, :n], Q[:, :, :, a])
+        A3 = A3 - _es('ijmb,mkc->bcijk', R[:, :, :, :n], t2[:, :, :n, a])
+        W = (A1 + A1.permute(1, 0, 2, 4, 3) + A2.permute(0, 1, 3, 2, 4)
+             + A3.permute(0, 1, 4, 2, 3) + A2.permute(1, 0, 3, 4, 2)
+             + A3.permute(1, 0, 4, 3, 2))
+        Vt = (_es('i,jkbc->bcijk', t1[:, a], S[:, :, :n, :n])
+              + _es('jb,ikc->bcijk', t1[:, :n], S[:, :, a, :n])
+              + _es('kc,ijb->bcijk', t1[:, :n], S[:, :, a, :n]))
+        r3 = _r3_torch(W + Vt)
+        bb, cc = np.meshgrid(np.arange(n), np.arange(n), indexing='ij')
+        deg = np.ones((n, n))
+        deg[(bb == a) | (cc == bb)] = 2.0
+        deg[cc == a] = 6.0
+        wgt = torch.as_tensor(np.where(cc <= bb, 1.0 / deg, 0.0))
+        d3 = Dijk[None, None] - (ev[a] + ev[:n, None] + ev[None, :n])[:, :, None, None, None]
+        energy = energy + ((W * r3 / d3).sum(dim=(2, 3, 4)) * wgt).sum()
+    return 2.0 * energy
+
+
+def triples_vjp(eri, eps, o, t1, t2):
+    """Reference gradient of E_(T) (numpy in, numpy out): (E_T, dE/dt1, dE/dt2, dE/deri)."""
+    E = torch.tensor(np.asarray(eri), dtype=torch.float64, requires_grad=True)
+    T1 = torch.tensor(np.asarray(t1), dtype=torch.float64, requires_grad=True)
+    T2 = torch.tensor(np.asarray(t2), dtype=torch.float64, requires_grad=True)
+    e_t = triples_energy(E, eps, o, T1, T2)
+    e_t.backward()
+    return float(e_t.detach()), T1.grad.numpy(), T2.grad.numpy(), E.grad.numpy()

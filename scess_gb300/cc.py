@@ -114,6 +114,11 @@ EXPORTS = {
                                    C.c_int32, _dp]),
     'scess_einsum': (C.c_int, [C.c_void_p, C.c_char_p, C.c_double, _dp, C.c_int32, _i64p, _dp,
                                C.c_int32, _i64p, C.c_double, _dp, C.c_int32, _i64p, C.c_int32]),
+    'scess_rccsd_triples_vjp': (C.c_int, [C.c_void_p, _dp, _dp, C.c_int64, C.c_int64, _dp, _dp,
+                                          C.c_double, C.POINTER(C.c_double), _dp, _dp, _dp]),
+    'scess_rccsd_triples_vjp_df': (C.c_int, [C.c_void_p, _dp, C.c_int64, _dp, C.c_int64,
+                                             C.c_int64, _dp, _dp, C.c_double,
+                                             C.POINTER(C.c_double), _dp, _dp, _dp]),
     'scess_einsum_static': (C.c_int, [C.c_char_p, C.c_double, C.c_void_p, C.c_int32, _i64p,
                                       C.c_void_p, C.c_int32, _i64p, C.c_double, C.c_void_p,
                                       C.c_int32, _i64p, C.c_void_p]),
@@ -371,6 +376,31 @@ class Context:
                                                    _ptr(gI))
         self._check(st, 'scess_rccsd_residual_vjp')
         return gt1, gt2, gI
+
+    def triples_vjp(self, eri=None, eps=None, nocc=None, t1=None, t2=None, g_e=1.0, B=None,
+                    want_integrals=False):
+        """(E_T, g_t1, g_t2, g_eri or g_B): g_e times the gradient of E_(T) (FP64)."""
+        eps = _f64(eps)
+        N = eps.shape[0]
+        o, v = int(nocc), N - int(nocc)
+        t1f, t2f = _f64(t1, (o, v)), _f64(t2, (o, o, v, v))
+        gt1 = np.zeros((o, v), order='F')
+        gt2 = np.zeros((o, o, v, v), order='F')
+        et = C.c_double(0.0)
+        if B is not None:
+            Bf = _f64(B)
+            gI = np.zeros(Bf.shape, order='F') if want_integrals else None
+            st = self.lib.scess_rccsd_triples_vjp_df(self.h, _ptr(Bf), Bf.shape[0], _ptr(eps), N, o,
+                                                     _ptr(t1f), _ptr(t2f), float(g_e), C.byref(et),
+                                                     _ptr(gt1), _ptr(gt2), _ptr(gI))
+        else:
+            ef = _f64(eri, (N, N, N, N))
+            gI = np.zeros((N, N, N, N), order='F') if want_integrals else None
+            st = self.lib.scess_rccsd_triples_vjp(self.h, _ptr(ef), _ptr(eps), N, o, _ptr(t1f),
+                                                  _ptr(t2f), float(g_e), C.byref(et), _ptr(gt1),
+                                                  _ptr(gt2), _ptr(gI))
+        self._check(st, 'scess_rccsd_triples_vjp')
+        return et.value, gt1, gt2, gI
 
     # -- Lambda equations and the one-particle density ---------------------------------------
     def lambda_solve(self, eri, eps, nocc, t1, t2, precision='fp64', **opts):

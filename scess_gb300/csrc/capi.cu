@@ -285,6 +285,88 @@ int scess_rccsd_triples_df(scess_ctx *ctx, const double *B, int64_t naux, const 
   return triples_common(ctx, nullptr, B, naux, eps, nmo, nocc, t1, t2, precision, e_t);
 }
 
+static int triples_vjp_common(scess_ctx *ctx, const double *eri, const double *B, int64_t naux,
+                              const double *eps, int64_t nmo, int64_t nocc, const double *t1,
+                              const double *t2, double g_e, double *e_t, double *g_t1,
+                              double *g_t2, double *g_eri, double *g_B) {
+  return guard(ctx, [&](scess::Ctx &c) {
+    check_shape(nmo, nocc);
+    need(eps, "eps");
+    need(t1, "t1");
+    need(t2, "t2");
+    need(g_t1, "g_t1");
+    need(g_t2, "g_t2");
+    if (!std::isfinite(g_e)) throw Error(SCESS_ERR_INVALID, "g_e is not finite");
+    const int64_t o = nocc, v = nmo - nocc, N = nmo, n1 = o * v, n2 = o * o * v * v;
+    const int64_t N4 = N * N * N * N;
+    host_finite(eps, nmo, "eps");
+    scess::Control ctl;
+    ctl.cancel = c.cancel;
+    ctl.user = c.user;
+    scess::DTensor d_eri({N, N, N, N}), dB;
+    scess::Tape dfTape;
+    if (eri) {
+      scess::upload(c, d_eri.p(), eri, N4);
+      device_finite(c, d_eri.p(), N4, "eri");
+    } else {
+      dB = scess::DTensor({naux, N, N});
+      scess::upload(c, dB.p(), B, naux * N * N);
+      device_finite(c, dB.p(), naux * N * N, "B");
+      c.tape = &dfTape;  // eri(p,q,r,s) = sum_Q B(Q,p,r) B(Q,q,s), recorded for g_B
+      scess::einsum(c, "Qpr,Qqs->pqrs", 1.0, dB.v, dB.v, 0.0, d_eri.v, scess::Backend::FP64);
+      c.tape = nullptr;
+    }
+    scess::DTensor d_eps({nmo}), d_t1({o, v}), d_t2({o, o, v, v}), gt1({o, v}), gt2({o, o, v, v});
+    scess::upload(c, d_eps.p(), eps, nmo);
+    scess::upload(c, d_t1.p(), t1, n1);
+    scess::upload(c, d_t2.p(), t2, n2);
+    device_finite(c, d_t1.p(), n1, "t1");
+    device_finite(c, d_t2.p(), n2, "t2");
+    SCESS_CUDA(cudaMemsetAsync(gt1.p(), 0, n1 * sizeof(double), c.stream));
+    SCESS_CUDA(cudaMemsetAsync(gt2.p(), 0, n2 * sizeof(double), c.stream));
+    const bool need_eri = g_eri || g_B;
+    scess::DTensor geri;
+    if (need_eri) {
+      geri = scess::DTensor({N, N, N, N});
+      SCESS_CUDA(cudaMemsetAsync(geri.p(), 0, N4 * sizeof(double), c.stream));
+    }
+    ctl.poll();
+    const double et = scess::rccsd_triples_vjp(c, d_eri.p(), nmo, nocc, d_eps.p(), d_t1.p(),
+                                               d_t2.p(), g_e, ctl, gt1.p(), gt2.p(),
+                                               need_eri ? geri.p() : nullptr);
+    if (e_t) *e_t = et;
+    scess::download(c, g_t1, gt1.p(), n1);
+    scess::download(c, g_t2, gt2.p(), n2);
+    if (g_eri) scess::download(c, g_eri, geri.p(), N4);
+    if (g_B) {
+      scess::DTensor gB({naux, N, N});
+      SCESS_CUDA(cudaMemsetAsync(gB.p(), 0, (size_t)naux * N * N * sizeof(double), c.stream));
+      scess::GradMap gm;
+      gm.add(d_eri.p(), N4, geri.p());
+      gm.add(dB.p(), naux * N * N, gB.p());
+      scess::reverse_sweep(c, dfTape, gm, scess::Backend::FP64);
+      scess::download(c, g_B, gB.p(), naux * N * N);
+    }
+  });
+}
+
+int scess_rccsd_triples_vjp(scess_ctx *ctx, const double *eri, const double *eps, int64_t nmo,
+                            int64_t nocc, const double *t1, const double *t2, double g_e,
+                            double *e_t, double *g_t1, double *g_t2, double *g_eri) {
+  if (!eri) return SCESS_ERR_INVALID;
+  return triples_vjp_common(ctx, eri, nullptr, 0, eps, nmo, nocc, t1, t2, g_e, e_t, g_t1, g_t2,
+                            g_eri, nullptr);
+}
+
+int scess_rccsd_triples_vjp_df(scess_ctx *ctx, const double *B, int64_t naux, const double *eps,
+                               int64_t nmo, int64_t nocc, const double *t1, const double *t2,
+                               double g_e, double *e_t, double *g_t1, double *g_t2,
+                               double *g_B) {
+  if (!B || naux <= 0) return SCESS_ERR_INVALID;
+  return triples_vjp_common(ctx, nullptr, B, naux, eps, nmo, nocc, t1, t2, g_e, e_t, g_t1, g_t2,
+                            nullptr, g_B);
+}
+
 static int state_create(scess_ctx *ctx, const double *eri, const double *B, int64_t naux,
                         const double *eps, int64_t nmo, int64_t nocc, const double *f12_residual,
                         const double *f12_energy, const scess_rccsd_options *opts,

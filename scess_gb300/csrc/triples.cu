@@ -301,6 +301,10 @@ struct DevTables {
 const int kPerm[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
 
 int choose_nb(int64_t o, int64_t v, size_t welem_bytes, size_t budget) {
+  if (const char *env = std::getenv("SCESS_T_NB")) {  // block size override (tests, tuning)
+    const int nb = std::atoi(env);
+    if (nb >= 1) return (int)std::min<int64_t>(nb, v);
+  }
   const double o3 = (double)o * o * o;
   int nb = (int)std::floor(std::cbrt((double)budget / (welem_bytes * o3)));
   nb = std::max(1, std::min<int>(nb, (int)v));
@@ -310,50 +314,37 @@ int choose_nb(int64_t o, int64_t v, size_t welem_bytes, size_t budget) {
   return nb;
 }
 
-// Block size of the grouped tensor-core form: GEMM rows (u, x_l) = o nb fill
-// the 128-row tiles well, the padded virtual range vp = NB nb stays close to v,
-// and the three W buffers (3 nb^3 o^3 floats) stay within 256 MiB; ties go to
-// the larger block (fewer, larger launches).  SCESS_T_NB overrides it.
-int choose_nb_grouped(int64_t o, int64_t v) {
-  if (const char *env = std::getenv("SCESS_T_NB")) {
-    const int nb = std::atoi(env);
-    if (nb >= 1) return (int)std::min<int64_t>(nb, v);
-  }
-  int best = 1;
-  double best_score = -1.0;
-  const double o3 = (double)o * o * o;
-  for (int nb = 1; nb <= std::min<int64_t>(v, 64); nb++) {
-    if (nb > 1 && 3.0 * nb * nb * nb * o3 * 4.0 > double(256 << 20)) break;
-    const double rows = (double)o * nb;
-    const double effM = rows / (128.0 * std::ceil(rows / 128.0));
-    const double vp = (double)ceil_div(v, nb) * nb;
-    const double effV = std::pow((double)v / vp, 3.0);
-    const double score = effM * effV;
-    if (score >= best_score * (1.0 - 1e-9)) {
-      best = nb;
-      best_score = std::max(score, best_score);
-    }
-  }
-  return best;
-}
+// W tables: W's unit-stride index i is kept first on the lane side (GEMM rows)
+// or on the per-thread side (GEMM columns) of every epilogue: when i is the k'
+// of a permutation the Q operand is taken in (k', j', z) column order, when it
+// is the j' of an R product the R operand is taken in (j', i', x) row order.
+bool q_swapped(const int *pi) { return pi[2] == 0; }
+bool r_swapped(const int *pi) { return pi[1] == 0; }
 
-}  // namespace
+// FP64 repacks of RCCSD_T.cpp:30-56 (virtuals padded to vp) and the offset
+// tables of the block-triple GEMMs: per permutation p the W rows / columns of
+// its P.Q and R.t2 products (dt.ptr[4p .. 4p+3]), then the operand tables
+// (dt.ptr[kOperand + 0 .. 9]).
+struct TriplesSetup {
+  int64_t o = 0, v = 0, N = 0, nb = 0, NB = 0, vp = 0;
+  DTensor P, Qt, Rt, T2p;
+  DevTables dt;
+  size_t kOperand = 0;
+  void build(Ctx &ctx, const double *d_eri, const double *d_t2);
+  int64_t Mpq() const { return o * nb * nb; }
+  int64_t Npq() const { return o * o * nb; }
+  int64_t Mr() const { return o * o * nb; }
+  int64_t Nr() const { return o * nb * nb; }
+};
 
-double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, const double *d_eps,
-                     const double *d_t1, const double *d_t2, bool mixed, const Control &ctl,
-                     TriplesStats *stats) {
-  const int64_t v = nmo - o, N = nmo;
+void TriplesSetup::build(Ctx &ctx, const double *d_eri, const double *d_t2) {
   cudaStream_t s = ctx.stream;
-  const int nb = mixed ? choose_nb_grouped(o, v) : choose_nb(o, v, 8, size_t(128) << 20);
-  const int64_t NB = ceil_div(v, nb), vp = NB * nb;
-  const int64_t o2 = o * o, o3 = o2 * o;
-  const int64_t N2 = N * N, N3 = N2 * N;
-
+  const int64_t o2 = o * o, o3 = o2 * o, N2 = N * N, N3 = N2 * N;
   // Zero-padded FP64 repacks (RCCSD_T.cpp:30-56), virtual indices padded to vp.
-  DTensor P({o, v, vp, vp});   // P(i,f,a,b) = (ia|bf) = eri(i, o+b, o+a, o+f)
-  DTensor Qt({v, o, o, vp});   // Q(f,j,k,c) = t2(k,j,c,f)
-  DTensor Rt({o, o, o, vp});   // R(i,j,m,a) = (ia|mj) = eri(i, m, o+a, j)
-  DTensor T2p({o, o, vp, vp}); // t2(m,k,b,c)
+  P = DTensor({o, v, vp, vp});   // P(i,f,a,b) = (ia|bf) = eri(i, o+b, o+a, o+f)
+  Qt = DTensor({v, o, o, vp});   // Q(f,j,k,c) = t2(k,j,c,f)
+  Rt = DTensor({o, o, o, vp});   // R(i,j,m,a) = (ia|mj) = eri(i, m, o+a, j)
+  T2p = DTensor({o, o, vp, vp}); // t2(m,k,b,c)
   SCESS_CUDA(cudaMemsetAsync(P.p(), 0, P.size() * sizeof(double), s));
   SCESS_CUDA(cudaMemsetAsync(Qt.p(), 0, Qt.size() * sizeof(double), s));
   SCESS_CUDA(cudaMemsetAsync(Rt.p(), 0, Rt.size() * sizeof(double), s));
@@ -396,8 +387,6 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   // (GEMM columns) of every epilogue: when i is the k' of a permutation the Q
   // operand is taken in (k', j', z) column order, when it is the j' of an R
   // product the R operand is taken in (j', i', x) row order.
-  auto q_swapped = [](const int *pi) { return pi[2] == 0; };
-  auto r_swapped = [](const int *pi) { return pi[1] == 0; };
   std::vector<std::vector<int64_t>> ts;
   for (int p = 0; p < 6; p++) {
     const int *pi = kPerm[p];
@@ -412,7 +401,7 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
       ts.push_back(table({{o, sw[pi[0]]}, {o, sw[pi[1]]}, {nb, su[pi[0]]}}));     // R rows (i',j',x)
     ts.push_back(table({{o, sw[pi[2]]}, {nb, su[pi[1]]}, {nb, su[pi[2]]}}));      // R cols (k',y,z)
   }
-  const size_t kOperand = ts.size();
+  kOperand = ts.size();
   // operand tables (FP64 path): P rows (i',x,y), f; Q cols (j',k',z), f; R rows, m; t2 cols, m
   ts.push_back(table({{o, 1}, {nb, o * v}, {nb, o * v * vp}}));                  // +0: P rows
   ts.push_back(table({{v, o}}));                                                 // +1: P k (f)
@@ -424,8 +413,296 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   ts.push_back(table({{o, 1}}));                                                 // +7: t2 k (m)
   ts.push_back(table({{o, v * o}, {o, v}, {nb, v * o2}}));                       // +8: Q cols (k,j,z)
   ts.push_back(table({{o, o}, {o, 1}, {nb, o3}}));                               // +9: R rows (j,i,x)
-  DevTables dt;
   dt.build(ts);
+}
+
+// The 12 FP64 GEMMs of block triple U = (A, B, C): W[(a_l,b_l,c_l)][i,j,k] =
+// sum over the six permutations of the raw P.Q - R.t2 product (GetW,
+// RCCSD_T.cpp:62-68), each added at its permuted position (Symmetrise :78-106).
+void w_block_fp64(Ctx &ctx, const TriplesSetup &T, const int64_t U[3], double *W, double *ws) {
+  cudaStream_t s = ctx.stream;
+  const int64_t o = T.o, v = T.v, nb = T.nb, vp = T.vp, o2 = o * o, o3 = o2 * o;
+  for (int p = 0; p < 6; p++) {
+    const int *pi = kPerm[p];
+    const int64_t X = U[pi[0]], Yb = U[pi[1]], Z = U[pi[2]];
+    const int64_t *rowPQ = T.dt.ptr[4 * p + 0], *colPQ = T.dt.ptr[4 * p + 1];
+    const int64_t *rowR = T.dt.ptr[4 * p + 2], *colR = T.dt.ptr[4 * p + 3];
+    TableGemm g;
+    g.A = T.P.p();
+    g.B = T.Qt.p();
+    g.C = W;
+    g.rowA = T.dt.ptr[T.kOperand + 0];
+    g.kA = T.dt.ptr[T.kOperand + 1];
+    g.colB = T.dt.ptr[T.kOperand + (q_swapped(pi) ? 8 : 2)];
+    g.kB = T.dt.ptr[T.kOperand + 3];
+    g.rowC = rowPQ;
+    g.colC = colPQ;
+    g.baseA = o * v * (X * nb) + o * v * vp * (Yb * nb);
+    g.baseB = v * o2 * (Z * nb);
+    g.M = T.Mpq();
+    g.N = T.Npq();
+    g.K = v;
+    g.alpha = 1.0;
+    g.beta = p == 0 ? 0.0 : 1.0;
+    g.aUnitM = 1;
+    g.bUnitN = 0;
+    {
+      TimedScope ts(ctx.timer, "dgemm_table", 2.0 * g.M * g.N * g.K, 0.0, s);
+      dgemm_table(g, ws, s);
+    }
+    TableGemm h;
+    h.A = T.Rt.p();
+    h.B = T.T2p.p();
+    h.C = W;
+    h.rowA = T.dt.ptr[T.kOperand + (r_swapped(pi) ? 9 : 4)];
+    h.kA = T.dt.ptr[T.kOperand + 5];
+    h.colB = T.dt.ptr[T.kOperand + 6];
+    h.kB = T.dt.ptr[T.kOperand + 7];
+    h.rowC = rowR;
+    h.colC = colR;
+    h.baseA = o3 * (X * nb);
+    h.baseB = o2 * (Yb * nb) + o2 * vp * (Z * nb);
+    h.M = T.Mr();
+    h.N = T.Nr();
+    h.K = o;
+    h.alpha = -1.0;
+    h.beta = 1.0;
+    h.aUnitM = r_swapped(pi) ? 0 : 1;
+    h.bUnitN = 0;
+    TimedScope ts(ctx.timer, "dgemm_table", 2.0 * h.M * h.N * h.K, 0.0, s);
+    dgemm_table(h, ws, s);
+  }
+}
+
+// Gradient of the block triple's energy with respect to its W and V (FP64).
+// With L = r3 (a symmetric linear map over the six orderings of (i,j,k): the
+// two cyclic shifts are each other's transposes, the three swaps are their own)
+// and the triple's term E_abc = (2/deg) sum W L(W + V) / D:
+//   dE/dW = (2/deg) [L(Y)/D + L(W/D)],   dE/dV = (2/deg) L(W/D),   Y = W + V.
+// G (W's layout) receives gE dE/dW, zero for triples outside a >= b >= c; dE/dV
+// flows into t1 and the (ia|jb) slices S (o x o x v x v) through
+// V_ijk = t1_ia S(j,k,b,c) + t1_jb S(i,k,a,c) + t1_kc S(i,j,a,b) (:70-75, :132)
+// with global FP64 atomics.  Also writes the triple's energy like the energy
+// kernel.  One CTA per (a_l, b_l, c_l); threads own (i, j) pairs and walk k.
+__global__ void __launch_bounds__(256) triples_grad_kernel(
+    const double *__restrict__ W, double *__restrict__ G, int64_t o, int64_t v, int64_t nb,
+    int64_t A, int64_t Bk, int64_t C, const double *__restrict__ eps,
+    const double *__restrict__ t1, const double *__restrict__ eri, int64_t N, double gE,
+    double *__restrict__ energies, double *__restrict__ g_t1, double *__restrict__ g_S) {
+  const int64_t al = blockIdx.x / (nb * nb), bl = (blockIdx.x / nb) % nb, cl = blockIdx.x % nb;
+  const int64_t a = A * nb + al, b = Bk * nb + bl, c = C * nb + cl;
+  const int oo = (int)o, o2 = oo * oo, o3 = o2 * oo;
+  const double *Wt = W + ((al * nb + bl) * nb + cl) * (int64_t)o3;
+  double *Gt = G + ((al * nb + bl) * nb + cl) * (int64_t)o3;
+  if (a >= v || b >= v || c >= v || b > a || c > b) {
+    for (int e = threadIdx.x; e < o3; e += blockDim.x) Gt[e] = 0.0;
+    return;
+  }
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  __shared__ double red[32];
+  const int p1 = oo | 1, p2 = (p1 * oo) | 1;
+  double *Y = reinterpret_cast<double *>(sm_raw);
+  double *Sbc = Y + p2 * oo, *Sac = Sbc + o2, *Sab = Sac + o2;
+  double *gSbc = Sab + o2, *gSac = gSbc + o2;
+  double *ta = gSac + o2, *tb = ta + oo, *tc = tb + oo, *eo = tc + oo;
+  double *gta = eo + oo, *gtb = gta + oo, *gtc = gtb + oo;
+  const int64_t N2 = N * N, N3 = N2 * N;
+  for (int e = threadIdx.x; e < o2; e += blockDim.x) {
+    const int i = e % oo, j = e / oo;
+    Sbc[e] = eri[i + N * j + (o + b) * N2 + (o + c) * N3];
+    Sac[e] = eri[i + N * j + (o + a) * N2 + (o + c) * N3];
+    Sab[e] = eri[i + N * j + (o + a) * N2 + (o + b) * N3];
+    gSbc[e] = 0.0;
+    gSac[e] = 0.0;
+  }
+  for (int i = threadIdx.x; i < oo; i += blockDim.x) {
+    ta[i] = t1[i + o * a];
+    tb[i] = t1[i + o * b];
+    tc[i] = t1[i + o * c];
+    eo[i] = eps[i];
+    gta[i] = gtb[i] = gtc[i] = 0.0;
+  }
+  __syncthreads();
+  const double evirt = eps[o + a] + eps[o + b] + eps[o + c];
+  double deg = 1.0;                                                                 // :135-139
+  if (a == c) deg = 6.0;
+  else if (a == b || b == c) deg = 2.0;
+  const double fac = gE * 2.0 / deg;
+  auto L = [&](int i, int j, int k) {  // r3 at (i,j,k) of the array in Y   :152-154
+    return 4.0 * Y[i + p1 * j + p2 * k] + Y[k + p1 * i + p2 * j] + Y[j + p1 * k + p2 * i] -
+           2.0 * (Y[k + p1 * j + p2 * i] + Y[i + p1 * k + p2 * j] + Y[j + p1 * i + p2 * k]);
+  };
+  // Y = W + V
+  for (int pr = threadIdx.x; pr < o2; pr += blockDim.x) {
+    const int i = pr % oo, j = pr / oo;
+    for (int k = 0; k < oo; k++)
+      Y[i + p1 * j + p2 * k] = Wt[pr + o2 * k] + ta[i] * Sbc[j + oo * k] + tb[j] * Sac[i + oo * k] +
+                               tc[k] * Sab[pr];
+  }
+  __syncthreads();
+  // G = fac L(Y)/D; energy term W L(Y)/D
+  double acc = 0.0;
+  for (int pr = threadIdx.x; pr < o2; pr += blockDim.x) {
+    const int i = pr % oo, j = pr / oo;
+    for (int k = 0; k < oo; k++) {
+      const double d = ((eo[i] + eo[j]) + eo[k]) - evirt;                           // :155
+      const double ly = L(i, j, k) / d;
+      Gt[pr + o2 * k] = fac * ly;
+      acc += Wt[pr + o2 * k] * ly;                                                  // :156
+    }
+  }
+  __syncthreads();
+  // Y = W/D
+  for (int pr = threadIdx.x; pr < o2; pr += blockDim.x) {
+    const int i = pr % oo, j = pr / oo;
+    for (int k = 0; k < oo; k++)
+      Y[i + p1 * j + p2 * k] = Wt[pr + o2 * k] / (((eo[i] + eo[j]) + eo[k]) - evirt);
+  }
+  __syncthreads();
+  // G += fac L(W/D); dE/dV = fac L(W/D) into t1 and S
+  for (int pr = threadIdx.x; pr < o2; pr += blockDim.x) {
+    const int i = pr % oo, j = pr / oo;
+    double sa = 0.0, sb = 0.0, sab = 0.0;
+    for (int k = 0; k < oo; k++) {
+      const double gv = fac * L(i, j, k);
+      Gt[pr + o2 * k] += gv;
+      sa += gv * Sbc[j + oo * k];      // t1_ia (jb|kc)
+      sb += gv * Sac[i + oo * k];      // t1_jb (ia|kc)
+      sab += gv * tc[k];               // (ia|jb) t1_kc
+      atomicAdd(&gtc[k], gv * Sab[pr]);
+      atomicAdd(&gSbc[j + oo * k], gv * ta[i]);
+      atomicAdd(&gSac[i + oo * k], gv * tb[j]);
+    }
+    atomicAdd(&gta[i], sa);
+    atomicAdd(&gtb[j], sb);
+    atomicAdd(&g_S[pr + o2 * (a + v * b)], sab);  // (i,j) owned by this thread
+  }
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+  const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+  if (lane == 0) red[wi] = acc;
+  __syncthreads();
+  for (int e = threadIdx.x; e < o2; e += blockDim.x) {
+    atomicAdd(&g_S[e + o2 * (b + v * c)], gSbc[e]);
+    atomicAdd(&g_S[e + o2 * (a + v * c)], gSac[e]);
+  }
+  for (int i = threadIdx.x; i < oo; i += blockDim.x) {
+    atomicAdd(&g_t1[i + o * a], gta[i]);
+    atomicAdd(&g_t1[i + o * b], gtb[i]);
+    atomicAdd(&g_t1[i + o * c], gtc[i]);
+  }
+  if (threadIdx.x == 0) {
+    double sum = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) sum += red[q];
+    energies[triple_id(a, b, c)] = sum / deg;
+  }
+}
+
+// Transposed GEMMs of w_block_fp64 for block triple U: with G = dE/dW,
+//   gP  += G Q,   gQ  += G^T P,   gR -= G' t2,   gt2 -= G'^T R
+// per permutation, G read through that permutation's W tables.
+void g_block_fp64(Ctx &ctx, const TriplesSetup &T, const int64_t U[3], const double *G, double *gP,
+                  double *gQt, double *gRt, double *gT2p, bool integrals, double *ws) {
+  cudaStream_t s = ctx.stream;
+  const int64_t o = T.o, v = T.v, nb = T.nb, vp = T.vp, o2 = o * o, o3 = o2 * o;
+  const size_t K0 = T.kOperand;
+  auto run = [&](TableGemm &g) {
+    TimedScope ts(ctx.timer, "dgemm_table", 2.0 * g.M * g.N * g.K, 0.0, s);
+    dgemm_table(g, ws, s);
+  };
+  for (int p = 0; p < 6; p++) {
+    const int *pi = kPerm[p];
+    const int64_t X = U[pi[0]], Yb = U[pi[1]], Z = U[pi[2]];
+    const int64_t *rowPQ = T.dt.ptr[4 * p + 0], *colPQ = T.dt.ptr[4 * p + 1];
+    const int64_t *rowR = T.dt.ptr[4 * p + 2], *colR = T.dt.ptr[4 * p + 3];
+    const int64_t *qcols = T.dt.ptr[K0 + (q_swapped(pi) ? 8 : 2)];
+    const int64_t *rrows = T.dt.ptr[K0 + (r_swapped(pi) ? 9 : 4)];
+    const int64_t baseP = o * v * (X * nb) + o * v * vp * (Yb * nb), baseQ = v * o2 * (Z * nb);
+    const int64_t baseR = o3 * (X * nb), baseT = o2 * (Yb * nb) + o2 * vp * (Z * nb);
+    if (integrals) {  // gP(m, f) += sum_n G(m, n) Q(n, f)
+      TableGemm g;
+      g.A = G; g.rowA = rowPQ; g.kA = colPQ;
+      g.B = T.Qt.p(); g.colB = T.dt.ptr[K0 + 3]; g.kB = qcols; g.baseB = baseQ;
+      g.C = gP; g.rowC = T.dt.ptr[K0 + 0]; g.colC = T.dt.ptr[K0 + 1]; g.baseC = baseP;
+      g.M = T.Mpq(); g.N = v; g.K = T.Npq(); g.alpha = 1.0; g.beta = 1.0;
+      run(g);
+    }
+    {  // gQ(n, f) += sum_m G(m, n) P(m, f)
+      TableGemm g;
+      g.A = G; g.rowA = colPQ; g.kA = rowPQ;
+      g.B = T.P.p(); g.colB = T.dt.ptr[K0 + 1]; g.kB = T.dt.ptr[K0 + 0]; g.baseB = baseP;
+      g.C = gQt; g.rowC = qcols; g.colC = T.dt.ptr[K0 + 3]; g.baseC = baseQ;
+      g.M = T.Npq(); g.N = v; g.K = T.Mpq(); g.alpha = 1.0; g.beta = 1.0;
+      run(g);
+    }
+    if (integrals) {  // gR(r, m) -= sum_n G(r, n) t2(n, m)
+      TableGemm g;
+      g.A = G; g.rowA = rowR; g.kA = colR;
+      g.B = T.T2p.p(); g.colB = T.dt.ptr[K0 + 7]; g.kB = T.dt.ptr[K0 + 6]; g.baseB = baseT;
+      g.C = gRt; g.rowC = rrows; g.colC = T.dt.ptr[K0 + 5]; g.baseC = baseR;
+      g.M = T.Mr(); g.N = o; g.K = T.Nr(); g.alpha = -1.0; g.beta = 1.0;
+      run(g);
+    }
+    {  // gt2(n, m) -= sum_r G(r, n) R(r, m)
+      TableGemm g;
+      g.A = G; g.rowA = colR; g.kA = rowR;
+      g.B = T.Rt.p(); g.colB = T.dt.ptr[K0 + 5]; g.kB = rrows; g.baseB = baseR;
+      g.C = gT2p; g.rowC = T.dt.ptr[K0 + 6]; g.colC = T.dt.ptr[K0 + 7]; g.baseC = baseT;
+      g.M = T.Nr(); g.N = o; g.K = T.Mr(); g.alpha = -1.0; g.beta = 1.0;
+      run(g);
+    }
+  }
+}
+
+// Block size of the grouped tensor-core form: GEMM rows (u, x_l) = o nb fill
+// the 128-row tiles well, the padded virtual range vp = NB nb stays close to v,
+// and the three W buffers (3 nb^3 o^3 floats) stay within 256 MiB; ties go to
+// the larger block (fewer, larger launches).  SCESS_T_NB overrides it.
+int choose_nb_grouped(int64_t o, int64_t v) {
+  if (const char *env = std::getenv("SCESS_T_NB")) {
+    const int nb = std::atoi(env);
+    if (nb >= 1) return (int)std::min<int64_t>(nb, v);
+  }
+  int best = 1;
+  double best_score = -1.0;
+  const double o3 = (double)o * o * o;
+  for (int nb = 1; nb <= std::min<int64_t>(v, 64); nb++) {
+    if (nb > 1 && 3.0 * nb * nb * nb * o3 * 4.0 > double(256 << 20)) break;
+    const double rows = (double)o * nb;
+    const double effM = rows / (128.0 * std::ceil(rows / 128.0));
+    const double vp = (double)ceil_div(v, nb) * nb;
+    const double effV = std::pow((double)v / vp, 3.0);
+    const double score = effM * effV;
+    if (score >= best_score * (1.0 - 1e-9)) {
+      best = nb;
+      best_score = std::max(score, best_score);
+    }
+  }
+  return best;
+}
+
+}  // namespace
+
+double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, const double *d_eps,
+                     const double *d_t1, const double *d_t2, bool mixed, const Control &ctl,
+                     TriplesStats *stats) {
+  const int64_t v = nmo - o, N = nmo;
+  cudaStream_t s = ctx.stream;
+  const int nb = mixed ? choose_nb_grouped(o, v) : choose_nb(o, v, 8, size_t(128) << 20);
+  const int64_t NB = ceil_div(v, nb), vp = NB * nb;
+  const int64_t o2 = o * o, o3 = o2 * o;
+  const int64_t N2 = N * N, N3 = N2 * N;
+
+  TriplesSetup T;
+  T.o = o;
+  T.v = v;
+  T.N = N;
+  T.nb = nb;
+  T.NB = NB;
+  T.vp = vp;
+  T.build(ctx, d_eri, d_t2);
+  const DTensor &P = T.P, &Qt = T.Qt, &Rt = T.Rt, &T2p = T.T2p;
+  const DevTables &dt = T.dt;
+  const size_t kOperand = T.kOperand;
 
   const int64_t ntrip = v * (v + 1) * (v + 2) / 6;
   DTensor energies({std::max<int64_t>(ntrip, 1)});
@@ -575,56 +852,7 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
           const double flops = 3.0 * nb * nb * 2.0 * (double)Mg * Ng * (2.0 * v + 2.0 * o);
           tc.gemm_grouped(ps, out, flops, "tc_gemm[triples]");
         } else {
-          for (int p = 0; p < 6; p++) {
-            const int *pi = kPerm[p];
-            const int64_t X = U[pi[0]], Yb = U[pi[1]], Z = U[pi[2]];
-            const int64_t *rowPQ = dt.ptr[4 * p + 0], *colPQ = dt.ptr[4 * p + 1];
-            const int64_t *rowR = dt.ptr[4 * p + 2], *colR = dt.ptr[4 * p + 3];
-            TableGemm g;
-            g.A = P.p();
-            g.B = Qt.p();
-            g.C = W.d();
-            g.rowA = dt.ptr[kOperand + 0];
-            g.kA = dt.ptr[kOperand + 1];
-            g.colB = dt.ptr[kOperand + (q_swapped(pi) ? 8 : 2)];
-            g.kB = dt.ptr[kOperand + 3];
-            g.rowC = rowPQ;
-            g.colC = colPQ;
-            g.baseA = o * v * (X * nb) + o * v * vp * (Yb * nb);
-            g.baseB = v * o2 * (Z * nb);
-            g.M = Mpq;
-            g.N = Npq;
-            g.K = v;
-            g.alpha = 1.0;
-            g.beta = p == 0 ? 0.0 : 1.0;
-            g.aUnitM = 1;
-            g.bUnitN = 0;
-            {
-              TimedScope ts(ctx.timer, "dgemm_table", 2.0 * g.M * g.N * g.K, 0.0, s);
-              dgemm_table(g, ws, s);
-            }
-            TableGemm h;
-            h.A = Rt.p();
-            h.B = T2p.p();
-            h.C = W.d();
-            h.rowA = dt.ptr[kOperand + (r_swapped(pi) ? 9 : 4)];
-            h.kA = dt.ptr[kOperand + 5];
-            h.colB = dt.ptr[kOperand + 6];
-            h.kB = dt.ptr[kOperand + 7];
-            h.rowC = rowR;
-            h.colC = colR;
-            h.baseA = o3 * (X * nb);
-            h.baseB = o2 * (Yb * nb) + o2 * vp * (Z * nb);
-            h.M = Mr;
-            h.N = Nr;
-            h.K = o;
-            h.alpha = -1.0;
-            h.beta = 1.0;
-            h.aUnitM = r_swapped(pi) ? 0 : 1;
-            h.bUnitN = 0;
-            TimedScope ts(ctx.timer, "dgemm_table", 2.0 * h.M * h.N * h.K, 0.0, s);
-            dgemm_table(h, ws, s);
-          }
+          w_block_fp64(ctx, T, U, W.d(), ws);
         }
         const unsigned nblk = (unsigned)(nb * nb * nb);
         TimedScope ts(ctx.timer, "triples_energy", 0.0, (double)nblk * o3 * (mixed ? 3 * 4 : 8), s);
@@ -646,6 +874,112 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
     stats->nb = nb;
     stats->block_triples = blocks_done;
   }
+  return ctx.hscalars[0];
+}
+
+double rccsd_triples_vjp(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o,
+                         const double *d_eps, const double *d_t1, const double *d_t2, double gE,
+                         const Control &ctl, double *d_gt1, double *d_gt2, double *d_geri) {
+  const int64_t v = nmo - o, N = nmo;
+  cudaStream_t s = ctx.stream;
+  const int nb = choose_nb(o, v, 8, size_t(64) << 20);  // W and G, nb^3 o^3 FP64 each
+  const int64_t NB = ceil_div(v, nb), vp = NB * nb;
+  const int64_t o2 = o * o, o3 = o2 * o, N2 = N * N, N3 = N2 * N;
+  TriplesSetup T;
+  T.o = o;
+  T.v = v;
+  T.N = N;
+  T.nb = nb;
+  T.NB = NB;
+  T.vp = vp;
+  T.build(ctx, d_eri, d_t2);
+  const bool integrals = d_geri != nullptr;
+  DTensor gP, gRt;
+  if (integrals) {
+    gP = DTensor({o, v, vp, vp});
+    gRt = DTensor({o, o, o, vp});
+    SCESS_CUDA(cudaMemsetAsync(gP.p(), 0, gP.size() * sizeof(double), s));
+    SCESS_CUDA(cudaMemsetAsync(gRt.p(), 0, gRt.size() * sizeof(double), s));
+  }
+  DTensor gQt({v, o, o, vp}), gT2p({o, o, vp, vp}), gS({o, o, v, v});
+  SCESS_CUDA(cudaMemsetAsync(gQt.p(), 0, gQt.size() * sizeof(double), s));
+  SCESS_CUDA(cudaMemsetAsync(gT2p.p(), 0, gT2p.size() * sizeof(double), s));
+  SCESS_CUDA(cudaMemsetAsync(gS.p(), 0, gS.size() * sizeof(double), s));
+  const int64_t ntrip = v * (v + 1) * (v + 2) / 6;
+  DTensor energies({std::max<int64_t>(ntrip, 1)});
+  SCESS_CUDA(cudaMemsetAsync(energies.p(), 0, energies.size() * sizeof(double), s));
+  DevMem W((size_t)o3 * nb * nb * nb * 8), G((size_t)o3 * nb * nb * nb * 8);
+  const int64_t p1 = o | 1, p2 = (p1 * o) | 1;
+  const size_t gsmem = (size_t)(p2 * o + 5 * o2 + 7 * o) * 8;
+  if (gsmem > 200 * 1024) throw Error(SCESS_ERR_UNSUPPORTED, "(T) gradient: o^3 too large for one CTA");
+  SCESS_CUDA(cudaFuncSetAttribute(triples_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)gsmem));
+  int64_t need = 0;
+  {
+    const int64_t shapes[6][3] = {{T.Mpq(), T.Npq(), v}, {T.Mr(), T.Nr(), o}, {T.Mpq(), v, T.Npq()},
+                                  {T.Npq(), v, T.Mpq()}, {T.Mr(), o, T.Nr()}, {T.Nr(), o, T.Mr()}};
+    for (auto &sh : shapes) {
+      TableGemm probe;
+      probe.M = sh[0];
+      probe.N = sh[1];
+      probe.K = sh[2];
+      need = std::max(need, dgemm_table_workspace(probe));
+    }
+  }
+  double *ws = ctx.ensure_workspace(need);
+  int64_t blocks_done = 0;
+  for (int64_t A = 0; A < NB; A++)
+    for (int64_t Bk = 0; Bk <= A; Bk++)
+      for (int64_t C = 0; C <= Bk; C++) {
+        if ((blocks_done & 15) == 0) ctl.poll();
+        const int64_t U[3] = {A, Bk, C};
+        w_block_fp64(ctx, T, U, W.d(), ws);
+        {
+          TimedScope ts(ctx.timer, "triples_grad", 0.0, 0.0, s);
+          triples_grad_kernel<<<(unsigned)(nb * nb * nb), 256, gsmem, s>>>(
+              W.d(), G.d(), o, v, nb, A, Bk, C, d_eps, d_t1, d_eri, N, gE, energies.p(), d_gt1,
+              gS.p());
+          SCESS_CHECK_LAUNCH();
+        }
+        g_block_fp64(ctx, T, U, G.d(), integrals ? gP.p() : nullptr, gQt.p(),
+                     integrals ? gRt.p() : nullptr, gT2p.p(), integrals, ws);
+        blocks_done++;
+      }
+  sum_energies_kernel<<<1, 1024, 0, s>>>(ntrip, energies.p(), ctx.dscalars);
+  SCESS_CHECK_LAUNCH();
+  SCESS_CUDA(cudaMemcpyAsync(ctx.hscalars, ctx.dscalars, sizeof(double), cudaMemcpyDeviceToHost, s));
+
+  // back through the repacks (RCCSD_T.cpp:30-56) into t2 and eri
+  const TV g_t2 = cm(d_gt2, {o, o, v, v});
+  TV q = gQt.v;  // Q(f,j,k,c) = t2(k,j,c,f)
+  q.ext[3] = v;
+  permute(ctx, "fjkc->kjcf", 1.0, q, 1.0, g_t2);
+  TV t = gT2p.v;
+  t.ext[2] = v;
+  t.ext[3] = v;
+  permute(ctx, "mkbc->mkbc", 1.0, t, 1.0, g_t2);
+  if (integrals) {
+    auto view = [&](int64_t off, std::initializer_list<int64_t> ext) {
+      TV e;
+      e.p = d_geri + off;
+      e.nd = 4;
+      int k = 0;
+      for (int64_t x : ext) e.ext[k++] = x;
+      const int64_t st[4] = {1, N, N2, N3};
+      std::memcpy(e.str, st, sizeof(st));
+      return e;
+    };
+    TV pv = gP.v;  // P(i,f,a,b) = eri(i, o+b, o+a, o+f)
+    pv.ext[2] = v;
+    pv.ext[3] = v;
+    permute(ctx, "ifab->ibaf", 1.0, pv, 1.0, view(o * N + o * N2 + o * N3, {o, v, v, v}));
+    TV rv = gRt.v;  // R(i,j,m,a) = eri(i, m, o+a, j)
+    rv.ext[3] = v;
+    permute(ctx, "ijma->imaj", 1.0, rv, 1.0, view(o * N2, {o, o, v, o}));
+    // S(i,j,a,b) = eri(i, j, o+a, o+b)
+    permute(ctx, "ijab->ijab", 1.0, gS.v, 1.0, view(o * N2 + o * N3, {o, o, v, v}));
+  }
+  ctx.sync();
   return ctx.hscalars[0];
 }
 
