@@ -176,6 +176,64 @@ def cpu_oracle_step(eri, eps, o, ints=None, tslices=3):
                           'triples_sampled': sampled, 'triples_total': total, 'E_iter': E}
 
 
+def triples_only(args, wl, config, ctx_factory, lib, bf16_peak, peak_kind, torch):
+    """(T) on the resident state built from the DF factors (eri formed on the device once),
+    with the seeded denominator-scaled amplitudes of the (T) workload; mixed timed over
+    --steps calls after --warmup, FP64 once, both on the same amplitudes."""
+    from scess_gb300.synthetic import make_workload
+    import oracle
+    o, v = args.o, args.v
+    amp = make_workload(o, v, seed=args.seed, with_amplitudes=True, sigma=wl.sigma)
+    ctx = ctx_factory()
+    t0 = time.perf_counter()
+    st = ctx.state(eps=wl.eps, nocc=o, B=wl.B, precision='fp64', max_iterations=1000)
+    st.set_amplitudes(amp.t1, amp.t2)
+    setup_s = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        st.triples('mixed')
+    clk = Clocks(0)
+    clk.start()
+    ctx.profile(True)
+    n0 = lib.scess_launch_count()
+    ms, ets = [], []
+    for _ in range(args.steps):
+        et, m = st.triples('mixed')
+        ms.append(m)
+        ets.append(et)
+    launches = int(lib.scess_launch_count() - n0)
+    prof = ctx.profile_report()
+    ctx.profile(False)
+    clocks = clk.stop()
+    t_mixed = float(np.mean(ms)) / 1e3
+    tc = prof.get('tc_gemm[triples]', {'launches': 0, 'ms': 0.0, 'flops': 0.0})
+    per_launch_alg = oracle.triples_flops(o, v) * args.steps / max(tc['launches'], 1)
+    avg_ms = tc['ms'] / max(tc['launches'], 1)
+    achieved = per_launch_alg / (avg_ms / 1e3) / 1e12 if avg_ms > 0 else 0.0
+    fp64 = None
+    if not args.no_fp64:
+        etf, mf = st.triples('fp64')
+        fp64 = {'triples_s': mf / 1e3, 'E_T_fp64': etf, 'dE_T_mixed_vs_fp64': abs(ets[-1] - etf),
+                'rel_dE_T': abs(ets[-1] - etf) / max(abs(etf), 1e-300),
+                'speedup_mixed_vs_fp64': (mf / 1e3) / t_mixed,
+                'fp64_tflops': oracle.triples_flops(o, v) / (mf / 1e3) / 1e12}
+    st.close()
+    peak_alg = bf16_peak / 3.0
+    print(json.dumps({
+        'metric': '(T) seconds, mixed vs FP64 GPU (fixed amplitudes)', 'value': t_mixed,
+        'unit': 's', 'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': t_mixed * 1e3, 'higher_is_better': False, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'f16x2-split (FP32 acc) + f64', 'data': 'synthetic',
+        'config': dict(config, workload=f'(T) alone, o={o} v={v}, seeded DF integrals '
+                                        f'(sigma_B={wl.sigma:.5f}) and seeded '
+                                        'denominator-scaled t1/t2'),
+        'E_T_mixed': ets[-1], 'state_setup_s': setup_s, 'fp64': fp64,
+        'roofline': {'kernel': 'tc_gemm_kernel, grouped (T) launch', 'bound': 'tensor',
+                     'achieved': achieved, 'peak': peak_alg, 'unit': 'TFLOP/s',
+                     'frac': achieved / peak_alg, 'avg_launch_ms': avg_ms,
+                     'launches': tc['launches'], 'traffic': None},
+        'kernel_timers': prof, 'gpu_launches': launches, 'clocks': clocks}))
+
+
 def rank_info():
     return (int(os.environ.get('RANK', 0)), int(os.environ.get('WORLD_SIZE', 1)),
             int(os.environ.get('LOCAL_RANK', 0)))
@@ -194,6 +252,8 @@ def main():
     ap.add_argument('--e2e-steps', type=int, default=2)
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-fp64', action='store_true')
+    ap.add_argument('--triples-only', action='store_true',
+                    help='(T) alone on fixed seeded amplitudes (e.g. --o 24 --v 240), mixed vs FP64')
     args = ap.parse_args()
     rank, world, local = rank_info()
     o, v = args.o, args.v
@@ -249,6 +309,10 @@ def main():
     import scess_gb300 as s
     lib = s.load_library()
     hbm, bf16_peak, peak_kind = peaks()
+
+    if args.triples_only:
+        return triples_only(args, wl, config, ctx_factory=lambda: s.Context(local), lib=lib,
+                            bf16_peak=bf16_peak, peak_kind=peak_kind, torch=torch)
 
     host_t, eri_h = build_eri_pinned(wl, torch)
     N = wl.nmo

@@ -208,6 +208,8 @@ struct TcArgs {
   TcSegArgs seg[4];
   int64_t cy, cz;    // output offset of problem (y, z, g): y * cy + z * cz + cg[g]
   int64_t cg[3];
+  const int64_t *rowCg[3], *colCg[3];  // per-group output tables (null: TcOut's)
+  int stcol[3];                        // group stores along columns (FP32, beta = 0)
   float *partial;    // split-K partials (nullptr: direct epilogue)
   int64_t part_stride;
   unsigned *err;
@@ -263,6 +265,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   // scatter and batches them (through a generic pointer every load would wait
   // for the previous store).
   __shared__ int64_t colOff[V2_BN];
+  __shared__ int64_t rowOffS[TC_BM];           // row offsets of a column-stored unit
+  __shared__ float stage[32][TC_BM + 1];       // 32-column chunk of such a unit
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tiles = a.tiles_m * a.tiles_n;
@@ -427,10 +431,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       asm volatile("bar.sync 1, 128;" ::: "memory");  // previous unit's colOff reads done
       if (!a.partial) {
         const int nn = n0 + et;
-        colOff[et] = nn < a.N ? out.baseC + py * a.cy + pz * a.cz + a.cg[pg] + out.colC[nn] : -1;
+        const int64_t *colT = a.colCg[pg] ? a.colCg[pg] : out.colC;
+        colOff[et] = nn < a.N ? out.baseC + py * a.cy + pz * a.cz + a.cg[pg] + colT[nn] : -1;
       }
       // issued now, used after the K loop: their latency hides behind the MMAs
-      const int64_t rowOff = (!a.partial && m < a.M) ? out.rowC[m] : 0;
+      const int64_t *rowT = a.rowCg[pg] ? a.rowCg[pg] : out.rowC;
+      const int64_t rowOff = (!a.partial && m < a.M) ? rowT[m] : 0;
       const unsigned errv = *(volatile unsigned *)a.err;
       float acc[V2_BN];
 #pragma unroll
@@ -457,6 +463,29 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       }
       asm volatile("bar.sync 1, 128;" ::: "memory");  // colOff of this unit written
       if (!ok || errv) break;
+      if (a.stcol[pg] && out.fp32 && out.beta == 0.0 && !a.partial) {
+        // Tile staged through shared memory 32 columns at a time, then each warp
+        // stores its 32 rows with the lanes along the columns: for outputs whose
+        // unit-stride index is a column index this writes contiguous runs.
+        float *C = (float *)out.C;
+        const float fa = s_falpha;
+        rowOffS[row] = m < a.M ? rowOff : -1;
+#pragma unroll
+        for (int j0 = 0; j0 < V2_BN; j0 += 32) {
+          asm volatile("bar.sync 1, 128;" ::: "memory");  // previous chunk read, rowOffS set
+#pragma unroll
+          for (int jj = 0; jj < 32; jj++) stage[jj][row] = fa * acc[j0 + jj];
+          asm volatile("bar.sync 1, 128;" ::: "memory");
+          const int64_t co = colOff[j0 + lane];
+#pragma unroll 4
+          for (int rr = 0; rr < 32; rr++) {
+            const int r = 32 * q + rr;
+            const int64_t ro = rowOffS[r];
+            if (ro >= 0 && co >= 0) C[ro + co] = stage[lane][r];
+          }
+        }
+        continue;
+      }
       if (m >= a.M) continue;
       if (a.partial) {
         const int sp = u / (tiles * nprob);
@@ -782,7 +811,12 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
   a.kbd = ps.kbd == 2 ? 2 : 1;
   a.cy = ps.cy;
   a.cz = ps.cz;
-  for (int q = 0; q < 3; q++) a.cg[q] = ps.cg[q];
+  for (int q = 0; q < 3; q++) {
+    a.cg[q] = ps.cg[q];
+    a.rowCg[q] = ps.rowC[q];
+    a.colCg[q] = ps.colC[q];
+    a.stcol[q] = ps.store_by_column[q] ? 1 : 0;
+  }
   a.partial = splits > 1 ? partial : nullptr;
   a.part_stride = ps.M * ps.N;
   a.err = err;
@@ -849,9 +883,13 @@ void TcEngine::gemm_grouped(const TcProblemSet &ps, const TcOut &out, double flo
                          stream ? stream : ctx_.stream);
 }
 
+// GB300's FP64 units run the table GEMM at ~1 TFLOP/s for large tiles and at a
+// fraction of that when M or N is small (a 64x64 tile holding a 20x20 result),
+// so any contraction above ~2e7 FLOPs is faster on the tensor cores, even with
+// most of a 128x128 tile idle; matrix-vector shapes stay on the FP64 GEMV.
 bool TcEngine::worth_it(const EinsumPlan &pl) {
-  const int64_t mx = std::max(pl.M, pl.N), mn = std::min(pl.M, pl.N);
-  return mx >= 64 && mn >= 16 && pl.K >= 8 && 2.0 * pl.M * pl.N * pl.K >= 2.0e7;
+  const int64_t mn = std::min(pl.M, pl.N);
+  return mn >= 4 && pl.K >= 16 && 2.0 * pl.M * pl.N * pl.K >= 2.0e7;
 }
 
 void TcEngine::pack(const double *src, const int64_t *rowOff, int64_t rows, const int64_t *kOff,

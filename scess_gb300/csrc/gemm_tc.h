@@ -72,6 +72,12 @@ struct TcProblemSet {
   int64_t cy = 0, cz = 0;
   int64_t cg[3] = {0, 0, 0};
   int kbd = 1;  // K blocks per TMEM drain: 1, or 2 (fewer drains, ~2x rounding)
+  // per-group output tables (null: the TcOut tables)
+  const int64_t *rowC[3] = {nullptr, nullptr, nullptr};
+  const int64_t *colC[3] = {nullptr, nullptr, nullptr};
+  // group g writes along columns (lanes over columns, through shared memory):
+  // for FP32 outputs with beta = 0 whose unit-stride index is a column index
+  bool store_by_column[3] = {false, false, false};
 };
 
 class TcEngine {

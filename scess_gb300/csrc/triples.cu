@@ -148,14 +148,13 @@ __global__ void ovov_f32_kernel(const double *__restrict__ eri, int64_t N, int64
 }
 
 // Energy of one block triple from the three grouped W buffers of the
-// tensor-core form.  W^{abc}_{ijk} = W0[b,c][a][i + o j + o^2 k]
-//   + W1[a,c][b][j + o i + o^2 k] + W2[a,b][c][k + o i + o^2 j]
-// (buffer g holds [y_l][z_l][x_l][o^3] for its roles (x, y, z)).  Each thread
-// owns index pairs and walks the third index with fixed strides: every buffer
-// is read along its own unit-stride index (coalesced across the threads) and
-// added into Y in shared memory; W is recovered as Y - V in the energy loop.
-// Otherwise as triples_energy_kernel (FP32 per element, FP64 per thread sum).
-__global__ void __launch_bounds__(512) triples_energy3_kernel(
+// tensor-core form: W^{abc}_{ijk} = W0[b,c][a] + W1[a,c][b] + W2[a,b][c], each
+// block of o^3 floats in (i, j, k) order (buffer g holds [y_l][z_l][x_l][o^3]
+// for its roles (x, y, z)).  Threads own (i, j) pairs and walk k: one pass of
+// coalesced loads forms Y = W + V in shared memory, W is recovered as Y - V in
+// the energy loop.  Otherwise as triples_energy_kernel (FP32 per element, FP64
+// per thread sum).
+__global__ void __launch_bounds__(256) triples_energy3_kernel(
     const float *__restrict__ W, int64_t o, int64_t v, int64_t nb, int64_t A, int64_t Bk,
     int64_t C, const double *__restrict__ eps, const double *__restrict__ t1,
     const float *__restrict__ S, double *__restrict__ energies) {
@@ -187,33 +186,17 @@ __global__ void __launch_bounds__(512) triples_energy3_kernel(
     eo[i] = (float)eps[i];
   }
   __syncthreads();
-  // Y = V + W0: pairs (i, j), k walks; V_ijk = t1_ia (jb|kc) + t1_jb (ia|kc) + t1_kc (ia|jb)
+  // Y = W0 + W1 + W2 + V;  V_ijk = t1_ia (jb|kc) + t1_jb (ia|kc) + t1_kc (ia|jb)
   for (int pr = threadIdx.x; pr < o2; pr += blockDim.x) {
     const int i = pr % oo, j = pr / oo;
     const float tai = ta[i], tbj = tb[j], sab = Sab[pr];
-    const float *w = W0 + pr;
     float *y = Y + i + p1 * j;
-#pragma unroll 4
-    for (int k = 0; k < oo; k++)
-      y[p2 * k] = w[o2 * k] + tai * Sbc[j + oo * k] + tbj * Sac[i + oo * k] + tc[k] * sab;
-  }
-  __syncthreads();
-  // Y += W1 (layout j + o i + o^2 k): pairs (j, i), k walks
-  for (int pr = threadIdx.x; pr < o2; pr += blockDim.x) {
-    const int j = pr % oo, i = pr / oo;
-    const float *w = W1 + pr;
-    float *y = Y + i + p1 * j;
-#pragma unroll 4
-    for (int k = 0; k < oo; k++) y[p2 * k] += w[o2 * k];
-  }
-  __syncthreads();
-  // Y += W2 (layout k + o i + o^2 j): pairs (k, i), j walks
-  for (int pr = threadIdx.x; pr < o2; pr += blockDim.x) {
-    const int k = pr % oo, i = pr / oo;
-    const float *w = W2 + pr;
-    float *y = Y + i + p2 * k;
-#pragma unroll 4
-    for (int j = 0; j < oo; j++) y[p1 * j] += w[o2 * j];
+#pragma unroll 8
+    for (int k = 0; k < oo; k++) {
+      const int e = pr + o2 * k;
+      y[p2 * k] = (W0[e] + W1[e]) + W2[e] + tai * Sbc[j + oo * k] + tbj * Sac[i + oo * k] +
+                  tc[k] * sab;
+    }
   }
   __syncthreads();
   const float evirt = (float)(eps[o + a] + eps[o + b] + eps[o + c]);
@@ -776,14 +759,21 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
     mR = TcEngine::map_of(pR, 128);
     mR2 = TcEngine::map_of(pR2, 128);
     mTx = TcEngine::map_of(pTx, 128);
-    // W_g[(y_l nb + z_l) nb + x_l][u + o s + o^2 t]: rows (u, x_l), columns (s, t)
-    gdt.build({table({{o, 1}, {nb, o3}}), table({{o, o}, {o, o2}})});
+    // W_g[(y_l nb + z_l) nb + x_l][i + o j + o^2 k]: every group stores its
+    // (u, s, t) in the (i, j, k) order of the triple, so that the energy kernel
+    // reads the three buffers alike.  g = 0: (u,s,t) = (i,j,k); g = 1: (j,i,k);
+    // g = 2: (k,i,j).  Rows (u, x_l), columns (s, t).
+    gdt.build({table({{o, 1}, {nb, o3}}), table({{o, o}, {o, o2}}),
+               table({{o, o}, {nb, o3}}), table({{o, 1}, {o, o2}}),
+               table({{o, o2}, {nb, o3}}), table({{o, 1}, {o, o}})});
     Sf.alloc((size_t)o2 * v * v * sizeof(float));
     ovov_f32_kernel<<<(unsigned)std::min<int64_t>(ceil_div(o2 * v * v, 256), 16 * kNumSMs), 256, 0, s>>>(
         d_eri, N, o, v, Sf.as<float>());
     SCESS_CHECK_LAUNCH();
   }
-  const unsigned e3threads = (unsigned)std::min<int64_t>(round_up(o2, 32), 512);
+  // (i, j) pairs spread evenly over at most 256 threads
+  const unsigned e3threads =
+      (unsigned)round_up(ceil_div(o2, ceil_div(o2, 256)), 32);
   double *ws = nullptr;
   if (!mixed) {
     TableGemm probe;
@@ -846,6 +836,11 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
           out.fp32 = 1;
           out.rowC = gdt.ptr[0];
           out.colC = gdt.ptr[1];
+          for (int g = 0; g < 3; g++) {
+            ps.rowC[g] = gdt.ptr[2 * g];
+            ps.colC[g] = gdt.ptr[2 * g + 1];
+            ps.store_by_column[g] = g > 0;  // i is a column index of groups 1 and 2
+          }
           out.alpha = 1.0;
           out.beta = 0.0;
           TcEngine::set_scales(out, pP, pQ);
