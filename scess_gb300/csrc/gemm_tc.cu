@@ -352,12 +352,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      const uint32_t idesc = idesc_f16kind(TC_BM, V2_BN, a.f16 ? 0u : 1u);
       int g = 0, c = 0;
       bool ok = true;
       for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
         int tm, tn, py, pz, pg, kb0, kb1;
         unit_coords(u, tm, tn, py, pz, pg, kb0, kb1);
+        // MMA width: the tile's valid columns rounded up to 16 (M = 128 takes any
+        // N = 16..256 in steps of 16; the MMA time scales with N)
+        const int nvalid = min(V2_BN, (a.N - tn * V2_BN + 15) & ~15);
+        const uint32_t idesc = idesc_f16kind(TC_BM, nvalid, a.f16 ? 0u : 1u);
         for (int kb = kb0; kb < kb1; kb++, g++) {
           int sg, lkb;
           seg_of(a, kb, sg, lkb);
