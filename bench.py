@@ -410,6 +410,17 @@ def main():
     del st
 
     # ---- e2e through the public API from pinned host buffers ----------------------------------
+    # host->device bandwidth of the pinned input right before the e2e steps (torch copy)
+    h2d_probe = None
+    if args.e2e_steps > 0:
+        tmp = torch.empty(host_t.numel(), dtype=torch.float64, device='cuda')
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        tmp.copy_(host_t, non_blocking=True)
+        torch.cuda.synchronize()
+        h2d_probe = host_t.numel() * 8 / (time.perf_counter() - t0) / 1e9
+        del tmp
+        torch.cuda.empty_cache()
     e2e_times, e2e_phases = [], []
     for _ in range(args.e2e_steps):
         torch.cuda.synchronize()
@@ -427,12 +438,25 @@ def main():
         e2e_times.append(t4 - t0)
         e2e_phases.append({'state_create_s': t1 - t0, 'iterate_s': t2 - t1, 'triples_s': t3 - t2,
                            'amplitudes_destroy_s': t4 - t3})
+    e2e_profile = None
+    if args.e2e_steps > 0:  # one more, untimed, with the library's phase timers on
+        ctx.profile(True)
+        se = ctx.state(eri_h, wl.eps, o, precision='mixed', max_iterations=1000)
+        se.iterate(1)
+        se.triples('mixed')
+        se.close()
+        rep = ctx.profile_report()
+        ctx.profile(False)
+        e2e_profile = {k: round(v['ms'], 3) for k, v in rep.items()
+                       if k.startswith('host:') or v['ms'] > 5.0}
     e2e = {'value': float(np.min(e2e_times)) if e2e_times else None, 'unit': UNIT,
            'h2d_bytes_per_step': int(8 * (N ** 4 + N)),
            'd2h_bytes_per_step': int(8 * (o * v + o * o * v * v) + 64),
            'path': 'scess_rccsd_state_create (eri from pinned host) + state_iterate(1) + '
                    'state_triples(MIXED) + state_amplitudes + destroy',
-           'phases': e2e_phases[int(np.argmin(e2e_times))] if e2e_times else None}
+           'phases': e2e_phases[int(np.argmin(e2e_times))] if e2e_times else None,
+           'all_times': e2e_times, 'profiled_ms': e2e_profile,
+           'pinned_h2d_gbps_torch_probe': h2d_probe}
 
     # ---- CPU baseline (rank 0 only) -------------------------------------------------------------
     cpu = None

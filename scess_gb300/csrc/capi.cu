@@ -1,5 +1,6 @@
 // C ABI of the engine (include/scess_cc.h): argument checks, host<->device
 // transfers and exception-to-status translation around the C++ drivers.
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -74,12 +75,22 @@ void device_finite(scess::Ctx &ctx, const double *x, int64_t n, const char *what
 }
 
 // eri (nmo^4) on the device, from the host eri or from DF factors (FP64 build).
+double ms_since(std::chrono::steady_clock::time_point t0) {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
 scess::DTensor device_eri(scess::Ctx &ctx, const double *eri, const double *B, int64_t naux,
                           int64_t N) {
+  auto t0 = std::chrono::steady_clock::now();
   scess::DTensor d({N, N, N, N});
+  ctx.timer.host("eri_alloc", ms_since(t0));
   if (eri) {
+    t0 = std::chrono::steady_clock::now();
     scess::upload(ctx, d.p(), eri, N * N * N * N);
+    ctx.timer.host("eri_upload", ms_since(t0));
+    t0 = std::chrono::steady_clock::now();
     device_finite(ctx, d.p(), N * N * N * N, "eri");
+    ctx.timer.host("eri_check", ms_since(t0));
   } else {
     scess::DTensor dB({naux, N, N});
     scess::upload(ctx, dB.p(), B, naux * N * N);
@@ -109,7 +120,11 @@ scess::RccsdState *make_state(scess::Ctx &c, const double *eri, const double *B,
   in.eps_host = eps;
   in.f12_residual = f12_residual;
   in.f12_energy = f12_energy;
-  return new scess::RccsdState(c, std::move(d_eri), nmo, nocc, in, o);
+  const auto t0 = std::chrono::steady_clock::now();
+  auto *st = new scess::RccsdState(c, std::move(d_eri), nmo, nocc, in, o);
+  c.sync();
+  c.timer.host("state_build", ms_since(t0));
+  return st;
 }
 
 int solve_common(scess_ctx *ctx, const double *eri, const double *B, int64_t naux,
@@ -379,8 +394,10 @@ static int state_create(scess_ctx *ctx, const double *eri, const double *B, int6
     else scess_rccsd_default_options(&o);
     std::unique_ptr<scess::RccsdState> st(
         make_state(c, eri, B, naux, eps, nmo, nocc, f12_residual, f12_energy, o));
+    const auto t0 = std::chrono::steady_clock::now();
     st->mp2_guess();
     c.sync();
+    c.timer.host("mp2_guess", ms_since(t0));
     auto *h = new scess_rccsd_state;
     h->ctx = ctx;
     h->impl = st.release();

@@ -155,6 +155,13 @@ void KernelTimer::end(cudaStream_t s) {
   if (recs_.size() >= 4096) collect();
 }
 
+void KernelTimer::host(const char *name, double ms) {
+  if (!on) return;
+  Agg &a = agg[std::string("host:") + name];
+  a.launches++;
+  a.ms += ms;
+}
+
 void KernelTimer::collect() {
   for (auto &r : recs_) {
     SCESS_CUDA(cudaEventSynchronize(r.b));

@@ -111,6 +111,8 @@ class KernelTimer {
   void begin(const char *name, double flops, double bytes, cudaStream_t s);
   void end(cudaStream_t s);
   void collect();  // waits for the recorded events and folds them into agg
+  // host-side phase (wall clock, ms), reported beside the kernels as "host:<name>"
+  void host(const char *name, double ms);
   void reset();
   std::map<std::string, Agg> agg;
 

@@ -641,11 +641,22 @@ __global__ void maxabs_kernel(const double *__restrict__ src, const int64_t *__r
   if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(maxbits, __float_as_uint(m));
 }
 
+// x s = hi + lo in FP16.  FP64 arithmetic runs at a small fraction of the FP32
+// rate on GB300, so x is converted to FP32 once (relative error 2^-24, below
+// the split's 2^-22) and the scaling (a power of two, exact) and the residual
+// (exact: hi is xs rounded) are FP32 operations.  `fast` is false only for
+// scales outside FP32's range (max|x| below ~2^-85), which keep the FP64 form.
 struct HalfPair {
-  __device__ static void split(double x, double s, __half &hi, __half &lo) {
-    const double xs = x * s;
-    hi = __double2half(xs);
-    lo = __double2half(xs - (double)__half2float(hi));
+  __device__ static void split(double x, double s, float sf, bool fast, __half &hi, __half &lo) {
+    if (fast) {
+      const float xs = (float)x * sf;
+      hi = __float2half_rn(xs);
+      lo = __float2half_rn(xs - __half2float(hi));
+    } else {
+      const double xs = x * s;
+      hi = __double2half(xs);
+      lo = __double2half(xs - (double)__half2float(hi));
+    }
   }
 };
 
@@ -674,6 +685,8 @@ __global__ void __launch_bounds__(256) pack_split_kernel(
     }
     if (blockIdx.x == 0 && blockIdx.y == 0 && t == 0) *scale_out = s;
   }
+  const bool fast = s <= 0x1p100 && s >= 0x1p-100;
+  const float sf = fast ? (float)s : 1.0f;
   __syncthreads();
 #pragma unroll
   for (int p = 0; p < 8; p++) {
@@ -696,13 +709,15 @@ __global__ void __launch_bounds__(256) pack_split_kernel(
     const double x = tile[rr][ch * 8 + j];
     if (F16) {
       __half h, l;
-      HalfPair::split(x, s, h, l);
+      HalfPair::split(x, s, sf, fast, h, l);
       hi[j] = __half_as_ushort(h);
       lo[j] = __half_as_ushort(l);
     } else {
-      const __nv_bfloat16 h = __double2bfloat16(x);
+      // BF16 shares FP32's exponent range: split the FP32 value (see HalfPair)
+      const float xf = (float)x;
+      const __nv_bfloat16 h = __float2bfloat16_rn(xf);
       hi[j] = __bfloat16_as_ushort(h);
-      lo[j] = __bfloat16_as_ushort(__double2bfloat16(x - (double)__bfloat162float(h)));
+      lo[j] = __bfloat16_as_ushort(__float2bfloat16_rn(xf - __bfloat162float(h)));
     }
   }
   const int64_t base = (r0 + rr) * 2 * Kpad + k0 + ch * 8;
