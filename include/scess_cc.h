@@ -144,7 +144,10 @@ int scess_rccsd_triples(scess_ctx *ctx, const double *eri, const double *eps, in
                         int64_t nocc, const double *t1, const double *t2, int32_t precision,
                         double *e_t);
 
-/* (T) from DF factors (only the ovvv, ooov and oovv blocks are built). */
+/* (T) from DF factors B (naux x nmo x nmo, (pq|rs) = sum_Q B(Q,p,q) B(Q,r,s)):
+ * the only integrals (T) reads, (ia|bf), (ia|mj) and (ia|jb), are contracted
+ * from B on the device (FP64, or on the tensor cores for MIXED); the nmo^4
+ * eri is never formed. */
 int scess_rccsd_triples_df(scess_ctx *ctx, const double *B, int64_t naux, const double *eps,
                            int64_t nmo, int64_t nocc, const double *t1, const double *t2,
                            int32_t precision, double *e_t);

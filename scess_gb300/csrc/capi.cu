@@ -273,7 +273,16 @@ static int triples_common(scess_ctx *ctx, const double *eri, const double *B, in
     scess::Control ctl;
     ctl.cancel = c.cancel;
     ctl.user = c.user;
-    scess::DTensor d_eri = device_eri(c, eri, B, naux, nmo);
+    // DF input: (T) reads only (ia|bf), (ia|mj) and (ia|jb), formed from B on
+    // the device; the nmo^4 eri is not built
+    scess::DTensor d_eri, dB;
+    if (eri) {
+      d_eri = device_eri(c, eri, nullptr, 0, nmo);
+    } else {
+      dB = scess::DTensor({naux, nmo, nmo});
+      scess::upload(c, dB.p(), B, naux * nmo * nmo);
+      device_finite(c, dB.p(), naux * nmo * nmo, "B");
+    }
     scess::DTensor d_eps({nmo}), d_t1({o, v}), d_t2({o, o, v, v});
     scess::upload(c, d_eps.p(), eps, nmo);
     scess::upload(c, d_t1.p(), t1, o * v);
@@ -282,7 +291,7 @@ static int triples_common(scess_ctx *ctx, const double *eri, const double *B, in
     device_finite(c, d_t2.p(), o * o * v * v, "t2");
     ctl.poll();
     *e_t = scess::rccsd_triples(c, d_eri.p(), nmo, nocc, d_eps.p(), d_t1.p(), d_t2.p(),
-                                precision == SCESS_PRECISION_MIXED, ctl);
+                                precision == SCESS_PRECISION_MIXED, ctl, nullptr, dB.p(), naux);
   });
 }
 

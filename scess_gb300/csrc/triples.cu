@@ -44,8 +44,8 @@ __device__ __forceinline__ double div_fast(double x, double y) { return x / y; }
 template <typename WT, typename CT>
 __global__ void __launch_bounds__(256) triples_energy_kernel(
     const WT *__restrict__ W, int64_t o, int64_t v, int64_t nb, int64_t A, int64_t Bk, int64_t C,
-    const double *__restrict__ eps, const double *__restrict__ t1, const double *__restrict__ eri,
-    int64_t N, double *__restrict__ energies) {
+    const double *__restrict__ eps, const double *__restrict__ t1, const double *__restrict__ S,
+    double *__restrict__ energies) {
   const int64_t al = blockIdx.x / (nb * nb), bl = (blockIdx.x / nb) % nb, cl = blockIdx.x % nb;
   const int64_t a = A * nb + al, b = Bk * nb + bl, c = C * nb + cl;
   if (a >= v || b >= v || c >= v || b > a || c > b) return;
@@ -59,13 +59,11 @@ __global__ void __launch_bounds__(256) triples_energy_kernel(
   CT *Sbc = Y + p2 * oo, *Sac = Sbc + o2, *Sab = Sac + o2;
   CT *ta = Sab + o2, *tb = ta + oo, *tc = tb + oo, *eo = tc + oo;
   const WT *Wt = W + ((al * nb + bl) * nb + cl) * (int64_t)o3;
-  // S(i,j,a,b) = (ia|jb) = eri(i, j, o+a, o+b)
-  const int64_t N2 = N * N, N3 = N2 * N;
+  // S(i,j,a,b) = (ia|jb) at i + o j + o^2 (a + v b)
   for (int e = threadIdx.x; e < o2; e += blockDim.x) {
-    const int i = e % oo, j = e / oo;
-    Sbc[e] = (CT)eri[i + N * j + (o + b) * N2 + (o + c) * N3];
-    Sac[e] = (CT)eri[i + N * j + (o + a) * N2 + (o + c) * N3];
-    Sab[e] = (CT)eri[i + N * j + (o + a) * N2 + (o + b) * N3];
+    Sbc[e] = (CT)S[e + o2 * (b + v * c)];
+    Sac[e] = (CT)S[e + o2 * (a + v * c)];
+    Sab[e] = (CT)S[e + o2 * (a + v * b)];
   }
   for (int i = threadIdx.x; i < oo; i += blockDim.x) {
     ta[i] = (CT)t1[i + o * a];
@@ -134,17 +132,11 @@ __global__ void __launch_bounds__(256) triples_energy_kernel(
   }
 }
 
-// S(i, j, a, b) = (ia|jb) = eri(i, j, o+a, o+b) as FP32 at i + o j + o^2 (a + v b):
-// the integral slices of the tensor-core energy kernel, read contiguously.
-__global__ void ovov_f32_kernel(const double *__restrict__ eri, int64_t N, int64_t o, int64_t v,
-                                float *__restrict__ out) {
-  const int64_t o2 = o * o, n = o2 * v * v, N2 = N * N, N3 = N2 * N;
+// FP32 copy of S(i, j, a, b) = (ia|jb) for the tensor-core energy kernel.
+__global__ void to_f32_kernel(const double *__restrict__ x, int64_t n, float *__restrict__ out) {
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t ij = e % o2, ab = e / o2;
-    const int64_t i = ij % o, j = ij / o, a = ab % v, b = ab / v;
-    out[e] = (float)eri[i + N * j + (o + a) * N2 + (o + b) * N3];
-  }
+       e += (int64_t)gridDim.x * blockDim.x)
+    out[e] = (float)x[e];
 }
 
 // Energy of one block triple from the three grouped W buffers of the
@@ -311,18 +303,25 @@ bool r_swapped(const int *pi) { return pi[1] == 0; }
 struct TriplesSetup {
   int64_t o = 0, v = 0, N = 0, nb = 0, NB = 0, vp = 0;
   DTensor P, Qt, Rt, T2p;
+  DTensor S;  // S(i,j,a,b) = (ia|jb), o x o x v x v
   DevTables dt;
   size_t kOperand = 0;
-  void build(Ctx &ctx, const double *d_eri, const double *d_t2);
+  // integrals from the eri (views) or, when d_B is given, from the DF factors
+  // B (naux x N x N): P, R, S are single B.B contractions (be: FP64 or tensor
+  // cores), so the N^4 eri is never formed
+  void build(Ctx &ctx, const double *d_eri, const double *d_t2, const double *d_B = nullptr,
+             int64_t naux = 0, Backend be = Backend::FP64);
   int64_t Mpq() const { return o * nb * nb; }
   int64_t Npq() const { return o * o * nb; }
   int64_t Mr() const { return o * o * nb; }
   int64_t Nr() const { return o * nb * nb; }
 };
 
-void TriplesSetup::build(Ctx &ctx, const double *d_eri, const double *d_t2) {
+void TriplesSetup::build(Ctx &ctx, const double *d_eri, const double *d_t2, const double *d_B,
+                         int64_t naux, Backend be) {
   cudaStream_t s = ctx.stream;
   const int64_t o2 = o * o, o3 = o2 * o, N2 = N * N, N3 = N2 * N;
+  S = DTensor({o, o, v, v});
   // Zero-padded FP64 repacks (RCCSD_T.cpp:30-56), virtual indices padded to vp.
   P = DTensor({o, v, vp, vp});   // P(i,f,a,b) = (ia|bf) = eri(i, o+b, o+a, o+f)
   Qt = DTensor({v, o, o, vp});   // Q(f,j,k,c) = t2(k,j,c,f)
@@ -333,25 +332,48 @@ void TriplesSetup::build(Ctx &ctx, const double *d_eri, const double *d_t2) {
   SCESS_CUDA(cudaMemsetAsync(Rt.p(), 0, Rt.size() * sizeof(double), s));
   SCESS_CUDA(cudaMemsetAsync(T2p.p(), 0, T2p.size() * sizeof(double), s));
   {
-    TV e;  // (i, b, a, f) -> eri(i, o+b, o+a, o+f)
-    e.p = const_cast<double *>(d_eri) + o * N + o * N2 + o * N3;
-    e.nd = 4;
-    int64_t ee[4] = {o, v, v, v}, es[4] = {1, N, N2, N3};
-    std::memcpy(e.ext, ee, sizeof(ee));
-    std::memcpy(e.str, es, sizeof(es));
     TV Pv = P.v;
     Pv.ext[2] = v;
     Pv.ext[3] = v;
-    permute(ctx, "ibaf->ifab", 1.0, e, 0.0, Pv);
-    TV r;  // (i, m, a, j) -> eri(i, m, o+a, j)
-    r.p = const_cast<double *>(d_eri) + o * N2;
-    r.nd = 4;
-    int64_t re[4] = {o, o, v, o}, rs[4] = {1, N, N2, N3};
-    std::memcpy(r.ext, re, sizeof(re));
-    std::memcpy(r.str, rs, sizeof(rs));
     TV Rv = Rt.v;
     Rv.ext[3] = v;
-    permute(ctx, "imaj->ijma", 1.0, r, 0.0, Rv);
+    if (d_B) {
+      // (pq|rs) = sum_Q B(Q,p,q) B(Q,r,s): P(i,f,a,b) = (ia|bf), R(i,j,m,a) = (ia|mj),
+      // S(i,j,a,b) = (ia|jb)
+      auto bview = [&](int64_t p0, int64_t q0, int64_t np, int64_t nq) {
+        TV b;
+        b.p = const_cast<double *>(d_B) + naux * p0 + naux * N * q0;
+        b.nd = 3;
+        const int64_t be3[3] = {naux, np, nq}, bs3[3] = {1, naux, naux * N};
+        std::memcpy(b.ext, be3, sizeof(be3));
+        std::memcpy(b.str, bs3, sizeof(bs3));
+        return b;
+      };
+      const TV Bov = bview(0, o, o, v), Bvv = bview(o, o, v, v), Boo = bview(0, 0, o, o);
+      einsum(ctx, "Qia,Qbf->ifab", 1.0, Bov, Bvv, 0.0, Pv, be);
+      einsum(ctx, "Qia,Qmj->ijma", 1.0, Bov, Boo, 0.0, Rv, be);
+      einsum(ctx, "Qia,Qjb->ijab", 1.0, Bov, Bov, 0.0, S.v, be);
+    } else {
+      TV e;  // (i, b, a, f) -> eri(i, o+b, o+a, o+f)
+      e.p = const_cast<double *>(d_eri) + o * N + o * N2 + o * N3;
+      e.nd = 4;
+      int64_t ee[4] = {o, v, v, v}, es[4] = {1, N, N2, N3};
+      std::memcpy(e.ext, ee, sizeof(ee));
+      std::memcpy(e.str, es, sizeof(es));
+      permute(ctx, "ibaf->ifab", 1.0, e, 0.0, Pv);
+      TV r;  // (i, m, a, j) -> eri(i, m, o+a, j)
+      r.p = const_cast<double *>(d_eri) + o * N2;
+      r.nd = 4;
+      int64_t re[4] = {o, o, v, o}, rs[4] = {1, N, N2, N3};
+      std::memcpy(r.ext, re, sizeof(re));
+      std::memcpy(r.str, rs, sizeof(rs));
+      permute(ctx, "imaj->ijma", 1.0, r, 0.0, Rv);
+      TV sv = r;  // (i, j, a, b) -> eri(i, j, o+a, o+b)
+      sv.p = const_cast<double *>(d_eri) + o * N2 + o * N3;
+      sv.ext[2] = v;
+      sv.ext[3] = v;
+      permute(ctx, "ijab->ijab", 1.0, sv, 0.0, S.v);
+    }
     const TV t2 = cm(const_cast<double *>(d_t2), {o, o, v, v});
     TV Qv = Qt.v;
     Qv.ext[3] = v;
@@ -470,7 +492,7 @@ void w_block_fp64(Ctx &ctx, const TriplesSetup &T, const int64_t U[3], double *W
 __global__ void __launch_bounds__(256) triples_grad_kernel(
     const double *__restrict__ W, double *__restrict__ G, int64_t o, int64_t v, int64_t nb,
     int64_t A, int64_t Bk, int64_t C, const double *__restrict__ eps,
-    const double *__restrict__ t1, const double *__restrict__ eri, int64_t N, double gE,
+    const double *__restrict__ t1, const double *__restrict__ Sg, double gE,
     double *__restrict__ energies, double *__restrict__ g_t1, double *__restrict__ g_S) {
   const int64_t al = blockIdx.x / (nb * nb), bl = (blockIdx.x / nb) % nb, cl = blockIdx.x % nb;
   const int64_t a = A * nb + al, b = Bk * nb + bl, c = C * nb + cl;
@@ -489,12 +511,10 @@ __global__ void __launch_bounds__(256) triples_grad_kernel(
   double *gSbc = Sab + o2, *gSac = gSbc + o2;
   double *ta = gSac + o2, *tb = ta + oo, *tc = tb + oo, *eo = tc + oo;
   double *gta = eo + oo, *gtb = gta + oo, *gtc = gtb + oo;
-  const int64_t N2 = N * N, N3 = N2 * N;
   for (int e = threadIdx.x; e < o2; e += blockDim.x) {
-    const int i = e % oo, j = e / oo;
-    Sbc[e] = eri[i + N * j + (o + b) * N2 + (o + c) * N3];
-    Sac[e] = eri[i + N * j + (o + a) * N2 + (o + c) * N3];
-    Sab[e] = eri[i + N * j + (o + a) * N2 + (o + b) * N3];
+    Sbc[e] = Sg[e + o2 * (b + v * c)];
+    Sac[e] = Sg[e + o2 * (a + v * c)];
+    Sab[e] = Sg[e + o2 * (a + v * b)];
     gSbc[e] = 0.0;
     gSac[e] = 0.0;
   }
@@ -667,7 +687,7 @@ int choose_nb_grouped(int64_t o, int64_t v) {
 
 double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, const double *d_eps,
                      const double *d_t1, const double *d_t2, bool mixed, const Control &ctl,
-                     TriplesStats *stats) {
+                     TriplesStats *stats, const double *d_B, int64_t naux) {
   const int64_t v = nmo - o, N = nmo;
   cudaStream_t s = ctx.stream;
   const int nb = mixed ? choose_nb_grouped(o, v) : choose_nb(o, v, 8, size_t(128) << 20);
@@ -682,7 +702,7 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   T.nb = nb;
   T.NB = NB;
   T.vp = vp;
-  T.build(ctx, d_eri, d_t2);
+  T.build(ctx, d_eri, d_t2, d_B, naux, mixed ? Backend::TENSOR : Backend::FP64);
   const DTensor &P = T.P, &Qt = T.Qt, &Rt = T.Rt, &T2p = T.T2p;
   const DevTables &dt = T.dt;
   const size_t kOperand = T.kOperand;
@@ -767,8 +787,8 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
                table({{o, o}, {nb, o3}}), table({{o, 1}, {o, o2}}),
                table({{o, o2}, {nb, o3}}), table({{o, 1}, {o, o}})});
     Sf.alloc((size_t)o2 * v * v * sizeof(float));
-    ovov_f32_kernel<<<(unsigned)std::min<int64_t>(ceil_div(o2 * v * v, 256), 16 * kNumSMs), 256, 0, s>>>(
-        d_eri, N, o, v, Sf.as<float>());
+    to_f32_kernel<<<(unsigned)std::min<int64_t>(ceil_div(o2 * v * v, 256), 16 * kNumSMs), 256, 0, s>>>(
+        T.S.p(), o2 * v * v, Sf.as<float>());
     SCESS_CHECK_LAUNCH();
   }
   // (i, j) pairs spread evenly over at most 256 threads
@@ -856,7 +876,7 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
               W.as<float>(), o, v, nb, A, Bk, C, d_eps, d_t1, Sf.as<float>(), energies.p());
         else
           triples_energy_kernel<double, double><<<nblk, 256, ysmem, s>>>(
-              W.d(), o, v, nb, A, Bk, C, d_eps, d_t1, d_eri, N, energies.p());
+              W.d(), o, v, nb, A, Bk, C, d_eps, d_t1, T.S.p(), energies.p());
         SCESS_CHECK_LAUNCH();
         blocks_done++;
       }
@@ -932,7 +952,7 @@ double rccsd_triples_vjp(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o,
         {
           TimedScope ts(ctx.timer, "triples_grad", 0.0, 0.0, s);
           triples_grad_kernel<<<(unsigned)(nb * nb * nb), 256, gsmem, s>>>(
-              W.d(), G.d(), o, v, nb, A, Bk, C, d_eps, d_t1, d_eri, N, gE, energies.p(), d_gt1,
+              W.d(), G.d(), o, v, nb, A, Bk, C, d_eps, d_t1, T.S.p(), gE, energies.p(), d_gt1,
               gS.p());
           SCESS_CHECK_LAUNCH();
         }

@@ -10,10 +10,13 @@ struct TriplesStats {
 };
 
 // E_(T) of RCCSD_TriplesCorrection (RCCSD_T.cpp:17-168) from device-resident
-// eri (nmo^4, <pq|rs>), eps (nmo), t1 (o x v) and t2 (o x o x v x v).
+// eri (nmo^4, <pq|rs>), eps (nmo), t1 (o x v) and t2 (o x o x v x v).  With d_B
+// (DF factors, naux x nmo x nmo) d_eri may be null: the integral slices (T)
+// reads are formed from B directly and the nmo^4 eri is never built.
 double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t nocc,
                      const double *d_eps, const double *d_t1, const double *d_t2, bool mixed,
-                     const Control &ctl, TriplesStats *stats = nullptr);
+                     const Control &ctl, TriplesStats *stats = nullptr,
+                     const double *d_B = nullptr, int64_t naux = 0);
 
 // Gradient of E_(T) (FP64; no counterpart in the reference): adds
 // gE * dE_T/dt1 (o x v) and gE * dE_T/dt2 (o x o x v x v) into d_gt1, d_gt2

@@ -40,4 +40,17 @@ def test_triples_df_equals_eri(gctx):
     w = make_workload(5, 19, seed=1, with_amplitudes=True)
     a = gctx.triples(w.eri(), w.eps, 5, w.t1, w.t2)
     b = gctx.triples(None, w.eps, 5, w.t1, w.t2, B=w.B)
-    assert abs(a - b) < 1e-12
+    assert abs(a - b) <= 1e-12 * max(1.0, abs(a))
+
+
+@pytest.mark.parametrize('precision,tol', [('fp64', 1e-12), ('mixed', 2e-6)])
+def test_triples_df_native_multiblock(gctx, monkeypatch, precision, tol):
+    """DF input, integrals contracted from B without the nmo^4 eri, several
+    block triples with padded virtuals; against the eri route in FP64."""
+    from scess_gb300.synthetic import convergent_sigma
+    monkeypatch.setenv('SCESS_T_NB', '7')
+    o, v = 6, 40
+    w = make_workload(o, v, seed=4, with_amplitudes=True, sigma=convergent_sigma(o, v))
+    ref = gctx.triples(w.eri(), w.eps, o, w.t1, w.t2, precision='fp64')
+    got = gctx.triples(None, w.eps, o, w.t1, w.t2, B=w.B, precision=precision)
+    assert abs(got - ref) <= tol * max(1.0, abs(ref))
