@@ -176,6 +176,57 @@ def cpu_oracle_step(eri, eps, o, ints=None, tslices=3):
                           'triples_sampled': sampled, 'triples_total': total, 'E_iter': E}
 
 
+def transform_only(args, wl, config, ctx_factory, lib, torch):
+    """AO->MO transform (scess_transform_tei) of chemists' integrals
+    (pq|rs) = sum_Q B(Q,p,q) B(Q,r,s) from the seeded DF factors (nao = nmo =
+    o + v) with a seeded orthogonal C, to physicists' order; host buffers in and
+    out.  Mixed timed over --steps calls after --warmup, FP64 once."""
+    N = wl.nmo
+    B = torch.from_numpy(wl.B).cuda()
+    host = torch.empty(N ** 4, dtype=torch.float64, pin_memory=True)
+    host.copy_(torch.einsum('Qpq,Qrs->srqp', B, B).contiguous().reshape(-1))  # column-major (pq|rs)
+    del B
+    torch.cuda.empty_cache()
+    tei = host.numpy().reshape((N, N, N, N), order='F')
+    g = torch.Generator().manual_seed(args.seed)
+    Cm = np.asfortranarray(torch.linalg.qr(torch.randn(N, N, dtype=torch.float64, generator=g))[0].numpy())
+    ctx = ctx_factory()
+    flops = 8.0 * N ** 5
+    for _ in range(args.warmup):
+        ctx.transform_tei(tei, Cm, chem_to_phys=True, precision='mixed')
+    ctx.profile(True)
+    n0 = lib.scess_launch_count()
+    walls = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        out_m = ctx.transform_tei(tei, Cm, chem_to_phys=True, precision='mixed')
+        walls.append(time.perf_counter() - t0)
+    launches = int(lib.scess_launch_count() - n0)
+    prof = ctx.profile_report()
+    ctx.profile(False)
+    kern_ms = sum(v['ms'] for k, v in prof.items() if not k.startswith('host:')) / args.steps
+    fp64 = None
+    if not args.no_fp64:
+        t0 = time.perf_counter()
+        out_f = ctx.transform_tei(tei, Cm, chem_to_phys=True, precision='fp64')
+        tf = time.perf_counter() - t0
+        fp64 = {'seconds': tf, 'tflops': flops / tf / 1e12,
+                'max_rel_diff_mixed': float(np.max(np.abs(out_m - out_f)) / np.max(np.abs(out_f)))}
+    t = float(np.mean(walls))
+    print(json.dumps({
+        'metric': 'AO->MO transform seconds (TransformTEI), mixed vs FP64 GPU', 'value': t,
+        'unit': 's', 'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': t * 1e3, 'higher_is_better': False, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f16x2-split (FP32 acc) + f64', 'data': 'synthetic',
+        'config': dict(config, workload=f'AO->MO transform, nao = nmo = {N}, chemists AO integrals '
+                                        'from the seeded DF factors, seeded orthogonal C'),
+        'algorithmic_tflop': flops / 1e12, 'kernel_ms_per_call': kern_ms,
+        'kernel_tflops': flops / (kern_ms / 1e3) / 1e12 if kern_ms > 0 else None,
+        'e2e': {'value': t, 'unit': 's', 'h2d_bytes_per_step': int(8 * (N ** 4 + 4 * N * N)),
+                'd2h_bytes_per_step': int(8 * N ** 4)},
+        'fp64': fp64, 'kernel_timers': prof, 'gpu_launches': launches}))
+
+
 def triples_only(args, wl, config, ctx_factory, lib, bf16_peak, peak_kind, torch):
     """(T) alone through scess_rccsd_triples_df on the seeded denominator-scaled
     amplitudes of the (T) workload: each call uploads B, contracts the integral
@@ -258,6 +309,8 @@ def main():
     ap.add_argument('--e2e-steps', type=int, default=2)
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-fp64', action='store_true')
+    ap.add_argument('--transform', action='store_true',
+                    help='AO->MO transform of nmo^4 integrals (TransformTEI), mixed vs FP64')
     ap.add_argument('--triples-only', action='store_true',
                     help='(T) alone on fixed seeded amplitudes (e.g. --o 24 --v 240), mixed vs FP64')
     args = ap.parse_args()
@@ -316,6 +369,9 @@ def main():
     lib = s.load_library()
     hbm, bf16_peak, peak_kind = peaks()
 
+    if args.transform:
+        return transform_only(args, wl, config, ctx_factory=lambda: s.Context(local), lib=lib,
+                              torch=torch)
     if args.triples_only:
         return triples_only(args, wl, config, ctx_factory=lambda: s.Context(local), lib=lib,
                             bf16_peak=bf16_peak, peak_kind=peak_kind, torch=torch)

@@ -259,6 +259,20 @@ int scess_einsum(scess_ctx *ctx, const char *spec, double alpha, const double *A
                  const int64_t *a_ext, const double *B, int32_t b_nd, const int64_t *b_ext,
                  double beta, double *C, int32_t c_nd, const int64_t *c_ext, int32_t precision);
 
+/* AO->MO transform of the two-electron integrals, TransformTEI
+ * (src/Quantum/Integrals/IntegralTransforms.cpp:32-59): tei is the chemists'
+ * AO tensor (mu nu|kap lam) (nao^4, column-major); A, B, C, D are AO x MO
+ * coefficient matrices (nao x na, ..., column-major).  out(p,q,r,s) =
+ * sum A(mu,p) B(nu,q) C(kap,r) D(lam,s) (mu nu|kap lam), transformed one index
+ * at a time (lam, kap, nu, mu) as the reference does; with chem_to_phys the
+ * result is reordered pqrs -> prqs (out is then na x nc x nb x nd), which with
+ * A = B = C = D is the physicists' eri of scess_rccsd_solve (RCCSD.cpp:399).
+ * precision: FP64 table GEMMs, or MIXED (tensor cores, split operands). */
+int scess_transform_tei(scess_ctx *ctx, const double *tei, int64_t nao, const double *A,
+                        int64_t na, const double *B, int64_t nb, const double *C, int64_t nc,
+                        const double *D, int64_t nd, int32_t chem_to_phys, int32_t precision,
+                        double *out);
+
 /* scess_einsum's FP64 contraction for callers that cannot allocate device
  * memory.  No counterpart in the reference.  Some host programs own every byte
  * of the GPU: a framework whose caching allocator has reserved the device's

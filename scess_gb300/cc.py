@@ -119,6 +119,8 @@ EXPORTS = {
     'scess_rccsd_triples_vjp_df': (C.c_int, [C.c_void_p, _dp, C.c_int64, _dp, C.c_int64,
                                              C.c_int64, _dp, _dp, C.c_double,
                                              C.POINTER(C.c_double), _dp, _dp, _dp]),
+    'scess_transform_tei': (C.c_int, [C.c_void_p, _dp, C.c_int64, _dp, C.c_int64, _dp, C.c_int64,
+                                      _dp, C.c_int64, _dp, C.c_int64, C.c_int32, C.c_int32, _dp]),
     'scess_einsum_static': (C.c_int, [C.c_char_p, C.c_double, C.c_void_p, C.c_int32, _i64p,
                                       C.c_void_p, C.c_int32, _i64p, C.c_double, C.c_void_p,
                                       C.c_int32, _i64p, C.c_void_p]),
@@ -401,6 +403,23 @@ class Context:
                                                   _ptr(gt2), _ptr(gI))
         self._check(st, 'scess_rccsd_triples_vjp')
         return et.value, gt1, gt2, gI
+
+    def transform_tei(self, tei, A, B=None, C_=None, D=None, chem_to_phys=False,
+                      precision='fp64'):
+        """TransformTEI (IntegralTransforms.cpp:32-59) on the GPU; B, C_, D default to A."""
+        t = _f64(tei)
+        n = t.shape[0]
+        mats = [_f64(m) for m in (A, A if B is None else B, A if C_ is None else C_,
+                                  A if D is None else D)]
+        na, nb, nc, nd = (m.shape[1] for m in mats)
+        shape = (na, nc, nb, nd) if chem_to_phys else (na, nb, nc, nd)
+        out = np.zeros(shape, order='F')
+        st = self.lib.scess_transform_tei(self.h, _ptr(t), n, _ptr(mats[0]), na, _ptr(mats[1]), nb,
+                                          _ptr(mats[2]), nc, _ptr(mats[3]), nd,
+                                          1 if chem_to_phys else 0, PRECISION[precision],
+                                          _ptr(out))
+        self._check(st, 'scess_transform_tei')
+        return out
 
     # -- Lambda equations and the one-particle density ---------------------------------------
     def lambda_solve(self, eri, eps, nocc, t1, t2, precision='fp64', **opts):

@@ -737,3 +737,56 @@ int scess_einsum(scess_ctx *ctx, const char *spec, double alpha, const double *A
 }
 
 }  // extern "C"
+
+extern "C" {
+
+int scess_transform_tei(scess_ctx *ctx, const double *tei, int64_t nao, const double *A,
+                        int64_t na, const double *B, int64_t nb, const double *C, int64_t nc,
+                        const double *D, int64_t nd, int32_t chem_to_phys, int32_t precision,
+                        double *out) {
+  return guard(ctx, [&](scess::Ctx &c) {
+    need(tei, "tei");
+    need(A, "A");
+    need(B, "B");
+    need(C, "C");
+    need(D, "D");
+    need(out, "out");
+    if (nao <= 0 || na <= 0 || nb <= 0 || nc <= 0 || nd <= 0)
+      throw Error(SCESS_ERR_INVALID, "bad dimensions");
+    if (precision != SCESS_PRECISION_FP64 && precision != SCESS_PRECISION_MIXED)
+      throw Error(SCESS_ERR_INVALID, "bad precision");
+    const scess::Backend be =
+        precision == SCESS_PRECISION_MIXED ? scess::Backend::TENSOR : scess::Backend::FP64;
+    const int64_t n = nao, n4 = n * n * n * n;
+    auto mat = [&](const double *h, int64_t cols, const char *name) {
+      scess::DTensor m({n, cols});
+      scess::upload(c, m.p(), h, n * cols);
+      device_finite(c, m.p(), n * cols, name);
+      return m;
+    };
+    scess::DTensor dA = mat(A, na, "A"), dB = mat(B, nb, "B"), dC = mat(C, nc, "C"),
+                   dD = mat(D, nd, "D");
+    // IntegralTransforms.cpp:44-55: one index at a time, at most two 4-index tensors alive
+    scess::DTensor x({n, n, n, n});
+    scess::upload(c, x.p(), tei, n4);
+    device_finite(c, x.p(), n4, "tei");
+    scess::DTensor y({n, n, n, nd});
+    scess::einsum(c, "mnkl,ls->mnks", 1.0, x.v, dD.v, 0.0, y.v, be);   // (mu nu|kap s)
+    x = scess::DTensor({n, n, nc, nd});
+    scess::einsum(c, "mnks,kr->mnrs", 1.0, y.v, dC.v, 0.0, x.v, be);   // (mu nu|r s)
+    y = scess::DTensor({n, nb, nc, nd});
+    scess::einsum(c, "mnrs,nq->mqrs", 1.0, x.v, dB.v, 0.0, y.v, be);   // (mu q|r s)
+    x = scess::DTensor({na, nb, nc, nd});
+    scess::einsum(c, "mqrs,mp->pqrs", 1.0, y.v, dA.v, 0.0, x.v, be);   // (p q|r s)
+    if (chem_to_phys) {                                                // :57-59, pqrs -> prqs
+      y = scess::DTensor({na, nc, nb, nd});
+      scess::permute(c, "pqrs->prqs", 1.0, x.v, 0.0, y.v);
+      scess::download(c, out, y.p(), na * nb * nc * nd);
+    } else {
+      scess::download(c, out, x.p(), na * nb * nc * nd);
+    }
+    if (precision == SCESS_PRECISION_MIXED) c.tensor_cores().check_error();
+  });
+}
+
+}  // extern "C"

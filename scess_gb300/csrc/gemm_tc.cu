@@ -672,7 +672,8 @@ __global__ void __launch_bounds__(256) pack_split_kernel(
   __shared__ double tile[32][65];
   __shared__ int64_t sr[32], sk[64];
   const int t = threadIdx.x;
-  const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 64;
+  // row blocks on grid.x (up to 2^31 - 1), K blocks on grid.y (<= 65535)
+  const int64_t r0 = (int64_t)blockIdx.x * 32, k0 = (int64_t)blockIdx.y * 64;
   if (t < 32) sr[t] = (r0 + t < rows) ? rowOff[r0 + t] : -1;
   else if (t < 96) sk[t - 32] = (k0 + t - 32 < K) ? kOff[k0 + t - 32] : -1;
   double s = 1.0;
@@ -929,7 +930,8 @@ void TcEngine::pack(const double *src, const int64_t *rowOff, int64_t rows, cons
                 (double)rows * K * 8 + (double)rows_pad * Kpad * 4, ctx_.stream);
   unsigned *maxbits = out.aux.as<unsigned>();
   double *scale = reinterpret_cast<double *>(out.aux.as<char>() + 8);
-  dim3 grid((unsigned)(Kpad / 64), (unsigned)(rows_pad / 32));
+  if (Kpad / 64 > 65535 || rows_pad / 32 > INT32_MAX) throw Error(SCESS_ERR_INVALID, "pack: too large");
+  dim3 grid((unsigned)(rows_pad / 32), (unsigned)(Kpad / 64));
   if (fmt_ == TcFormat::FP16) {
     SCESS_CUDA(cudaMemsetAsync(maxbits, 0, sizeof(unsigned), ctx_.stream));
     const int64_t n = rows * K;
@@ -975,7 +977,8 @@ void TcEngine::pack_with_max(const double *src, const int64_t *rowOff, int64_t r
   TimedScope ts(ctx_.timer, "pack_split", 0.0,
                 (double)rows * K * 8 + (double)rows_pad * Kpad * 4, ctx_.stream);
   double *scale = reinterpret_cast<double *>(out.aux.as<char>() + 8);
-  dim3 grid((unsigned)(Kpad / 64), (unsigned)(rows_pad / 32));
+  if (Kpad / 64 > 65535 || rows_pad / 32 > INT32_MAX) throw Error(SCESS_ERR_INVALID, "pack: too large");
+  dim3 grid((unsigned)(rows_pad / 32), (unsigned)(Kpad / 64));
   if (fmt_ == TcFormat::FP16) {
     pack_split_kernel<true><<<grid, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, unitK ? 1 : 0,
                                                            out.mem.as<uint16_t>(), Kpad, maxbits,

@@ -35,8 +35,14 @@ def unpack_unique(vals: np.ndarray, n: int) -> np.ndarray:
 
 
 def load(tag: str):
-    """Returns dict(eri (phys, N^4), eps, nocc, E_RHF) for a molecule fixture."""
+    """Returns dict(eri (phys, N^4), eps, nocc, E_RHF, and, when stored, ao_chem
+    (AO (mu nu|kap lam), N^4) and C (AO x MO)) for a molecule fixture."""
     d = np.load(os.path.join(HERE, tag + '.npz'))
     n = int(d['nmo'])
-    return {'eri': unpack_unique(d['eri_unique'], n), 'eps': d['eps'], 'nocc': int(d['nocc']),
-            'E_RHF': float(d['E_RHF'])}
+    out = {'eri': unpack_unique(d['eri_unique'], n), 'eps': d['eps'], 'nocc': int(d['nocc']),
+           'E_RHF': float(d['E_RHF'])}
+    if 'ao_unique' in d.files:
+        nao = d['C'].shape[0]
+        out['ao_chem'] = np.ascontiguousarray(unpack_unique(d['ao_unique'], nao).transpose(0, 2, 1, 3))
+        out['C'] = d['C']
+    return out

@@ -5,7 +5,9 @@ of H2/STO-3G, H2O/STO-3G and H2O/cc-pVDZ.  The reference's own integral stack
 (Libint2) cannot be built here, so this script computes the integrals from the
 McMurchie-Davidson Hermite-Gaussian formulas, runs a closed-shell RHF (DIIS,
 1e-12), and writes the MO-basis physicists' integrals ``eri[p,q,r,s] =
-<pq|rs>`` (occupied first) with the orbital energies.  The tests then check the
+<pq|rs>`` (occupied first) with the orbital energies, plus the AO integrals
+and the MO coefficients they were transformed with (inputs of the AO->MO
+transform test).  The tests then check the
 oracle's CCSD/(T) energies on these inputs against the pins, and the CUDA
 engine against the oracle.
 
@@ -351,7 +353,7 @@ def compute(name, basis_path, nocc):
     E, eps, C = rhf(S, H, eri, nocc, enuc)
     mo_chem = np.einsum('pi,qj,pqrs,rk,sl->ijkl', C, C, eri, C, C, optimize=True)
     mo_phys = mo_chem.transpose(0, 2, 1, 3)
-    return E, eps, mo_phys
+    return E, eps, mo_phys, eri, C
 
 
 def pack_unique(eri_phys):
@@ -374,9 +376,12 @@ def main():
             ('h2o_sto3g', 'h2o', os.path.join(basis, 'Pople', 'STO-3G.json'), 5),
             ('h2o_ccpvdz', 'h2o', os.path.join(basis, 'Dunning', 'cc-pVDZ.json'), 5)]
     for tag, mol, path, nocc in jobs:
-        E, eps, eri = compute(mol, path, nocc)
+        E, eps, eri, eri_ao, C = compute(mol, path, nocc)
+        # AO integrals (chemists', normalised basis) and RHF coefficients C(mu, p):
+        # inputs of the AO->MO transform, whose result is eri_unique
         np.savez_compressed(os.path.join(out, tag + '.npz'), E_RHF=E, eps=eps, nocc=nocc,
-                            nmo=len(eps), eri_unique=pack_unique(eri))
+                            nmo=len(eps), eri_unique=pack_unique(eri),
+                            ao_unique=pack_unique(eri_ao.transpose(0, 2, 1, 3)), C=C)
         print(f'{tag}: nmo={len(eps)} E(RHF) = {E:.10f}')
 
 
