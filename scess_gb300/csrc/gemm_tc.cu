@@ -29,7 +29,6 @@ constexpr int TC_BM = 128;
 constexpr int TC_BK = 64;  // 64 BF16 = 128 B = one SWIZZLE_128B row
 constexpr int TC_STAGES = 4;
 constexpr int TC_MAX_BN = 256;
-constexpr int TC_THREADS = 192;
 constexpr uint32_t A_STAGE_BYTES = TC_BM * TC_BK * 2;      // 16 KiB
 constexpr uint32_t B_STAGE_BYTES = TC_MAX_BN * TC_BK * 2;  // 32 KiB
 constexpr uint32_t TMEM_COLS = 256;
@@ -230,16 +229,34 @@ struct TcArgs {
 // per-element rounding error, still K-independent).
 // A problem's K range may span several segments with different operands
 // (up to 4), each optionally negated through the instruction descriptor.
-constexpr int V2_BN = 128;
-constexpr int V2_STAGES = 3;
+constexpr int V2_BN = 128;  // tile width of the einsum launches
 constexpr uint32_t V2_TILE_BYTES = 128 * TC_BK * 2;  // 16 KiB: 128 rows x 128 B
-constexpr uint32_t V2_STAGE_BYTES = 4 * V2_TILE_BYTES;
-// TMEM accumulator buffers: all 512 columns as four 128-column buffers, so the
-// MMA warp can run four K blocks ahead while the epilogue scatters a unit.
-constexpr int V2_NBUF = 4;
-constexpr uint32_t V2_TMEM_COLS = V2_NBUF * V2_BN;
-constexpr size_t V2_SMEM_BYTES = 1024 + V2_STAGES * V2_STAGE_BYTES +
-                                 (2 * V2_STAGES + 2 * V2_NBUF + 1) * 8 + 8;
+
+// Shape of a kernel instantiation by tile width BN (128 or 256):
+//   BN = 128: 3 stages of 64 KiB, four 128-column TMEM accumulators, 192
+//             threads (warps 2-5 drain and store);
+//   BN = 256: 2 stages of 96 KiB, two 256-column accumulators, 384 threads
+//             (warps 2-3 idle, warps 4-7 / 8-11 drain and store columns
+//             0-127 / 128-255).  With more than one warp per scheduler beside
+//             the epilogue the block is capped at 168 registers a thread, so
+//             the warpgroups rebalance with setmaxnreg: 56 for warps 0-3,
+//             224 for the epilogue (3 x 168 = 56 + 2 x 224 per scheduler).
+// Every epilogue thread holds 128 columns of one row.
+template <int BN>
+struct TcShape {
+  static constexpr int STAGES = BN == 256 ? 2 : 3;
+  static constexpr int NBUF = 512 / BN;
+  static constexpr int EPI0 = BN == 256 ? 4 : 2;   // first epilogue warp
+  static constexpr int NEPI = BN / 32;              // epilogue warps
+  static constexpr int THREADS = 32 * (EPI0 + NEPI);
+  static constexpr int CH = BN == 256 ? 16 : 32;    // columns per staged chunk
+  static constexpr uint32_t B_BYTES = (uint32_t)BN * TC_BK * 2;
+  static constexpr uint32_t STAGE_BYTES = 2 * V2_TILE_BYTES + 2 * B_BYTES;
+  static constexpr uint32_t TMEM_COLS = 512;
+  static constexpr size_t SMEM_BYTES =
+      1024 + STAGES * STAGE_BYTES + (2 * STAGES + 2 * NBUF + 1) * 8 + 8;
+};
+constexpr int kEpiRegs256 = 224, kCtlRegs256 = 56, kLaunchRegs256 = 168;
 
 __device__ __forceinline__ void seg_of(const TcArgs &a, int kb, int &s, int &lkb) {
   s = 0;
@@ -250,23 +267,51 @@ __device__ __forceinline__ void seg_of(const TcArgs &a, int kb, int &s, int &lkb
   }
 }
 
-__global__ void __launch_bounds__(TC_THREADS, 1)
+// Persistent tcgen05 GEMM over work units (problem, 128 x BN output tile, K range).
+//   warp 0     TMA producer: per 64-wide K block one smem stage holding A_hi,
+//              B_hi, A_lo, B_lo (128 / BN rows x 128 B, 128B swizzle);
+//   warp 1     TMEM owner + MMA issuer: the block's products lo*hi, hi*lo,
+//              hi*hi (4 x K=16 each) go into one of the BN-column TMEM
+//              buffers, starting from zero, then tcgen05.commit;
+//   epilogue   drain each buffer into an FP32 register accumulator (one row,
+//              128 columns per thread, round-to-nearest adds) and, after the
+//              unit's last K block, scatter alpha*acc + beta*C through the
+//              offset tables.
+// Draining every K block (kbd = 1) bounds the truncating accumulation inside
+// TMEM to the 12 products of one block, so the result's error does not grow
+// with K; kbd = 2 drains every second block (half the drains, about twice the
+// per-element rounding error, still K-independent).
+// A problem's K range may span several segments with different operands
+// (up to 4), each optionally negated through the instruction descriptor.
+template <int BN>
+__global__ void __launch_bounds__(TcShape<BN>::THREADS, 1)
     tc_gemm_kernel(const __grid_constant__ TcMaps maps, TcOut out, TcArgs a) {
+  using SH = TcShape<BN>;
+  constexpr int STAGES = SH::STAGES, NBUF = SH::NBUF, HC = 128;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t *full = (uint64_t *)(smem + V2_STAGES * V2_STAGE_BYTES);
-  uint64_t *empty = full + V2_STAGES;
-  uint64_t *tfull = empty + V2_STAGES;   // [V2_NBUF]
-  uint64_t *tempty = tfull + V2_NBUF;    // [V2_NBUF]
-  uint64_t *done = tempty + V2_NBUF;     // [1]
+  uint64_t *full = (uint64_t *)(smem + STAGES * SH::STAGE_BYTES);
+  uint64_t *empty = full + STAGES;
+  uint64_t *tfull = empty + STAGES;      // [NBUF]
+  uint64_t *tempty = tfull + NBUF;       // [NBUF]
+  uint64_t *done = tempty + NBUF;        // [1]
   uint32_t *tmem_slot = (uint32_t *)(done + 1);
   // Column offsets of the current unit.  A statically declared shared array:
   // the compiler then knows these loads cannot alias the global stores of the
   // scatter and batches them (through a generic pointer every load would wait
   // for the previous store).
-  __shared__ int64_t colOff[V2_BN];
-  __shared__ int64_t rowOffS[TC_BM];           // row offsets of a column-stored unit
-  __shared__ float stage[32][TC_BM + 1];       // 32-column chunk of such a unit
+  __shared__ int64_t colOff[BN];
+  __shared__ int64_t rowOffS[BN / 128][TC_BM];        // row offsets of a column-stored unit
+  // chunk of such a unit; row pitch 129 (CH = 32) or 130 (CH = 16, two rows a
+  // warp step) keeps the column-wise reads free of bank conflicts
+  __shared__ float stage[BN / 128][SH::CH][TC_BM + (SH::CH == 16 ? 2 : 1)];
+  // Output scaling, once per CTA: alpha / (sA sB) with power-of-two pack
+  // scales sA, sB.  FP32 outputs multiply by it in FP32; FP64 outputs multiply
+  // by the user's alpha in FP32 and apply 2^-log2(sA sB) to the exponent field
+  // (exact, no FP64 arithmetic per element).
+  __shared__ double s_alpha;
+  __shared__ float s_falpha, s_fuser;
+  __shared__ int s_shift, s_shift_ok;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tiles = a.tiles_m * a.tiles_n;
@@ -274,22 +319,32 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const int units = tiles * nprob * a.splits;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < V2_STAGES; s++) {
+    for (int s = 0; s < STAGES; s++) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    for (int b = 0; b < V2_NBUF; b++) {
+    for (int b = 0; b < NBUF; b++) {
       mbar_init(&tfull[b], 1);
-      mbar_init(&tempty[b], 4);  // one arrival per epilogue warp
+      mbar_init(&tempty[b], SH::NEPI);  // one arrival per epilogue warp
     }
     mbar_init(done, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    double sc = 1.0;
+    if (out.scaleA) sc *= *out.scaleA;
+    if (out.scaleB) sc *= *out.scaleB;
+    s_alpha = out.alpha / sc;
+    s_falpha = (float)(out.alpha / sc);
+    s_fuser = (float)out.alpha;
+    int e = 0;
+    const double f = frexp(sc, &e);  // sc = 0.5 * 2^e exactly for a power of two
+    s_shift = 1 - e;
+    s_shift_ok = (f == 0.5 && e > -400 && e < 400) ? 1 : 0;
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
-                 "r"(V2_TMEM_COLS)
+                 "r"(SH::TMEM_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -313,14 +368,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     kb1 = min(a.kb_total, kb0 + a.kb_per_split);
   };
 
+  if (warp < SH::EPI0) {  // control warps: TMA producer, MMA issuer (and idle warps)
+    if constexpr (BN == 256) asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(kCtlRegs256));
   if (warp == 0) {
     if (lane == 0) {
       for (int i = 0; i < 6; i++)
         asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&maps.m[i]) : "memory");
-      const uint32_t bytes = a.split3 ? V2_STAGE_BYTES : 2 * V2_TILE_BYTES;
+      const uint32_t bytes = a.split3 ? SH::STAGE_BYTES : V2_TILE_BYTES + SH::B_BYTES;
       int g = 0;
-      int last[V2_STAGES];
-      for (int s = 0; s < V2_STAGES; s++) last[s] = -1;
+      int last[STAGES];
+      for (int s = 0; s < STAGES; s++) last[s] = -1;
       bool ok = true;
       for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
         int tm, tn, py, pz, pg, kb0, kb1;
@@ -330,25 +387,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           seg_of(a, kb, sg, lkb);
           const TcSegArgs &S = a.seg[sg];
           const int ya = (int)(S.rowA0[pg] + py * S.rowAy[pg] + pz * S.rowAz[pg]) + tm * TC_BM;
-          const int yb = (int)(S.rowB0[pg] + py * S.rowBy[pg] + pz * S.rowBz[pg]) + tn * V2_BN;
-          const int s = g % V2_STAGES;
-          const uint32_t ph = (uint32_t)(g / V2_STAGES) & 1u;
+          const int yb = (int)(S.rowB0[pg] + py * S.rowBy[pg] + pz * S.rowBz[pg]) + tn * BN;
+          const int s = g % STAGES;
+          const uint32_t ph = (uint32_t)(g / STAGES) & 1u;
           if (!mbar_wait(&empty[s], ph ^ 1u, a.err, ERR_EMPTY_WAIT)) { ok = false; break; }
-          uint8_t *st = smem + s * V2_STAGE_BYTES;
+          uint8_t *st = smem + s * SH::STAGE_BYTES;
           const CUtensorMap *mA = &maps.m[S.mapA], *mB = &maps.m[S.mapB];
           mbar_expect_tx(&full[s], bytes);
           const int x = lkb * TC_BK;
-          tma_load_2d(st, mA, x, ya, &full[s]);                          // A hi
-          tma_load_2d(st + V2_TILE_BYTES, mB, x, yb, &full[s]);          // B hi
+          tma_load_2d(st, mA, x, ya, &full[s]);                                  // A hi
+          tma_load_2d(st + V2_TILE_BYTES, mB, x, yb, &full[s]);                  // B hi
           if (a.split3) {
-            tma_load_2d(st + 2 * V2_TILE_BYTES, mA, S.kpad + x, ya, &full[s]);  // A lo
-            tma_load_2d(st + 3 * V2_TILE_BYTES, mB, S.kpad + x, yb, &full[s]);  // B lo
+            tma_load_2d(st + V2_TILE_BYTES + SH::B_BYTES, mA, S.kpad + x, ya, &full[s]);  // A lo
+            tma_load_2d(st + 2 * V2_TILE_BYTES + SH::B_BYTES, mB, S.kpad + x, yb, &full[s]);  // B lo
           }
           last[s] = g;
         }
       }
-      for (int s = 0; s < V2_STAGES; s++)
-        if (last[s] >= 0) mbar_drain(&full[s], (uint32_t)(last[s] / V2_STAGES) & 1u);
+      for (int s = 0; s < STAGES; s++)
+        if (last[s] >= 0) mbar_drain(&full[s], (uint32_t)(last[s] / STAGES) & 1u);
     }
   } else if (warp == 1) {
     if (lane == 0) {
@@ -359,25 +416,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         unit_coords(u, tm, tn, py, pz, pg, kb0, kb1);
         // MMA width: the tile's valid columns rounded up to 16 (M = 128 takes any
         // N = 16..256 in steps of 16; the MMA time scales with N)
-        const int nvalid = min(V2_BN, (a.N - tn * V2_BN + 15) & ~15);
+        const int nvalid = min(BN, (a.N - tn * BN + 15) & ~15);
         const uint32_t idesc = idesc_f16kind(TC_BM, nvalid, a.f16 ? 0u : 1u);
         for (int kb = kb0; kb < kb1; kb++, g++) {
           int sg, lkb;
           seg_of(a, kb, sg, lkb);
           const uint32_t id = idesc | (a.seg[sg].negA ? (1u << 13) : 0u);  // negate A
-          const int s = g % V2_STAGES;
-          const uint32_t ph = (uint32_t)(g / V2_STAGES) & 1u;
-          const int b = c % V2_NBUF;
-          const uint32_t bph = (uint32_t)(c / V2_NBUF) & 1u;
+          const int s = g % STAGES;
+          const uint32_t ph = (uint32_t)(g / STAGES) & 1u;
+          const int b = c % NBUF;
+          const uint32_t bph = (uint32_t)(c / NBUF) & 1u;
           const bool first = (kb - kb0) % a.kbd == 0;
           const bool last = (kb - kb0) % a.kbd == a.kbd - 1 || kb == kb1 - 1;
           if (first && !mbar_wait(&tempty[b], bph ^ 1u, a.err, ERR_EMPTY_WAIT)) { ok = false; break; }
           if (!mbar_wait(&full[s], ph, a.err, ERR_FULL_WAIT)) { ok = false; break; }
           tc_fence_after();
-          const uint32_t st = smem_u32(smem + s * V2_STAGE_BYTES);
+          const uint32_t st = smem_u32(smem + s * SH::STAGE_BYTES);
           const uint32_t ahi = st, bhi = st + V2_TILE_BYTES;
-          const uint32_t alo = st + 2 * V2_TILE_BYTES, blo = st + 3 * V2_TILE_BYTES;
-          const uint32_t d = tmem + (uint32_t)(b * V2_BN);
+          const uint32_t alo = st + V2_TILE_BYTES + SH::B_BYTES;
+          const uint32_t blo = st + 2 * V2_TILE_BYTES + SH::B_BYTES;
+          const uint32_t d = tmem + (uint32_t)(b * BN);
           uint32_t acc = first ? 0u : 1u;
           if (a.split3) {
 #pragma unroll
@@ -401,62 +459,48 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       mma_commit(done);
       mbar_drain(done, 0);
     }
-  } else {
+  }
+  } else {  // epilogue warps
+    if constexpr (BN == 256) asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(kEpiRegs256));
     const int q = warp & 3;
     const int row = 32 * q + lane;
-    const int et = threadIdx.x - 64;  // 0..127
-    // Output scaling, once per CTA: alpha / (sA sB) with power-of-two pack
-    // scales sA, sB.  FP32 outputs multiply by it in FP32; FP64 outputs multiply
-    // by the user's alpha in FP32 and apply 2^-log2(sA sB) to the exponent field
-    // (exact, no FP64 arithmetic per element).
-    __shared__ double s_alpha;
-    __shared__ float s_falpha, s_fuser;
-    __shared__ int s_shift, s_shift_ok;
-    if (et == 0) {
-      double sc = 1.0;
-      if (out.scaleA) sc *= *out.scaleA;
-      if (out.scaleB) sc *= *out.scaleB;
-      s_alpha = out.alpha / sc;
-      s_falpha = (float)(out.alpha / sc);
-      s_fuser = (float)out.alpha;
-      int e = 0;
-      const double f = frexp(sc, &e);  // sc = 0.5 * 2^e exactly for a power of two
-      s_shift = 1 - e;
-      s_shift_ok = (f == 0.5 && e > -400 && e < 400) ? 1 : 0;
-    }
+    const int h = (warp - SH::EPI0) >> 2;                 // column half (BN = 256)
+    const int et = threadIdx.x - 32 * SH::EPI0 - 128 * h;  // 0..127 within the half
+    const int bar = 1 + h;                                // named barrier of the half
+    int64_t *colH = colOff + HC * h;
     int c = 0;
     bool ok = true;
     for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
       int tm, tn, py, pz, pg, kb0, kb1;
       unit_coords(u, tm, tn, py, pz, pg, kb0, kb1);
       const int m = tm * TC_BM + row;
-      const int n0 = tn * V2_BN;
-      asm volatile("bar.sync 1, 128;" ::: "memory");  // previous unit's colOff reads done
+      const int n0 = tn * BN + HC * h;
+      asm volatile("bar.sync %0, 128;" ::"r"(bar) : "memory");  // previous unit's colOff reads done
       if (!a.partial) {
         const int nn = n0 + et;
         const int64_t *colT = a.colCg[pg] ? a.colCg[pg] : out.colC;
-        colOff[et] = nn < a.N ? out.baseC + py * a.cy + pz * a.cz + a.cg[pg] + colT[nn] : -1;
+        colH[et] = nn < a.N ? out.baseC + py * a.cy + pz * a.cz + a.cg[pg] + colT[nn] : -1;
       }
       // issued now, used after the K loop: their latency hides behind the MMAs
       const int64_t *rowT = a.rowCg[pg] ? a.rowCg[pg] : out.rowC;
       const int64_t rowOff = (!a.partial && m < a.M) ? rowT[m] : 0;
       const unsigned errv = *(volatile unsigned *)a.err;
-      float acc[V2_BN];
+      float acc[HC];
 #pragma unroll
-      for (int j = 0; j < V2_BN; j++) acc[j] = 0.0f;
+      for (int j = 0; j < HC; j++) acc[j] = 0.0f;
       for (int kb = kb0; kb < kb1; kb += a.kbd, c++) {
-        const int b = c % V2_NBUF;
-        const uint32_t bph = (uint32_t)(c / V2_NBUF) & 1u;
+        const int b = c % NBUF;
+        const uint32_t bph = (uint32_t)(c / NBUF) & 1u;
         if (!mbar_wait(&tfull[b], bph, a.err, ERR_ACCUM_WAIT)) { ok = false; break; }
         tc_fence_after();
-        const uint32_t t0 = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * V2_BN);
+        const uint32_t t0 = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * BN + HC * h);
 #pragma unroll
-        for (int j = 0; j < V2_BN; j += 16 * SCESS_TC_LDB) {
+        for (int j = 0; j < HC; j += 16 * SCESS_TC_LDB) {
           uint32_t r[16 * SCESS_TC_LDB];
 #pragma unroll
-          for (int h = 0; h < SCESS_TC_LDB; h++) tmem_ld16_async(t0 + (uint32_t)(j + 16 * h), r + 16 * h);
+          for (int hh = 0; hh < SCESS_TC_LDB; hh++) tmem_ld16_async(t0 + (uint32_t)(j + 16 * hh), r + 16 * hh);
 #pragma unroll
-          for (int h = 0; h < SCESS_TC_LDB; h++) tmem_wait16(r + 16 * h);
+          for (int hh = 0; hh < SCESS_TC_LDB; hh++) tmem_wait16(r + 16 * hh);
 #pragma unroll
           for (int i = 0; i < 16 * SCESS_TC_LDB; i++) acc[j + i] += __uint_as_float(r[i]);
         }
@@ -464,27 +508,33 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         __syncwarp();
         if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[b])) : "memory");
       }
-      asm volatile("bar.sync 1, 128;" ::: "memory");  // colOff of this unit written
+      asm volatile("bar.sync %0, 128;" ::"r"(bar) : "memory");  // colOff of this unit written
       if (!ok || errv) break;
       if (a.stcol[pg] && out.fp32 && out.beta == 0.0 && !a.partial) {
-        // Tile staged through shared memory 32 columns at a time, then each warp
+        // Tile staged through shared memory CH columns at a time, then each warp
         // stores its 32 rows with the lanes along the columns: for outputs whose
         // unit-stride index is a column index this writes contiguous runs.
         float *C = (float *)out.C;
         const float fa = s_falpha;
-        rowOffS[row] = m < a.M ? rowOff : -1;
+        constexpr int CH = SH::CH;
+        rowOffS[h][row] = m < a.M ? rowOff : -1;
 #pragma unroll
-        for (int j0 = 0; j0 < V2_BN; j0 += 32) {
-          asm volatile("bar.sync 1, 128;" ::: "memory");  // previous chunk read, rowOffS set
+        for (int j0 = 0; j0 < HC; j0 += CH) {
+          // each warp stages and stores only its own 32 rows: warp-level ordering
+          __syncwarp();  // previous chunk read, rowOffS set
 #pragma unroll
-          for (int jj = 0; jj < 32; jj++) stage[jj][row] = fa * acc[j0 + jj];
-          asm volatile("bar.sync 1, 128;" ::: "memory");
-          const int64_t co = colOff[j0 + lane];
+          for (int jj = 0; jj < CH; jj++) stage[h][jj][row] = fa * acc[j0 + jj];
+          __syncwarp();
+          // lanes take column lane % CH of row rr + lane / CH (CH = 16: two rows a step)
+          const int cl = lane % CH;
+          const int rsub = lane / CH;
+          constexpr int RSTEP = 32 / CH;
+          const int64_t co = colH[j0 + cl];
 #pragma unroll 4
-          for (int rr = 0; rr < 32; rr++) {
-            const int r = 32 * q + rr;
-            const int64_t ro = rowOffS[r];
-            if (ro >= 0 && co >= 0) C[ro + co] = stage[lane][r];
+          for (int rr = 0; rr < 32; rr += RSTEP) {
+            const int r = 32 * q + rr + rsub;
+            const int64_t ro = rowOffS[h][r];
+            if (ro >= 0 && co >= 0) C[ro + co] = stage[h][cl][r];
           }
         }
         continue;
@@ -494,7 +544,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const int sp = u / (tiles * nprob);
         float *P = a.partial + (int64_t)sp * a.part_stride;
 #pragma unroll
-        for (int j = 0; j < V2_BN; j++) {
+        for (int j = 0; j < HC; j++) {
           const int n = n0 + j;
           if (n < a.N) P[(int64_t)m + (int64_t)a.M * n] = acc[j];
         }
@@ -509,28 +559,28 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const float fa = s_falpha, fb = (float)out.beta;
         if (out.beta == 1.0) {
 #pragma unroll
-          for (int j = 0; j < V2_BN; j++) {
-            const int64_t co = colOff[j];
+          for (int j = 0; j < HC; j++) {
+            const int64_t co = colH[j];
             if (co >= 0) atomicAdd(C + rowOff + co, fa * acc[j]);
           }
         } else if (out.beta == 0.0) {
 #pragma unroll
-          for (int j = 0; j < V2_BN; j++) {
-            const int64_t co = colOff[j];
+          for (int j = 0; j < HC; j++) {
+            const int64_t co = colH[j];
             if (co >= 0) C[rowOff + co] = fa * acc[j];
           }
         } else {
 #pragma unroll
-          for (int j = 0; j < V2_BN; j += 16) {
+          for (int j = 0; j < HC; j += 16) {
             float old[16];
 #pragma unroll
             for (int i = 0; i < 16; i++) {
-              const int64_t co = colOff[j + i];
+              const int64_t co = colH[j + i];
               old[i] = co >= 0 ? C[rowOff + co] : 0.0f;
             }
 #pragma unroll
             for (int i = 0; i < 16; i++) {
-              const int64_t co = colOff[j + i];
+              const int64_t co = colH[j + i];
               if (co >= 0) C[rowOff + co] = fa * acc[j + i] + fb * old[i];
             }
           }
@@ -546,40 +596,40 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         };
         if (s_shift_ok && out.beta == 1.0) {
 #pragma unroll
-          for (int j = 0; j < V2_BN; j++) {
-            const int64_t co = colOff[j];
+          for (int j = 0; j < HC; j++) {
+            const int64_t co = colH[j];
             if (co >= 0) atomicAdd(C + rowOff + co, scaled(acc[j]));
           }
         } else if (s_shift_ok && out.beta == 0.0) {
 #pragma unroll
-          for (int j = 0; j < V2_BN; j++) {
-            const int64_t co = colOff[j];
+          for (int j = 0; j < HC; j++) {
+            const int64_t co = colH[j];
             if (co >= 0) C[rowOff + co] = scaled(acc[j]);
           }
         } else if (out.beta == 1.0) {
 #pragma unroll
-          for (int j = 0; j < V2_BN; j++) {
-            const int64_t co = colOff[j];
+          for (int j = 0; j < HC; j++) {
+            const int64_t co = colH[j];
             if (co >= 0) atomicAdd(C + rowOff + co, alpha * (double)acc[j]);
           }
         } else if (out.beta == 0.0) {
 #pragma unroll
-          for (int j = 0; j < V2_BN; j++) {
-            const int64_t co = colOff[j];
+          for (int j = 0; j < HC; j++) {
+            const int64_t co = colH[j];
             if (co >= 0) C[rowOff + co] = alpha * (double)acc[j];
           }
         } else {
 #pragma unroll
-          for (int j = 0; j < V2_BN; j += 16) {
+          for (int j = 0; j < HC; j += 16) {
             double old[16];
 #pragma unroll
             for (int i = 0; i < 16; i++) {
-              const int64_t co = colOff[j + i];
+              const int64_t co = colH[j + i];
               old[i] = co >= 0 ? C[rowOff + co] : 0.0;
             }
 #pragma unroll
             for (int i = 0; i < 16; i++) {
-              const int64_t co = colOff[j + i];
+              const int64_t co = colH[j + i];
               if (co >= 0) C[rowOff + co] = alpha * (double)acc[j + i] + out.beta * old[i];
             }
           }
@@ -592,7 +642,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   if (warp == 1) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                 "r"(V2_TMEM_COLS)
+                 "r"(SH::TMEM_COLS)
                  : "memory");
   }
 }
@@ -769,10 +819,21 @@ CUtensorMap TcEngine::map_of(const Packed &p, int box_rows) {
 void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &out, int nseg,
                             int splits, float *partial, unsigned *err, cudaStream_t stream) {
   static std::once_flag once;
+  static bool wide_ok = false;
   std::call_once(once, [] {
-    cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)V2_SMEM_BYTES);
+    cudaFuncSetAttribute(tc_gemm_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)TcShape<128>::SMEM_BYTES);
+    cudaFuncSetAttribute(tc_gemm_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)TcShape<256>::SMEM_BYTES);
+    // The 256-wide kernel's setmaxnreg split assumes it is launched with exactly
+    // kLaunchRegs256 registers a thread (3 x 168 = 56 + 2 x 224 per scheduler).
+    cudaFuncAttributes fa;
+    wide_ok = cudaFuncGetAttributes(&fa, tc_gemm_kernel<256>) == cudaSuccess &&
+              fa.numRegs == kLaunchRegs256;
+    cudaGetLastError();
   });
+  const int bn = ps.bn == 256 ? 256 : 128;
+  if (bn == 256 && !wide_ok) throw Error(SCESS_ERR_UNSUPPORTED, "tc_gemm: 256-wide kernel unavailable");
   if (ps.M <= 0 || ps.N <= 0 || ps.ny <= 0 || ps.nz <= 0 || ps.ng <= 0) return;
   if (ps.ng > 3) throw Error(SCESS_ERR_INVALID, "tc_gemm: groups");
   if (nseg != 1 && nseg != 3) throw Error(SCESS_ERR_INVALID, "tc_gemm: nseg");
@@ -783,7 +844,7 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
   a.M = (int)ps.M;
   a.N = (int)ps.N;
   a.tiles_m = (int)ceil_div(ps.M, TC_BM);
-  a.tiles_n = (int)ceil_div(ps.N, V2_BN);
+  a.tiles_n = (int)ceil_div(ps.N, bn);
   a.ny = ps.ny;
   a.nz = ps.nz;
   a.ng = ps.ng;
@@ -797,7 +858,7 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
       const int64_t maxA = g.rowA0[q] + (int64_t)(ps.ny - 1) * g.rowAy[q] +
                            (int64_t)(ps.nz - 1) * g.rowAz[q] + a.tiles_m * TC_BM;
       const int64_t maxB = g.rowB0[q] + (int64_t)(ps.ny - 1) * g.rowBy[q] +
-                           (int64_t)(ps.nz - 1) * g.rowBz[q] + a.tiles_n * V2_BN;
+                           (int64_t)(ps.nz - 1) * g.rowBz[q] + a.tiles_n * bn;
       if (maxA > INT32_MAX || maxB > INT32_MAX || g.rowA0[q] < 0 || g.rowB0[q] < 0 ||
           g.rowAy[q] < 0 || g.rowAz[q] < 0 || g.rowBy[q] < 0 || g.rowBz[q] < 0)
         throw Error(SCESS_ERR_INVALID, "tc_gemm: row coordinates");
@@ -845,7 +906,10 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
   const int64_t units = (int64_t)a.tiles_m * a.tiles_n * ps.ny * ps.nz * ps.ng * splits;
   if (units > INT32_MAX) throw Error(SCESS_ERR_INVALID, "tc_gemm: too many work units");
   const unsigned grid = (unsigned)std::min<int64_t>(units, kNumSMs);
-  tc_gemm_kernel<<<grid, TC_THREADS, V2_SMEM_BYTES, stream>>>(maps, out, a);
+  if (bn == 256)
+    tc_gemm_kernel<256><<<grid, TcShape<256>::THREADS, TcShape<256>::SMEM_BYTES, stream>>>(maps, out, a);
+  else
+    tc_gemm_kernel<128><<<grid, TcShape<128>::THREADS, TcShape<128>::SMEM_BYTES, stream>>>(maps, out, a);
   SCESS_CHECK_LAUNCH();
   if (splits > 1) {
     const int64_t MN = ps.M * ps.N;

@@ -72,6 +72,9 @@ struct TcProblemSet {
   int64_t cy = 0, cz = 0;
   int64_t cg[3] = {0, 0, 0};
   int kbd = 1;  // K blocks per TMEM drain: 1, or 2 (fewer drains, ~2x rounding)
+  // tile width: 128, or 256 (B-side maps must then have 256-row boxes; half the
+  // shared-memory traffic per FLOP for the A operand)
+  int bn = 128;
   // per-group output tables (null: the TcOut tables)
   const int64_t *rowC[3] = {nullptr, nullptr, nullptr};
   const int64_t *colC[3] = {nullptr, nullptr, nullptr};

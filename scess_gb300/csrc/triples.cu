@@ -737,6 +737,8 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   // the A side (P, t2) and the B side (Q, R) each share one scale so that all
   // segments carry the same scale product.
   Packed pP, pQ, pQ2, pR, pR2, pTx;
+  int tbn = 256;
+  if (const char *env = std::getenv("SCESS_T_BN")) tbn = std::atoi(env) == 128 ? 128 : 256;
   CUtensorMap mP{}, mQ{}, mQ2{}, mR{}, mR2{}, mTx{};
   DevTables gdt;  // W_g row / column tables
   DevMem Sf;      // (ia|jb) as FP32 for the energy kernel
@@ -774,10 +776,12 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
     tc.pack_with_max(Rt.p(), pdt.ptr[5], o2 * vp, dt.ptr[kOperand + 5], o, false, 128, mx + 1, false, pR2);
     ctx.sync();
     mP = TcEngine::map_of(pP, 128);
-    mQ = TcEngine::map_of(pQ, 128);
-    mQ2 = TcEngine::map_of(pQ2, 128);
-    mR = TcEngine::map_of(pR, 128);
-    mR2 = TcEngine::map_of(pR2, 128);
+    // B side (Q, R rows): tiles of tbn columns; 256 halves the A-operand
+    // shared-memory traffic per FLOP (SCESS_T_BN=128 selects the narrow tiles)
+    mQ = TcEngine::map_of(pQ, tbn);
+    mQ2 = TcEngine::map_of(pQ2, tbn);
+    mR = TcEngine::map_of(pR, tbn);
+    mR2 = TcEngine::map_of(pR2, tbn);
     mTx = TcEngine::map_of(pTx, 128);
     // W_g[(y_l nb + z_l) nb + x_l][i + o j + o^2 k]: every group stores its
     // (u, s, t) in the (i, j, k) order of the triple, so that the energy kernel
@@ -830,6 +834,7 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
           ps.ng = 3;
           ps.nseg = 4;
           ps.kbd = 2;  // E_T within ~5e-7 relative of FP64 (1.8e-7 with kbd = 1)
+          ps.bn = tbn;
           ps.cy = nb * nb * o3;
           ps.cz = nb * o3;
           const int kRoles[3][3] = {{0, 1, 2}, {1, 0, 2}, {2, 0, 1}};  // (x, y, z) of group g
