@@ -44,9 +44,9 @@ CPU_SAMPLE = ('one full FP64 CCSD iteration of the NumPy oracle (MP2 guess, BLAS
 
 
 # DRAM bytes (read + write) of one grouped (T) GEMM launch at o=20, nb=12,
-# measured with ncu: the three W buffers (166 MB) are written once, 109 MB of
+# measured with ncu: the three W buffers (166 MB) are written once, 112 MB of
 # them reach DRAM, operands are read mostly from L2.
-TRIPLES_LAUNCH_TRAFFIC = 138.9e6
+TRIPLES_LAUNCH_TRAFFIC = 133.1e6
 
 
 def peaks():
@@ -442,7 +442,7 @@ def main():
                 'traffic': TRIPLES_LAUNCH_TRAFFIC if (o, v) == (20, 180) else None,
                 'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of one grouped '
                                   '(T) launch at o=20 v=96, which has the same launch shape '
-                                  '(nb=12, 3456 work units) as o=20 v=180',
+                                  '(nb=12, 1728 work units of 128 x 256) as o=20 v=180',
                 'top_kernel_by_time': top}
     share = {k: round(v['ms'] / max(sum(x['ms'] for x in prof.values()), 1e-9), 4) for k, v in prof.items()}
 
