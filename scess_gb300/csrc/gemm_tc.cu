@@ -1,13 +1,17 @@
-// tcgen05 / TMEM / TMA tensor-core GEMM for sm_103a (split BF16 hi+lo, FP32 accumulate).
+// tcgen05 / TMEM / TMA tensor-core GEMM for sm_103a (split 16-bit hi+lo, FP32 accumulate).
 //
-// One CTA computes a 128 x bn tile (bn <= 256, multiple of 16):
-//   warp 0      TMA producer: 128B-swizzled 128x64 (A) and bn x 64 (B) BF16 tiles
-//               into a 4-stage shared-memory ring (full/empty mbarriers);
-//   warp 1      allocates 256 TMEM columns; one thread issues tcgen05.mma
-//               (kind::f16, M=128, N=bn, K=16) and tcgen05.commit to free stages;
-//   warps 2..5  epilogue: tcgen05.ld 32x32b from their TMEM lane quarter and
-//               scatter alpha*acc + beta*C through the output offset tables.
-// The K loop runs three segments over the packed operands (hi*hi, hi*lo,
+// A persistent CTA per SM walks work units (problem, 128 x BN tile, K range):
+//   warp 0      TMA producer: 128B-swizzled 128x64 (A) and BNx64 (B) tiles of
+//               the hi and lo halves into a shared-memory ring (full/empty
+//               mbarriers; 3 stages at BN = 128, 2 at BN = 256);
+//   warp 1      allocates all 512 TMEM columns (512 / BN accumulators); one
+//               thread issues tcgen05.mma (kind::f16, M=128, N<=BN, K=16) and
+//               tcgen05.commit to free stages and hand accumulators over;
+//   the rest    epilogue warps (one warpgroup per 128 columns): tcgen05.ld
+//               32x32b from their TMEM lane quarter every K block (or every
+//               second), FP32 accumulation in registers, and the scatter of
+//               alpha*acc + beta*C through the output offset tables.
+// The K loop runs three products over the packed operands (hi*hi, hi*lo,
 // lo*hi).  Every mbarrier wait is bounded (~2 s): on expiry the kernel sets an
 // error word, lets its in-flight TMA copies land, frees TMEM and returns.
 #include <cuda.h>
@@ -20,6 +24,7 @@
 #include <mutex>
 
 #include "gemm_tc.h"
+#include "mbarrier.cuh"
 
 namespace scess {
 
@@ -36,58 +41,6 @@ constexpr size_t TC_SMEM_BYTES = 1024 /*align slack*/ + TC_STAGES * (A_STAGE_BYT
                                  (2 * TC_STAGES + 1) * 8 + 8 + TC_MAX_BN * 8;
 
 enum : unsigned { ERR_FULL_WAIT = 1, ERR_EMPTY_WAIT = 2, ERR_ACCUM_WAIT = 3 };
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-               "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// Bounded wait: false (and the error word set) after ~2^32 cycles or when
-// another role of the CTA already gave up.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, unsigned *err,
-                                          unsigned code) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const long long t0 = clock64();
-  for (unsigned spin = 1;; spin++) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if ((spin & 1023u) == 0) {
-      if (*(volatile unsigned *)err) return false;
-      if (clock64() - t0 > (1ll << 32)) {
-        atomicCAS(err, 0u, code);
-        return false;
-      }
-    }
-  }
-}
-
-// Bounded wait that ignores the error word: used to let issued TMA copies land
-// before the CTA exits (returns after ~2^32 cycles at the latest).
-__device__ __forceinline__ void mbar_drain(uint64_t *bar, uint32_t parity) {
-  const long long t0 = clock64();
-  while (!mbar_try_wait(bar, parity))
-    if (clock64() - t0 > (1ll << 32)) return;
-}
 
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *tm, int x, int y,
                                             uint64_t *bar) {

@@ -130,6 +130,8 @@ class TcEngine {
                  int nseg = 3, cudaStream_t stream = nullptr);
   // Device error word set by bounded waits inside the kernels (0 = fine).
   void check_error();
+  // The word itself, for other kernels with bounded waits (checked by check_error).
+  unsigned *error_word() { return err_.as<unsigned>(); }
   // Cached packings of constant operands are keyed by device pointer and
   // tagged with the owner that keeps those pointers alive: a resident
   // RccsdState (its address) or 0 for a single C-ABI call.  clear_cache(owner)
