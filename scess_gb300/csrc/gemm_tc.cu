@@ -31,14 +31,7 @@ namespace scess {
 namespace {
 
 constexpr int TC_BM = 128;
-constexpr int TC_BK = 64;  // 64 BF16 = 128 B = one SWIZZLE_128B row
-constexpr int TC_STAGES = 4;
-constexpr int TC_MAX_BN = 256;
-constexpr uint32_t A_STAGE_BYTES = TC_BM * TC_BK * 2;      // 16 KiB
-constexpr uint32_t B_STAGE_BYTES = TC_MAX_BN * TC_BK * 2;  // 32 KiB
-constexpr uint32_t TMEM_COLS = 256;
-constexpr size_t TC_SMEM_BYTES = 1024 /*align slack*/ + TC_STAGES * (A_STAGE_BYTES + B_STAGE_BYTES) +
-                                 (2 * TC_STAGES + 1) * 8 + 8 + TC_MAX_BN * 8;
+constexpr int TC_BK = 64;  // K padding of the packs; 64 x 16 bit = 128 B = one SWIZZLE_128B row
 
 enum : unsigned { ERR_FULL_WAIT = 1, ERR_EMPTY_WAIT = 2, ERR_ACCUM_WAIT = 3 };
 
@@ -58,15 +51,20 @@ __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row
-// core-matrix groups 1024 B apart (SBO), descriptor version 1 (sm_100 family).
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+// Shared-memory matrix descriptor of a K-major operand whose rows are SWZ
+// bytes (one swizzle span: 128 or 64): 8-row core-matrix groups 8 x SWZ bytes
+// apart (SBO), descriptor version 1 (sm_100 family), layout type 2
+// (SWIZZLE_128B) or 4 (SWIZZLE_64B).  The leading byte offset is unused for
+// swizzled K-major operands (one MMA's K = 16 x 16 bit = 32 B stays inside a row).
+template <int SWZ>
+__device__ __forceinline__ uint64_t sw_desc(uint32_t saddr) {
+  static_assert(SWZ == 128 || SWZ == 64, "swizzle span");
   uint64_t d = 0;
   d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
-  d |= (uint64_t)1 << 16;             // leading byte offset (unused for SW128 K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset
-  d |= (uint64_t)1 << 46;             // version
-  d |= (uint64_t)2 << 61;             // SWIZZLE_128B
+  d |= (uint64_t)1 << 16;                   // leading byte offset (unused)
+  d |= (uint64_t)((8 * SWZ) >> 4) << 32;    // stride byte offset
+  d |= (uint64_t)1 << 46;                   // version
+  d |= (uint64_t)(SWZ == 128 ? 2 : 4) << 61;
   return d;
 }
 
@@ -183,31 +181,39 @@ struct TcArgs {
 // A problem's K range may span several segments with different operands
 // (up to 4), each optionally negated through the instruction descriptor.
 constexpr int V2_BN = 128;  // tile width of the einsum launches
-constexpr uint32_t V2_TILE_BYTES = 128 * TC_BK * 2;  // 16 KiB: 128 rows x 128 B
 
 // Shape of a kernel instantiation by tile width BN (128 or 256):
-//   BN = 128: 3 stages of 64 KiB, four 128-column TMEM accumulators, 192
-//             threads (warps 2-5 drain and store);
-//   BN = 256: 2 stages of 96 KiB, two 256-column accumulators, 384 threads
-//             (warps 2-3 idle, warps 4-7 / 8-11 drain and store columns
-//             0-127 / 128-255).  With more than one warp per scheduler beside
-//             the epilogue the block is capped at 168 registers a thread, so
-//             the warpgroups rebalance with setmaxnreg: 56 for warps 0-3,
-//             224 for the epilogue (3 x 168 = 56 + 2 x 224 per scheduler).
+//   BN = 128: K blocks of 64 (128-byte rows, SWIZZLE_128B), 3 stages of
+//             64 KiB, four 128-column TMEM accumulators, 192 threads (warps
+//             2-5 drain and store);
+//   BN = 256: K blocks of 32 (64-byte rows, SWIZZLE_64B), 4 stages of 48 KiB
+//             (the same 192 KiB as 2 stages of 64-wide blocks, but three
+//             stages in flight while one is consumed), two 256-column
+//             accumulators, 384 threads (warps 2-3 idle, warps 4-7 / 8-11
+//             drain and store columns 0-127 / 128-255).  With more than one
+//             warp per scheduler beside the epilogue the block is capped at
+//             168 registers a thread, so the warpgroups rebalance with
+//             setmaxnreg: 56 for warps 0-3, 224 for the epilogue (3 x 168 =
+//             56 + 2 x 224 per scheduler).
 // Every epilogue thread holds 128 columns of one row.
 template <int BN>
 struct TcShape {
-  static constexpr int STAGES = BN == 256 ? 2 : 3;
+  static constexpr int BK = BN == 256 ? 32 : 64;   // K per stage (16-bit elements)
+  static constexpr int SWZ = 2 * BK;               // row bytes = swizzle span
+  static constexpr int STAGES = BN == 256 ? 4 : 3;
   static constexpr int NBUF = 512 / BN;
   static constexpr int EPI0 = BN == 256 ? 4 : 2;   // first epilogue warp
   static constexpr int NEPI = BN / 32;              // epilogue warps
   static constexpr int THREADS = 32 * (EPI0 + NEPI);
   static constexpr int CH = BN == 256 ? 16 : 32;    // columns per staged chunk
-  static constexpr uint32_t B_BYTES = (uint32_t)BN * TC_BK * 2;
-  static constexpr uint32_t STAGE_BYTES = 2 * V2_TILE_BYTES + 2 * B_BYTES;
+  static constexpr uint32_t A_BYTES = (uint32_t)TC_BM * BK * 2;
+  static constexpr uint32_t B_BYTES = (uint32_t)BN * BK * 2;
+  static constexpr uint32_t STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
   static constexpr uint32_t TMEM_COLS = 512;
+  // 1 KiB alignment slack in front, the barriers behind the stages, and 1 KiB
+  // of tail slack so that no descriptor-addressed read can leave the allocation
   static constexpr size_t SMEM_BYTES =
-      1024 + STAGES * STAGE_BYTES + (2 * STAGES + 2 * NBUF + 1) * 8 + 8;
+      1024 + STAGES * STAGE_BYTES + (2 * STAGES + 2 * NBUF + 1) * 8 + 8 + 1024;
 };
 constexpr int kEpiRegs256 = 224, kCtlRegs256 = 56, kLaunchRegs256 = 168;
 
@@ -327,7 +333,7 @@ __global__ void __launch_bounds__(TcShape<BN>::THREADS, 1)
     if (lane == 0) {
       for (int i = 0; i < 6; i++)
         asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&maps.m[i]) : "memory");
-      const uint32_t bytes = a.split3 ? SH::STAGE_BYTES : V2_TILE_BYTES + SH::B_BYTES;
+      const uint32_t bytes = a.split3 ? SH::STAGE_BYTES : SH::A_BYTES + SH::B_BYTES;
       int g = 0;
       int last[STAGES];
       for (int s = 0; s < STAGES; s++) last[s] = -1;
@@ -347,12 +353,12 @@ __global__ void __launch_bounds__(TcShape<BN>::THREADS, 1)
           uint8_t *st = smem + s * SH::STAGE_BYTES;
           const CUtensorMap *mA = &maps.m[S.mapA], *mB = &maps.m[S.mapB];
           mbar_expect_tx(&full[s], bytes);
-          const int x = lkb * TC_BK;
+          const int x = lkb * SH::BK;
           tma_load_2d(st, mA, x, ya, &full[s]);                                  // A hi
-          tma_load_2d(st + V2_TILE_BYTES, mB, x, yb, &full[s]);                  // B hi
+          tma_load_2d(st + SH::A_BYTES, mB, x, yb, &full[s]);                    // B hi
           if (a.split3) {
-            tma_load_2d(st + V2_TILE_BYTES + SH::B_BYTES, mA, S.kpad + x, ya, &full[s]);  // A lo
-            tma_load_2d(st + 2 * V2_TILE_BYTES + SH::B_BYTES, mB, S.kpad + x, yb, &full[s]);  // B lo
+            tma_load_2d(st + SH::A_BYTES + SH::B_BYTES, mA, S.kpad + x, ya, &full[s]);  // A lo
+            tma_load_2d(st + 2 * SH::A_BYTES + SH::B_BYTES, mB, S.kpad + x, yb, &full[s]);  // B lo
           }
           last[s] = g;
         }
@@ -385,22 +391,22 @@ __global__ void __launch_bounds__(TcShape<BN>::THREADS, 1)
           if (!mbar_wait(&full[s], ph, a.err, ERR_FULL_WAIT)) { ok = false; break; }
           tc_fence_after();
           const uint32_t st = smem_u32(smem + s * SH::STAGE_BYTES);
-          const uint32_t ahi = st, bhi = st + V2_TILE_BYTES;
-          const uint32_t alo = st + V2_TILE_BYTES + SH::B_BYTES;
-          const uint32_t blo = st + 2 * V2_TILE_BYTES + SH::B_BYTES;
+          const uint32_t ahi = st, bhi = st + SH::A_BYTES;
+          const uint32_t alo = st + SH::A_BYTES + SH::B_BYTES;
+          const uint32_t blo = st + 2 * SH::A_BYTES + SH::B_BYTES;
           const uint32_t d = tmem + (uint32_t)(b * BN);
           uint32_t acc = first ? 0u : 1u;
           if (a.split3) {
 #pragma unroll
-            for (int k = 0; k < TC_BK / 16; k++, acc = 1)
-              mma_bf16(d, sw128_desc(alo + 32 * k), sw128_desc(bhi + 32 * k), id, acc);
+            for (int k = 0; k < SH::BK / 16; k++, acc = 1)
+              mma_bf16(d, sw_desc<SH::SWZ>(alo + 32 * k), sw_desc<SH::SWZ>(bhi + 32 * k), id, acc);
 #pragma unroll
-            for (int k = 0; k < TC_BK / 16; k++)
-              mma_bf16(d, sw128_desc(ahi + 32 * k), sw128_desc(blo + 32 * k), id, 1u);
+            for (int k = 0; k < SH::BK / 16; k++)
+              mma_bf16(d, sw_desc<SH::SWZ>(ahi + 32 * k), sw_desc<SH::SWZ>(blo + 32 * k), id, 1u);
           }
 #pragma unroll
-          for (int k = 0; k < TC_BK / 16; k++, acc = 1)
-            mma_bf16(d, sw128_desc(ahi + 32 * k), sw128_desc(bhi + 32 * k), id, acc);
+          for (int k = 0; k < SH::BK / 16; k++, acc = 1)
+            mma_bf16(d, sw_desc<SH::SWZ>(ahi + 32 * k), sw_desc<SH::SWZ>(bhi + 32 * k), id, acc);
           mma_commit(&empty[s]);
           if (last) {
             mma_commit(&tfull[b]);
@@ -744,17 +750,22 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
   return fn;
 }
 
-CUtensorMap make_map(const void *base, int64_t rows_pad, int64_t Kpad, int box_rows, TcFormat fmt) {
+// Boxes of box_rows x bk 16-bit values: bk = 64 (128-byte rows, SWIZZLE_128B)
+// or 32 (64-byte rows, SWIZZLE_64B), matching the kernel's K block.
+CUtensorMap make_map(const void *base, int64_t rows_pad, int64_t Kpad, int box_rows, int bk,
+                     TcFormat fmt) {
+  if (bk != 64 && bk != 32) throw Error(SCESS_ERR_INVALID, "tc_gemm: K block of a map");
   CUtensorMap m;
   std::memset(&m, 0, sizeof(m));
   cuuint64_t dims[2] = {(cuuint64_t)(2 * Kpad), (cuuint64_t)rows_pad};
   cuuint64_t strides[1] = {(cuuint64_t)(2 * Kpad * 2)};
-  cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows};
+  cuuint32_t box[2] = {(cuuint32_t)bk, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = get_encode()(&m, fmt == TcFormat::FP16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
                                                       : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
                             2, const_cast<void *>(base), dims, strides,
-                            box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                            box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                            bk == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS)
     throw Error(SCESS_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
@@ -765,9 +776,11 @@ CUtensorMap make_map(const void *base, int64_t rows_pad, int64_t Kpad, int box_r
 
 int TcEngine::tile_n(int64_t) { return V2_BN; }
 
-CUtensorMap TcEngine::map_of(const Packed &p, int box_rows) {
-  return make_map(p.p(), p.rows_pad, p.Kpad, box_rows, p.fmt);
+CUtensorMap TcEngine::map_of(const Packed &p, int box_rows, int bk) {
+  return make_map(p.p(), p.rows_pad, p.Kpad, box_rows, bk, p.fmt);
 }
+
+int TcEngine::k_block(int bn) { return bn == 256 ? TcShape<256>::BK : TcShape<128>::BK; }
 
 void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &out, int nseg,
                             int splits, float *partial, unsigned *err, cudaStream_t stream) {
@@ -818,7 +831,7 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
     }
     a.seg[s].mapA = g.mapA;
     a.seg[s].mapB = g.mapB;
-    a.seg[s].nkb = (int)(g.Kpad / TC_BK);
+    a.seg[s].nkb = (int)(g.Kpad / (bn == 256 ? TcShape<256>::BK : TcShape<128>::BK));
     a.seg[s].kpad = (int)g.Kpad;
     a.seg[s].negA = g.negate ? 1 : 0;
     for (int q = 0; q < 3; q++) {
@@ -841,7 +854,7 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
   a.splits = splits;
   a.f16 = fmt == TcFormat::FP16 ? 1 : 0;
   a.split3 = nseg == 3 ? 1 : 0;
-  a.kbd = ps.kbd == 2 ? 2 : 1;
+  a.kbd = (ps.kbd == 2 || ps.kbd == 4) ? ps.kbd : 1;
   a.cy = ps.cy;
   a.cz = ps.cz;
   for (int q = 0; q < 3; q++) {

@@ -71,9 +71,12 @@ struct TcProblemSet {
   TcSegment seg[4];
   int64_t cy = 0, cz = 0;
   int64_t cg[3] = {0, 0, 0};
-  int kbd = 1;  // K blocks per TMEM drain: 1, or 2 (fewer drains, ~2x rounding)
+  // K blocks per TMEM drain: 1, 2 or 4 (fewer drains, more products
+  // accumulated in TMEM between drains).  A K block is k_block(bn) wide.
+  int kbd = 1;
   // tile width: 128, or 256 (B-side maps must then have 256-row boxes; half the
-  // shared-memory traffic per FLOP for the A operand)
+  // shared-memory traffic per FLOP for the A operand).  All maps must have
+  // k_block(bn)-wide boxes: map_of(p, rows, k_block(bn)).
   int bn = 128;
   // per-group output tables (null: the TcOut tables)
   const int64_t *rowC[3] = {nullptr, nullptr, nullptr};
@@ -113,8 +116,11 @@ class TcEngine {
             const TcOut &out, int nseg = 3, int force_splits = 0);
   // Tile width used for an N-column product (multiple of 16, <= 256).
   static int tile_n(int64_t N);
-  // TMA descriptor of a packed operand with boxes of box_rows x 64.
-  static CUtensorMap map_of(const Packed &p, int box_rows);
+  // TMA descriptor of a packed operand with boxes of box_rows x bk (bk = 64:
+  // SWIZZLE_128B, bk = 32: SWIZZLE_64B).
+  static CUtensorMap map_of(const Packed &p, int box_rows, int bk = 64);
+  // K block (16-bit values per stage row) of the kernel with tile width bn.
+  static int k_block(int bn);
   // TcOut scale pointers of a product of two packed operands.
   static void set_scales(TcOut &out, const Packed &A, const Packed &B) {
     out.scaleA = A.scale();
@@ -130,8 +136,6 @@ class TcEngine {
                  int nseg = 3, cudaStream_t stream = nullptr);
   // Device error word set by bounded waits inside the kernels (0 = fine).
   void check_error();
-  // The word itself, for other kernels with bounded waits (checked by check_error).
-  unsigned *error_word() { return err_.as<unsigned>(); }
   // Cached packings of constant operands are keyed by device pointer and
   // tagged with the owner that keeps those pointers alive: a resident
   // RccsdState (its address) or 0 for a single C-ABI call.  clear_cache(owner)

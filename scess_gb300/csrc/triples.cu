@@ -25,7 +25,6 @@
 #include <vector>
 
 #include "gemm_tc.h"
-#include "mbarrier.cuh"
 #include "triples.h"
 
 namespace scess {
@@ -145,12 +144,11 @@ __global__ void to_f32_rows_kernel(const double *__restrict__ x, int64_t rows, i
   }
 }
 
-// Layout of the grouped W buffers and the FP32 copies the mixed energy kernels
-// read: rows of o^2 (i, j) pairs are padded to o2p = o^2 rounded up to a
-// multiple of 4 floats, so that every k row and every o^3 block starts on a
-// 16-byte boundary (bulk copies need that).  W_g[((y_l nb + z_l) nb + x_l) o3p
-// + i + o j + o2p k] with o3p = o o2p; S as [(a + v b) o2p + i + o j]; t1 as
-// [a op + i] with op = o rounded up to a multiple of 4.
+// Layout of the grouped W buffers and the FP32 copy of S the mixed energy
+// kernel reads: rows of o^2 (i, j) pairs are padded to o2p = o^2 rounded up to
+// a multiple of 4 floats, so that every k row and every o^3 block starts on a
+// 16-byte boundary.  W_g[((y_l nb + z_l) nb + x_l) o3p + i + o j + o2p k] with
+// o3p = o o2p; S as [(a + v b) o2p + i + o j].
 __host__ __device__ inline int64_t pad4(int64_t n) { return (n + 3) & ~int64_t(3); }
 
 // Energy of one block triple from the three grouped W buffers of the
@@ -159,7 +157,7 @@ __host__ __device__ inline int64_t pad4(int64_t n) { return (n + 3) & ~int64_t(3
 // for its roles (x, y, z)).  Threads own (i, j) pairs and walk k: one pass of
 // coalesced loads forms Y = W + V in shared memory, W is recovered as Y - V in
 // the energy loop.  Otherwise as triples_energy_kernel (FP32 per element, FP64
-// per thread sum).  Used when triples_energy4_kernel's ring does not fit.
+// per thread sum).
 __global__ void __launch_bounds__(256) triples_energy3_kernel(
     const float *__restrict__ W, int64_t o, int64_t v, int64_t nb, int64_t A, int64_t Bk,
     int64_t C, const double *__restrict__ eps, const double *__restrict__ t1,
@@ -236,227 +234,6 @@ __global__ void __launch_bounds__(256) triples_energy3_kernel(
     else if (a == b || b == c) deg = 2.0;
     energies[triple_id(a, b, c)] = sum / deg;
   }
-}
-
-// Shared-memory plan of triples_energy4_kernel (byte offsets into the dynamic
-// allocation, all 128-byte aligned).
-struct E4Plan {
-  int o = 0, o2p = 0, op = 0;
-  int kc = 0, nch = 0, ns = 0;  // k rows per chunk, chunks per triple, ring slots
-  int threads = 0;
-  uint32_t y_off = 0, small_off[2] = {0, 0}, eps_off = 0, ring_off = 0, bar_off = 0, bytes = 0;
-  uint32_t slot_floats = 0;     // 3 kc o2p
-  bool fits = false;
-};
-
-constexpr unsigned ERR_ENERGY_WAIT = 4;
-
-// Persistent form of triples_energy3_kernel: one CTA per SM walks the triples
-// (a_l, b_l, c_l) = blockIdx.x, blockIdx.x + gridDim.x, ... of the block triple.
-// Thread 0 streams each triple's W rows (chunks of kc k-rows from the three
-// buffers) into a ring of ns shared-memory slots with cp.async.bulk, ns chunks
-// ahead of the consumers, and the triple's S and t1 slices into one of two
-// small buffers one triple ahead; so the loads of the next triple are in
-// flight while the current one runs its r3 / energy loop.  Per triple the
-// arithmetic is that of triples_energy3_kernel.  Waits are bounded: on expiry
-// the CTA sets the error word, lets its issued copies land and returns.
-__global__ void __launch_bounds__(512, 1) triples_energy4_kernel(
-    const float *__restrict__ W, int64_t v, int64_t nb, int64_t A, int64_t Bk, int64_t C,
-    const double *__restrict__ eps, const float *__restrict__ t1p, const float *__restrict__ Sp,
-    double *__restrict__ energies, unsigned *err, const E4Plan pl) {
-  extern __shared__ __align__(128) unsigned char sm4[];
-  __shared__ double red[32];
-  const int oo = pl.o, o2 = oo * oo, o2p = pl.o2p, op = pl.op, kc = pl.kc, nch = pl.nch,
-            ns = pl.ns;
-  const int64_t o3p = (int64_t)oo * o2p, nb3 = nb * nb * nb;
-  const int p1 = oo | 1, p2 = (p1 * oo) | 1;
-  float *Y = reinterpret_cast<float *>(sm4 + pl.y_off);
-  float *eo = reinterpret_cast<float *>(sm4 + pl.eps_off);
-  float *ring = reinterpret_cast<float *>(sm4 + pl.ring_off);
-  uint64_t *full = reinterpret_cast<uint64_t *>(sm4 + pl.bar_off), *sbar = full + ns;
-  const int tid = threadIdx.x, nthr = blockDim.x;
-
-  // valid local triple u: a >= b >= c inside the virtual range
-  auto next_unit = [&](int64_t u) -> int64_t {
-    for (; u < nb3; u += gridDim.x) {
-      const int64_t al = u / (nb * nb), bl = (u / nb) % nb, cl = u % nb;
-      const int64_t a = A * nb + al, b = Bk * nb + bl, c = C * nb + cl;
-      if (a < v && b < v && c < v && b <= a && c <= b) return u;
-    }
-    return nb3;
-  };
-  auto small_buf = [&](int64_t n) {
-    return reinterpret_cast<float *>(sm4 + ((n & 1) ? pl.small_off[1] : pl.small_off[0]));
-  };
-
-  if (tid == 0) {
-    for (int q = 0; q < ns + 2; q++) mbar_init(&full[q], 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    fence_proxy_async_smem();
-  }
-  for (int i = tid; i < oo; i += nthr) eo[i] = (float)eps[i];
-  __syncthreads();
-
-  // issuer state (thread 0): next chunk (unit iu, chunk ic), chunks and
-  // small-slice sets issued so far
-  int64_t iu = next_unit(blockIdx.x), nissued = 0, sissued = 0;
-  int ic = 0;
-  auto issue_chunk = [&]() {
-    if (iu >= nb3) return;
-    const int slot = (int)(nissued % ns);
-    const int k0 = ic * kc, kn = min(kc, oo - k0);
-    const uint32_t bytes = (uint32_t)kn * o2p * 4u;
-    const int64_t al = iu / (nb * nb), bl = (iu / nb) % nb, cl = iu % nb;
-    const float *src = W + (int64_t)k0 * o2p;
-    float *dst = ring + (int64_t)slot * pl.slot_floats;
-    const int64_t dg = (int64_t)kc * o2p;
-    fence_proxy_async_smem();
-    mbar_expect_tx(&full[slot], 3u * bytes);
-    bulk_g2s(dst, src + ((bl * nb + cl) * nb + al) * o3p, bytes, &full[slot]);
-    bulk_g2s(dst + dg, src + (nb3 + (al * nb + cl) * nb + bl) * o3p, bytes, &full[slot]);
-    bulk_g2s(dst + 2 * dg, src + (2 * nb3 + (al * nb + bl) * nb + cl) * o3p, bytes, &full[slot]);
-    nissued++;
-    if (++ic == nch) {
-      ic = 0;
-      iu = next_unit(iu + gridDim.x);
-    }
-  };
-  auto issue_small = [&](int64_t u) {
-    const int64_t al = u / (nb * nb), bl = (u / nb) % nb, cl = u % nb;
-    const int64_t a = A * nb + al, b = Bk * nb + bl, c = C * nb + cl;
-    float *d = small_buf(sissued);
-    uint64_t *bar = &sbar[sissued & 1];
-    const uint32_t sb = (uint32_t)o2p * 4u, tb = (uint32_t)op * 4u;
-    fence_proxy_async_smem();
-    mbar_expect_tx(bar, 3u * (sb + tb));
-    bulk_g2s(d, Sp + (b + v * c) * o2p, sb, bar);
-    bulk_g2s(d + o2p, Sp + (a + v * c) * o2p, sb, bar);
-    bulk_g2s(d + 2 * o2p, Sp + (a + v * b) * o2p, sb, bar);
-    bulk_g2s(d + 3 * o2p, t1p + a * op, tb, bar);
-    bulk_g2s(d + 3 * o2p + op, t1p + b * op, tb, bar);
-    bulk_g2s(d + 3 * o2p + 2 * op, t1p + c * op, tb, bar);
-    sissued++;
-  };
-
-  int64_t cu = next_unit(blockIdx.x);
-  if (tid == 0 && cu < nb3) {
-    issue_small(cu);
-    for (int q = 0; q < ns; q++) issue_chunk();
-  }
-  int64_t nq = 0, nu = 0;  // chunks / triples consumed
-  bool aborted = false;
-  while (cu < nb3) {
-    const int64_t al = cu / (nb * nb), bl = (cu / nb) % nb, cl = cu % nb;
-    const int64_t a = A * nb + al, b = Bk * nb + bl, c = C * nb + cl;
-    const float *sm = small_buf(nu);
-    const float *Sbc = sm, *Sac = sm + o2p, *Sab = sm + 2 * o2p, *ta = sm + 3 * o2p,
-                *tb = ta + op, *tc = tb + op;
-    bool ok = mbar_wait(&sbar[nu & 1], (uint32_t)(nu >> 1) & 1u, err, ERR_ENERGY_WAIT);
-    // Y = W0 + W1 + W2 + V, chunk by chunk as the rows land
-    for (int ch = 0; ch < nch; ch++) {
-      const int slot = (int)(nq % ns);
-      ok = ok && mbar_wait(&full[slot], (uint32_t)(nq / ns) & 1u, err, ERR_ENERGY_WAIT);
-      if (ok) {
-        const float *r0 = ring + (int64_t)slot * pl.slot_floats, *r1 = r0 + kc * o2p,
-                    *r2 = r1 + kc * o2p;
-        const int k0 = ch * kc, kn = min(kc, oo - k0);
-        for (int pr = tid; pr < o2; pr += nthr) {
-          const int i = pr % oo, j = pr / oo;
-          const float tai = ta[i], tbj = tb[j], sab = Sab[pr];
-          float *y = Y + i + p1 * j;
-#pragma unroll 4
-          for (int kk = 0; kk < kn; kk++) {
-            const int k = k0 + kk, e = pr + o2p * kk;
-            y[p2 * k] = (r0[e] + r1[e]) + r2[e] + tai * Sbc[j + oo * k] + tbj * Sac[i + oo * k] +
-                        tc[k] * sab;
-          }
-        }
-      }
-      if (__syncthreads_or(!ok)) {
-        aborted = true;
-        break;
-      }
-      nq++;
-      if (tid == 0) issue_chunk();  // into the slot just released
-    }
-    if (aborted) break;
-    nu++;
-    const int64_t nxt = next_unit(cu + gridDim.x);
-    if (tid == 0 && nxt < nb3) issue_small(nxt);
-    const float evirt = (float)(eps[oo + a] + eps[oo + b] + eps[oo + c]);
-    double acc = 0.0;
-    for (int pr = tid; pr < o2; pr += nthr) {
-      const int i = pr % oo, j = pr / oo;
-      const float tai = ta[i], tbj = tb[j], sab = Sab[pr], eij = eo[i] + eo[j];
-      float part = 0.0f;
-#pragma unroll 2
-      for (int k = 0; k < oo; k++) {
-        const float y = Y[i + p1 * j + p2 * k];
-        // r3(Y) = 4 Y_ijk + Y_kij + Y_jki - 2 Y_kji - 2 Y_ikj - 2 Y_jik         :152-154
-        const float r3 = 4.0f * y + Y[k + p1 * i + p2 * j] + Y[j + p1 * k + p2 * i] -
-                         2.0f * (Y[k + p1 * j + p2 * i] + Y[i + p1 * k + p2 * j] + Y[j + p1 * i + p2 * k]);
-        const float wv = y - (tai * Sbc[j + oo * k] + tbj * Sac[i + oo * k] + tc[k] * sab);
-        const float d = (eij + eo[k]) - evirt;                                     // :155
-        part += __fdividef(wv * r3, d);                                             // :156
-      }
-      acc += (double)part;
-    }
-    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
-    if ((tid & 31) == 0) red[tid >> 5] = acc;
-    __syncthreads();  // also: every thread is done with Y and this triple's slices
-    if (tid == 0) {
-      double sum = 0.0;
-      for (int q = 0; q < (nthr >> 5); q++) sum += red[q];
-      double deg = 1.0;                                                             // :135-139
-      if (a == c) deg = 6.0;
-      else if (a == b || b == c) deg = 2.0;
-      energies[triple_id(a, b, c)] = sum / deg;
-    }
-    cu = nxt;
-  }
-  if (tid == 0) {  // let every issued copy land before the CTA's memory goes away
-    for (int64_t q = nq; q < nissued; q++) mbar_drain(&full[q % ns], (uint32_t)(q / ns) & 1u);
-    for (int64_t n = nu; n < sissued; n++) mbar_drain(&sbar[n & 1], (uint32_t)(n >> 1) & 1u);
-  }
-}
-
-// Shared-memory plan for o occupied orbitals (fits = false: use the
-// one-CTA-per-triple kernel).
-E4Plan plan_energy4(int64_t o) {
-  E4Plan p;
-  const int64_t o2 = o * o, o2p = pad4(o2), op = pad4(o);
-  const int64_t p1 = o | 1, p2 = (p1 * o) | 1;
-  auto al = [](int64_t b) { return (b + 127) & ~int64_t(127); };
-  int64_t off = 0;
-  p.y_off = 0;
-  off = al(p2 * o * 4);
-  p.small_off[0] = (uint32_t)off;
-  off += al((3 * o2p + 3 * op) * 4);
-  p.small_off[1] = (uint32_t)off;
-  off += al((3 * o2p + 3 * op) * 4);
-  p.eps_off = (uint32_t)off;
-  off += al(op * 4);
-  p.bar_off = (uint32_t)off;
-  const int64_t kMaxSlots = 12;
-  off += al((kMaxSlots + 2) * 8);
-  p.ring_off = (uint32_t)off;
-  // static shared memory (red) and slack below the 227 KB per-CTA limit
-  const int64_t budget = 227 * 1024 - 1024;
-  const int64_t kc = std::max<int64_t>(1, std::min<int64_t>(o, 24576 / (12 * o2p)));
-  const int64_t slot = kc * 3 * o2p * 4;
-  const int64_t nch = ceil_div(o, kc);
-  const int64_t ns = std::min(std::min(kMaxSlots, 2 * nch), (budget - off) / slot);
-  p.o = (int)o;
-  p.o2p = (int)o2p;
-  p.op = (int)op;
-  p.kc = (int)kc;
-  p.nch = (int)nch;
-  p.ns = (int)std::max<int64_t>(ns, 0);
-  p.slot_floats = (uint32_t)(3 * kc * o2p);
-  p.bytes = (uint32_t)(off + std::max<int64_t>(ns, 0) * slot);
-  p.threads = (int)std::min<int64_t>(512, std::max<int64_t>(128, round_up(o2, 32)));
-  p.fits = ns >= 2;
-  return p;
 }
 
 __global__ void sum_energies_kernel(int64_t n, const double *__restrict__ e, double *out) {
@@ -979,7 +756,7 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   if (const char *env = std::getenv("SCESS_T_BN")) tbn = std::atoi(env) == 128 ? 128 : 256;
   CUtensorMap mP{}, mQ{}, mQ2{}, mR{}, mR2{}, mTx{};
   DevTables gdt;  // W_g row / column tables
-  DevMem Sf, t1f;  // (ia|jb) and t1 as FP32 for the energy kernel (padded rows)
+  DevMem Sf;  // (ia|jb) as FP32 for the energy kernel (padded rows)
   const int64_t Mg = o * nb, Ng = o2;
   const int64_t Mpq = o * nb * nb, Npq = o2 * nb, Mr = o2 * nb, Nr = o * nb * nb;  // FP64 GEMMs
   if (mixed) {
@@ -1013,14 +790,16 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
     tc.pack_with_max(Rt.p(), pdt.ptr[2], o2 * vp, dt.ptr[kOperand + 5], o, false, 128, mx + 1, false, pR);
     tc.pack_with_max(Rt.p(), pdt.ptr[5], o2 * vp, dt.ptr[kOperand + 5], o, false, 128, mx + 1, false, pR2);
     ctx.sync();
-    mP = TcEngine::map_of(pP, 128);
     // B side (Q, R rows): tiles of tbn columns; 256 halves the A-operand
-    // shared-memory traffic per FLOP (SCESS_T_BN=128 selects the narrow tiles)
-    mQ = TcEngine::map_of(pQ, tbn);
-    mQ2 = TcEngine::map_of(pQ2, tbn);
-    mR = TcEngine::map_of(pR, tbn);
-    mR2 = TcEngine::map_of(pR2, tbn);
-    mTx = TcEngine::map_of(pTx, 128);
+    // shared-memory traffic per FLOP (SCESS_T_BN=128 selects the narrow tiles).
+    // Boxes as wide as the kernel's K block.
+    const int tbk = TcEngine::k_block(tbn);
+    mP = TcEngine::map_of(pP, 128, tbk);
+    mQ = TcEngine::map_of(pQ, tbn, tbk);
+    mQ2 = TcEngine::map_of(pQ2, tbn, tbk);
+    mR = TcEngine::map_of(pR, tbn, tbk);
+    mR2 = TcEngine::map_of(pR2, tbn, tbk);
+    mTx = TcEngine::map_of(pTx, 128, tbk);
     // W_g[(y_l nb + z_l) nb + x_l][i + o j + o2p k]: every group stores its
     // (u, s, t) in the (i, j, k) order of the triple, so that the energy kernel
     // reads the three buffers alike.  g = 0: (u,s,t) = (i,j,k); g = 1: (j,i,k);
@@ -1032,18 +811,7 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
     to_f32_rows_kernel<<<(unsigned)std::min<int64_t>(ceil_div(o2p * v * v, 256), 16 * kNumSMs), 256, 0, s>>>(
         T.S.p(), v * v, o2, o2p, Sf.as<float>());
     SCESS_CHECK_LAUNCH();
-    t1f.alloc((size_t)pad4(o) * v * sizeof(float));
-    to_f32_rows_kernel<<<(unsigned)ceil_div(pad4(o) * v, 256), 256, 0, s>>>(d_t1, v, o, pad4(o),
-                                                                           t1f.as<float>());
-    SCESS_CHECK_LAUNCH();
   }
-  // MIXED energy: the persistent streaming kernel where its ring fits
-  // (SCESS_T_ENERGY=3 selects the one-CTA-per-triple kernel)
-  E4Plan e4 = plan_energy4(o);
-  if (const char *env = std::getenv("SCESS_T_ENERGY")) e4.fits = e4.fits && std::atoi(env) != 3;
-  if (mixed && e4.fits)
-    SCESS_CUDA(cudaFuncSetAttribute(triples_energy4_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)e4.bytes));
   // (i, j) pairs spread evenly over at most 256 threads
   const unsigned e3threads =
       (unsigned)round_up(ceil_div(o2, ceil_div(o2, 256)), 32);
@@ -1082,7 +850,9 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
           ps.nz = nb;
           ps.ng = 3;
           ps.nseg = 4;
-          ps.kbd = 2;  // E_T within ~5e-7 relative of FP64 (1.8e-7 with kbd = 1)
+          // one TMEM drain per 128 K (24 MMAs): E_T within ~5e-7 relative of
+          // FP64 (1.8e-7 with a drain per 64 K)
+          ps.kbd = 128 / TcEngine::k_block(tbn);
           ps.bn = tbn;
           ps.cy = nb * nb * o3p;
           ps.cz = nb * o3p;
@@ -1125,11 +895,7 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
         }
         const unsigned nblk = (unsigned)(nb * nb * nb);
         TimedScope ts(ctx.timer, "triples_energy", 0.0, (double)nblk * o3 * (mixed ? 3 * 4 : 8), s);
-        if (mixed && e4.fits)
-          triples_energy4_kernel<<<(unsigned)std::min<int64_t>(nblk, kNumSMs), e4.threads, e4.bytes, s>>>(
-              W.as<float>(), v, nb, A, Bk, C, d_eps, t1f.as<float>(), Sf.as<float>(), energies.p(),
-              ctx.tensor_cores().error_word(), e4);
-        else if (mixed)
+        if (mixed)
           triples_energy3_kernel<<<nblk, e3threads, ysmem, s>>>(
               W.as<float>(), o, v, nb, A, Bk, C, d_eps, d_t1, Sf.as<float>(), energies.p());
         else
