@@ -186,9 +186,9 @@ constexpr int V2_BN = 128;  // tile width of the einsum launches
 //   BN = 128: K blocks of 64 (128-byte rows, SWIZZLE_128B), 3 stages of
 //             64 KiB, four 128-column TMEM accumulators, 192 threads (warps
 //             2-5 drain and store);
-//   BN = 256: K blocks of 32 (64-byte rows, SWIZZLE_64B), 4 stages of 48 KiB
-//             (the same 192 KiB as 2 stages of 64-wide blocks, but three
-//             stages in flight while one is consumed), two 256-column
+//   BN = 256: K blocks of 64 in 2 stages of 96 KiB, or of 32 (64-byte rows,
+//             SWIZZLE_64B) in 4 stages of 48 KiB (the same 192 KiB, three
+//             stages in flight while one is consumed); two 256-column
 //             accumulators, 384 threads (warps 2-3 idle, warps 4-7 / 8-11
 //             drain and store columns 0-127 / 128-255).  With more than one
 //             warp per scheduler beside the epilogue the block is capped at
@@ -196,11 +196,12 @@ constexpr int V2_BN = 128;  // tile width of the einsum launches
 //             setmaxnreg: 56 for warps 0-3, 224 for the epilogue (3 x 168 =
 //             56 + 2 x 224 per scheduler).
 // Every epilogue thread holds 128 columns of one row.
-template <int BN>
+template <int BN, int BK_>
 struct TcShape {
-  static constexpr int BK = BN == 256 ? 32 : 64;   // K per stage (16-bit elements)
+  static_assert((BN == 128 && BK_ == 64) || (BN == 256 && (BK_ == 64 || BK_ == 32)), "shape");
+  static constexpr int BK = BK_;                   // K per stage (16-bit elements)
   static constexpr int SWZ = 2 * BK;               // row bytes = swizzle span
-  static constexpr int STAGES = BN == 256 ? 4 : 3;
+  static constexpr int STAGES = BN == 128 ? 3 : (BK == 64 ? 2 : 4);
   static constexpr int NBUF = 512 / BN;
   static constexpr int EPI0 = BN == 256 ? 4 : 2;   // first epilogue warp
   static constexpr int NEPI = BN / 32;              // epilogue warps
@@ -242,10 +243,10 @@ __device__ __forceinline__ void seg_of(const TcArgs &a, int kb, int &s, int &lkb
 // per-element rounding error, still K-independent).
 // A problem's K range may span several segments with different operands
 // (up to 4), each optionally negated through the instruction descriptor.
-template <int BN>
-__global__ void __launch_bounds__(TcShape<BN>::THREADS, 1)
+template <int BN, int BK>
+__global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
     tc_gemm_kernel(const __grid_constant__ TcMaps maps, TcOut out, TcArgs a) {
-  using SH = TcShape<BN>;
+  using SH = TcShape<BN, BK>;
   constexpr int STAGES = SH::STAGES, NBUF = SH::NBUF, HC = 128;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -312,6 +313,18 @@ __global__ void __launch_bounds__(TcShape<BN>::THREADS, 1)
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
+  // The CTA's it-th unit: round it of a round-robin over the grid whose odd
+  // rounds swap neighbouring CTAs, so that with an even grid and two column
+  // tiles per problem (a full one and a narrower remainder) every CTA gets
+  // both kinds in turn instead of always the same one.
+  auto unit_at = [&](int it) -> int {
+    int b = (int)blockIdx.x;
+    if (it & 1) {
+      const int p = b ^ 1;
+      if (p < (int)gridDim.x) b = p;
+    }
+    return it * (int)gridDim.x + b;
+  };
   // unit -> (tile m, tile n, problem y, z, g, K-block range)
   auto unit_coords = [&](int u, int &tm, int &tn, int &py, int &pz, int &pg, int &kb0, int &kb1) {
     const int tile = u % tiles;
@@ -338,7 +351,9 @@ __global__ void __launch_bounds__(TcShape<BN>::THREADS, 1)
       int last[STAGES];
       for (int s = 0; s < STAGES; s++) last[s] = -1;
       bool ok = true;
-      for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
+      for (int it = 0; it * (int)gridDim.x < units && ok; it++) {
+        const int u = unit_at(it);
+        if (u >= units) continue;
         int tm, tn, py, pz, pg, kb0, kb1;
         unit_coords(u, tm, tn, py, pz, pg, kb0, kb1);
         for (int kb = kb0; kb < kb1; kb++, g++) {
@@ -370,7 +385,9 @@ __global__ void __launch_bounds__(TcShape<BN>::THREADS, 1)
     if (lane == 0) {
       int g = 0, c = 0;
       bool ok = true;
-      for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
+      for (int it = 0; it * (int)gridDim.x < units && ok; it++) {
+        const int u = unit_at(it);
+        if (u >= units) continue;
         int tm, tn, py, pz, pg, kb0, kb1;
         unit_coords(u, tm, tn, py, pz, pg, kb0, kb1);
         // MMA width: the tile's valid columns rounded up to 16 (M = 128 takes any
@@ -429,7 +446,9 @@ __global__ void __launch_bounds__(TcShape<BN>::THREADS, 1)
     int64_t *colH = colOff + HC * h;
     int c = 0;
     bool ok = true;
-    for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
+    for (int it = 0; it * (int)gridDim.x < units && ok; it++) {
+      const int u = unit_at(it);
+      if (u >= units) continue;
       int tm, tn, py, pz, pg, kb0, kb1;
       unit_coords(u, tm, tn, py, pz, pg, kb0, kb1);
       const int m = tm * TC_BM + row;
@@ -780,26 +799,41 @@ CUtensorMap TcEngine::map_of(const Packed &p, int box_rows, int bk) {
   return make_map(p.p(), p.rows_pad, p.Kpad, box_rows, bk, p.fmt);
 }
 
-int TcEngine::k_block(int bn) { return bn == 256 ? TcShape<256>::BK : TcShape<128>::BK; }
+// K block of the 256-wide kernel: 64 (2 stages), or 32 (4 stages) with
+// SCESS_TC_BK256=32.
+int TcEngine::k_block(int bn) {
+  static const int bk256 = [] {
+    const char *e = std::getenv("SCESS_TC_BK256");
+    return (e && std::atoi(e) == 32) ? 32 : 64;
+  }();
+  return bn == 256 ? bk256 : 64;
+}
 
 void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &out, int nseg,
                             int splits, float *partial, unsigned *err, cudaStream_t stream) {
   static std::once_flag once;
   static bool wide_ok = false;
   std::call_once(once, [] {
-    cudaFuncSetAttribute(tc_gemm_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)TcShape<128>::SMEM_BYTES);
-    cudaFuncSetAttribute(tc_gemm_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)TcShape<256>::SMEM_BYTES);
-    // The 256-wide kernel's setmaxnreg split assumes it is launched with exactly
-    // kLaunchRegs256 registers a thread (3 x 168 = 56 + 2 x 224 per scheduler).
-    cudaFuncAttributes fa;
-    wide_ok = cudaFuncGetAttributes(&fa, tc_gemm_kernel<256>) == cudaSuccess &&
-              fa.numRegs == kLaunchRegs256;
+    cudaFuncSetAttribute(tc_gemm_kernel<128, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)TcShape<128, 64>::SMEM_BYTES);
+    cudaFuncSetAttribute(tc_gemm_kernel<256, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)TcShape<256, 64>::SMEM_BYTES);
+    cudaFuncSetAttribute(tc_gemm_kernel<256, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)TcShape<256, 32>::SMEM_BYTES);
+    // The 256-wide kernels' setmaxnreg split assumes they are launched with
+    // exactly kLaunchRegs256 registers a thread (3 x 168 = 56 + 2 x 224 per scheduler).
+    cudaFuncAttributes fa, fb;
+    wide_ok = cudaFuncGetAttributes(&fa, tc_gemm_kernel<256, 64>) == cudaSuccess &&
+              fa.numRegs == kLaunchRegs256 &&
+              cudaFuncGetAttributes(&fb, tc_gemm_kernel<256, 32>) == cudaSuccess &&
+              fb.numRegs == kLaunchRegs256;
     cudaGetLastError();
   });
   const int bn = ps.bn == 256 ? 256 : 128;
   if (bn == 256 && !wide_ok) throw Error(SCESS_ERR_UNSUPPORTED, "tc_gemm: 256-wide kernel unavailable");
+  // the maps' boxes were made for this K block (a mismatch would overrun the stages)
+  const int bk = TcEngine::k_block(bn);
+  if (ps.bk != bk) throw Error(SCESS_ERR_INVALID, "tc_gemm: maps built for another K block");
   if (ps.M <= 0 || ps.N <= 0 || ps.ny <= 0 || ps.nz <= 0 || ps.ng <= 0) return;
   if (ps.ng > 3) throw Error(SCESS_ERR_INVALID, "tc_gemm: groups");
   if (nseg != 1 && nseg != 3) throw Error(SCESS_ERR_INVALID, "tc_gemm: nseg");
@@ -831,7 +865,7 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
     }
     a.seg[s].mapA = g.mapA;
     a.seg[s].mapB = g.mapB;
-    a.seg[s].nkb = (int)(g.Kpad / (bn == 256 ? TcShape<256>::BK : TcShape<128>::BK));
+    a.seg[s].nkb = (int)(g.Kpad / bk);
     a.seg[s].kpad = (int)g.Kpad;
     a.seg[s].negA = g.negate ? 1 : 0;
     for (int q = 0; q < 3; q++) {
@@ -873,9 +907,15 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
   if (units > INT32_MAX) throw Error(SCESS_ERR_INVALID, "tc_gemm: too many work units");
   const unsigned grid = (unsigned)std::min<int64_t>(units, kNumSMs);
   if (bn == 256)
-    tc_gemm_kernel<256><<<grid, TcShape<256>::THREADS, TcShape<256>::SMEM_BYTES, stream>>>(maps, out, a);
+    if (bk == 32)
+      tc_gemm_kernel<256, 32><<<grid, TcShape<256, 32>::THREADS, TcShape<256, 32>::SMEM_BYTES, stream>>>(
+          maps, out, a);
+    else
+      tc_gemm_kernel<256, 64><<<grid, TcShape<256, 64>::THREADS, TcShape<256, 64>::SMEM_BYTES, stream>>>(
+          maps, out, a);
   else
-    tc_gemm_kernel<128><<<grid, TcShape<128>::THREADS, TcShape<128>::SMEM_BYTES, stream>>>(maps, out, a);
+    tc_gemm_kernel<128, 64><<<grid, TcShape<128, 64>::THREADS, TcShape<128, 64>::SMEM_BYTES, stream>>>(
+        maps, out, a);
   SCESS_CHECK_LAUNCH();
   if (splits > 1) {
     const int64_t MN = ps.M * ps.N;

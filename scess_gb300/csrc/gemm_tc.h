@@ -76,8 +76,9 @@ struct TcProblemSet {
   int kbd = 1;
   // tile width: 128, or 256 (B-side maps must then have 256-row boxes; half the
   // shared-memory traffic per FLOP for the A operand).  All maps must have
-  // k_block(bn)-wide boxes: map_of(p, rows, k_block(bn)).
+  // k_block(bn)-wide boxes: map_of(p, rows, k_block(bn)), and bk must say so.
   int bn = 128;
+  int bk = 64;
   // per-group output tables (null: the TcOut tables)
   const int64_t *rowC[3] = {nullptr, nullptr, nullptr};
   const int64_t *colC[3] = {nullptr, nullptr, nullptr};

@@ -754,6 +754,7 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   Packed pP, pQ, pQ2, pR, pR2, pTx;
   int tbn = 256;
   if (const char *env = std::getenv("SCESS_T_BN")) tbn = std::atoi(env) == 128 ? 128 : 256;
+  const int tbk = TcEngine::k_block(tbn);
   CUtensorMap mP{}, mQ{}, mQ2{}, mR{}, mR2{}, mTx{};
   DevTables gdt;  // W_g row / column tables
   DevMem Sf;  // (ia|jb) as FP32 for the energy kernel (padded rows)
@@ -793,7 +794,6 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
     // B side (Q, R rows): tiles of tbn columns; 256 halves the A-operand
     // shared-memory traffic per FLOP (SCESS_T_BN=128 selects the narrow tiles).
     // Boxes as wide as the kernel's K block.
-    const int tbk = TcEngine::k_block(tbn);
     mP = TcEngine::map_of(pP, 128, tbk);
     mQ = TcEngine::map_of(pQ, tbn, tbk);
     mQ2 = TcEngine::map_of(pQ2, tbn, tbk);
@@ -854,6 +854,7 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
           // FP64 (1.8e-7 with a drain per 64 K)
           ps.kbd = 128 / TcEngine::k_block(tbn);
           ps.bn = tbn;
+          ps.bk = tbk;
           ps.cy = nb * nb * o3p;
           ps.cz = nb * o3p;
           const int kRoles[3][3] = {{0, 1, 2}, {1, 0, 2}, {2, 0, 1}};  // (x, y, z) of group g
