@@ -145,19 +145,20 @@ __global__ void to_f32_rows_kernel(const double *__restrict__ x, int64_t rows, i
 }
 
 // Layout of the grouped W buffers and the FP32 copy of S the mixed energy
-// kernel reads: rows of o^2 (i, j) pairs are padded to o2p = o^2 rounded up to
-// a multiple of 4 floats, so that every k row and every o^3 block starts on a
-// 16-byte boundary.  W_g[((y_l nb + z_l) nb + x_l) o3p + i + o j + o2p k] with
-// o3p = o o2p; S as [(a + v b) o2p + i + o j].
+// kernel reads: rows of o^2 values are padded to o2p = o^2 rounded up to a
+// multiple of 4 floats (16-byte row pitch for TMA).  W_g holds the products of
+// group g row-major, [y_l nb + z_l][u + o x_l][s + o t] with pitch o2p; S as
+// [(a + v b) o2p + i + o j].
 __host__ __device__ inline int64_t pad4(int64_t n) { return (n + 3) & ~int64_t(3); }
 
 // Energy of one block triple from the three grouped W buffers of the
-// tensor-core form: W^{abc}_{ijk} = W0[b,c][a] + W1[a,c][b] + W2[a,b][c], each
-// block of o^3 floats in (i, j, k) order (buffer g holds [y_l][z_l][x_l][o^3]
-// for its roles (x, y, z)).  Threads own (i, j) pairs and walk k: one pass of
-// coalesced loads forms Y = W + V in shared memory, W is recovered as Y - V in
-// the energy loop.  Otherwise as triples_energy_kernel (FP32 per element, FP64
-// per thread sum).
+// tensor-core form: W^{abc}_{ijk} = W0[b,c](i + o a_l, j + o k)
+// + W1[a,c](j + o b_l, i + o k) + W2[a,b](k + o c_l, i + o j) (problem, row,
+// column).  Three passes, each reading one buffer's o rows of o^2 contiguous
+// values with threads along the columns, form Y = W + V in shared memory; W is
+// recovered as Y - V in the energy loop, where threads own (i, j) pairs and
+// walk k.  Otherwise as triples_energy_kernel (FP32 per element, FP64 per
+// thread sum).
 __global__ void __launch_bounds__(256) triples_energy3_kernel(
     const float *__restrict__ W, int64_t o, int64_t v, int64_t nb, int64_t A, int64_t Bk,
     int64_t C, const double *__restrict__ eps, const double *__restrict__ t1,
@@ -168,16 +169,16 @@ __global__ void __launch_bounds__(256) triples_energy3_kernel(
   extern __shared__ __align__(16) unsigned char sm_raw[];
   __shared__ double red[32];
   const int oo = (int)o, o2 = oo * oo;
-  const int64_t o2p = pad4(o2), o3p = oo * o2p;
+  const int64_t o2p = pad4(o2);
   // Y(i,j,k) at i + p1 j + p2 k with odd p1, p2 (conflict-free permuted reads)
   const int p1 = oo | 1, p2 = (p1 * oo) | 1;
   float *Y = reinterpret_cast<float *>(sm_raw);
   float *Sbc = Y + p2 * oo, *Sac = Sbc + o2, *Sab = Sac + o2;
   float *ta = Sab + o2, *tb = ta + oo, *tc = tb + oo, *eo = tc + oo;
-  const int64_t nb3o3 = nb * nb * nb * o3p;
-  const float *W0 = W + ((bl * nb + cl) * nb + al) * o3p;
-  const float *W1 = W + nb3o3 + ((al * nb + cl) * nb + bl) * o3p;
-  const float *W2 = W + 2 * nb3o3 + ((al * nb + bl) * nb + cl) * o3p;
+  const int64_t Mg = oo * nb, gsz = nb * nb * Mg * o2p;
+  const float *W0 = W + ((bl * nb + cl) * Mg + oo * al) * o2p;            // row i, column j + o k
+  const float *W1 = W + gsz + ((al * nb + cl) * Mg + oo * bl) * o2p;      // row j, column i + o k
+  const float *W2 = W + 2 * gsz + ((al * nb + bl) * Mg + oo * cl) * o2p;  // row k, column i + o j
   const float *S_bc = S + (b + v * c) * o2p, *S_ac = S + (a + v * c) * o2p, *S_ab = S + (a + v * b) * o2p;
   for (int e = threadIdx.x; e < o2; e += blockDim.x) {
     Sbc[e] = S_bc[e];
@@ -191,17 +192,28 @@ __global__ void __launch_bounds__(256) triples_energy3_kernel(
     eo[i] = (float)eps[i];
   }
   __syncthreads();
-  // Y = W0 + W1 + W2 + V;  V_ijk = t1_ia (jb|kc) + t1_jb (ia|kc) + t1_kc (ia|jb)
-  for (int pr = threadIdx.x; pr < o2; pr += blockDim.x) {
-    const int i = pr % oo, j = pr / oo;
-    const float tai = ta[i], tbj = tb[j], sab = Sab[pr];
+  // Y = W0 + V, then += W1, += W2;  V_ijk = t1_ia (jb|kc) + t1_jb (ia|kc) + t1_kc (ia|jb)
+  for (int n = threadIdx.x; n < o2; n += blockDim.x) {  // n = j + o k, rows i
+    const int j = n % oo, k = n / oo;
+    const float sbc = Sbc[n], tbj = tb[j], tck = tc[k];
+    float *y = Y + p1 * j + p2 * k;
+#pragma unroll 8
+    for (int i = 0; i < oo; i++)
+      y[i] = W0[(int64_t)i * o2p + n] + ta[i] * sbc + tbj * Sac[i + oo * k] + tck * Sab[i + oo * j];
+  }
+  __syncthreads();
+  for (int n = threadIdx.x; n < o2; n += blockDim.x) {  // n = i + o k, rows j
+    const int i = n % oo, k = n / oo;
+    float *y = Y + i + p2 * k;
+#pragma unroll 8
+    for (int j = 0; j < oo; j++) y[p1 * j] += W1[(int64_t)j * o2p + n];
+  }
+  __syncthreads();
+  for (int n = threadIdx.x; n < o2; n += blockDim.x) {  // n = i + o j, rows k
+    const int i = n % oo, j = n / oo;
     float *y = Y + i + p1 * j;
 #pragma unroll 8
-    for (int k = 0; k < oo; k++) {
-      const int64_t e = pr + o2p * k;
-      y[p2 * k] = (W0[e] + W1[e]) + W2[e] + tai * Sbc[j + oo * k] + tbj * Sac[i + oo * k] +
-                  tc[k] * sab;
-    }
+    for (int k = 0; k < oo; k++) y[p2 * k] += W2[(int64_t)k * o2p + n];
   }
   __syncthreads();
   const float evirt = (float)(eps[o + a] + eps[o + b] + eps[o + c]);
@@ -706,7 +718,6 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   const int nb = mixed ? choose_nb_grouped(o, v) : choose_nb(o, v, 8, size_t(128) << 20);
   const int64_t NB = ceil_div(v, nb), vp = NB * nb;
   const int64_t o2 = o * o, o3 = o2 * o;
-  const int64_t N2 = N * N, N3 = N2 * N;
 
   TriplesSetup T;
   T.o = o;
@@ -756,7 +767,8 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   if (const char *env = std::getenv("SCESS_T_BN")) tbn = std::atoi(env) == 128 ? 128 : 256;
   const int tbk = TcEngine::k_block(tbn);
   CUtensorMap mP{}, mQ{}, mQ2{}, mR{}, mR2{}, mTx{};
-  DevTables gdt;  // W_g row / column tables
+  DevTables gdt;          // W_g row / column tables (128-wide kernel)
+  CUtensorMap wmaps[3]{};  // W_g as TMA-store maps (256-wide kernel)
   DevMem Sf;  // (ia|jb) as FP32 for the energy kernel (padded rows)
   const int64_t Mg = o * nb, Ng = o2;
   const int64_t Mpq = o * nb * nb, Npq = o2 * nb, Mr = o2 * nb, Nr = o * nb * nb;  // FP64 GEMMs
@@ -800,13 +812,13 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
     mR = TcEngine::map_of(pR, tbn, tbk);
     mR2 = TcEngine::map_of(pR2, tbn, tbk);
     mTx = TcEngine::map_of(pTx, 128, tbk);
-    // W_g[(y_l nb + z_l) nb + x_l][i + o j + o2p k]: every group stores its
-    // (u, s, t) in the (i, j, k) order of the triple, so that the energy kernel
-    // reads the three buffers alike.  g = 0: (u,s,t) = (i,j,k); g = 1: (j,i,k);
-    // g = 2: (k,i,j).  Rows (u, x_l), columns (s, t).
-    gdt.build({table({{o, 1}, {nb, o3p}}), table({{o, o}, {o, o2p}}),
-               table({{o, o}, {nb, o3p}}), table({{o, 1}, {o, o2p}}),
-               table({{o, o2p}, {nb, o3p}}), table({{o, 1}, {o, o}})});
+    // W_g[y_l nb + z_l][u + o x_l][s + o t] (pitch o2p): problem (y_l, z_l)
+    // of group g row-major, rows (u, x_l), columns (s, t).  The 256-wide
+    // kernel writes it with TMA tile stores; the 128-wide one through these
+    // tables (rows m -> m o2p, columns n -> n), column-wise.
+    gdt.build({table({{Mg, o2p}}), table({{Ng, 1}})});
+    for (int g = 0; g < 3; g++)
+      wmaps[g] = TcEngine::out_map_f32(W.as<float>() + g * nb * nb * Mg * o2p, Ng, o2p, Mg, nb * nb);
     Sf.alloc((size_t)o2p * v * v * sizeof(float));
     to_f32_rows_kernel<<<(unsigned)std::min<int64_t>(ceil_div(o2p * v * v, 256), 16 * kNumSMs), 256, 0, s>>>(
         T.S.p(), v * v, o2, o2p, Sf.as<float>());
@@ -855,8 +867,8 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
           ps.kbd = 128 / TcEngine::k_block(tbn);
           ps.bn = tbn;
           ps.bk = tbk;
-          ps.cy = nb * nb * o3p;
-          ps.cz = nb * o3p;
+          ps.cy = nb * Mg * o2p;
+          ps.cz = Mg * o2p;
           const int kRoles[3][3] = {{0, 1, 2}, {1, 0, 2}, {2, 0, 1}};  // (x, y, z) of group g
           const int64_t rp = o * nb * nb, rq = o2 * nb;                 // block strides of the packs
           TcSegment &s0 = ps.seg[0], &s1 = ps.seg[1], &s2 = ps.seg[2], &s3 = ps.seg[3];
@@ -866,7 +878,7 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
           s3.mapA = 5; s3.mapB = 4; s3.Kpad = pTx.Kpad;  // -t2(m,u,y,x) R(t,s,m,z)
           for (int g = 0; g < 3; g++) {
             const int64_t X = U[kRoles[g][0]], Yb = U[kRoles[g][1]], Z = U[kRoles[g][2]];
-            ps.cg[g] = g * nb * nb * nb * o3p;
+            ps.cg[g] = g * nb * nb * Mg * o2p;
             s0.rowA0[g] = rp * (Yb + NB * X); s0.rowAy[g] = o * nb;
             s0.rowB0[g] = rq * Z;             s0.rowBz[g] = o2;
             s1.rowA0[g] = rp * (Z + NB * X);  s1.rowAz[g] = o * nb;
@@ -881,10 +893,10 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
           out.fp32 = 1;
           out.rowC = gdt.ptr[0];
           out.colC = gdt.ptr[1];
+          ps.tma_store = tbn == 256;
           for (int g = 0; g < 3; g++) {
-            ps.rowC[g] = gdt.ptr[2 * g];
-            ps.colC[g] = gdt.ptr[2 * g + 1];
-            ps.store_by_column[g] = g > 0;  // i is a column index of groups 1 and 2
+            ps.store_by_column[g] = true;  // (s, t) columns are the unit-stride index
+            ps.out_maps[g] = wmaps[g];
           }
           out.alpha = 1.0;
           out.beta = 0.0;
