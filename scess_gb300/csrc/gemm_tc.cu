@@ -44,23 +44,6 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *tm, in
       : "memory");
 }
 
-// Tile store shared -> global through a 3D map (x = column, y = row, z =
-// problem); elements outside the map's extent are not written.
-__device__ __forceinline__ void tma_store_3d(const CUtensorMap *tm, const void *src, int x, int y,
-                                             int z) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(
-          (uint64_t)tm),
-      "r"(smem_u32(src)), "r"(x), "r"(y), "r"(z)
-      : "memory");
-}
-__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-// Wait until at most 0 committed bulk groups still read shared memory / are incomplete.
-__device__ __forceinline__ void bulk_wait_read0() {
-  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-}
-__device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
-
 __device__ __forceinline__ void tc_fence_before() {
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
 }
@@ -145,7 +128,6 @@ struct TcSegArgs {
 
 struct TcMaps {
   CUtensorMap m[6];
-  CUtensorMap out[3];  // FP32 output of group g as [problem][M][N] (TMA-store mode)
 };
 
 struct TcArgs {
@@ -164,7 +146,6 @@ struct TcArgs {
   int64_t cg[3];
   const int64_t *rowCg[3], *colCg[3];  // per-group output tables (null: TcOut's)
   int stcol[3];                        // group stores along columns (FP32, beta = 0)
-  int tma_store;                       // write tiles through maps.out (BN = 256, FP32, beta = 0)
   float *partial;    // split-K partials (nullptr: direct epilogue)
   int64_t part_stride;
   unsigned *err;
@@ -268,14 +249,8 @@ __global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
   __shared__ int64_t colOff[BN];
   __shared__ int64_t rowOffS[BN / 128][TC_BM];        // row offsets of a column-stored unit
   // chunk of such a unit; row pitch 129 (CH = 32) or 130 (CH = 16, two rows a
-  // warp step) keeps the column-wise reads free of bank conflicts.  In
-  // TMA-store mode the same memory holds, per column half, two 128 x 8 FP32
-  // boxes (32-byte rows, 32-byte swizzle) that alternate as store sources.
-  constexpr int kStagePitch = TC_BM + (SH::CH == 16 ? 2 : 1);
-  constexpr int kStageFloats = (BN / 128) * SH::CH * kStagePitch;
-  static_assert(kStageFloats >= (BN / 128) * 2 * TC_BM * 8, "TMA store boxes fit the staging memory");
-  __shared__ __align__(1024) float stage_raw[kStageFloats];
-  auto stage = reinterpret_cast<float(*)[SH::CH][kStagePitch]>(stage_raw);
+  // warp step) keeps the column-wise reads free of bank conflicts
+  __shared__ float stage[BN / 128][SH::CH][TC_BM + (SH::CH == 16 ? 2 : 1)];
   // Output scaling, once per CTA: alpha / (sA sB) with power-of-two pack
   // scales sA, sB.  FP32 outputs multiply by it in FP32; FP64 outputs multiply
   // by the user's alpha in FP32 and apply 2^-log2(sA sB) to the exponent field
@@ -456,7 +431,6 @@ __global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
     const int bar = 1 + h;                                // named barrier of the half
     int64_t *colH = colOff + HC * h;
     int c = 0;
-    int tchunk = 0;  // TMA-store boxes issued by this half (alternating sources)
     bool ok = true;
     for (int it = 0; it * (int)gridDim.x < units && ok; it++) {
       const int u = unit_at(it);
@@ -466,17 +440,14 @@ __global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
       const int m = tm * TC_BM + row;
       const int n0 = tn * BN + HC * h;
       asm volatile("bar.sync %0, 128;" ::"r"(bar) : "memory");  // previous unit's colOff reads done
-      int64_t rowOff = 0;
-      if constexpr (BN != 256) {  // (the 256-wide kernel stores through TMA maps)
-        if (!a.partial) {
-          const int nn = n0 + et;
-          const int64_t *colT = a.colCg[pg] ? a.colCg[pg] : out.colC;
-          colH[et] = nn < a.N ? out.baseC + py * a.cy + pz * a.cz + a.cg[pg] + colT[nn] : -1;
-        }
-        // issued now, used after the K loop: their latency hides behind the MMAs
-        const int64_t *rowT = a.rowCg[pg] ? a.rowCg[pg] : out.rowC;
-        rowOff = (!a.partial && m < a.M) ? rowT[m] : 0;
+      if (!a.partial) {
+        const int nn = n0 + et;
+        const int64_t *colT = a.colCg[pg] ? a.colCg[pg] : out.colC;
+        colH[et] = nn < a.N ? out.baseC + py * a.cy + pz * a.cz + a.cg[pg] + colT[nn] : -1;
       }
+      // issued now, used after the K loop: their latency hides behind the MMAs
+      const int64_t *rowT = a.rowCg[pg] ? a.rowCg[pg] : out.rowC;
+      const int64_t rowOff = (!a.partial && m < a.M) ? rowT[m] : 0;
       const unsigned errv = *(volatile unsigned *)a.err;
       float acc[HC];
 #pragma unroll
@@ -503,37 +474,6 @@ __global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
       }
       asm volatile("bar.sync %0, 128;" ::"r"(bar) : "memory");  // colOff of this unit written
       if (!ok || errv) break;
-      if constexpr (BN == 256) {
-        {
-          // The half's 128 x 128 block in 8-column boxes: every thread writes its
-          // row's 8 values (two 16-byte chunks, swizzled by row bits 2) into one of
-          // two boxes, and one thread stores the box.  Before the barrier that
-          // releases the next box's writes it waits until the store issued two
-          // boxes earlier (same memory) has read its source.
-          const float fa = s_falpha;
-          const int zp = py * a.nz + pz;
-          const bool lead = et == 0;
-          const uint32_t sw = (uint32_t)((row >> 2) & 1);
-#pragma unroll
-          for (int j0 = 0; j0 < HC; j0 += 8) {
-            const int x = tn * BN + HC * h + j0;
-            if (x >= a.N) break;  // the same for the whole half
-            float *box = stage_raw + (h * 2 + (tchunk & 1)) * (TC_BM * 8);
-            float4 *rp = reinterpret_cast<float4 *>(box + row * 8);
-            rp[0 ^ sw] = make_float4(fa * acc[j0], fa * acc[j0 + 1], fa * acc[j0 + 2], fa * acc[j0 + 3]);
-            rp[1 ^ sw] = make_float4(fa * acc[j0 + 4], fa * acc[j0 + 5], fa * acc[j0 + 6], fa * acc[j0 + 7]);
-            fence_proxy_async_smem();
-            if (lead) bulk_wait_read0();
-            asm volatile("bar.sync %0, 128;" ::"r"(bar) : "memory");
-            if (lead) {
-              tma_store_3d(&maps.out[pg], box, x, tm * TC_BM, zp);
-              bulk_commit();
-            }
-            tchunk++;
-          }
-          continue;
-        }
-      } else {
       if (a.stcol[pg] && out.fp32 && out.beta == 0.0 && !a.partial) {
         // Tile staged through shared memory CH columns at a time, then each warp
         // stores its 32 rows with the lanes along the columns: for outputs whose
@@ -659,12 +599,7 @@ __global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
           }
         }
       }
-      }  // BN != 256
     }
-  }
-  if constexpr (BN == 256) {
-    // the TMA stores of this CTA have completed before it exits
-    if (warp >= SH::EPI0 && ((threadIdx.x - 32 * SH::EPI0) & 127) == 0) bulk_wait0();
   }
   tc_fence_before();
   __syncthreads();
@@ -852,24 +787,6 @@ CUtensorMap TcEngine::map_of(const Packed &p, int box_rows, int bk) {
 
 // K block of the 256-wide kernel: 64 (2 stages), or 32 (4 stages) with
 // SCESS_TC_BK256=32.
-CUtensorMap TcEngine::out_map_f32(float *base, int64_t cols, int64_t ld, int64_t rows,
-                                  int64_t nprob) {
-  if (ld % 4 != 0 || cols > ld || cols <= 0 || rows <= 0 || nprob <= 0)
-    throw Error(SCESS_ERR_INVALID, "tc_gemm: output map shape");
-  CUtensorMap m;
-  std::memset(&m, 0, sizeof(m));
-  cuuint64_t dims[3] = {(cuuint64_t)cols, (cuuint64_t)rows, (cuuint64_t)nprob};
-  cuuint64_t strides[2] = {(cuuint64_t)(ld * 4), (cuuint64_t)(ld * rows * 4)};
-  cuuint32_t box[3] = {8, (cuuint32_t)TC_BM, 1};  // the epilogue's 128 x 8 boxes
-  cuuint32_t estr[3] = {1, 1, 1};
-  CUresult r = get_encode()(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, estr,
-                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B,
-                            CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS)
-    throw Error(SCESS_ERR_CUDA, "cuTensorMapEncodeTiled (output) failed (" + std::to_string((int)r) + ")");
-  return m;
-}
-
 int TcEngine::k_block(int bn) {
   static const int bk256 = [] {
     const char *e = std::getenv("SCESS_TC_BK256");
@@ -967,20 +884,11 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
     a.stcol[q] = ps.store_by_column[q] ? 1 : 0;
   }
   a.partial = splits > 1 ? partial : nullptr;
-  // the 256-wide kernel writes only through TMA-store maps
-  if (ps.tma_store != (bn == 256))
-    throw Error(SCESS_ERR_INVALID, "tc_gemm: TMA-store mode is the 256-wide kernel's (and only its)");
-  if (ps.tma_store) {
-    if (!out.fp32 || out.beta != 0.0 || splits != 1)
-      throw Error(SCESS_ERR_INVALID, "tc_gemm: TMA-store mode needs FP32, beta 0, no split");
-    a.tma_store = 1;
-  }
   a.part_stride = ps.M * ps.N;
   a.err = err;
   if (splits > 1 && !partial) throw Error(SCESS_ERR_INVALID, "tc_gemm: split-K needs partials");
   TcMaps maps;
   for (int i = 0; i < 6; i++) maps.m[i] = ps.maps[std::min(i, ps.nmaps - 1)];
-  for (int g = 0; g < 3; g++) maps.out[g] = ps.tma_store ? ps.out_maps[std::min(g, ps.ng - 1)] : ps.maps[0];
   const int64_t units = (int64_t)a.tiles_m * a.tiles_n * ps.ny * ps.nz * ps.ng * splits;
   if (units > INT32_MAX) throw Error(SCESS_ERR_INVALID, "tc_gemm: too many work units");
   const unsigned grid = (unsigned)std::min<int64_t>(units, kNumSMs);

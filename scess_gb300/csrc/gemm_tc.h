@@ -85,12 +85,6 @@ struct TcProblemSet {
   // group g writes along columns (lanes over columns, through shared memory):
   // for FP32 outputs with beta = 0 whose unit-stride index is a column index
   bool store_by_column[3] = {false, false, false};
-  // TMA-store mode (bn = 256, FP32 output, beta = 0): problem (y, z, g) writes
-  // its M x N product row-major into out_maps[g], a 3D map (column, row,
-  // problem y nz + z) from out_map_f32; the output tables, cy, cz and cg are
-  // not used.
-  bool tma_store = false;
-  CUtensorMap out_maps[3];
 };
 
 class TcEngine {
@@ -128,10 +122,6 @@ class TcEngine {
   static CUtensorMap map_of(const Packed &p, int box_rows, int bk = 64);
   // K block (16-bit values per stage row) of the kernel with tile width bn.
   static int k_block(int bn);
-  // TMA-store map of an FP32 array [nprob][rows][ld] (columns < cols written;
-  // ld a multiple of 4).
-  static CUtensorMap out_map_f32(float *base, int64_t cols, int64_t ld, int64_t rows,
-                                 int64_t nprob);
   // TcOut scale pointers of a product of two packed operands.
   static void set_scales(TcOut &out, const Packed &A, const Packed &B) {
     out.scaleA = A.scale();

@@ -144,18 +144,19 @@ __global__ void to_f32_rows_kernel(const double *__restrict__ x, int64_t rows, i
   }
 }
 
-// Layout of the grouped W buffers and the FP32 copy of S the mixed energy
-// kernel reads: rows of o^2 values are padded to o2p = o^2 rounded up to a
-// multiple of 4 floats (16-byte row pitch for TMA).  W_g holds the products of
-// group g row-major, [y_l nb + z_l][u + o x_l][s + o t] with pitch o2p; S as
+// The FP32 copy of S the mixed energy kernel reads has its rows of o^2 (i, j)
+// pairs padded to o2p = o^2 rounded up to a multiple of 4 floats:
 // [(a + v b) o2p + i + o j].
 __host__ __device__ inline int64_t pad4(int64_t n) { return (n + 3) & ~int64_t(3); }
 
 // Energy of one block triple from the three grouped W buffers of the
-// tensor-core form: W^{abc}_{ijk} = W0[b,c](i + o a_l, j + o k)
-// + W1[a,c](j + o b_l, i + o k) + W2[a,b](k + o c_l, i + o j) (problem, row,
-// column).  Three passes, each reading one buffer's o rows of o^2 contiguous
-// values with threads along the columns, form Y = W + V in shared memory; W is
+// tensor-core form, each [problem][column][row] with M = o nb rows:
+//   W^{abc}_{ijk} = W0[b,c](row i + o a_l, column j + o k)
+//                 + W1[a,c](row j + o b_l, column i + o k)
+//                 + W2[a,b](row k + o c_l, column i + o j).
+// A triple's part of a buffer is o^2 runs of o consecutive rows.  Three
+// passes (one per buffer; 4-row vector loads when o % 4 == 0, the whole part
+// of a buffer in flight per CTA) form Y = W + V in shared memory; W is
 // recovered as Y - V in the energy loop, where threads own (i, j) pairs and
 // walk k.  Otherwise as triples_energy_kernel (FP32 per element, FP64 per
 // thread sum).
@@ -175,10 +176,10 @@ __global__ void __launch_bounds__(256) triples_energy3_kernel(
   float *Y = reinterpret_cast<float *>(sm_raw);
   float *Sbc = Y + p2 * oo, *Sac = Sbc + o2, *Sab = Sac + o2;
   float *ta = Sab + o2, *tb = ta + oo, *tc = tb + oo, *eo = tc + oo;
-  const int64_t Mg = oo * nb, gsz = nb * nb * Mg * o2p;
-  const float *W0 = W + ((bl * nb + cl) * Mg + oo * al) * o2p;            // row i, column j + o k
-  const float *W1 = W + gsz + ((al * nb + cl) * Mg + oo * bl) * o2p;      // row j, column i + o k
-  const float *W2 = W + 2 * gsz + ((al * nb + bl) * Mg + oo * cl) * o2p;  // row k, column i + o j
+  const int64_t Mg = oo * nb, pstride = (int64_t)o2 * Mg, gsz = nb * nb * pstride;
+  const float *W0 = W + (bl * nb + cl) * pstride + oo * al;            // [j + o k][i]
+  const float *W1 = W + gsz + (al * nb + cl) * pstride + oo * bl;      // [i + o k][j]
+  const float *W2 = W + 2 * gsz + (al * nb + bl) * pstride + oo * cl;  // [i + o j][k]
   const float *S_bc = S + (b + v * c) * o2p, *S_ac = S + (a + v * c) * o2p, *S_ab = S + (a + v * b) * o2p;
   for (int e = threadIdx.x; e < o2; e += blockDim.x) {
     Sbc[e] = S_bc[e];
@@ -192,28 +193,72 @@ __global__ void __launch_bounds__(256) triples_energy3_kernel(
     eo[i] = (float)eps[i];
   }
   __syncthreads();
-  // Y = W0 + V, then += W1, += W2;  V_ijk = t1_ia (jb|kc) + t1_jb (ia|kc) + t1_kc (ia|jb)
-  for (int n = threadIdx.x; n < o2; n += blockDim.x) {  // n = j + o k, rows i
-    const int j = n % oo, k = n / oo;
-    const float sbc = Sbc[n], tbj = tb[j], tck = tc[k];
-    float *y = Y + p1 * j + p2 * k;
-#pragma unroll 8
-    for (int i = 0; i < oo; i++)
-      y[i] = W0[(int64_t)i * o2p + n] + ta[i] * sbc + tbj * Sac[i + oo * k] + tck * Sab[i + oo * j];
+  // Y = W0 + V, then += W1, += W2;  V_ijk = t1_ia (jb|kc) + t1_jb (ia|kc) + t1_kc (ia|jb).
+  // Pass g visits (column n, row r) of its buffer; f enumerates them with the
+  // row fastest, R rows (1 or 4) per step.
+  const bool vec = (oo & 3) == 0 && (Mg & 3) == 0;
+  const int R = vec ? 4 : 1, rq = oo / R, nf = rq * o2;
+  auto load = [&](const float *base, int f, float *w) {
+    const int n = f / rq, r0 = (f - n * rq) * R;
+    const float *p = base + (int64_t)n * Mg + r0;
+    if (vec) {
+      const float4 x = __ldg(reinterpret_cast<const float4 *>(p));
+      w[0] = x.x; w[1] = x.y; w[2] = x.z; w[3] = x.w;
+    } else {
+      w[0] = __ldg(p);
+    }
+  };
+  constexpr int kB = 4;  // steps whose loads are issued together
+  for (int f0 = threadIdx.x; f0 < nf; f0 += kB * blockDim.x) {  // rows i, columns j + o k
+    float w[kB][4];
+#pragma unroll
+    for (int u = 0; u < kB; u++) {
+      const int f = f0 + u * blockDim.x;
+      if (f < nf) load(W0, f, w[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < kB; u++) {
+      const int f = f0 + u * blockDim.x;
+      if (f >= nf) break;
+      const int n = f / rq, i0 = (f - n * rq) * R, j = n % oo, k = n / oo;
+      const float sbc = Sbc[n], tbj = tb[j], tck = tc[k];
+      for (int e = 0; e < R; e++) {
+        const int i = i0 + e;
+        Y[i + p1 * j + p2 * k] = w[u][e] + ta[i] * sbc + tbj * Sac[i + oo * k] + tck * Sab[i + oo * j];
+      }
+    }
   }
   __syncthreads();
-  for (int n = threadIdx.x; n < o2; n += blockDim.x) {  // n = i + o k, rows j
-    const int i = n % oo, k = n / oo;
-    float *y = Y + i + p2 * k;
-#pragma unroll 8
-    for (int j = 0; j < oo; j++) y[p1 * j] += W1[(int64_t)j * o2p + n];
+  for (int f0 = threadIdx.x; f0 < nf; f0 += kB * blockDim.x) {  // rows j, columns i + o k
+    float w[kB][4];
+#pragma unroll
+    for (int u = 0; u < kB; u++) {
+      const int f = f0 + u * blockDim.x;
+      if (f < nf) load(W1, f, w[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < kB; u++) {
+      const int f = f0 + u * blockDim.x;
+      if (f >= nf) break;
+      const int n = f / rq, j0 = (f - n * rq) * R, i = n % oo, k = n / oo;
+      for (int e = 0; e < R; e++) Y[i + p1 * (j0 + e) + p2 * k] += w[u][e];
+    }
   }
   __syncthreads();
-  for (int n = threadIdx.x; n < o2; n += blockDim.x) {  // n = i + o j, rows k
-    const int i = n % oo, j = n / oo;
-    float *y = Y + i + p1 * j;
-#pragma unroll 8
-    for (int k = 0; k < oo; k++) y[p2 * k] += W2[(int64_t)k * o2p + n];
+  for (int f0 = threadIdx.x; f0 < nf; f0 += kB * blockDim.x) {  // rows k, columns i + o j
+    float w[kB][4];
+#pragma unroll
+    for (int u = 0; u < kB; u++) {
+      const int f = f0 + u * blockDim.x;
+      if (f < nf) load(W2, f, w[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < kB; u++) {
+      const int f = f0 + u * blockDim.x;
+      if (f >= nf) break;
+      const int n = f / rq, k0 = (f - n * rq) * R, i = n % oo, j = n / oo;
+      for (int e = 0; e < R; e++) Y[i + p1 * j + p2 * (k0 + e)] += w[u][e];
+    }
   }
   __syncthreads();
   const float evirt = (float)(eps[o + a] + eps[o + b] + eps[o + c]);
@@ -735,9 +780,9 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   DTensor energies({std::max<int64_t>(ntrip, 1)});
   SCESS_CUDA(cudaMemsetAsync(energies.p(), 0, energies.size() * sizeof(double), s));
   // FP64: one W; MIXED: the three grouped buffers W0 | W1 | W2
-  // MIXED rows of (i, j) pairs padded to o2p floats (see pad4)
-  const int64_t o2p = pad4(o2), o3p = o * o2p;
-  const size_t wbytes = (size_t)nb * nb * nb * (mixed ? 3 * 4 * o3p : 8 * o3);
+  // MIXED: S rows of (i, j) pairs padded to o2p floats (see pad4)
+  const int64_t o2p = pad4(o2);
+  const size_t wbytes = (size_t)nb * nb * nb * o3 * (mixed ? 3 * 4 : 8);
   DevMem W(wbytes);
   const int64_t p1 = o | 1, p2 = (p1 * o) | 1;
   const size_t ysmem = (size_t)(p2 * o + 3 * o2 + 4 * o) * (mixed ? 4 : 8);
@@ -767,8 +812,7 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   if (const char *env = std::getenv("SCESS_T_BN")) tbn = std::atoi(env) == 128 ? 128 : 256;
   const int tbk = TcEngine::k_block(tbn);
   CUtensorMap mP{}, mQ{}, mQ2{}, mR{}, mR2{}, mTx{};
-  DevTables gdt;          // W_g row / column tables (128-wide kernel)
-  CUtensorMap wmaps[3]{};  // W_g as TMA-store maps (256-wide kernel)
+  DevTables gdt;  // W_g row / column tables
   DevMem Sf;  // (ia|jb) as FP32 for the energy kernel (padded rows)
   const int64_t Mg = o * nb, Ng = o2;
   const int64_t Mpq = o * nb * nb, Npq = o2 * nb, Mr = o2 * nb, Nr = o * nb * nb;  // FP64 GEMMs
@@ -812,13 +856,10 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
     mR = TcEngine::map_of(pR, tbn, tbk);
     mR2 = TcEngine::map_of(pR2, tbn, tbk);
     mTx = TcEngine::map_of(pTx, 128, tbk);
-    // W_g[y_l nb + z_l][u + o x_l][s + o t] (pitch o2p): problem (y_l, z_l)
-    // of group g row-major, rows (u, x_l), columns (s, t).  The 256-wide
-    // kernel writes it with TMA tile stores; the 128-wide one through these
-    // tables (rows m -> m o2p, columns n -> n), column-wise.
-    gdt.build({table({{Mg, o2p}}), table({{Ng, 1}})});
-    for (int g = 0; g < 3; g++)
-      wmaps[g] = TcEngine::out_map_f32(W.as<float>() + g * nb * nb * Mg * o2p, Ng, o2p, Mg, nb * nb);
+    // W_g[y_l nb + z_l][s + o t][u + o x_l]: problem (y_l, z_l) of group g
+    // column-major, rows (u, x_l) the unit-stride index, so that every
+    // group's epilogue writes 32 consecutive rows per warp store.
+    gdt.build({table({{Mg, 1}}), table({{Ng, Mg}})});
     Sf.alloc((size_t)o2p * v * v * sizeof(float));
     to_f32_rows_kernel<<<(unsigned)std::min<int64_t>(ceil_div(o2p * v * v, 256), 16 * kNumSMs), 256, 0, s>>>(
         T.S.p(), v * v, o2, o2p, Sf.as<float>());
@@ -867,8 +908,8 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
           ps.kbd = 128 / TcEngine::k_block(tbn);
           ps.bn = tbn;
           ps.bk = tbk;
-          ps.cy = nb * Mg * o2p;
-          ps.cz = Mg * o2p;
+          ps.cy = nb * Ng * Mg;
+          ps.cz = Ng * Mg;
           const int kRoles[3][3] = {{0, 1, 2}, {1, 0, 2}, {2, 0, 1}};  // (x, y, z) of group g
           const int64_t rp = o * nb * nb, rq = o2 * nb;                 // block strides of the packs
           TcSegment &s0 = ps.seg[0], &s1 = ps.seg[1], &s2 = ps.seg[2], &s3 = ps.seg[3];
@@ -878,7 +919,7 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
           s3.mapA = 5; s3.mapB = 4; s3.Kpad = pTx.Kpad;  // -t2(m,u,y,x) R(t,s,m,z)
           for (int g = 0; g < 3; g++) {
             const int64_t X = U[kRoles[g][0]], Yb = U[kRoles[g][1]], Z = U[kRoles[g][2]];
-            ps.cg[g] = g * nb * nb * Mg * o2p;
+            ps.cg[g] = g * nb * nb * Ng * Mg;
             s0.rowA0[g] = rp * (Yb + NB * X); s0.rowAy[g] = o * nb;
             s0.rowB0[g] = rq * Z;             s0.rowBz[g] = o2;
             s1.rowA0[g] = rp * (Z + NB * X);  s1.rowAz[g] = o * nb;
@@ -893,11 +934,6 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
           out.fp32 = 1;
           out.rowC = gdt.ptr[0];
           out.colC = gdt.ptr[1];
-          ps.tma_store = tbn == 256;
-          for (int g = 0; g < 3; g++) {
-            ps.store_by_column[g] = true;  // (s, t) columns are the unit-stride index
-            ps.out_maps[g] = wmaps[g];
-          }
           out.alpha = 1.0;
           out.beta = 0.0;
           TcEngine::set_scales(out, pP, pQ);

@@ -57,10 +57,10 @@ def test_triples_df_native_multiblock(gctx, monkeypatch, precision, tol):
 
 
 
-@pytest.mark.parametrize('o,v,nb', [(5, 18, 4), (7, 23, 5)])
-def test_triples_mixed_padded_rows(gctx, monkeypatch, o, v, nb):
-    """Odd o: the grouped W buffers and the FP32 S copy carry (i, j) rows padded
-    to a multiple of 4 floats; several block triples with padded virtuals."""
+@pytest.mark.parametrize('o,v,nb', [(5, 18, 4), (7, 23, 5), (8, 30, 5), (12, 26, 9)])
+def test_triples_mixed_block_layouts(gctx, monkeypatch, o, v, nb):
+    """Several block triples with padded virtuals; odd o (scalar reads of the
+    grouped W buffers, padded S rows) and o % 4 == 0 (4-row vector reads)."""
     from scess_gb300.synthetic import convergent_sigma
     monkeypatch.setenv('SCESS_T_NB', str(nb))
     w = make_workload(o, v, seed=6, with_amplitudes=True, sigma=convergent_sigma(o, v))
