@@ -160,7 +160,7 @@ __host__ __device__ inline int64_t pad4(int64_t n) { return (n + 3) & ~int64_t(3
 // recovered as Y - V in the energy loop, where threads own (i, j) pairs and
 // walk k.  Otherwise as triples_energy_kernel (FP32 per element, FP64 per
 // thread sum).
-__global__ void __launch_bounds__(256) triples_energy3_kernel(
+__global__ void __launch_bounds__(256, 4) triples_energy3_kernel(
     const float *__restrict__ W, int64_t o, int64_t v, int64_t nb, int64_t A, int64_t Bk,
     int64_t C, const double *__restrict__ eps, const double *__restrict__ t1,
     const float *__restrict__ S, double *__restrict__ energies) {
@@ -174,8 +174,8 @@ __global__ void __launch_bounds__(256) triples_energy3_kernel(
   // Y(i,j,k) at i + p1 j + p2 k with odd p1, p2 (conflict-free permuted reads)
   const int p1 = oo | 1, p2 = (p1 * oo) | 1;
   float *Y = reinterpret_cast<float *>(sm_raw);
-  float *Sbc = Y + p2 * oo, *Sac = Sbc + o2, *Sab = Sac + o2;
-  float *ta = Sab + o2, *tb = ta + oo, *tc = tb + oo, *eo = tc + oo;
+  float *Sbc = Y + p2 * oo, *Sac = Sbc + o2, *Sab = Sac + o2, *SabT = Sab + o2;
+  float *ta = SabT + o2, *tb = ta + oo, *tc = tb + oo, *eo = tc + oo;
   const int64_t Mg = oo * nb, pstride = (int64_t)o2 * Mg, gsz = nb * nb * pstride;
   const float *W0 = W + (bl * nb + cl) * pstride + oo * al;            // [j + o k][i]
   const float *W1 = W + gsz + (al * nb + cl) * pstride + oo * bl;      // [i + o k][j]
@@ -184,7 +184,9 @@ __global__ void __launch_bounds__(256) triples_energy3_kernel(
   for (int e = threadIdx.x; e < o2; e += blockDim.x) {
     Sbc[e] = S_bc[e];
     Sac[e] = S_ac[e];
-    Sab[e] = S_ab[e];
+    const float x = S_ab[e];
+    Sab[e] = x;
+    SabT[e / oo + oo * (e % oo)] = x;  // (ia|jb) at j + o i
   }
   for (int i = threadIdx.x; i < oo; i += blockDim.x) {
     ta[i] = (float)t1[i + o * a];
@@ -194,72 +196,54 @@ __global__ void __launch_bounds__(256) triples_energy3_kernel(
   }
   __syncthreads();
   // Y = W0 + V, then += W1, += W2;  V_ijk = t1_ia (jb|kc) + t1_jb (ia|kc) + t1_kc (ia|jb).
-  // Pass g visits (column n, row r) of its buffer; f enumerates them with the
-  // row fastest, R rows (1 or 4) per step.
+  // Threads own columns n = c0 + o c1 of a buffer and read its o rows, up to
+  // kRows at a time (4-row vectors when o % 4 == 0).  Pass g puts row r of
+  // column n at Y[ybase + r ystep]: g = 0: (i, j, k) = (r, c0, c1); g = 1:
+  // (c0, r, c1); g = 2: (c0, c1, r).
   const bool vec = (oo & 3) == 0 && (Mg & 3) == 0;
-  const int R = vec ? 4 : 1, rq = oo / R, nf = rq * o2;
-  auto load = [&](const float *base, int f, float *w) {
-    const int n = f / rq, r0 = (f - n * rq) * R;
-    const float *p = base + (int64_t)n * Mg + r0;
-    if (vec) {
-      const float4 x = __ldg(reinterpret_cast<const float4 *>(p));
-      w[0] = x.x; w[1] = x.y; w[2] = x.z; w[3] = x.w;
-    } else {
-      w[0] = __ldg(p);
-    }
-  };
-  constexpr int kB = 4;  // steps whose loads are issued together
-  for (int f0 = threadIdx.x; f0 < nf; f0 += kB * blockDim.x) {  // rows i, columns j + o k
-    float w[kB][4];
+  constexpr int kRows = 24;
+  auto pass = [&](const float *base, int g) {
+    const int ystep = g == 0 ? 1 : (g == 1 ? p1 : p2);
+    for (int n = threadIdx.x; n < o2; n += blockDim.x) {
+      const int c0 = n % oo, c1 = n / oo;
+      const int ybase = g == 0 ? p1 * c0 + p2 * c1 : (g == 1 ? c0 + p2 * c1 : c0 + p1 * c1);
+      const float *col = base + (int64_t)n * Mg;
+      const float sbc = Sbc[n], tbj = tb[c0], tck = tc[c1];  // (g = 0: n = j + o k)
+      for (int r0 = 0; r0 < oo; r0 += kRows) {
+        float w[kRows];
+        if (vec) {
 #pragma unroll
-    for (int u = 0; u < kB; u++) {
-      const int f = f0 + u * blockDim.x;
-      if (f < nf) load(W0, f, w[u]);
-    }
+          for (int q = 0; q < kRows / 4; q++)
+            if (r0 + 4 * q < oo) {
+              const float4 x = __ldg(reinterpret_cast<const float4 *>(col + r0 + 4 * q));
+              w[4 * q] = x.x;
+              w[4 * q + 1] = x.y;
+              w[4 * q + 2] = x.z;
+              w[4 * q + 3] = x.w;
+            }
+        } else {
 #pragma unroll
-    for (int u = 0; u < kB; u++) {
-      const int f = f0 + u * blockDim.x;
-      if (f >= nf) break;
-      const int n = f / rq, i0 = (f - n * rq) * R, j = n % oo, k = n / oo;
-      const float sbc = Sbc[n], tbj = tb[j], tck = tc[k];
-      for (int e = 0; e < R; e++) {
-        const int i = i0 + e;
-        Y[i + p1 * j + p2 * k] = w[u][e] + ta[i] * sbc + tbj * Sac[i + oo * k] + tck * Sab[i + oo * j];
+          for (int q = 0; q < kRows; q++)
+            if (r0 + q < oo) w[q] = __ldg(col + r0 + q);
+        }
+#pragma unroll
+        for (int q = 0; q < kRows; q++) {
+          const int r = r0 + q;
+          if (r >= oo) break;
+          float *y = Y + ybase + r * ystep;
+          if (g == 0)
+            *y = w[q] + ta[r] * sbc + tbj * Sac[r + oo * c1] + tck * SabT[c0 + oo * r];
+          else
+            *y += w[q];
+        }
       }
     }
-  }
+  };
+  pass(W0, 0);
   __syncthreads();
-  for (int f0 = threadIdx.x; f0 < nf; f0 += kB * blockDim.x) {  // rows j, columns i + o k
-    float w[kB][4];
-#pragma unroll
-    for (int u = 0; u < kB; u++) {
-      const int f = f0 + u * blockDim.x;
-      if (f < nf) load(W1, f, w[u]);
-    }
-#pragma unroll
-    for (int u = 0; u < kB; u++) {
-      const int f = f0 + u * blockDim.x;
-      if (f >= nf) break;
-      const int n = f / rq, j0 = (f - n * rq) * R, i = n % oo, k = n / oo;
-      for (int e = 0; e < R; e++) Y[i + p1 * (j0 + e) + p2 * k] += w[u][e];
-    }
-  }
+  pass(W1, 1);
   __syncthreads();
-  for (int f0 = threadIdx.x; f0 < nf; f0 += kB * blockDim.x) {  // rows k, columns i + o j
-    float w[kB][4];
-#pragma unroll
-    for (int u = 0; u < kB; u++) {
-      const int f = f0 + u * blockDim.x;
-      if (f < nf) load(W2, f, w[u]);
-    }
-#pragma unroll
-    for (int u = 0; u < kB; u++) {
-      const int f = f0 + u * blockDim.x;
-      if (f >= nf) break;
-      const int n = f / rq, k0 = (f - n * rq) * R, i = n % oo, j = n / oo;
-      for (int e = 0; e < R; e++) Y[i + p1 * j + p2 * (k0 + e)] += w[u][e];
-    }
-  }
+  pass(W2, 2);
   __syncthreads();
   const float evirt = (float)(eps[o + a] + eps[o + b] + eps[o + c]);
   double acc = 0.0;
@@ -785,7 +769,9 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   const size_t wbytes = (size_t)nb * nb * nb * o3 * (mixed ? 3 * 4 : 8);
   DevMem W(wbytes);
   const int64_t p1 = o | 1, p2 = (p1 * o) | 1;
-  const size_t ysmem = (size_t)(p2 * o + 3 * o2 + 4 * o) * (mixed ? 4 : 8);
+  // FP64 kernel: Y, three S slices, t1 columns and eps; the mixed kernel adds
+  // a transposed copy of one S slice
+  const size_t ysmem = (size_t)(p2 * o + (mixed ? 4 : 3) * o2 + 4 * o) * (mixed ? 4 : 8);
   if (ysmem > 200 * 1024) throw Error(SCESS_ERR_UNSUPPORTED, "(T): o^3 too large for one CTA");
   if (mixed) {
     SCESS_CUDA(cudaFuncSetAttribute(triples_energy3_kernel,
