@@ -144,23 +144,21 @@ __global__ void to_f32_rows_kernel(const double *__restrict__ x, int64_t rows, i
   }
 }
 
-// The FP32 copy of S the mixed energy kernel reads has its rows of o^2 (i, j)
-// pairs padded to o2p = o^2 rounded up to a multiple of 4 floats:
-// [(a + v b) o2p + i + o j].
+// Layout of the grouped W buffers and the FP32 copy of S the mixed energy
+// kernel reads: rows of o^2 (i, j) pairs are padded to o2p = o^2 rounded up to
+// a multiple of 4 floats, so that every k row and every o^3 block starts on a
+// 16-byte boundary.  W_g[((y_l nb + z_l) nb + x_l) o3p + i + o j + o2p k] with
+// o3p = o o2p; S as [(a + v b) o2p + i + o j].
 __host__ __device__ inline int64_t pad4(int64_t n) { return (n + 3) & ~int64_t(3); }
 
 // Energy of one block triple from the three grouped W buffers of the
-// tensor-core form, each [problem][column][row] with M = o nb rows:
-//   W^{abc}_{ijk} = W0[b,c](row i + o a_l, column j + o k)
-//                 + W1[a,c](row j + o b_l, column i + o k)
-//                 + W2[a,b](row k + o c_l, column i + o j).
-// A triple's part of a buffer is o^2 runs of o consecutive rows.  Three
-// passes (one per buffer; 4-row vector loads when o % 4 == 0, the whole part
-// of a buffer in flight per CTA) form Y = W + V in shared memory; W is
-// recovered as Y - V in the energy loop, where threads own (i, j) pairs and
-// walk k.  Otherwise as triples_energy_kernel (FP32 per element, FP64 per
-// thread sum).
-__global__ void __launch_bounds__(256, 4) triples_energy3_kernel(
+// tensor-core form: W^{abc}_{ijk} = W0[b,c][a] + W1[a,c][b] + W2[a,b][c], each
+// block of o^3 floats in (i, j, k) order (buffer g holds [y_l][z_l][x_l][o^3]
+// for its roles (x, y, z)).  Threads own (i, j) pairs and walk k: one pass of
+// coalesced loads forms Y = W + V in shared memory, W is recovered as Y - V in
+// the energy loop.  Otherwise as triples_energy_kernel (FP32 per element, FP64
+// per thread sum).
+__global__ void __launch_bounds__(256) triples_energy3_kernel(
     const float *__restrict__ W, int64_t o, int64_t v, int64_t nb, int64_t A, int64_t Bk,
     int64_t C, const double *__restrict__ eps, const double *__restrict__ t1,
     const float *__restrict__ S, double *__restrict__ energies) {
@@ -170,23 +168,21 @@ __global__ void __launch_bounds__(256, 4) triples_energy3_kernel(
   extern __shared__ __align__(16) unsigned char sm_raw[];
   __shared__ double red[32];
   const int oo = (int)o, o2 = oo * oo;
-  const int64_t o2p = pad4(o2);
+  const int64_t o2p = pad4(o2), o3p = oo * o2p;
   // Y(i,j,k) at i + p1 j + p2 k with odd p1, p2 (conflict-free permuted reads)
   const int p1 = oo | 1, p2 = (p1 * oo) | 1;
   float *Y = reinterpret_cast<float *>(sm_raw);
-  float *Sbc = Y + p2 * oo, *Sac = Sbc + o2, *Sab = Sac + o2, *SabT = Sab + o2;
-  float *ta = SabT + o2, *tb = ta + oo, *tc = tb + oo, *eo = tc + oo;
-  const int64_t Mg = oo * nb, pstride = (int64_t)o2 * Mg, gsz = nb * nb * pstride;
-  const float *W0 = W + (bl * nb + cl) * pstride + oo * al;            // [j + o k][i]
-  const float *W1 = W + gsz + (al * nb + cl) * pstride + oo * bl;      // [i + o k][j]
-  const float *W2 = W + 2 * gsz + (al * nb + bl) * pstride + oo * cl;  // [i + o j][k]
+  float *Sbc = Y + p2 * oo, *Sac = Sbc + o2, *Sab = Sac + o2;
+  float *ta = Sab + o2, *tb = ta + oo, *tc = tb + oo, *eo = tc + oo;
+  const int64_t nb3o3 = nb * nb * nb * o3p;
+  const float *W0 = W + ((bl * nb + cl) * nb + al) * o3p;
+  const float *W1 = W + nb3o3 + ((al * nb + cl) * nb + bl) * o3p;
+  const float *W2 = W + 2 * nb3o3 + ((al * nb + bl) * nb + cl) * o3p;
   const float *S_bc = S + (b + v * c) * o2p, *S_ac = S + (a + v * c) * o2p, *S_ab = S + (a + v * b) * o2p;
   for (int e = threadIdx.x; e < o2; e += blockDim.x) {
     Sbc[e] = S_bc[e];
     Sac[e] = S_ac[e];
-    const float x = S_ab[e];
-    Sab[e] = x;
-    SabT[e / oo + oo * (e % oo)] = x;  // (ia|jb) at j + o i
+    Sab[e] = S_ab[e];
   }
   for (int i = threadIdx.x; i < oo; i += blockDim.x) {
     ta[i] = (float)t1[i + o * a];
@@ -195,55 +191,18 @@ __global__ void __launch_bounds__(256, 4) triples_energy3_kernel(
     eo[i] = (float)eps[i];
   }
   __syncthreads();
-  // Y = W0 + V, then += W1, += W2;  V_ijk = t1_ia (jb|kc) + t1_jb (ia|kc) + t1_kc (ia|jb).
-  // Threads own columns n = c0 + o c1 of a buffer and read its o rows, up to
-  // kRows at a time (4-row vectors when o % 4 == 0).  Pass g puts row r of
-  // column n at Y[ybase + r ystep]: g = 0: (i, j, k) = (r, c0, c1); g = 1:
-  // (c0, r, c1); g = 2: (c0, c1, r).
-  const bool vec = (oo & 3) == 0 && (Mg & 3) == 0;
-  constexpr int kRows = 24;
-  auto pass = [&](const float *base, int g) {
-    const int ystep = g == 0 ? 1 : (g == 1 ? p1 : p2);
-    for (int n = threadIdx.x; n < o2; n += blockDim.x) {
-      const int c0 = n % oo, c1 = n / oo;
-      const int ybase = g == 0 ? p1 * c0 + p2 * c1 : (g == 1 ? c0 + p2 * c1 : c0 + p1 * c1);
-      const float *col = base + (int64_t)n * Mg;
-      const float sbc = Sbc[n], tbj = tb[c0], tck = tc[c1];  // (g = 0: n = j + o k)
-      for (int r0 = 0; r0 < oo; r0 += kRows) {
-        float w[kRows];
-        if (vec) {
-#pragma unroll
-          for (int q = 0; q < kRows / 4; q++)
-            if (r0 + 4 * q < oo) {
-              const float4 x = __ldg(reinterpret_cast<const float4 *>(col + r0 + 4 * q));
-              w[4 * q] = x.x;
-              w[4 * q + 1] = x.y;
-              w[4 * q + 2] = x.z;
-              w[4 * q + 3] = x.w;
-            }
-        } else {
-#pragma unroll
-          for (int q = 0; q < kRows; q++)
-            if (r0 + q < oo) w[q] = __ldg(col + r0 + q);
-        }
-#pragma unroll
-        for (int q = 0; q < kRows; q++) {
-          const int r = r0 + q;
-          if (r >= oo) break;
-          float *y = Y + ybase + r * ystep;
-          if (g == 0)
-            *y = w[q] + ta[r] * sbc + tbj * Sac[r + oo * c1] + tck * SabT[c0 + oo * r];
-          else
-            *y += w[q];
-        }
-      }
+  // Y = W0 + W1 + W2 + V;  V_ijk = t1_ia (jb|kc) + t1_jb (ia|kc) + t1_kc (ia|jb)
+  for (int pr = threadIdx.x; pr < o2; pr += blockDim.x) {
+    const int i = pr % oo, j = pr / oo;
+    const float tai = ta[i], tbj = tb[j], sab = Sab[pr];
+    float *y = Y + i + p1 * j;
+#pragma unroll 8
+    for (int k = 0; k < oo; k++) {
+      const int64_t e = pr + o2p * k;
+      y[p2 * k] = (W0[e] + W1[e]) + W2[e] + tai * Sbc[j + oo * k] + tbj * Sac[i + oo * k] +
+                  tc[k] * sab;
     }
-  };
-  pass(W0, 0);
-  __syncthreads();
-  pass(W1, 1);
-  __syncthreads();
-  pass(W2, 2);
+  }
   __syncthreads();
   const float evirt = (float)(eps[o + a] + eps[o + b] + eps[o + c]);
   double acc = 0.0;
@@ -764,14 +723,12 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   DTensor energies({std::max<int64_t>(ntrip, 1)});
   SCESS_CUDA(cudaMemsetAsync(energies.p(), 0, energies.size() * sizeof(double), s));
   // FP64: one W; MIXED: the three grouped buffers W0 | W1 | W2
-  // MIXED: S rows of (i, j) pairs padded to o2p floats (see pad4)
-  const int64_t o2p = pad4(o2);
-  const size_t wbytes = (size_t)nb * nb * nb * o3 * (mixed ? 3 * 4 : 8);
+  // MIXED rows of (i, j) pairs padded to o2p floats (see pad4)
+  const int64_t o2p = pad4(o2), o3p = o * o2p;
+  const size_t wbytes = (size_t)nb * nb * nb * (mixed ? 3 * 4 * o3p : 8 * o3);
   DevMem W(wbytes);
   const int64_t p1 = o | 1, p2 = (p1 * o) | 1;
-  // FP64 kernel: Y, three S slices, t1 columns and eps; the mixed kernel adds
-  // a transposed copy of one S slice
-  const size_t ysmem = (size_t)(p2 * o + (mixed ? 4 : 3) * o2 + 4 * o) * (mixed ? 4 : 8);
+  const size_t ysmem = (size_t)(p2 * o + 3 * o2 + 4 * o) * (mixed ? 4 : 8);
   if (ysmem > 200 * 1024) throw Error(SCESS_ERR_UNSUPPORTED, "(T): o^3 too large for one CTA");
   if (mixed) {
     SCESS_CUDA(cudaFuncSetAttribute(triples_energy3_kernel,
@@ -842,10 +799,13 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
     mR = TcEngine::map_of(pR, tbn, tbk);
     mR2 = TcEngine::map_of(pR2, tbn, tbk);
     mTx = TcEngine::map_of(pTx, 128, tbk);
-    // W_g[y_l nb + z_l][s + o t][u + o x_l]: problem (y_l, z_l) of group g
-    // column-major, rows (u, x_l) the unit-stride index, so that every
-    // group's epilogue writes 32 consecutive rows per warp store.
-    gdt.build({table({{Mg, 1}}), table({{Ng, Mg}})});
+    // W_g[(y_l nb + z_l) nb + x_l][i + o j + o2p k]: every group stores its
+    // (u, s, t) in the (i, j, k) order of the triple, so that the energy kernel
+    // reads the three buffers alike.  g = 0: (u,s,t) = (i,j,k); g = 1: (j,i,k);
+    // g = 2: (k,i,j).  Rows (u, x_l), columns (s, t).
+    gdt.build({table({{o, 1}, {nb, o3p}}), table({{o, o}, {o, o2p}}),
+               table({{o, o}, {nb, o3p}}), table({{o, 1}, {o, o2p}}),
+               table({{o, o2p}, {nb, o3p}}), table({{o, 1}, {o, o}})});
     Sf.alloc((size_t)o2p * v * v * sizeof(float));
     to_f32_rows_kernel<<<(unsigned)std::min<int64_t>(ceil_div(o2p * v * v, 256), 16 * kNumSMs), 256, 0, s>>>(
         T.S.p(), v * v, o2, o2p, Sf.as<float>());
@@ -889,13 +849,18 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
           ps.nz = nb;
           ps.ng = 3;
           ps.nseg = 4;
-          // one TMEM drain per 128 K (24 MMAs): E_T within ~5e-7 relative of
-          // FP64 (1.8e-7 with a drain per 64 K)
+          // TMEM drains per tile: one per 128 K (24 MMAs) gives E_T within
+          // ~5e-7 relative of FP64 (1.8e-7 with one per 64 K); SCESS_T_KBD
+          // sets the K blocks per drain (1, 2 or 4)
           ps.kbd = 128 / TcEngine::k_block(tbn);
+          if (const char *env = std::getenv("SCESS_T_KBD")) {
+            const int kb = std::atoi(env);
+            if (kb == 1 || kb == 2 || kb == 4) ps.kbd = kb;
+          }
           ps.bn = tbn;
           ps.bk = tbk;
-          ps.cy = nb * Ng * Mg;
-          ps.cz = Ng * Mg;
+          ps.cy = nb * nb * o3p;
+          ps.cz = nb * o3p;
           const int kRoles[3][3] = {{0, 1, 2}, {1, 0, 2}, {2, 0, 1}};  // (x, y, z) of group g
           const int64_t rp = o * nb * nb, rq = o2 * nb;                 // block strides of the packs
           TcSegment &s0 = ps.seg[0], &s1 = ps.seg[1], &s2 = ps.seg[2], &s3 = ps.seg[3];
@@ -905,7 +870,7 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
           s3.mapA = 5; s3.mapB = 4; s3.Kpad = pTx.Kpad;  // -t2(m,u,y,x) R(t,s,m,z)
           for (int g = 0; g < 3; g++) {
             const int64_t X = U[kRoles[g][0]], Yb = U[kRoles[g][1]], Z = U[kRoles[g][2]];
-            ps.cg[g] = g * nb * nb * Ng * Mg;
+            ps.cg[g] = g * nb * nb * nb * o3p;
             s0.rowA0[g] = rp * (Yb + NB * X); s0.rowAy[g] = o * nb;
             s0.rowB0[g] = rq * Z;             s0.rowBz[g] = o2;
             s1.rowA0[g] = rp * (Z + NB * X);  s1.rowAz[g] = o * nb;
@@ -920,6 +885,11 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
           out.fp32 = 1;
           out.rowC = gdt.ptr[0];
           out.colC = gdt.ptr[1];
+          for (int g = 0; g < 3; g++) {
+            ps.rowC[g] = gdt.ptr[2 * g];
+            ps.colC[g] = gdt.ptr[2 * g + 1];
+            ps.store_by_column[g] = g > 0;  // i is a column index of groups 1 and 2
+          }
           out.alpha = 1.0;
           out.beta = 0.0;
           TcEngine::set_scales(out, pP, pQ);
