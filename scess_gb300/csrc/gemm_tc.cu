@@ -639,20 +639,45 @@ __global__ void tc_reduce_kernel(TcOut out, int64_t M, int64_t N, int splits,
 
 // max|x| over the gathered operand, as float bits (positive floats order like
 // unsigned integers).
-__global__ void maxabs_kernel(const double *__restrict__ src, const int64_t *__restrict__ rowOff,
-                              int64_t rows, const int64_t *__restrict__ kOff, int64_t K, int unitK,
-                              unsigned *__restrict__ maxbits) {
+// max|x| over the gather of pack_split_kernel, in the same 32-row x 64-column
+// tiles (offset tables staged in shared memory, eight independent loads a
+// thread); a persistent grid walks the tiles.  The block's maximum goes to
+// *maxbits as float bits with one atomicMax (exact: |x| rounded to FP32 is
+// monotone in |x|).
+__global__ void __launch_bounds__(256) maxabs_kernel(
+    const double *__restrict__ src, const int64_t *__restrict__ rowOff, int64_t rows,
+    const int64_t *__restrict__ kOff, int64_t K, int unitK, unsigned *__restrict__ maxbits) {
+  __shared__ int64_t sr[32], sk[64];
+  __shared__ float red[8];
+  const int t = threadIdx.x;
+  const int64_t trow = (rows + 31) / 32, tk = (K + 63) / 64, ntiles = trow * tk;
   float m = 0.0f;
-  const int64_t n = rows * K;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    int64_t r, k;
-    if (unitK) { k = e % K; r = e / K; }
-    else { r = e % rows; k = e / rows; }
-    m = fmaxf(m, (float)fabs(src[rowOff[r] + kOff[k]]));
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t r0 = (tile % trow) * 32, k0 = (tile / trow) * 64;
+    __syncthreads();  // previous tile's table reads done
+    if (t < 32) sr[t] = (r0 + t < rows) ? rowOff[r0 + t] : -1;
+    else if (t < 96) sk[t - 32] = (k0 + t - 32 < K) ? kOff[k0 + t - 32] : -1;
+    __syncthreads();
+    double x[8];
+#pragma unroll
+    for (int p = 0; p < 8; p++) {
+      int rr, kk;
+      if (unitK) { kk = t & 63; rr = (t >> 6) + 4 * p; }
+      else { rr = t & 31; kk = (t >> 5) + 8 * p; }
+      const int64_t ro = sr[rr], ko = sk[kk];
+      x[p] = (ro >= 0 && ko >= 0) ? src[ro + ko] : 0.0;
+    }
+#pragma unroll
+    for (int p = 0; p < 8; p++) m = fmaxf(m, fabsf((float)x[p]));
   }
   for (int off = 16; off > 0; off >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, off));
-  if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(maxbits, __float_as_uint(m));
+  if ((t & 31) == 0) red[t >> 5] = m;
+  __syncthreads();
+  if (t == 0) {
+    float b = 0.0f;
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) b = fmaxf(b, red[q]);
+    if (b > 0.0f) atomicMax(maxbits, __float_as_uint(b));
+  }
 }
 
 // x s = hi + lo in FP16.  FP64 arithmetic runs at a small fraction of the FP32
@@ -967,6 +992,14 @@ bool TcEngine::worth_it(const EinsumPlan &pl) {
   return mn >= 4 && pl.K >= 16 && 2.0 * pl.M * pl.N * pl.K >= 2.0e7;
 }
 
+namespace {
+// Persistent grid of maxabs_kernel: at most 8 blocks an SM, at least one tile each.
+unsigned maxabs_blocks(int64_t rows, int64_t K) {
+  const int64_t tiles = ceil_div(std::max<int64_t>(rows, 1), 32) * ceil_div(std::max<int64_t>(K, 1), 64);
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(tiles, 8 * kNumSMs));
+}
+}  // namespace
+
 void TcEngine::pack(const double *src, const int64_t *rowOff, int64_t rows, const int64_t *kOff,
                     int64_t K, bool unitK, int64_t row_align, Packed &out) {
   const int64_t Kpad = round_up(std::max<int64_t>(K, 1), TC_BK);
@@ -990,9 +1023,8 @@ void TcEngine::pack(const double *src, const int64_t *rowOff, int64_t rows, cons
   dim3 grid((unsigned)(rows_pad / 32), (unsigned)(Kpad / 64));
   if (fmt_ == TcFormat::FP16) {
     SCESS_CUDA(cudaMemsetAsync(maxbits, 0, sizeof(unsigned), ctx_.stream));
-    const int64_t n = rows * K;
-    const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), 4 * kNumSMs));
-    maxabs_kernel<<<blocks, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, unitK ? 1 : 0, maxbits);
+    maxabs_kernel<<<maxabs_blocks(rows, K), 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K,
+                                                                  unitK ? 1 : 0, maxbits);
     SCESS_CHECK_LAUNCH();
     pack_split_kernel<true><<<grid, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, unitK ? 1 : 0,
                                                            out.mem.as<uint16_t>(), Kpad, maxbits, scale, 0);
@@ -1007,10 +1039,9 @@ void TcEngine::pack(const double *src, const int64_t *rowOff, int64_t rows, cons
 
 void TcEngine::maxabs_into(const double *src, const int64_t *rowOff, int64_t rows,
                            const int64_t *kOff, int64_t K, bool unitK, unsigned *maxbits) {
-  const int64_t n = rows * K;
-  if (n <= 0) return;
-  const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), 4 * kNumSMs));
-  maxabs_kernel<<<blocks, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, unitK ? 1 : 0, maxbits);
+  if (rows <= 0 || K <= 0) return;
+  maxabs_kernel<<<maxabs_blocks(rows, K), 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K,
+                                                                unitK ? 1 : 0, maxbits);
   SCESS_CHECK_LAUNCH();
 }
 

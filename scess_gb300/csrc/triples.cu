@@ -849,10 +849,14 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
           ps.nz = nb;
           ps.ng = 3;
           ps.nseg = 4;
-          // TMEM drains per tile: one per 128 K (24 MMAs) gives E_T within
-          // ~5e-7 relative of FP64 (1.8e-7 with one per 64 K); SCESS_T_KBD
-          // sets the K blocks per drain (1, 2 or 4)
-          ps.kbd = 128 / TcEngine::k_block(tbn);
+          // TMEM drains per tile.  The FP32 accumulation inside the tensor
+          // core truncates, so the error of E_T grows with the products
+          // accumulated between drains: measured 1.7e-7 / 4.6e-7 / 1.1e-6
+          // relative to FP64 with a drain per 64 / 128 / 256 K.  One per 256 K
+          // (two per tile at this K) lets a tile's stores overlap the whole
+          // next tile's MMAs (each TMEM buffer then holds half a tile).
+          // SCESS_T_KBD sets the K blocks (of 64) per drain: 1, 2 or 4.
+          ps.kbd = 256 / TcEngine::k_block(tbn);
           if (const char *env = std::getenv("SCESS_T_KBD")) {
             const int kb = std::atoi(env);
             if (kb == 1 || kb == 2 || kb == 4) ps.kbd = kb;
