@@ -306,7 +306,7 @@ def main():
     ap.add_argument('--v', type=int, default=180)
     ap.add_argument('--seed', type=int, default=0)
     ap.add_argument('--fp64-steps', type=int, default=1)
-    ap.add_argument('--e2e-steps', type=int, default=2)
+    ap.add_argument('--e2e-steps', type=int, default=4)
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-fp64', action='store_true')
     ap.add_argument('--transform', action='store_true',
@@ -422,7 +422,8 @@ def main():
     # over the launches of one (T); the launches also compute the repeated triples of
     # the diagonal block triples, which the timer's own count includes.
     tc = prof.get('tc_gemm[triples]', {'launches': 0, 'ms': 0.0, 'flops': 0.0})
-    top = max(prof.items(), key=lambda kv: kv[1]['ms'])[0] if prof else None
+    top = max(((k, v) for k, v in prof.items() if not k.startswith('phase:')),
+              key=lambda kv: kv[1]['ms'], default=(None, None))[0]
     n_t = max(args.steps, 1)
     per_launch_alg = oracle.triples_flops(o, v) * n_t / max(tc['launches'], 1)
     avg_ms = tc['ms'] / max(tc['launches'], 1)
@@ -444,7 +445,9 @@ def main():
                                   '(T) launch at o=20 v=96, which has the same launch shape '
                                   '(nb=12, 1728 work units of 128 x 256) as o=20 v=180',
                 'top_kernel_by_time': top}
-    share = {k: round(v['ms'] / max(sum(x['ms'] for x in prof.values()), 1e-9), 4) for k, v in prof.items()}
+    # "phase:" timers enclose kernel timers: shown, but not part of the shares
+    kern = {k: v for k, v in prof.items() if not k.startswith('phase:')}
+    share = {k: round(v['ms'] / max(sum(x['ms'] for x in kern.values()), 1e-9), 4) for k, v in kern.items()}
 
     # ---- FP64 form on the same workload -------------------------------------------------------
     fp64 = None

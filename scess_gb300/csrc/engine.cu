@@ -147,12 +147,14 @@ cudaEvent_t KernelTimer::get() {
 void KernelTimer::begin(const char *name, double flops, double bytes, cudaStream_t s) {
   Rec r{name, get(), get(), flops, bytes};
   SCESS_CUDA(cudaEventRecord(r.a, s));
+  open_.push_back(recs_.size());
   recs_.push_back(r);
 }
 
 void KernelTimer::end(cudaStream_t s) {
-  SCESS_CUDA(cudaEventRecord(recs_.back().b, s));
-  if (recs_.size() >= 4096) collect();
+  SCESS_CUDA(cudaEventRecord(recs_[open_.back()].b, s));
+  open_.pop_back();
+  if (open_.empty() && recs_.size() >= 4096) collect();
 }
 
 void KernelTimer::host(const char *name, double ms) {

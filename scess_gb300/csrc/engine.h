@@ -124,6 +124,7 @@ class KernelTimer {
   };
   cudaEvent_t get();
   std::vector<Rec> recs_;
+  std::vector<size_t> open_;  // records whose end() is pending (scopes nest)
   std::vector<cudaEvent_t> pool_;
 };
 

@@ -714,7 +714,10 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   T.nb = nb;
   T.NB = NB;
   T.vp = vp;
-  T.build(ctx, d_eri, d_t2, d_B, naux, mixed ? Backend::TENSOR : Backend::FP64);
+  {  // (device time of the whole setup; "phase:" timers enclose other timers)
+    TimedScope ts(ctx.timer, "phase:triples_setup", 0.0, 0.0, s);
+    T.build(ctx, d_eri, d_t2, d_B, naux, mixed ? Backend::TENSOR : Backend::FP64);
+  }
   const DTensor &P = T.P, &Qt = T.Qt, &Rt = T.Rt, &T2p = T.T2p;
   const DevTables &dt = T.dt;
   const size_t kOperand = T.kOperand;
@@ -760,6 +763,7 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   const int64_t Mg = o * nb, Ng = o2;
   const int64_t Mpq = o * nb * nb, Npq = o2 * nb, Mr = o2 * nb, Nr = o * nb * nb;  // FP64 GEMMs
   if (mixed) {
+    TimedScope ts(ctx.timer, "phase:triples_pack", 0.0, 0.0, s);
     TcEngine &tc = ctx.tensor_cores();
     std::vector<std::vector<int64_t>> pt;
     // P rows r = i + o(x + nb(y + nb(Y + NB X))):  P(i, f, X nb + x, Y nb + y)
