@@ -250,36 +250,83 @@ __global__ void sum_energies_kernel(int64_t n, const double *__restrict__ e, dou
   }
 }
 
-// Offset table over a list of (extent, stride) dims, first fastest.
-std::vector<int64_t> table(std::initializer_list<std::pair<int64_t, int64_t>> dims) {
-  int64_t n = 1;
-  for (auto &d : dims) n *= d.first;
-  std::vector<int64_t> t((size_t)n);
-  for (int64_t e = 0; e < n; e++) {
-    int64_t r = e, off = 0;
-    for (auto &d : dims) {
-      off += (r % d.first) * d.second;
-      r /= d.first;
-    }
-    t[(size_t)e] = off;
+// Offset table over a list of (extent, stride) dims, first fastest:
+// entry e = sum_d i_d stride_d for e = i_0 + ext_0 (i_1 + ext_1 (...)).  Kept
+// as a spec and filled on the device (DevTables::build).
+struct TableSpec {
+  int nd = 0;
+  int64_t ext[6] = {1, 1, 1, 1, 1, 1}, str[6] = {0, 0, 0, 0, 0, 0};
+  int64_t size() const {
+    int64_t n = 1;
+    for (int d = 0; d < nd; d++) n *= ext[d];
+    return n;
+  }
+};
+
+TableSpec table(std::initializer_list<std::pair<int64_t, int64_t>> dims) {
+  TableSpec t;
+  if (dims.size() > 6) throw Error(SCESS_ERR_INVALID, "offset table: too many dims");
+  for (auto &d : dims) {
+    t.ext[t.nd] = d.first;
+    t.str[t.nd] = d.second;
+    t.nd++;
   }
   return t;
+}
+
+constexpr int kMaxTables = 24;
+struct TableBatch {
+  int nt = 0;
+  int64_t start[kMaxTables + 1] = {};
+  TableSpec spec[kMaxTables];
+  int64_t *out = nullptr;
+};
+
+__global__ void fill_tables_kernel(const __grid_constant__ TableBatch b) {
+  const int64_t total = b.start[b.nt];
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int t = 0;
+    while (e >= b.start[t + 1]) t++;
+    const TableSpec &sp = b.spec[t];
+    int64_t r = e - b.start[t], off = 0;
+    for (int d = 0; d < sp.nd; d++) {
+      const int64_t q = r / sp.ext[d];
+      off += (r - q * sp.ext[d]) * sp.str[d];
+      r = q;
+    }
+    b.out[e] = off;
+  }
 }
 
 struct DevTables {
   DevMem mem;
   std::vector<const int64_t *> ptr;
-  void build(const std::vector<std::vector<int64_t>> &ts) {
+  // One allocation, filled by one kernel per kMaxTables tables on ctx's stream.
+  void build(Ctx &ctx, const std::vector<TableSpec> &ts) {
     size_t tot = 0;
-    for (auto &t : ts) tot += t.size();
+    for (auto &t : ts) tot += (size_t)t.size();
     mem.alloc(std::max<size_t>(tot, 1) * sizeof(int64_t));
-    size_t off = 0;
     ptr.clear();
-    for (auto &t : ts) {
-      ptr.push_back(mem.as<int64_t>() + off);
-      SCESS_CUDA(cudaMemcpy(mem.as<int64_t>() + off, t.data(), t.size() * sizeof(int64_t),
-                            cudaMemcpyHostToDevice));
-      off += t.size();
+    size_t off = 0;
+    for (size_t i0 = 0; i0 < ts.size(); i0 += kMaxTables) {
+      TableBatch b;
+      b.out = mem.as<int64_t>() + off;
+      b.nt = (int)std::min<size_t>(kMaxTables, ts.size() - i0);
+      int64_t n = 0;
+      for (int t = 0; t < b.nt; t++) {
+        b.spec[t] = ts[i0 + t];
+        b.start[t] = n;
+        ptr.push_back(mem.as<int64_t>() + off + n);
+        n += ts[i0 + t].size();
+      }
+      b.start[b.nt] = n;
+      if (n > 0) {
+        fill_tables_kernel<<<(unsigned)std::min<int64_t>(ceil_div(n, 256), 8 * kNumSMs), 256, 0,
+                             ctx.stream>>>(b);
+        SCESS_CHECK_LAUNCH();
+      }
+      off += (size_t)n;
     }
   }
 };
@@ -405,7 +452,7 @@ void TriplesSetup::build(Ctx &ctx, const double *d_eri, const double *d_t2, cons
   // (GEMM columns) of every epilogue: when i is the k' of a permutation the Q
   // operand is taken in (k', j', z) column order, when it is the j' of an R
   // product the R operand is taken in (j', i', x) row order.
-  std::vector<std::vector<int64_t>> ts;
+  std::vector<TableSpec> ts;
   for (int p = 0; p < 6; p++) {
     const int *pi = kPerm[p];
     ts.push_back(table({{o, sw[pi[0]]}, {nb, su[pi[0]]}, {nb, su[pi[1]]}}));      // PQ rows (i',x,y)
@@ -431,7 +478,7 @@ void TriplesSetup::build(Ctx &ctx, const double *d_eri, const double *d_t2, cons
   ts.push_back(table({{o, 1}}));                                                 // +7: t2 k (m)
   ts.push_back(table({{o, v * o}, {o, v}, {nb, v * o2}}));                       // +8: Q cols (k,j,z)
   ts.push_back(table({{o, o}, {o, 1}, {nb, o3}}));                               // +9: R rows (j,i,x)
-  dt.build(ts);
+  dt.build(ctx, ts);
 }
 
 // The 12 FP64 GEMMs of block triple U = (A, B, C): W[(a_l,b_l,c_l)][i,j,k] =
@@ -765,7 +812,7 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   if (mixed) {
     TimedScope ts(ctx.timer, "phase:triples_pack", 0.0, 0.0, s);
     TcEngine &tc = ctx.tensor_cores();
-    std::vector<std::vector<int64_t>> pt;
+    std::vector<TableSpec> pt;
     // P rows r = i + o(x + nb(y + nb(Y + NB X))):  P(i, f, X nb + x, Y nb + y)
     pt.push_back(table({{o, 1}, {nb, o * v}, {nb, o * v * vp}, {NB, o * v * vp * nb}, {NB, o * v * nb}}));
     // Q rows r = j + o(k + o(z + nb Z)):  Q(f, j, k, Z nb + z)
@@ -779,7 +826,7 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
     // R rows in (j, i) order: r = j + o(i + o(x + nb X))
     pt.push_back(table({{o, o}, {o, 1}, {nb, o3}, {NB, o3 * nb}}));
     DevTables pdt;
-    pdt.build(pt);
+    pdt.build(ctx, pt);
     DevMem maxw(2 * sizeof(unsigned));
     unsigned *mx = maxw.as<unsigned>();
     SCESS_CUDA(cudaMemsetAsync(mx, 0, 2 * sizeof(unsigned), s));
@@ -807,7 +854,7 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
     // (u, s, t) in the (i, j, k) order of the triple, so that the energy kernel
     // reads the three buffers alike.  g = 0: (u,s,t) = (i,j,k); g = 1: (j,i,k);
     // g = 2: (k,i,j).  Rows (u, x_l), columns (s, t).
-    gdt.build({table({{o, 1}, {nb, o3p}}), table({{o, o}, {o, o2p}}),
+    gdt.build(ctx, {table({{o, 1}, {nb, o3p}}), table({{o, o}, {o, o2p}}),
                table({{o, o}, {nb, o3p}}), table({{o, 1}, {o, o2p}}),
                table({{o, o2p}, {nb, o3p}}), table({{o, 1}, {o, o}})});
     Sf.alloc((size_t)o2p * v * v * sizeof(float));
