@@ -226,6 +226,20 @@ struct Lbl {
   int64_t sa, sb, sc;
 };
 
+// Stride s if the group's offsets are e * s for e = 0, 1, ... (labels of
+// extent 1 ignored; 0 for an empty group), else -1.
+int64_t affine_stride(const std::vector<Lbl> &ls, int which) {
+  int64_t s = -1, next = -1;
+  for (auto &l : ls) {
+    if (l.ext == 1) continue;
+    const int64_t st = which == 0 ? l.sa : (which == 1 ? l.sb : l.sc);
+    if (s < 0) s = st;
+    else if (st != next) return -1;
+    next = st * l.ext;
+  }
+  return s < 0 ? 0 : s;
+}
+
 std::vector<int64_t> offsets(const std::vector<Lbl> &ls, int which) {
   int64_t n = 1;
   for (auto &l : ls) n *= l.ext;
@@ -308,6 +322,10 @@ const EinsumPlan &plan_einsum(Ctx &ctx, const char *spec, const TV &A, const TV 
   pl->bUnitK = false;
   for (auto &l : K)
     if (l.sb == 1) pl->bUnitK = true;
+  pl->aRowStride = affine_stride(M, 0);
+  pl->aKStride = affine_stride(K, 0);
+  pl->bColStride = affine_stride(N, 1);
+  pl->bKStride = affine_stride(K, 1);
   const size_t tot = pl->rowA.size() + pl->kA.size() + pl->colB.size() + pl->kB.size() +
                      pl->rowC.size() + pl->colC.size();
   pl->dev = std::make_shared<DevMem>(tot * sizeof(int64_t));

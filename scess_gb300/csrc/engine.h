@@ -69,6 +69,8 @@ struct EinsumPlan {
   const int64_t *d_rowC = nullptr, *d_colC = nullptr;
   bool aUnitM = false, bUnitN = false, aUnitK = false, bUnitK = false;
   bool cUnitM = false, cUnitN = false;  // C's unit-stride label leads the M / N group
+  // the operand offset tables as plain strides (offset = index * stride), or -1
+  int64_t aRowStride = -1, aKStride = -1, bColStride = -1, bKStride = -1;
   std::string key;
   std::string spec;
 };

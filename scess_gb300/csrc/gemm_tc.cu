@@ -644,9 +644,12 @@ __global__ void tc_reduce_kernel(TcOut out, int64_t M, int64_t N, int splits,
 // thread); a persistent grid walks the tiles.  The block's maximum goes to
 // *maxbits as float bits with one atomicMax (exact: |x| rounded to FP32 is
 // monotone in |x|).
+// AFFINE: the offsets are r * rs and k * ks (no tables).
+template <bool AFFINE>
 __global__ void __launch_bounds__(256) maxabs_kernel(
     const double *__restrict__ src, const int64_t *__restrict__ rowOff, int64_t rows,
-    const int64_t *__restrict__ kOff, int64_t K, int unitK, unsigned *__restrict__ maxbits) {
+    const int64_t *__restrict__ kOff, int64_t K, int unitK, unsigned *__restrict__ maxbits,
+    int64_t rs, int64_t ks) {
   __shared__ int64_t sr[32], sk[64];
   __shared__ float red[8];
   const int t = threadIdx.x;
@@ -655,8 +658,8 @@ __global__ void __launch_bounds__(256) maxabs_kernel(
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int64_t r0 = (tile % trow) * 32, k0 = (tile / trow) * 64;
     __syncthreads();  // previous tile's table reads done
-    if (t < 32) sr[t] = (r0 + t < rows) ? rowOff[r0 + t] : -1;
-    else if (t < 96) sk[t - 32] = (k0 + t - 32 < K) ? kOff[k0 + t - 32] : -1;
+    if (t < 32) sr[t] = (r0 + t < rows) ? (AFFINE ? (r0 + t) * rs : rowOff[r0 + t]) : -1;
+    else if (t < 96) sk[t - 32] = (k0 + t - 32 < K) ? (AFFINE ? (k0 + t - 32) * ks : kOff[k0 + t - 32]) : -1;
     __syncthreads();
     double x[8];
 #pragma unroll
@@ -674,6 +677,31 @@ __global__ void __launch_bounds__(256) maxabs_kernel(
   if ((t & 31) == 0) red[t >> 5] = m;
   __syncthreads();
   if (t == 0) {
+    float b = 0.0f;
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) b = fmaxf(b, red[q]);
+    if (b > 0.0f) atomicMax(maxbits, __float_as_uint(b));
+  }
+}
+
+// max|x| over n contiguous values (a gather that covers its source span).
+__global__ void __launch_bounds__(256) maxabs_flat_kernel(const double *__restrict__ src, int64_t n,
+                                                          unsigned *__restrict__ maxbits) {
+  __shared__ float red[8];
+  float m = 0.0f;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  for (; e + 7 * stride < n; e += 8 * stride) {
+    double x[8];
+#pragma unroll
+    for (int p = 0; p < 8; p++) x[p] = __ldg(src + e + p * stride);
+#pragma unroll
+    for (int p = 0; p < 8; p++) m = fmaxf(m, fabsf((float)x[p]));
+  }
+  for (; e < n; e += stride) m = fmaxf(m, fabsf((float)src[e]));
+  for (int off = 16; off > 0; off >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, off));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
     float b = 0.0f;
     for (int q = 0; q < (int)(blockDim.x >> 5); q++) b = fmaxf(b, red[q]);
     if (b > 0.0f) atomicMax(maxbits, __float_as_uint(b));
@@ -702,19 +730,20 @@ struct HalfPair {
 // Gathers rows x K FP64 values through offset tables into 16-bit hi/lo rows.
 // FP16 format: values are scaled by s = 2^(15 - e), max|x| = f 2^e, f in [0.5, 1),
 // which block (0,0) also stores for the epilogue.
-template <bool F16>
+// AFFINE: the offsets are r * rs and k * ks (no tables).
+template <bool F16, bool AFFINE>
 __global__ void __launch_bounds__(256) pack_split_kernel(
     const double *__restrict__ src, const int64_t *__restrict__ rowOff, int64_t rows,
     const int64_t *__restrict__ kOff, int64_t K, int unitK, uint16_t *__restrict__ dst,
     int64_t Kpad, const unsigned *__restrict__ maxbits, double *__restrict__ scale_out,
-    int negate) {
+    int negate, int64_t rs, int64_t ks) {
   __shared__ double tile[32][65];
   __shared__ int64_t sr[32], sk[64];
   const int t = threadIdx.x;
   // row blocks on grid.x (up to 2^31 - 1), K blocks on grid.y (<= 65535)
   const int64_t r0 = (int64_t)blockIdx.x * 32, k0 = (int64_t)blockIdx.y * 64;
-  if (t < 32) sr[t] = (r0 + t < rows) ? rowOff[r0 + t] : -1;
-  else if (t < 96) sk[t - 32] = (k0 + t - 32 < K) ? kOff[k0 + t - 32] : -1;
+  if (t < 32) sr[t] = (r0 + t < rows) ? (AFFINE ? (r0 + t) * rs : rowOff[r0 + t]) : -1;
+  else if (t < 96) sk[t - 32] = (k0 + t - 32 < K) ? (AFFINE ? (k0 + t - 32) * ks : kOff[k0 + t - 32]) : -1;
   double s = 1.0;
   if (F16) {
     const float mx = __uint_as_float(*maxbits);
@@ -1001,7 +1030,9 @@ unsigned maxabs_blocks(int64_t rows, int64_t K) {
 }  // namespace
 
 void TcEngine::pack(const double *src, const int64_t *rowOff, int64_t rows, const int64_t *kOff,
-                    int64_t K, bool unitK, int64_t row_align, Packed &out) {
+                    int64_t K, bool unitK, int64_t row_align, Packed &out, int64_t rs,
+                    int64_t ks) {
+  const bool aff = rs >= 0 && ks >= 0;
   const int64_t Kpad = round_up(std::max<int64_t>(K, 1), TC_BK);
   const int64_t rows_pad = round_up(std::max<int64_t>(rows, 1), std::max<int64_t>(row_align, 32));
   const size_t bytes = (size_t)rows_pad * 2 * Kpad * sizeof(uint16_t);
@@ -1021,18 +1052,38 @@ void TcEngine::pack(const double *src, const int64_t *rowOff, int64_t rows, cons
   double *scale = reinterpret_cast<double *>(out.aux.as<char>() + 8);
   if (Kpad / 64 > 65535 || rows_pad / 32 > INT32_MAX) throw Error(SCESS_ERR_INVALID, "pack: too large");
   dim3 grid((unsigned)(rows_pad / 32), (unsigned)(Kpad / 64));
+  uint16_t *dst = out.mem.as<uint16_t>();
+  const int u = unitK ? 1 : 0;
   if (fmt_ == TcFormat::FP16) {
     SCESS_CUDA(cudaMemsetAsync(maxbits, 0, sizeof(unsigned), ctx_.stream));
-    maxabs_kernel<<<maxabs_blocks(rows, K), 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K,
-                                                                  unitK ? 1 : 0, maxbits);
+    const int64_t n = rows * K;
+    if (aff && ((rs == 1 && ks == rows) || (ks == 1 && rs == K))) {  // the gather is src[0, n)
+      const unsigned blocks =
+          (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256 * 8), 8 * kNumSMs));
+      maxabs_flat_kernel<<<blocks, 256, 0, ctx_.stream>>>(src, n, maxbits);
+    } else if (aff) {
+      maxabs_kernel<true><<<maxabs_blocks(rows, K), 256, 0, ctx_.stream>>>(src, nullptr, rows, nullptr,
+                                                                          K, u, maxbits, rs, ks);
+    } else {
+      maxabs_kernel<false><<<maxabs_blocks(rows, K), 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K,
+                                                                           u, maxbits, 0, 0);
+    }
     SCESS_CHECK_LAUNCH();
-    pack_split_kernel<true><<<grid, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, unitK ? 1 : 0,
-                                                           out.mem.as<uint16_t>(), Kpad, maxbits, scale, 0);
+    if (aff)
+      pack_split_kernel<true, true><<<grid, 256, 0, ctx_.stream>>>(src, nullptr, rows, nullptr, K, u, dst,
+                                                                   Kpad, maxbits, scale, 0, rs, ks);
+    else
+      pack_split_kernel<true, false><<<grid, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, u, dst,
+                                                                    Kpad, maxbits, scale, 0, 0, 0);
   } else {
     const double one = 1.0;
     SCESS_CUDA(cudaMemcpyAsync(scale, &one, sizeof(double), cudaMemcpyHostToDevice, ctx_.stream));
-    pack_split_kernel<false><<<grid, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, unitK ? 1 : 0,
-                                                            out.mem.as<uint16_t>(), Kpad, maxbits, scale, 0);
+    if (aff)
+      pack_split_kernel<false, true><<<grid, 256, 0, ctx_.stream>>>(src, nullptr, rows, nullptr, K, u, dst,
+                                                                    Kpad, maxbits, scale, 0, rs, ks);
+    else
+      pack_split_kernel<false, false><<<grid, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, u, dst,
+                                                                     Kpad, maxbits, scale, 0, 0, 0);
   }
   SCESS_CHECK_LAUNCH();
 }
@@ -1040,8 +1091,8 @@ void TcEngine::pack(const double *src, const int64_t *rowOff, int64_t rows, cons
 void TcEngine::maxabs_into(const double *src, const int64_t *rowOff, int64_t rows,
                            const int64_t *kOff, int64_t K, bool unitK, unsigned *maxbits) {
   if (rows <= 0 || K <= 0) return;
-  maxabs_kernel<<<maxabs_blocks(rows, K), 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K,
-                                                                unitK ? 1 : 0, maxbits);
+  maxabs_kernel<false><<<maxabs_blocks(rows, K), 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K,
+                                                                       unitK ? 1 : 0, maxbits, 0, 0);
   SCESS_CHECK_LAUNCH();
 }
 
@@ -1067,15 +1118,15 @@ void TcEngine::pack_with_max(const double *src, const int64_t *rowOff, int64_t r
   if (Kpad / 64 > 65535 || rows_pad / 32 > INT32_MAX) throw Error(SCESS_ERR_INVALID, "pack: too large");
   dim3 grid((unsigned)(rows_pad / 32), (unsigned)(Kpad / 64));
   if (fmt_ == TcFormat::FP16) {
-    pack_split_kernel<true><<<grid, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, unitK ? 1 : 0,
-                                                           out.mem.as<uint16_t>(), Kpad, maxbits,
-                                                           scale, negate ? 1 : 0);
+    pack_split_kernel<true, false><<<grid, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, unitK ? 1 : 0,
+                                                                  out.mem.as<uint16_t>(), Kpad, maxbits,
+                                                                  scale, negate ? 1 : 0, 0, 0);
   } else {
     const double one = 1.0;
     SCESS_CUDA(cudaMemcpyAsync(scale, &one, sizeof(double), cudaMemcpyHostToDevice, ctx_.stream));
-    pack_split_kernel<false><<<grid, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, unitK ? 1 : 0,
-                                                            out.mem.as<uint16_t>(), Kpad, maxbits,
-                                                            scale, negate ? 1 : 0);
+    pack_split_kernel<false, false><<<grid, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, unitK ? 1 : 0,
+                                                                   out.mem.as<uint16_t>(), Kpad, maxbits,
+                                                                   scale, negate ? 1 : 0, 0, 0);
   }
   SCESS_CHECK_LAUNCH();
 }
@@ -1141,25 +1192,28 @@ void TcEngine::contract(const EinsumPlan &pl, double alpha, const double *A, con
   const bool uX = swap ? pl.bUnitK : pl.aUnitK, uY = swap ? pl.aUnitK : pl.bUnitK;
   const int64_t MX = swap ? pl.N : pl.M, NY = swap ? pl.M : pl.N;
 
+  const int64_t rsX = swap ? pl.bColStride : pl.aRowStride, ksX = swap ? pl.bKStride : pl.aKStride;
+  const int64_t rsY = swap ? pl.aRowStride : pl.bColStride, ksY = swap ? pl.aKStride : pl.bKStride;
   auto get = [&](const double *src, const int64_t *rows, int64_t nrows, const int64_t *ks,
-                 bool unitK, bool isConst, const char *tag, Packed &tmp) -> const Packed & {
+                 bool unitK, bool isConst, const char *tag, Packed &tmp, int64_t rstr,
+                 int64_t kstr) -> const Packed & {
     if (!isConst) {
-      pack(src, rows, nrows, ks, pl.K, unitK, TC_BM, tmp);
+      pack(src, rows, nrows, ks, pl.K, unitK, TC_BM, tmp, rstr, kstr);
       return tmp;
     }
     std::string key = pl.key + tag + std::to_string((uintptr_t)src);
     auto it = cache_.find(key);
     if (it != cache_.end() && it->second.first == owner_) return *it->second.second;
     auto pk = std::make_unique<Packed>();
-    pack(src, rows, nrows, ks, pl.K, unitK, TC_BM, *pk);
+    pack(src, rows, nrows, ks, pl.K, unitK, TC_BM, *pk, rstr, kstr);
     auto &ref = *pk;
     cache_[key] = std::make_pair(owner_, std::move(pk));
     return ref;
   };
   const std::string tname = "tc_gemm[" + pl.spec + "]";
   timer_name_ = tname.c_str();
-  const Packed &PX = get(X, rowX, MX, kX, uX, cX, swap ? "#B" : "#A", tmpA_);
-  const Packed &PY = get(Y, rowY, NY, kY, uY, cY, swap ? "#A" : "#B", tmpB_);
+  const Packed &PX = get(X, rowX, MX, kX, uX, cX, swap ? "#B" : "#A", tmpA_, rsX, ksX);
+  const Packed &PY = get(Y, rowY, NY, kY, uY, cY, swap ? "#A" : "#B", tmpB_, rsY, ksY);
   TcOut o;
   o.C = C;
   o.fp32 = 0;
