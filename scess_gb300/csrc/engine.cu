@@ -1,4 +1,5 @@
 // Host engine: device memory, context, einsum compiler (spec -> offset-table GEMM).
+#include <algorithm>
 #include <cstdarg>
 #include <cstring>
 
@@ -240,6 +241,41 @@ int64_t affine_stride(const std::vector<Lbl> &ls, int which) {
   return s < 0 ? 0 : s;
 }
 
+// Tiling hint for a gathered group: the label with the smallest stride in the
+// operand (extent > 1).  Rows r = pre + P (f + E post) with f its index, P the
+// product of the extents before it (group order) and E its extent.
+void fast_label(const std::vector<Lbl> &ls, int which, int64_t &P, int64_t &E) {
+  int64_t best = -1, bs = 0, prod = 1;
+  P = 1;
+  E = 1;
+  for (auto &l : ls) {
+    const int64_t st = which == 0 ? l.sa : l.sb;
+    if (l.ext > 1 && (best < 0 || st < bs)) {
+      best = 1;
+      bs = st;
+      P = prod;
+      E = l.ext;
+    }
+    prod *= l.ext;
+  }
+  if (best < 0) E = prod;  // all extents 1
+}
+
+// Whether the labels of two groups together enumerate src[0, n) exactly once.
+bool dense_gather(const std::vector<Lbl> &g1, const std::vector<Lbl> &g2, int which) {
+  std::vector<std::pair<int64_t, int64_t>> d;  // (stride, extent)
+  for (auto *g : {&g1, &g2})
+    for (auto &l : *g)
+      if (l.ext > 1) d.push_back({which == 0 ? l.sa : l.sb, l.ext});
+  std::sort(d.begin(), d.end());
+  int64_t next = 1;
+  for (auto &x : d) {
+    if (x.first != next) return false;
+    next = x.first * x.second;
+  }
+  return true;
+}
+
 std::vector<int64_t> offsets(const std::vector<Lbl> &ls, int which) {
   int64_t n = 1;
   for (auto &l : ls) n *= l.ext;
@@ -322,6 +358,10 @@ const EinsumPlan &plan_einsum(Ctx &ctx, const char *spec, const TV &A, const TV 
   pl->bUnitK = false;
   for (auto &l : K)
     if (l.sb == 1) pl->bUnitK = true;
+  fast_label(M, 0, pl->aRowP, pl->aRowE);
+  fast_label(N, 1, pl->bColP, pl->bColE);
+  pl->aDense = dense_gather(M, K, 0);
+  pl->bDense = dense_gather(N, K, 1);
   pl->aRowStride = affine_stride(M, 0);
   pl->aKStride = affine_stride(K, 0);
   pl->bColStride = affine_stride(N, 1);

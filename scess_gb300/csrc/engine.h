@@ -71,6 +71,10 @@ struct EinsumPlan {
   bool cUnitM = false, cUnitN = false;  // C's unit-stride label leads the M / N group
   // the operand offset tables as plain strides (offset = index * stride), or -1
   int64_t aRowStride = -1, aKStride = -1, bColStride = -1, bKStride = -1;
+  // packing hints: rows r = pre + P (f + E post), f along the operand's
+  // smallest-stride row label; dense: the gather is a permutation of src[0, n)
+  int64_t aRowP = 1, aRowE = 1, bColP = 1, bColE = 1;
+  bool aDense = false, bDense = false;
   std::string key;
   std::string spec;
 };

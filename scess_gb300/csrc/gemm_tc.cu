@@ -644,21 +644,48 @@ __global__ void tc_reduce_kernel(TcOut out, int64_t M, int64_t N, int splits,
 // thread); a persistent grid walks the tiles.  The block's maximum goes to
 // *maxbits as float bits with one atomicMax (exact: |x| rounded to FP32 is
 // monotone in |x|).
+// Row tiles of 32 rows along a group's smallest-stride label: row tile x holds
+// rows r = pre + P (32 ft + t + E post), t < 32 (-1 past the label's extent),
+// so that a tile's source values are contiguous when that stride is 1.
+struct RowTiles {
+  int64_t P = 1, E = 1, nft = 1, count = 0;
+  static RowTiles make(int64_t rows, int64_t P, int64_t E) {
+    RowTiles r;
+    if (P < 1 || E < 1 || rows % (P * E) != 0) {  // not a product grouping: plain tiles
+      P = 1;
+      E = std::max<int64_t>(rows, 1);
+    }
+    r.P = P;
+    r.E = E;
+    r.nft = (E + 31) / 32;
+    r.count = P * r.nft * (std::max<int64_t>(rows, 1) / (P * E));
+    return r;
+  }
+  __device__ int64_t row(int64_t x, int t) const {
+    const int64_t pre = x % P, rem = x / P, ft = rem % nft, post = rem / nft;
+    const int64_t f = ft * 32 + t;
+    return f < E ? pre + P * (f + E * post) : -1;
+  }
+};
+
 // AFFINE: the offsets are r * rs and k * ks (no tables).
 template <bool AFFINE>
 __global__ void __launch_bounds__(256) maxabs_kernel(
     const double *__restrict__ src, const int64_t *__restrict__ rowOff, int64_t rows,
     const int64_t *__restrict__ kOff, int64_t K, int unitK, unsigned *__restrict__ maxbits,
-    int64_t rs, int64_t ks) {
+    int64_t rs, int64_t ks, const RowTiles rt) {
   __shared__ int64_t sr[32], sk[64];
   __shared__ float red[8];
   const int t = threadIdx.x;
-  const int64_t trow = (rows + 31) / 32, tk = (K + 63) / 64, ntiles = trow * tk;
+  const int64_t trow = rt.count, tk = (K + 63) / 64, ntiles = trow * tk;
   float m = 0.0f;
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int64_t r0 = (tile % trow) * 32, k0 = (tile / trow) * 64;
+    const int64_t k0 = (tile / trow) * 64;
     __syncthreads();  // previous tile's table reads done
-    if (t < 32) sr[t] = (r0 + t < rows) ? (AFFINE ? (r0 + t) * rs : rowOff[r0 + t]) : -1;
+    if (t < 32) {
+      const int64_t r = rt.row(tile % trow, t);
+      sr[t] = (r >= 0 && r < rows) ? (AFFINE ? r * rs : rowOff[r]) : -1;
+    }
     else if (t < 96) sk[t - 32] = (k0 + t - 32 < K) ? (AFFINE ? (k0 + t - 32) * ks : kOff[k0 + t - 32]) : -1;
     __syncthreads();
     double x[8];
@@ -736,13 +763,17 @@ __global__ void __launch_bounds__(256) pack_split_kernel(
     const double *__restrict__ src, const int64_t *__restrict__ rowOff, int64_t rows,
     const int64_t *__restrict__ kOff, int64_t K, int unitK, uint16_t *__restrict__ dst,
     int64_t Kpad, const unsigned *__restrict__ maxbits, double *__restrict__ scale_out,
-    int negate, int64_t rs, int64_t ks) {
+    int negate, int64_t rs, int64_t ks, const RowTiles rt) {
   __shared__ double tile[32][65];
-  __shared__ int64_t sr[32], sk[64];
+  __shared__ int64_t sr[32], sk[64], srow[32];
   const int t = threadIdx.x;
-  // row blocks on grid.x (up to 2^31 - 1), K blocks on grid.y (<= 65535)
-  const int64_t r0 = (int64_t)blockIdx.x * 32, k0 = (int64_t)blockIdx.y * 64;
-  if (t < 32) sr[t] = (r0 + t < rows) ? (AFFINE ? (r0 + t) * rs : rowOff[r0 + t]) : -1;
+  // row tiles on grid.x (up to 2^31 - 1), K blocks on grid.y (<= 65535)
+  const int64_t k0 = (int64_t)blockIdx.y * 64;
+  if (t < 32) {
+    const int64_t r = rt.row(blockIdx.x, t);
+    srow[t] = (r >= 0 && r < rows) ? r : -1;
+    sr[t] = srow[t] >= 0 ? (AFFINE ? r * rs : rowOff[r]) : -1;
+  }
   else if (t < 96) sk[t - 32] = (k0 + t - 32 < K) ? (AFFINE ? (k0 + t - 32) * ks : kOff[k0 + t - 32]) : -1;
   double s = 1.0;
   if (F16) {
@@ -789,7 +820,9 @@ __global__ void __launch_bounds__(256) pack_split_kernel(
       lo[j] = __bfloat16_as_ushort(__float2bfloat16_rn(xf - __bfloat162float(h)));
     }
   }
-  const int64_t base = (r0 + rr) * 2 * Kpad + k0 + ch * 8;
+  const int64_t r = srow[rr];
+  if (r < 0) return;  // past the label's extent (padding rows are cleared by the host)
+  const int64_t base = r * 2 * Kpad + k0 + ch * 8;
   *reinterpret_cast<uint4 *>(dst + base) = *reinterpret_cast<const uint4 *>(hi);
   *reinterpret_cast<uint4 *>(dst + base + Kpad) = *reinterpret_cast<const uint4 *>(lo);
 }
@@ -1023,16 +1056,24 @@ bool TcEngine::worth_it(const EinsumPlan &pl) {
 
 namespace {
 // Persistent grid of maxabs_kernel: at most 8 blocks an SM, at least one tile each.
-unsigned maxabs_blocks(int64_t rows, int64_t K) {
-  const int64_t tiles = ceil_div(std::max<int64_t>(rows, 1), 32) * ceil_div(std::max<int64_t>(K, 1), 64);
+unsigned maxabs_blocks(const RowTiles &rt, int64_t K) {
+  const int64_t tiles = rt.count * ceil_div(std::max<int64_t>(K, 1), 64);
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>(tiles, 8 * kNumSMs));
+}
+
+// Rows [rows, rows_pad) of a packed operand are zero.
+void clear_pad_rows(uint16_t *dst, int64_t rows, int64_t rows_pad, int64_t Kpad, cudaStream_t s) {
+  if (rows_pad > rows)
+    SCESS_CUDA(cudaMemsetAsync(dst + rows * 2 * Kpad, 0,
+                               (size_t)(rows_pad - rows) * 2 * Kpad * sizeof(uint16_t), s));
 }
 }  // namespace
 
 void TcEngine::pack(const double *src, const int64_t *rowOff, int64_t rows, const int64_t *kOff,
                     int64_t K, bool unitK, int64_t row_align, Packed &out, int64_t rs,
-                    int64_t ks) {
+                    int64_t ks, int64_t rP, int64_t rE, bool dense) {
   const bool aff = rs >= 0 && ks >= 0;
+  const RowTiles rt = RowTiles::make(rows, rP, rE > 0 ? rE : rows);
   const int64_t Kpad = round_up(std::max<int64_t>(K, 1), TC_BK);
   const int64_t rows_pad = round_up(std::max<int64_t>(rows, 1), std::max<int64_t>(row_align, 32));
   const size_t bytes = (size_t)rows_pad * 2 * Kpad * sizeof(uint16_t);
@@ -1050,40 +1091,41 @@ void TcEngine::pack(const double *src, const int64_t *rowOff, int64_t rows, cons
                 (double)rows * K * 8 + (double)rows_pad * Kpad * 4, ctx_.stream);
   unsigned *maxbits = out.aux.as<unsigned>();
   double *scale = reinterpret_cast<double *>(out.aux.as<char>() + 8);
-  if (Kpad / 64 > 65535 || rows_pad / 32 > INT32_MAX) throw Error(SCESS_ERR_INVALID, "pack: too large");
-  dim3 grid((unsigned)(rows_pad / 32), (unsigned)(Kpad / 64));
+  if (Kpad / 64 > 65535 || rt.count > INT32_MAX) throw Error(SCESS_ERR_INVALID, "pack: too large");
+  dim3 grid((unsigned)rt.count, (unsigned)(Kpad / 64));
   uint16_t *dst = out.mem.as<uint16_t>();
+  clear_pad_rows(dst, rows, rows_pad, Kpad, ctx_.stream);
   const int u = unitK ? 1 : 0;
   if (fmt_ == TcFormat::FP16) {
     SCESS_CUDA(cudaMemsetAsync(maxbits, 0, sizeof(unsigned), ctx_.stream));
     const int64_t n = rows * K;
-    if (aff && ((rs == 1 && ks == rows) || (ks == 1 && rs == K))) {  // the gather is src[0, n)
+    if (dense || (aff && ((rs == 1 && ks == rows) || (ks == 1 && rs == K)))) {  // the gather is src[0, n)
       const unsigned blocks =
           (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256 * 8), 8 * kNumSMs));
       maxabs_flat_kernel<<<blocks, 256, 0, ctx_.stream>>>(src, n, maxbits);
     } else if (aff) {
-      maxabs_kernel<true><<<maxabs_blocks(rows, K), 256, 0, ctx_.stream>>>(src, nullptr, rows, nullptr,
-                                                                          K, u, maxbits, rs, ks);
+      maxabs_kernel<true><<<maxabs_blocks(rt, K), 256, 0, ctx_.stream>>>(src, nullptr, rows, nullptr,
+                                                                        K, u, maxbits, rs, ks, rt);
     } else {
-      maxabs_kernel<false><<<maxabs_blocks(rows, K), 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K,
-                                                                           u, maxbits, 0, 0);
+      maxabs_kernel<false><<<maxabs_blocks(rt, K), 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K,
+                                                                         u, maxbits, 0, 0, rt);
     }
     SCESS_CHECK_LAUNCH();
     if (aff)
       pack_split_kernel<true, true><<<grid, 256, 0, ctx_.stream>>>(src, nullptr, rows, nullptr, K, u, dst,
-                                                                   Kpad, maxbits, scale, 0, rs, ks);
+                                                                   Kpad, maxbits, scale, 0, rs, ks, rt);
     else
       pack_split_kernel<true, false><<<grid, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, u, dst,
-                                                                    Kpad, maxbits, scale, 0, 0, 0);
+                                                                    Kpad, maxbits, scale, 0, 0, 0, rt);
   } else {
     const double one = 1.0;
     SCESS_CUDA(cudaMemcpyAsync(scale, &one, sizeof(double), cudaMemcpyHostToDevice, ctx_.stream));
     if (aff)
       pack_split_kernel<false, true><<<grid, 256, 0, ctx_.stream>>>(src, nullptr, rows, nullptr, K, u, dst,
-                                                                    Kpad, maxbits, scale, 0, rs, ks);
+                                                                    Kpad, maxbits, scale, 0, rs, ks, rt);
     else
       pack_split_kernel<false, false><<<grid, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, u, dst,
-                                                                     Kpad, maxbits, scale, 0, 0, 0);
+                                                                     Kpad, maxbits, scale, 0, 0, 0, rt);
   }
   SCESS_CHECK_LAUNCH();
 }
@@ -1091,8 +1133,9 @@ void TcEngine::pack(const double *src, const int64_t *rowOff, int64_t rows, cons
 void TcEngine::maxabs_into(const double *src, const int64_t *rowOff, int64_t rows,
                            const int64_t *kOff, int64_t K, bool unitK, unsigned *maxbits) {
   if (rows <= 0 || K <= 0) return;
-  maxabs_kernel<false><<<maxabs_blocks(rows, K), 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K,
-                                                                       unitK ? 1 : 0, maxbits, 0, 0);
+  const RowTiles rt = RowTiles::make(rows, 1, rows);
+  maxabs_kernel<false><<<maxabs_blocks(rt, K), 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K,
+                                                                     unitK ? 1 : 0, maxbits, 0, 0, rt);
   SCESS_CHECK_LAUNCH();
 }
 
@@ -1115,18 +1158,20 @@ void TcEngine::pack_with_max(const double *src, const int64_t *rowOff, int64_t r
   TimedScope ts(ctx_.timer, "pack_split", 0.0,
                 (double)rows * K * 8 + (double)rows_pad * Kpad * 4, ctx_.stream);
   double *scale = reinterpret_cast<double *>(out.aux.as<char>() + 8);
-  if (Kpad / 64 > 65535 || rows_pad / 32 > INT32_MAX) throw Error(SCESS_ERR_INVALID, "pack: too large");
-  dim3 grid((unsigned)(rows_pad / 32), (unsigned)(Kpad / 64));
+  const RowTiles rt = RowTiles::make(rows, 1, rows);
+  if (Kpad / 64 > 65535 || rt.count > INT32_MAX) throw Error(SCESS_ERR_INVALID, "pack: too large");
+  dim3 grid((unsigned)rt.count, (unsigned)(Kpad / 64));
+  clear_pad_rows(out.mem.as<uint16_t>(), rows, rows_pad, Kpad, ctx_.stream);
   if (fmt_ == TcFormat::FP16) {
     pack_split_kernel<true, false><<<grid, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, unitK ? 1 : 0,
                                                                   out.mem.as<uint16_t>(), Kpad, maxbits,
-                                                                  scale, negate ? 1 : 0, 0, 0);
+                                                                  scale, negate ? 1 : 0, 0, 0, rt);
   } else {
     const double one = 1.0;
     SCESS_CUDA(cudaMemcpyAsync(scale, &one, sizeof(double), cudaMemcpyHostToDevice, ctx_.stream));
     pack_split_kernel<false, false><<<grid, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, unitK ? 1 : 0,
                                                                    out.mem.as<uint16_t>(), Kpad, maxbits,
-                                                                   scale, negate ? 1 : 0, 0, 0);
+                                                                   scale, negate ? 1 : 0, 0, 0, rt);
   }
   SCESS_CHECK_LAUNCH();
 }
@@ -1192,28 +1237,33 @@ void TcEngine::contract(const EinsumPlan &pl, double alpha, const double *A, con
   const bool uX = swap ? pl.bUnitK : pl.aUnitK, uY = swap ? pl.aUnitK : pl.bUnitK;
   const int64_t MX = swap ? pl.N : pl.M, NY = swap ? pl.M : pl.N;
 
-  const int64_t rsX = swap ? pl.bColStride : pl.aRowStride, ksX = swap ? pl.bKStride : pl.aKStride;
-  const int64_t rsY = swap ? pl.aRowStride : pl.bColStride, ksY = swap ? pl.aKStride : pl.bKStride;
+  struct Hint {
+    int64_t rs, ks, P, E;
+    bool dense;
+  };
+  const Hint hA{pl.aRowStride, pl.aKStride, pl.aRowP, pl.aRowE, pl.aDense};
+  const Hint hB{pl.bColStride, pl.bKStride, pl.bColP, pl.bColE, pl.bDense};
+  const Hint &hX = swap ? hB : hA, &hY = swap ? hA : hB;
   auto get = [&](const double *src, const int64_t *rows, int64_t nrows, const int64_t *ks,
-                 bool unitK, bool isConst, const char *tag, Packed &tmp, int64_t rstr,
-                 int64_t kstr) -> const Packed & {
+                 bool unitK, bool isConst, const char *tag, Packed &tmp,
+                 const Hint &h) -> const Packed & {
     if (!isConst) {
-      pack(src, rows, nrows, ks, pl.K, unitK, TC_BM, tmp, rstr, kstr);
+      pack(src, rows, nrows, ks, pl.K, unitK, TC_BM, tmp, h.rs, h.ks, h.P, h.E, h.dense);
       return tmp;
     }
     std::string key = pl.key + tag + std::to_string((uintptr_t)src);
     auto it = cache_.find(key);
     if (it != cache_.end() && it->second.first == owner_) return *it->second.second;
     auto pk = std::make_unique<Packed>();
-    pack(src, rows, nrows, ks, pl.K, unitK, TC_BM, *pk, rstr, kstr);
+    pack(src, rows, nrows, ks, pl.K, unitK, TC_BM, *pk, h.rs, h.ks, h.P, h.E, h.dense);
     auto &ref = *pk;
     cache_[key] = std::make_pair(owner_, std::move(pk));
     return ref;
   };
   const std::string tname = "tc_gemm[" + pl.spec + "]";
   timer_name_ = tname.c_str();
-  const Packed &PX = get(X, rowX, MX, kX, uX, cX, swap ? "#B" : "#A", tmpA_, rsX, ksX);
-  const Packed &PY = get(Y, rowY, NY, kY, uY, cY, swap ? "#A" : "#B", tmpB_, rsY, ksY);
+  const Packed &PX = get(X, rowX, MX, kX, uX, cX, swap ? "#B" : "#A", tmpA_, hX);
+  const Packed &PY = get(Y, rowY, NY, kY, uY, cY, swap ? "#A" : "#B", tmpB_, hY);
   TcOut o;
   o.C = C;
   o.fp32 = 0;

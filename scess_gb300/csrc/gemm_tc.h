@@ -99,10 +99,12 @@ class TcEngine {
   // Pack rows x K values src[rowOff[r] + kOff[k]] into `out` (rows padded to a
   // multiple of `row_align`, K to a multiple of 64).  unitK: the source is
   // contiguous along k (load-coalescing hint).  rs, ks >= 0: the tables are
-  // rowOff[r] = r rs, kOff[k] = k ks (they are then not read).
+  // rowOff[r] = r rs, kOff[k] = k ks (they are then not read).  rP, rE: tiles
+  // take 32 rows r = pre + rP (f + rE post) along one label of the row group
+  // (rE = 0: consecutive rows).  dense: the gather visits src[0, rows K) once.
   void pack(const double *src, const int64_t *rowOff, int64_t rows, const int64_t *kOff,
             int64_t K, bool unitK, int64_t row_align, Packed &out, int64_t rs = -1,
-            int64_t ks = -1);
+            int64_t ks = -1, int64_t rP = 1, int64_t rE = 0, bool dense = false);
   // max|x| over the same gather, folded into *maxbits (float bits, atomic max:
   // several calls into one word give the max over all their tensors).
   void maxabs_into(const double *src, const int64_t *rowOff, int64_t rows, const int64_t *kOff,
