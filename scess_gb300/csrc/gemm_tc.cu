@@ -495,19 +495,13 @@ __global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
           const int rsub = lane / CH;
           constexpr int RSTEP = 32 / CH;
           const int64_t co = colH[j0 + cl];
-          if (a.stream_out) {
 #pragma unroll 4
-            for (int rr = 0; rr < 32; rr += RSTEP) {
-              const int r = 32 * q + rr + rsub;
-              const int64_t ro = rowOffS[h][r];
-              if (ro >= 0 && co >= 0) __stcs(C + ro + co, stage[h][cl][r]);
-            }
-          } else {
-#pragma unroll 4
-            for (int rr = 0; rr < 32; rr += RSTEP) {
-              const int r = 32 * q + rr + rsub;
-              const int64_t ro = rowOffS[h][r];
-              if (ro >= 0 && co >= 0) C[ro + co] = stage[h][cl][r];
+          for (int rr = 0; rr < 32; rr += RSTEP) {
+            const int r = 32 * q + rr + rsub;
+            const int64_t ro = rowOffS[h][r];
+            if (ro >= 0 && co >= 0) {
+              if (a.stream_out) __stcs(C + ro + co, stage[h][cl][r]);
+              else C[ro + co] = stage[h][cl][r];
             }
           }
         }
@@ -537,17 +531,14 @@ __global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
             const int64_t co = colH[j];
             if (co >= 0) atomicAdd(C + rowOff + co, fa * acc[j]);
           }
-        } else if (out.beta == 0.0 && a.stream_out) {
-#pragma unroll
-          for (int j = 0; j < HC; j++) {
-            const int64_t co = colH[j];
-            if (co >= 0) __stcs(C + rowOff + co, fa * acc[j]);
-          }
         } else if (out.beta == 0.0) {
 #pragma unroll
           for (int j = 0; j < HC; j++) {
             const int64_t co = colH[j];
-            if (co >= 0) C[rowOff + co] = fa * acc[j];
+            if (co >= 0) {
+              if (a.stream_out) __stcs(C + rowOff + co, fa * acc[j]);
+              else C[rowOff + co] = fa * acc[j];
+            }
           }
         } else {
 #pragma unroll
