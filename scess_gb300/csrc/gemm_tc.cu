@@ -146,7 +146,6 @@ struct TcArgs {
   int64_t cg[3];
   const int64_t *rowCg[3], *colCg[3];  // per-group output tables (null: TcOut's)
   int stcol[3];                        // group stores along columns (FP32, beta = 0)
-  int stream_out;                      // FP32 beta = 0 stores with the evict-first hint
   float *partial;    // split-K partials (nullptr: direct epilogue)
   int64_t part_stride;
   unsigned *err;
@@ -499,10 +498,7 @@ __global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
           for (int rr = 0; rr < 32; rr += RSTEP) {
             const int r = 32 * q + rr + rsub;
             const int64_t ro = rowOffS[h][r];
-            if (ro >= 0 && co >= 0) {
-              if (a.stream_out) __stcs(C + ro + co, stage[h][cl][r]);
-              else C[ro + co] = stage[h][cl][r];
-            }
+            if (ro >= 0 && co >= 0) C[ro + co] = stage[h][cl][r];
           }
         }
         continue;
@@ -535,10 +531,7 @@ __global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
 #pragma unroll
           for (int j = 0; j < HC; j++) {
             const int64_t co = colH[j];
-            if (co >= 0) {
-              if (a.stream_out) __stcs(C + rowOff + co, fa * acc[j]);
-              else C[rowOff + co] = fa * acc[j];
-            }
+            if (co >= 0) C[rowOff + co] = fa * acc[j];
           }
         } else {
 #pragma unroll
@@ -969,7 +962,6 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
   a.f16 = fmt == TcFormat::FP16 ? 1 : 0;
   a.split3 = nseg == 3 ? 1 : 0;
   a.kbd = (ps.kbd == 2 || ps.kbd == 4) ? ps.kbd : 1;
-  a.stream_out = ps.stream_out ? 1 : 0;
   a.cy = ps.cy;
   a.cz = ps.cz;
   for (int q = 0; q < 3; q++) {

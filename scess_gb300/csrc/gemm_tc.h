@@ -85,9 +85,6 @@ struct TcProblemSet {
   // group g writes along columns (lanes over columns, through shared memory):
   // for FP32 outputs with beta = 0 whose unit-stride index is a column index
   bool store_by_column[3] = {false, false, false};
-  // FP32 beta = 0 outputs stored with the streaming (evict-first) cache hint:
-  // for outputs read once, later, by another kernel
-  bool stream_out = false;
 };
 
 class TcEngine {

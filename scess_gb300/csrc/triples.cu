@@ -804,9 +804,6 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   int tbn = 256;
   if (const char *env = std::getenv("SCESS_T_BN")) tbn = std::atoi(env) == 128 ? 128 : 256;
   const int tbk = TcEngine::k_block(tbn);
-  // W stores with the evict-first hint (SCESS_T_STREAM_W=0 turns it off)
-  bool stream_w = true;
-  if (const char *env = std::getenv("SCESS_T_STREAM_W")) stream_w = std::atoi(env) != 0;
   CUtensorMap mP{}, mQ{}, mQ2{}, mR{}, mR2{}, mTx{};
   DevTables gdt;  // W_g row / column tables
   DevMem Sf;  // (ia|jb) as FP32 for the energy kernel (padded rows)
@@ -916,7 +913,6 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
             if (kb == 1 || kb == 2 || kb == 4) ps.kbd = kb;
           }
           ps.bn = tbn;
-          ps.stream_out = stream_w;
           ps.bk = tbk;
           ps.cy = nb * nb * o3p;
           ps.cz = nb * o3p;
