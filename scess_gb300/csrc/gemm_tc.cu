@@ -146,6 +146,7 @@ struct TcArgs {
   int64_t cg[3];
   const int64_t *rowCg[3], *colCg[3];  // per-group output tables (null: TcOut's)
   int stcol[3];                        // group stores along columns (FP32, beta = 0)
+  int stvec[3];                        // ... in contiguous aligned quads of columns
   float *partial;    // split-K partials (nullptr: direct epilogue)
   int64_t part_stride;
   unsigned *err;
@@ -489,16 +490,43 @@ __global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
 #pragma unroll
           for (int jj = 0; jj < CH; jj++) stage[h][jj][row] = fa * acc[j0 + jj];
           __syncwarp();
-          // lanes take column lane % CH of row rr + lane / CH (CH = 16: two rows a step)
-          const int cl = lane % CH;
-          const int rsub = lane / CH;
-          constexpr int RSTEP = 32 / CH;
-          const int64_t co = colH[j0 + cl];
+          if (BN == 256 && a.stvec[pg]) {  // (the (T) launch; einsums keep the scalar form)
+            // every aligned quad of columns is a contiguous 16-byte run: lanes
+            // take quad lane % QPR of row rr + lane / QPR (conflict-free reads:
+            // the staging pitch is 2 mod 32 words)
+            constexpr int QPR = CH / 4, RSTEP4 = 32 / QPR;
+            const int cq = lane % QPR, rsub4 = lane / QPR;
+            const int64_t co = colH[j0 + 4 * cq];
+#pragma unroll
+            for (int rr = 0; rr < 32; rr += RSTEP4) {
+              const int r = 32 * q + rr + rsub4;
+              const int64_t ro = rowOffS[h][r];
+              if (ro >= 0 && co >= 0) {
+                const float v0 = stage[h][4 * cq][r], v1 = stage[h][4 * cq + 1][r];
+                const float v2 = stage[h][4 * cq + 2][r], v3 = stage[h][4 * cq + 3][r];
+                float *d = C + ro + co;
+                if (((uintptr_t)d & 15) == 0) {
+                  *reinterpret_cast<float4 *>(d) = make_float4(v0, v1, v2, v3);
+                } else {  // (not expected: the host asks for quads only when aligned)
+                  d[0] = v0;
+                  d[1] = v1;
+                  d[2] = v2;
+                  d[3] = v3;
+                }
+              }
+            }
+          } else {
+            // lanes take column lane % CH of row rr + lane / CH (CH = 16: two rows a step)
+            const int cl = lane % CH;
+            const int rsub = lane / CH;
+            constexpr int RSTEP = 32 / CH;
+            const int64_t co = colH[j0 + cl];
 #pragma unroll 4
-          for (int rr = 0; rr < 32; rr += RSTEP) {
-            const int r = 32 * q + rr + rsub;
-            const int64_t ro = rowOffS[h][r];
-            if (ro >= 0 && co >= 0) C[ro + co] = stage[h][cl][r];
+            for (int rr = 0; rr < 32; rr += RSTEP) {
+              const int r = 32 * q + rr + rsub;
+              const int64_t ro = rowOffS[h][r];
+              if (ro >= 0 && co >= 0) C[ro + co] = stage[h][cl][r];
+            }
           }
         }
         continue;
@@ -969,6 +997,7 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
     a.rowCg[q] = ps.rowC[q];
     a.colCg[q] = ps.colC[q];
     a.stcol[q] = ps.store_by_column[q] ? 1 : 0;
+    a.stvec[q] = ps.store_by_column[q] && ps.store_quads[q] ? 1 : 0;
   }
   a.partial = splits > 1 ? partial : nullptr;
   a.part_stride = ps.M * ps.N;

@@ -85,6 +85,9 @@ struct TcProblemSet {
   // group g writes along columns (lanes over columns, through shared memory):
   // for FP32 outputs with beta = 0 whose unit-stride index is a column index
   bool store_by_column[3] = {false, false, false};
+  // ... and every aligned quad of columns (4 c .. 4 c + 3) goes to 4 contiguous
+  // floats at a 16-byte aligned address (vector stores)
+  bool store_quads[3] = {false, false, false};
 };
 
 class TcEngine {

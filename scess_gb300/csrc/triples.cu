@@ -944,6 +944,9 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
             ps.rowC[g] = gdt.ptr[2 * g];
             ps.colC[g] = gdt.ptr[2 * g + 1];
             ps.store_by_column[g] = g > 0;  // i is a column index of groups 1 and 2
+            // columns (i, t) with i fastest: quads of i are contiguous and, with
+            // o % 4 == 0 (o2p, o3p too), 16-byte aligned
+            ps.store_quads[g] = g > 0 && o % 4 == 0;
           }
           out.alpha = 1.0;
           out.beta = 0.0;
