@@ -850,7 +850,6 @@ __global__ void __launch_bounds__(256) pack_split_kernel(
   }
   const int64_t r = srow[rr];
   if (r < 0) return;  // past the label's extent (padding rows are cleared by the host)
-  if (k0 + ch * 8 >= Kpad) return;  // Kpad a multiple of 32: the tile's last 32 columns are past it
   const int64_t base = r * 2 * Kpad + k0 + ch * 8;
   *reinterpret_cast<uint4 *>(dst + base) = *reinterpret_cast<const uint4 *>(hi);
   *reinterpret_cast<uint4 *>(dst + base + Kpad) = *reinterpret_cast<const uint4 *>(lo);
@@ -901,12 +900,12 @@ CUtensorMap TcEngine::map_of(const Packed &p, int box_rows, int bk) {
   return make_map(p.p(), p.rows_pad, p.Kpad, box_rows, bk, p.fmt);
 }
 
-// K block of the 256-wide kernel: 32 (4 stages; operands may then be packed
-// with K padded to 32), or 64 (2 stages) with SCESS_TC_BK256=64.
+// K block of the 256-wide kernel: 64 (2 stages), or 32 (4 stages) with
+// SCESS_TC_BK256=32.
 int TcEngine::k_block(int bn) {
   static const int bk256 = [] {
     const char *e = std::getenv("SCESS_TC_BK256");
-    return (e && std::atoi(e) == 64) ? 64 : 32;
+    return (e && std::atoi(e) == 32) ? 32 : 64;
   }();
   return bn == 256 ? bk256 : 64;
 }
@@ -954,8 +953,8 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
   int kbt = 0;
   for (int s = 0; s < ps.nseg; s++) {
     const TcSegment &g = ps.seg[s];
-    if (g.Kpad % bk != 0 || g.Kpad <= 0 || 2 * g.Kpad > INT32_MAX)
-      throw Error(SCESS_ERR_INVALID, "tc_gemm: segment K not a multiple of the K block");
+    if (g.Kpad % TC_BK != 0 || g.Kpad <= 0 || 2 * g.Kpad > INT32_MAX)
+      throw Error(SCESS_ERR_INVALID, "tc_gemm: Kpad % 64");
     for (int q = 0; q < ps.ng; q++) {
       const int64_t maxA = g.rowA0[q] + (int64_t)(ps.ny - 1) * g.rowAy[q] +
                            (int64_t)(ps.nz - 1) * g.rowAz[q] + a.tiles_m * TC_BM;
@@ -990,7 +989,7 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
   a.splits = splits;
   a.f16 = fmt == TcFormat::FP16 ? 1 : 0;
   a.split3 = nseg == 3 ? 1 : 0;
-  a.kbd = (ps.kbd == 2 || ps.kbd == 4 || ps.kbd == 8) ? ps.kbd : 1;
+  a.kbd = (ps.kbd == 2 || ps.kbd == 4) ? ps.kbd : 1;
   a.cy = ps.cy;
   a.cz = ps.cz;
   for (int q = 0; q < 3; q++) {
@@ -1171,9 +1170,8 @@ void TcEngine::maxabs_into(const double *src, const int64_t *rowOff, int64_t row
 
 void TcEngine::pack_with_max(const double *src, const int64_t *rowOff, int64_t rows,
                              const int64_t *kOff, int64_t K, bool unitK, int64_t row_align,
-                             const unsigned *maxbits, bool negate, Packed &out, int64_t k_align) {
-  if (k_align != 32 && k_align != 64) throw Error(SCESS_ERR_INVALID, "pack: K alignment");
-  const int64_t Kpad = round_up(std::max<int64_t>(K, 1), k_align);
+                             const unsigned *maxbits, bool negate, Packed &out) {
+  const int64_t Kpad = round_up(std::max<int64_t>(K, 1), TC_BK);
   const int64_t rows_pad = round_up(std::max<int64_t>(rows, 1), std::max<int64_t>(row_align, 32));
   const size_t bytes = (size_t)rows_pad * 2 * Kpad * sizeof(uint16_t);
   if (out.mem.bytes() < bytes || !out.aux.bytes()) {
@@ -1190,8 +1188,8 @@ void TcEngine::pack_with_max(const double *src, const int64_t *rowOff, int64_t r
                 (double)rows * K * 8 + (double)rows_pad * Kpad * 4, ctx_.stream);
   double *scale = reinterpret_cast<double *>(out.aux.as<char>() + 8);
   const RowTiles rt = RowTiles::make(rows, 1, rows);
-  if (ceil_div(Kpad, 64) > 65535 || rt.count > INT32_MAX) throw Error(SCESS_ERR_INVALID, "pack: too large");
-  dim3 grid((unsigned)rt.count, (unsigned)ceil_div(Kpad, 64));
+  if (Kpad / 64 > 65535 || rt.count > INT32_MAX) throw Error(SCESS_ERR_INVALID, "pack: too large");
+  dim3 grid((unsigned)rt.count, (unsigned)(Kpad / 64));
   clear_pad_rows(out.mem.as<uint16_t>(), rows, rows_pad, Kpad, ctx_.stream);
   if (fmt_ == TcFormat::FP16) {
     pack_split_kernel<true, false><<<grid, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, unitK ? 1 : 0,

@@ -114,11 +114,9 @@ class TcEngine {
                    int64_t K, bool unitK, unsigned *maxbits);
   // pack() with the FP16 scale taken from a given max word (so that several
   // packs share one scale), optionally negating the values (exact).
-  // K is padded to a multiple of k_align (64, or 32 for operands of the
-  // 256-wide kernel with 32-wide K blocks).
   void pack_with_max(const double *src, const int64_t *rowOff, int64_t rows, const int64_t *kOff,
                      int64_t K, bool unitK, int64_t row_align, const unsigned *maxbits,
-                     bool negate, Packed &out, int64_t k_align = 64);
+                     bool negate, Packed &out);
   TcFormat format() const { return fmt_; }
   // D(m, n) = sum_k A(rowA0 + m, k) B(rowB0 + n, k) for m < M, n < N, written
   // through `out`.  nseg = 3 (split hi/lo) or 1 (hi only, BF16 accuracy).

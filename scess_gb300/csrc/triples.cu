@@ -834,12 +834,12 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
     tc.maxabs_into(T2p.p(), pdt.ptr[3], o * vp * vp, dt.ptr[kOperand + 7], o, true, mx);
     tc.maxabs_into(Qt.p(), pdt.ptr[1], o2 * vp, dt.ptr[kOperand + 3], v, true, mx + 1);
     tc.maxabs_into(Rt.p(), pdt.ptr[2], o2 * vp, dt.ptr[kOperand + 5], o, false, mx + 1);
-    tc.pack_with_max(P.p(), pdt.ptr[0], o * vp * vp, dt.ptr[kOperand + 1], v, false, 128, mx, false, pP, tbk);
-    tc.pack_with_max(T2p.p(), pdt.ptr[3], o * vp * vp, dt.ptr[kOperand + 7], o, true, 128, mx, true, pTx, tbk);
-    tc.pack_with_max(Qt.p(), pdt.ptr[1], o2 * vp, dt.ptr[kOperand + 3], v, true, 128, mx + 1, false, pQ, tbk);
-    tc.pack_with_max(Qt.p(), pdt.ptr[4], o2 * vp, dt.ptr[kOperand + 3], v, true, 128, mx + 1, false, pQ2, tbk);
-    tc.pack_with_max(Rt.p(), pdt.ptr[2], o2 * vp, dt.ptr[kOperand + 5], o, false, 128, mx + 1, false, pR, tbk);
-    tc.pack_with_max(Rt.p(), pdt.ptr[5], o2 * vp, dt.ptr[kOperand + 5], o, false, 128, mx + 1, false, pR2, tbk);
+    tc.pack_with_max(P.p(), pdt.ptr[0], o * vp * vp, dt.ptr[kOperand + 1], v, false, 128, mx, false, pP);
+    tc.pack_with_max(T2p.p(), pdt.ptr[3], o * vp * vp, dt.ptr[kOperand + 7], o, true, 128, mx, true, pTx);
+    tc.pack_with_max(Qt.p(), pdt.ptr[1], o2 * vp, dt.ptr[kOperand + 3], v, true, 128, mx + 1, false, pQ);
+    tc.pack_with_max(Qt.p(), pdt.ptr[4], o2 * vp, dt.ptr[kOperand + 3], v, true, 128, mx + 1, false, pQ2);
+    tc.pack_with_max(Rt.p(), pdt.ptr[2], o2 * vp, dt.ptr[kOperand + 5], o, false, 128, mx + 1, false, pR);
+    tc.pack_with_max(Rt.p(), pdt.ptr[5], o2 * vp, dt.ptr[kOperand + 5], o, false, 128, mx + 1, false, pR2);
     ctx.sync();
     // B side (Q, R rows): tiles of tbn columns; 256 halves the A-operand
     // shared-memory traffic per FLOP (SCESS_T_BN=128 selects the narrow tiles).
@@ -906,13 +906,11 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
           // relative to FP64 with a drain per 64 / 128 / 256 K.  One per 256 K
           // (two per tile at this K) lets a tile's stores overlap the whole
           // next tile's MMAs (each TMEM buffer then holds half a tile).
-          // SCESS_T_KBD sets the K blocks (of 64) per drain: 1, 2 or 4.  The
-          // operands are packed with K padded to the kernel's K block (32 by
-          // default): the t2.R segments (K = o) then waste less than with 64.
-          ps.kbd = 256 / tbk;
+          // SCESS_T_KBD sets the K blocks (of 64) per drain: 1, 2 or 4.
+          ps.kbd = 256 / TcEngine::k_block(tbn);
           if (const char *env = std::getenv("SCESS_T_KBD")) {
             const int kb = std::atoi(env);
-            if (kb == 1 || kb == 2 || kb == 4) ps.kbd = kb * 64 / tbk;
+            if (kb == 1 || kb == 2 || kb == 4) ps.kbd = kb;
           }
           ps.bn = tbn;
           ps.bk = tbk;
