@@ -434,8 +434,10 @@ void scess_rccsd_state_destroy(scess_rccsd_state *state) {
   if (state->impl) {
     cudaSetDevice(state->ctx->impl->device);
     cudaStreamSynchronize(state->ctx->impl->stream);
+    const auto t0 = std::chrono::steady_clock::now();
     if (state->ctx->impl->tc) state->ctx->impl->tc->clear_cache(state->impl);
     delete state->impl;
+    state->ctx->impl->timer.host("state_destroy", ms_since(t0));
   }
   delete state;
 }
@@ -488,7 +490,11 @@ int scess_rccsd_state_triples(scess_rccsd_state *state, int32_t precision, doubl
 
 int scess_rccsd_state_amplitudes(scess_rccsd_state *state, double *t1_out, double *t2_out) {
   if (!state || !state->impl) return SCESS_ERR_INVALID;
-  return guard(state->ctx, [&](scess::Ctx &) { state->impl->get_amplitudes(t1_out, t2_out); });
+  return guard(state->ctx, [&](scess::Ctx &c) {
+    const auto t0 = std::chrono::steady_clock::now();
+    state->impl->get_amplitudes(t1_out, t2_out);
+    c.timer.host("amplitudes_download", ms_since(t0));
+  });
 }
 
 int scess_rccsd_state_set_amplitudes(scess_rccsd_state *state, const double *t1,
