@@ -28,6 +28,7 @@ template <class F>
 int guard(scess_ctx *ctx, F &&f) {
   if (!ctx || !ctx->impl) return SCESS_ERR_INVALID;
   int code = SCESS_OK;
+  scess::CurrentCtx cur(ctx->impl);  // device blocks released during the call are cached
   try {
     SCESS_CUDA(cudaSetDevice(ctx->impl->device));
     f(*ctx->impl);
@@ -435,6 +436,7 @@ void scess_rccsd_state_destroy(scess_rccsd_state *state) {
     cudaSetDevice(state->ctx->impl->device);
     cudaStreamSynchronize(state->ctx->impl->stream);
     const auto t0 = std::chrono::steady_clock::now();
+    scess::CurrentCtx cur(state->ctx->impl);  // the state's blocks go to its context's cache
     if (state->ctx->impl->tc) state->ctx->impl->tc->clear_cache(state->impl);
     delete state->impl;
     state->ctx->impl->timer.host("state_destroy", ms_since(t0));

@@ -10,10 +10,55 @@ namespace scess {
 
 std::atomic<long long> g_launches{0};
 
+namespace {
+thread_local Ctx *t_ctx = nullptr;
+}
+
+Ctx *current_ctx() { return t_ctx; }
+CurrentCtx::CurrentCtx(Ctx *c) : prev(t_ctx) { t_ctx = c; }
+CurrentCtx::~CurrentCtx() { t_ctx = prev; }
+
+void *BlockCache::take(size_t bytes) {
+  auto it = free_.find(bytes);
+  if (it == free_.end()) return nullptr;
+  void *p = it->second;
+  free_.erase(it);
+  total_ -= bytes;
+  return p;
+}
+
+bool BlockCache::give(void *p, size_t bytes) {
+  if (bytes < kMinBytes || total_ + bytes > kMaxCached) return false;
+  free_.emplace(bytes, p);
+  total_ += bytes;
+  return true;
+}
+
+void BlockCache::flush() {
+  for (auto &kv : free_) cudaFree(kv.second);
+  free_.clear();
+  total_ = 0;
+}
+
 void DevMem::alloc(size_t bytes) {
   release();
   if (bytes == 0) return;
+  Ctx *c = current_ctx();
+  if (c && bytes >= BlockCache::kMinBytes) {
+    if (void *p = c->blocks.take(bytes)) {
+      p_ = p;
+      bytes_ = bytes;
+      owner_ = c;
+      return;
+    }
+  }
   cudaError_t e = cudaMalloc(&p_, bytes);
+  if (e == cudaErrorMemoryAllocation && c && c->blocks.bytes() > 0) {
+    cudaGetLastError();
+    cudaStreamSynchronize(c->stream);
+    c->blocks.flush();
+    e = cudaMalloc(&p_, bytes);
+  }
   if (e != cudaSuccess) {
     p_ = nullptr;
     cudaGetLastError();
@@ -21,12 +66,17 @@ void DevMem::alloc(size_t bytes) {
                 "cudaMalloc(" + std::to_string(bytes) + " B): " + cudaGetErrorString(e));
   }
   bytes_ = bytes;
+  owner_ = c;
 }
 
 void DevMem::release() {
-  if (p_) cudaFree(p_);
+  if (p_) {
+    Ctx *c = current_ctx();
+    if (!(c && owner_ == c && c->blocks.give(p_, bytes_))) cudaFree(p_);
+  }
   p_ = nullptr;
   bytes_ = 0;
+  owner_ = nullptr;
 }
 
 TV cm(double *p, std::initializer_list<int64_t> ext) {
@@ -80,6 +130,7 @@ Ctx::Ctx(int dev) : device(dev) {
 
 Ctx::~Ctx() {
   if (stream) cudaStreamSynchronize(stream);
+  blocks.flush();
   tc.reset();
   plans.clear();
   workspace.release();
@@ -374,7 +425,10 @@ const EinsumPlan &plan_einsum(Ctx &ctx, const char *spec, const TV &A, const TV 
   auto put = [&](const std::vector<int64_t> &v, const int64_t *&dptr) {
     dptr = base + off;
     if (!v.empty())
-      SCESS_CUDA(cudaMemcpy(base + off, v.data(), v.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
+      // on the context's stream: the block may be a reused one that earlier
+      // kernels on that stream still read (the host vectors live in the plan)
+      SCESS_CUDA(cudaMemcpyAsync(base + off, v.data(), v.size() * sizeof(int64_t),
+                                 cudaMemcpyHostToDevice, ctx.stream));
     off += v.size();
   };
   put(pl->rowA, pl->d_rowA);

@@ -12,6 +12,36 @@
 namespace scess {
 
 // Owning device allocation (freed on destruction).
+struct Ctx;
+
+// Large device blocks released while an API call of their context runs are
+// kept by that context (exact sizes) instead of going back through cudaFree,
+// which synchronises the whole device; later allocations of the same size in
+// the same context reuse them.  All of a context's kernels run on its one
+// stream, so a reused block's earlier work precedes its new work.  The cache
+// is emptied when an allocation fails and with the context.
+class BlockCache {
+ public:
+  static constexpr size_t kMinBytes = size_t(1) << 20;
+  static constexpr size_t kMaxCached = size_t(96) << 30;
+  void *take(size_t bytes);
+  bool give(void *p, size_t bytes);  // false: the caller frees it
+  void flush();
+  size_t bytes() const { return total_; }
+
+ private:
+  std::multimap<size_t, void *> free_;
+  size_t total_ = 0;
+};
+
+// The context whose API call runs on this thread (null outside calls).
+Ctx *current_ctx();
+struct CurrentCtx {
+  Ctx *prev;
+  explicit CurrentCtx(Ctx *c);
+  ~CurrentCtx();
+};
+
 class DevMem {
  public:
   DevMem() = default;
@@ -19,9 +49,21 @@ class DevMem {
   ~DevMem() { release(); }
   DevMem(const DevMem &) = delete;
   DevMem &operator=(const DevMem &) = delete;
-  DevMem(DevMem &&o) noexcept : p_(o.p_), bytes_(o.bytes_) { o.p_ = nullptr; o.bytes_ = 0; }
+  DevMem(DevMem &&o) noexcept : p_(o.p_), bytes_(o.bytes_), owner_(o.owner_) {
+    o.p_ = nullptr;
+    o.bytes_ = 0;
+    o.owner_ = nullptr;
+  }
   DevMem &operator=(DevMem &&o) noexcept {
-    if (this != &o) { release(); p_ = o.p_; bytes_ = o.bytes_; o.p_ = nullptr; o.bytes_ = 0; }
+    if (this != &o) {
+      release();
+      p_ = o.p_;
+      bytes_ = o.bytes_;
+      owner_ = o.owner_;
+      o.p_ = nullptr;
+      o.bytes_ = 0;
+      o.owner_ = nullptr;
+    }
     return *this;
   }
   void alloc(size_t bytes);
@@ -33,6 +75,7 @@ class DevMem {
  private:
   void *p_ = nullptr;
   size_t bytes_ = 0;
+  Ctx *owner_ = nullptr;  // context whose API call allocated it
 };
 
 // Strided view of an FP64 tensor in device memory: element (i_0, ..., i_{nd-1})
@@ -166,6 +209,7 @@ struct Ctx {
   std::unique_ptr<TcEngine> tc;
   KernelTimer timer;
   Tape *tape = nullptr;  // recording target while an adjoint forward pass runs
+  BlockCache blocks;     // released large device blocks (see BlockCache)
 
   explicit Ctx(int dev);
   ~Ctx();
