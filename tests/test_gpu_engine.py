@@ -21,6 +21,12 @@ CASES = [
     ('kcld,ld->kc', (10, 90, 10, 90), (10, 90)),
     ('kc,kica->ia', (10, 90), (10, 10, 90, 90)),
     ('ia,jb->ijab', (7, 11), (7, 11)),
+    # operand packs whose tiles run along a row label that is not the first of
+    # the row group (a of (i, a, b)), and gathers that cover their whole source
+    ('abic,jc->ijab', (40, 40, 6, 40), (6, 40)),
+    ('kibc,ka->abic', (6, 6, 40, 40), (6, 40)),
+    ('cbai,jc->ijab', (36, 36, 36, 5), (5, 36)),
+    ('ldkc,ilda->akic', (5, 33, 5, 33), (5, 5, 33, 33)),
 ]
 
 
