@@ -147,7 +147,7 @@ void rccsd_residual_vjp(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t nocc
     gbuf.push_back(std::move(g));
   };
   for (const DTensor *t : {&w.tau, &w.Foo, &w.Fvv, &w.Fov, &w.Fovt1, &w.Loo, &w.Lvv, &w.X,
-                           &w.tmp_abic, &w.tmp_akij, &w.Woooo, &w.Wvvvv, &w.Wvoov, &w.Wvovo,
+                           &w.tmp_abic, &w.tmp_kibj, &w.tmp_akij, &w.Woooo, &w.Wvvvv, &w.Wvoov, &w.Wvovo,
                            &w.tmp_lkci, &w.tmp_lcki, &w.Yd, &B.L_oovv, &B.L_ovov})
     track(*t);
   SCESS_CUDA(cudaMemsetAsync(d_gAmp, 0, (size_t)n * sizeof(double), s));
@@ -307,7 +307,7 @@ struct Lagrangian {
       return ptr;
     };
     for (const DTensor *t : {&w.tau, &w.Foo, &w.Fvv, &w.Fov, &w.Fovt1, &w.Loo, &w.Lvv, &w.X,
-                             &w.tmp_abic, &w.tmp_akij, &w.Woooo, &w.Wvvvv, &w.Wvoov, &w.Wvovo,
+                             &w.tmp_abic, &w.tmp_kibj, &w.tmp_akij, &w.Woooo, &w.Wvvvv, &w.Wvoov, &w.Wvovo,
                              &w.tmp_lkci, &w.tmp_lcki, &w.Yd, &tmpF, &lvvF, &looF, &X2F})
       track(*t);
     g_foo = track(foo);

@@ -18,8 +18,8 @@ struct RccsdBlocks {
 
 // Device work arrays of one residual evaluation.
 struct RccsdWork {
-  DTensor tau, Foo, Fvv, Fov, Fovt1, Loo, Lvv, X, tmp_abic, tmp_akij, Woooo, Wvvvv, Wvoov,
-      Wvovo, tmp_lkci, tmp_lcki, Yd;
+  DTensor tau, Foo, Fvv, Fov, Fovt1, Loo, Lvv, X, tmp_abic, tmp_kibj, tmp_akij, Woooo, Wvvvv,
+      Wvoov, Wvovo, tmp_lkci, tmp_lcki, Yd;
   void alloc(int64_t o, int64_t v, bool direct_vvvv);
 };
 
