@@ -1116,7 +1116,11 @@ void TcEngine::pack(const double *src, const int64_t *rowOff, int64_t rows, cons
   out.K = K;
   out.Kpad = Kpad;
   out.fmt = fmt_;
-  TimedScope ts(ctx_.timer, "pack_split", 0.0,
+  // timed per contraction: "pack[spec]" inside an einsum ("tc_gemm[spec]")
+  const std::string tname =
+      timer_name_ && std::strncmp(timer_name_, "tc_gemm", 7) == 0 ? std::string("pack") + (timer_name_ + 7)
+                                                                  : std::string("pack_split");
+  TimedScope ts(ctx_.timer, tname.c_str(), 0.0,
                 (double)rows * K * 8 + (double)rows_pad * Kpad * 4, ctx_.stream);
   unsigned *maxbits = out.aux.as<unsigned>();
   double *scale = reinterpret_cast<double *>(out.aux.as<char>() + 8);
