@@ -145,6 +145,8 @@ struct TcArgs {
   int64_t cy, cz;    // output offset of problem (y, z, g): y * cy + z * cz + cg[g]
   int64_t cg[3];
   const int64_t *rowCg[3], *colCg[3];  // per-group output tables (null: TcOut's)
+  int tri[3];                          // group g keeps only the problems with y >= z (ny == nz)
+  int gstart[4];                       // first problem index of each group (gstart[ng] = total)
   int stcol[3];                        // group stores along columns (FP32, beta = 0)
   int stvec[3];                        // ... in contiguous aligned quads of columns
   float *partial;    // split-K partials (nullptr: direct epilogue)
@@ -262,7 +264,7 @@ __global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tiles = a.tiles_m * a.tiles_n;
-  const int nprob = a.ny * a.nz * a.ng;
+  const int nprob = a.gstart[a.ng];
   const int units = tiles * nprob * a.splits;
 
   if (threadIdx.x == 0) {
@@ -320,9 +322,27 @@ __global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
     const int sp = rest / nprob;
     tn = tile % a.tiles_n;
     tm = tile / a.tiles_n;
-    py = q % a.ny;
-    pz = (q / a.ny) % a.nz;
-    pg = q / (a.ny * a.nz);
+    if constexpr (BN != 256) {  // (einsum launches: no triangular groups)
+      py = q % a.ny;
+      pz = (q / a.ny) % a.nz;
+      pg = q / (a.ny * a.nz);
+      kb0 = sp * a.kb_per_split;
+      kb1 = min(a.kb_total, kb0 + a.kb_per_split);
+      return;
+    }
+    pg = 0;
+    while (pg + 1 < a.ng && q >= a.gstart[pg + 1]) pg++;
+    const int lq = q - a.gstart[pg];
+    if (a.tri[pg]) {  // lq = y (y + 1) / 2 + z, z <= y
+      int y = (int)((sqrtf(8.0f * (float)lq + 1.0f) - 1.0f) * 0.5f);
+      while (y * (y + 1) / 2 > lq) y--;
+      while ((y + 1) * (y + 2) / 2 <= lq) y++;
+      py = y;
+      pz = lq - y * (y + 1) / 2;
+    } else {
+      py = lq % a.ny;
+      pz = lq / a.ny;
+    }
     kb0 = sp * a.kb_per_split;
     kb1 = min(a.kb_total, kb0 + a.kb_per_split);
   };
@@ -1005,7 +1025,19 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
   if (splits > 1 && !partial) throw Error(SCESS_ERR_INVALID, "tc_gemm: split-K needs partials");
   TcMaps maps;
   for (int i = 0; i < 6; i++) maps.m[i] = ps.maps[std::min(i, ps.nmaps - 1)];
-  const int64_t units = (int64_t)a.tiles_m * a.tiles_n * ps.ny * ps.nz * ps.ng * splits;
+  {  // problems per group: all ny nz, or the ny (ny + 1) / 2 with y >= z
+    int64_t start = 0;
+    for (int g = 0; g < ps.ng; g++) {
+      a.tri[g] = ps.tri[g] ? 1 : 0;
+      if (a.tri[g] && (ps.ny != ps.nz || bn != 256))
+        throw Error(SCESS_ERR_INVALID, "tc_gemm: triangular groups need ny == nz and the 256-wide kernel");
+      a.gstart[g] = (int)start;
+      start += a.tri[g] ? (int64_t)ps.ny * (ps.ny + 1) / 2 : (int64_t)ps.ny * ps.nz;
+    }
+    if (start > INT32_MAX) throw Error(SCESS_ERR_INVALID, "tc_gemm: too many problems");
+    a.gstart[ps.ng] = (int)start;
+  }
+  const int64_t units = (int64_t)a.tiles_m * a.tiles_n * a.gstart[ps.ng] * splits;
   if (units > INT32_MAX) throw Error(SCESS_ERR_INVALID, "tc_gemm: too many work units");
   const unsigned grid = (unsigned)std::min<int64_t>(units, kNumSMs);
   if (bn == 256)

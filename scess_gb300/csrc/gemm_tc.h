@@ -74,6 +74,8 @@ struct TcProblemSet {
   // K blocks per TMEM drain: 1, 2 or 4 (fewer drains, more products
   // accumulated in TMEM between drains).  A K block is k_block(bn) wide.
   int kbd = 1;
+  // group g computes only its problems with y >= z (requires ny == nz)
+  bool tri[3] = {false, false, false};
   // tile width: 128, or 256 (B-side maps must then have 256-row boxes; half the
   // shared-memory traffic per FLOP for the A operand).  All maps must have
   // k_block(bn)-wide boxes: map_of(p, rows, k_block(bn)), and bk must say so.

@@ -951,7 +951,15 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
           out.alpha = 1.0;
           out.beta = 0.0;
           TcEngine::set_scales(out, pP, pQ);
-          const double flops = 3.0 * nb * nb * 2.0 * (double)Mg * Ng * (2.0 * v + 2.0 * o);
+          // In a diagonal block triple a group's problems with y_l < z_l feed no
+          // unique triple a >= b >= c: g0 (y, z) = (b, c) when B = C, g1 (a, c)
+          // when A = C, g2 (a, b) when A = B.
+          ps.tri[0] = tbn == 256 && Bk == C;
+          ps.tri[1] = tbn == 256 && A == C;
+          ps.tri[2] = tbn == 256 && A == Bk;
+          double nprob = 0.0;
+          for (int g = 0; g < 3; g++) nprob += ps.tri[g] ? nb * (nb + 1) / 2.0 : (double)nb * nb;
+          const double flops = nprob * 2.0 * (double)Mg * Ng * (2.0 * v + 2.0 * o);
           tc.gemm_grouped(ps, out, flops, "tc_gemm[triples]");
         } else {
           w_block_fp64(ctx, T, U, W.d(), ws);
