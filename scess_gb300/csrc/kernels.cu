@@ -132,8 +132,21 @@ __global__ void dgemv_table_kernel(TableGemm g) {
   const double *__restrict__ B = g.B + g.baseB + g.colB[0];
   for (int64_t m = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; m < g.M; m += warps) {
     const double *__restrict__ A = g.A + g.baseA + g.rowA[m];
-    double s = 0.0;
-    for (int64_t k = lane; k < g.K; k += 32) s = fma(A[g.kA[k]], B[g.kB[k]], s);
+    // four independent partial sums a lane: four loads in flight, fixed order
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int64_t k = lane;
+    for (; k + 96 < g.K; k += 128) {
+      const int64_t ka0 = g.kA[k], ka1 = g.kA[k + 32], ka2 = g.kA[k + 64], ka3 = g.kA[k + 96];
+      const int64_t kb0 = g.kB[k], kb1 = g.kB[k + 32], kb2 = g.kB[k + 64], kb3 = g.kB[k + 96];
+      const double a0 = A[ka0], a1 = A[ka1], a2 = A[ka2], a3 = A[ka3];
+      const double b0 = B[kb0], b1 = B[kb1], b2 = B[kb2], b3 = B[kb3];
+      s0 = fma(a0, b0, s0);
+      s1 = fma(a1, b1, s1);
+      s2 = fma(a2, b2, s2);
+      s3 = fma(a3, b3, s3);
+    }
+    for (; k < g.K; k += 32) s0 = fma(A[g.kA[k]], B[g.kB[k]], s0);
+    double s = (s0 + s1) + (s2 + s3);
     for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
     if (lane == 0) {
       const int64_t off = g.baseC + g.rowC[m] + g.colC[0];
