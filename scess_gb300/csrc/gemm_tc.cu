@@ -120,7 +120,8 @@ __device__ __forceinline__ void tmem_wait16(uint32_t *r) {
 // first A/B row of problem (y, z) of group g: row0[g] + y * row_y[g] + z * row_z[g].
 struct TcSegArgs {
   int mapA, mapB;
-  int nkb;   // K blocks of 64
+  int nkb;   // K blocks of this segment
+  int bk;    // their width: the kernel's BK, or 32 (64-byte swizzle, half-filled stages)
   int kpad;  // lo offset in the packed rows (elements)
   int negA;  // negate this segment's products
   int64_t rowA0[3], rowAy[3], rowAz[3], rowB0[3], rowBy[3], rowBz[3];
@@ -374,8 +375,9 @@ __global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
           if (!mbar_wait(&empty[s], ph ^ 1u, a.err, ERR_EMPTY_WAIT)) { ok = false; break; }
           uint8_t *st = smem + s * SH::STAGE_BYTES;
           const CUtensorMap *mA = &maps.m[S.mapA], *mB = &maps.m[S.mapB];
-          mbar_expect_tx(&full[s], bytes);
-          const int x = lkb * SH::BK;
+          // a 32-wide block of a segment in a 64-wide kernel fills half a stage
+          mbar_expect_tx(&full[s], S.bk == SH::BK ? bytes : bytes / 2);
+          const int x = lkb * S.bk;
           tma_load_2d(st, mA, x, ya, &full[s]);                                  // A hi
           tma_load_2d(st + SH::A_BYTES, mB, x, yb, &full[s]);                    // B hi
           if (a.split3) {
@@ -420,17 +422,32 @@ __global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
           const uint32_t blo = st + 2 * SH::A_BYTES + SH::B_BYTES;
           const uint32_t d = tmem + (uint32_t)(b * BN);
           uint32_t acc = first ? 0u : 1u;
-          if (a.split3) {
+          if (SH::BK == 64 && a.seg[sg].bk == 32) {
+            // half-filled stage of a 32-wide segment: 64-byte rows, 64-byte swizzle
+            if (a.split3) {
+#pragma unroll
+              for (int k = 0; k < 2; k++, acc = 1)
+                mma_bf16(d, sw_desc<64>(alo + 32 * k), sw_desc<64>(bhi + 32 * k), id, acc);
+#pragma unroll
+              for (int k = 0; k < 2; k++)
+                mma_bf16(d, sw_desc<64>(ahi + 32 * k), sw_desc<64>(blo + 32 * k), id, 1u);
+            }
+#pragma unroll
+            for (int k = 0; k < 2; k++, acc = 1)
+              mma_bf16(d, sw_desc<64>(ahi + 32 * k), sw_desc<64>(bhi + 32 * k), id, acc);
+          } else {
+            if (a.split3) {
+#pragma unroll
+              for (int k = 0; k < SH::BK / 16; k++, acc = 1)
+                mma_bf16(d, sw_desc<SH::SWZ>(alo + 32 * k), sw_desc<SH::SWZ>(bhi + 32 * k), id, acc);
+#pragma unroll
+              for (int k = 0; k < SH::BK / 16; k++)
+                mma_bf16(d, sw_desc<SH::SWZ>(ahi + 32 * k), sw_desc<SH::SWZ>(blo + 32 * k), id, 1u);
+            }
 #pragma unroll
             for (int k = 0; k < SH::BK / 16; k++, acc = 1)
-              mma_bf16(d, sw_desc<SH::SWZ>(alo + 32 * k), sw_desc<SH::SWZ>(bhi + 32 * k), id, acc);
-#pragma unroll
-            for (int k = 0; k < SH::BK / 16; k++)
-              mma_bf16(d, sw_desc<SH::SWZ>(ahi + 32 * k), sw_desc<SH::SWZ>(blo + 32 * k), id, 1u);
+              mma_bf16(d, sw_desc<SH::SWZ>(ahi + 32 * k), sw_desc<SH::SWZ>(bhi + 32 * k), id, acc);
           }
-#pragma unroll
-          for (int k = 0; k < SH::BK / 16; k++, acc = 1)
-            mma_bf16(d, sw_desc<SH::SWZ>(ahi + 32 * k), sw_desc<SH::SWZ>(bhi + 32 * k), id, acc);
           mma_commit(&empty[s]);
           if (last) {
             mma_commit(&tfull[b]);
@@ -870,6 +887,7 @@ __global__ void __launch_bounds__(256) pack_split_kernel(
   }
   const int64_t r = srow[rr];
   if (r < 0) return;  // past the label's extent (padding rows are cleared by the host)
+  if (k0 + ch * 8 >= Kpad) return;  // Kpad a multiple of 32: the tile's last 32 columns are past it
   const int64_t base = r * 2 * Kpad + k0 + ch * 8;
   *reinterpret_cast<uint4 *>(dst + base) = *reinterpret_cast<const uint4 *>(hi);
   *reinterpret_cast<uint4 *>(dst + base + Kpad) = *reinterpret_cast<const uint4 *>(lo);
@@ -973,8 +991,13 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
   int kbt = 0;
   for (int s = 0; s < ps.nseg; s++) {
     const TcSegment &g = ps.seg[s];
-    if (g.Kpad % TC_BK != 0 || g.Kpad <= 0 || 2 * g.Kpad > INT32_MAX)
-      throw Error(SCESS_ERR_INVALID, "tc_gemm: Kpad % 64");
+    // a segment may use 32-wide K blocks in the 64-wide kernel (maps with
+    // 32-wide boxes, K padded to 32); otherwise the kernel's K block
+    const int sbk = g.bk ? g.bk : bk;
+    if (!(sbk == bk || (sbk == 32 && bk == 64)))
+      throw Error(SCESS_ERR_INVALID, "tc_gemm: segment K block");
+    if (g.Kpad % sbk != 0 || g.Kpad <= 0 || 2 * g.Kpad > INT32_MAX)
+      throw Error(SCESS_ERR_INVALID, "tc_gemm: segment K not a multiple of its K block");
     for (int q = 0; q < ps.ng; q++) {
       const int64_t maxA = g.rowA0[q] + (int64_t)(ps.ny - 1) * g.rowAy[q] +
                            (int64_t)(ps.nz - 1) * g.rowAz[q] + a.tiles_m * TC_BM;
@@ -986,7 +1009,8 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
     }
     a.seg[s].mapA = g.mapA;
     a.seg[s].mapB = g.mapB;
-    a.seg[s].nkb = (int)(g.Kpad / bk);
+    a.seg[s].nkb = (int)(g.Kpad / sbk);
+    a.seg[s].bk = sbk;
     a.seg[s].kpad = (int)g.Kpad;
     a.seg[s].negA = g.negate ? 1 : 0;
     for (int q = 0; q < 3; q++) {
@@ -1206,8 +1230,9 @@ void TcEngine::maxabs_into(const double *src, const int64_t *rowOff, int64_t row
 
 void TcEngine::pack_with_max(const double *src, const int64_t *rowOff, int64_t rows,
                              const int64_t *kOff, int64_t K, bool unitK, int64_t row_align,
-                             const unsigned *maxbits, bool negate, Packed &out) {
-  const int64_t Kpad = round_up(std::max<int64_t>(K, 1), TC_BK);
+                             const unsigned *maxbits, bool negate, Packed &out, int64_t k_align) {
+  if (k_align != 32 && k_align != 64) throw Error(SCESS_ERR_INVALID, "pack: K alignment");
+  const int64_t Kpad = round_up(std::max<int64_t>(K, 1), k_align);
   const int64_t rows_pad = round_up(std::max<int64_t>(rows, 1), std::max<int64_t>(row_align, 32));
   const size_t bytes = (size_t)rows_pad * 2 * Kpad * sizeof(uint16_t);
   if (out.mem.bytes() < bytes || !out.aux.bytes()) {
@@ -1224,8 +1249,8 @@ void TcEngine::pack_with_max(const double *src, const int64_t *rowOff, int64_t r
                 (double)rows * K * 8 + (double)rows_pad * Kpad * 4, ctx_.stream);
   double *scale = reinterpret_cast<double *>(out.aux.as<char>() + 8);
   const RowTiles rt = RowTiles::make(rows, 1, rows);
-  if (Kpad / 64 > 65535 || rt.count > INT32_MAX) throw Error(SCESS_ERR_INVALID, "pack: too large");
-  dim3 grid((unsigned)rt.count, (unsigned)(Kpad / 64));
+  if (ceil_div(Kpad, 64) > 65535 || rt.count > INT32_MAX) throw Error(SCESS_ERR_INVALID, "pack: too large");
+  dim3 grid((unsigned)rt.count, (unsigned)ceil_div(Kpad, 64));
   clear_pad_rows(out.mem.as<uint16_t>(), rows, rows_pad, Kpad, ctx_.stream);
   if (fmt_ == TcFormat::FP16) {
     pack_split_kernel<true, false><<<grid, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, unitK ? 1 : 0,

@@ -58,6 +58,9 @@ struct TcOut {
 struct TcSegment {
   int mapA = 0, mapB = 1;
   int64_t Kpad = 0;
+  // K block of this segment: 0 = the kernel's; 32 in the 64-wide kernel (its
+  // maps then have 32-wide boxes and Kpad is a multiple of 32)
+  int bk = 0;
   bool negate = false;
   int64_t rowA0[3] = {0, 0, 0}, rowAy[3] = {0, 0, 0}, rowAz[3] = {0, 0, 0};
   int64_t rowB0[3] = {0, 0, 0}, rowBy[3] = {0, 0, 0}, rowBz[3] = {0, 0, 0};
@@ -116,9 +119,11 @@ class TcEngine {
                    int64_t K, bool unitK, unsigned *maxbits);
   // pack() with the FP16 scale taken from a given max word (so that several
   // packs share one scale), optionally negating the values (exact).
+  // K is padded to a multiple of k_align (64, or 32 for segments with 32-wide
+  // K blocks).
   void pack_with_max(const double *src, const int64_t *rowOff, int64_t rows, const int64_t *kOff,
                      int64_t K, bool unitK, int64_t row_align, const unsigned *maxbits,
-                     bool negate, Packed &out);
+                     bool negate, Packed &out, int64_t k_align = 64);
   TcFormat format() const { return fmt_; }
   // D(m, n) = sum_k A(rowA0 + m, k) B(rowB0 + n, k) for m < M, n < N, written
   // through `out`.  nseg = 3 (split hi/lo) or 1 (hi only, BF16 accuracy).

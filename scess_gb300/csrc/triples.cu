@@ -804,6 +804,9 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   int tbn = 256;
   if (const char *env = std::getenv("SCESS_T_BN")) tbn = std::atoi(env) == 128 ? 128 : 256;
   const int tbk = TcEngine::k_block(tbn);
+  // K block of the t2.R segments (K = o): 32 in the 64-wide kernel when o <= 32
+  // (half-filled stages instead of mostly-padding 64-wide ones)
+  const int rbk = (tbk == 64 && o <= 32) ? 32 : tbk;
   CUtensorMap mP{}, mQ{}, mQ2{}, mR{}, mR2{}, mTx{};
   DevTables gdt;  // W_g row / column tables
   DevMem Sf;  // (ia|jb) as FP32 for the energy kernel (padded rows)
@@ -835,11 +838,11 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
     tc.maxabs_into(Qt.p(), pdt.ptr[1], o2 * vp, dt.ptr[kOperand + 3], v, true, mx + 1);
     tc.maxabs_into(Rt.p(), pdt.ptr[2], o2 * vp, dt.ptr[kOperand + 5], o, false, mx + 1);
     tc.pack_with_max(P.p(), pdt.ptr[0], o * vp * vp, dt.ptr[kOperand + 1], v, false, 128, mx, false, pP);
-    tc.pack_with_max(T2p.p(), pdt.ptr[3], o * vp * vp, dt.ptr[kOperand + 7], o, true, 128, mx, true, pTx);
+    tc.pack_with_max(T2p.p(), pdt.ptr[3], o * vp * vp, dt.ptr[kOperand + 7], o, true, 128, mx, true, pTx, rbk);
     tc.pack_with_max(Qt.p(), pdt.ptr[1], o2 * vp, dt.ptr[kOperand + 3], v, true, 128, mx + 1, false, pQ);
     tc.pack_with_max(Qt.p(), pdt.ptr[4], o2 * vp, dt.ptr[kOperand + 3], v, true, 128, mx + 1, false, pQ2);
-    tc.pack_with_max(Rt.p(), pdt.ptr[2], o2 * vp, dt.ptr[kOperand + 5], o, false, 128, mx + 1, false, pR);
-    tc.pack_with_max(Rt.p(), pdt.ptr[5], o2 * vp, dt.ptr[kOperand + 5], o, false, 128, mx + 1, false, pR2);
+    tc.pack_with_max(Rt.p(), pdt.ptr[2], o2 * vp, dt.ptr[kOperand + 5], o, false, 128, mx + 1, false, pR, rbk);
+    tc.pack_with_max(Rt.p(), pdt.ptr[5], o2 * vp, dt.ptr[kOperand + 5], o, false, 128, mx + 1, false, pR2, rbk);
     ctx.sync();
     // B side (Q, R rows): tiles of tbn columns; 256 halves the A-operand
     // shared-memory traffic per FLOP (SCESS_T_BN=128 selects the narrow tiles).
@@ -847,9 +850,9 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
     mP = TcEngine::map_of(pP, 128, tbk);
     mQ = TcEngine::map_of(pQ, tbn, tbk);
     mQ2 = TcEngine::map_of(pQ2, tbn, tbk);
-    mR = TcEngine::map_of(pR, tbn, tbk);
-    mR2 = TcEngine::map_of(pR2, tbn, tbk);
-    mTx = TcEngine::map_of(pTx, 128, tbk);
+    mR = TcEngine::map_of(pR, tbn, rbk);
+    mR2 = TcEngine::map_of(pR2, tbn, rbk);
+    mTx = TcEngine::map_of(pTx, 128, rbk);
     // W_g[(y_l nb + z_l) nb + x_l][i + o j + o2p k]: every group stores its
     // (u, s, t) in the (i, j, k) order of the triple, so that the energy kernel
     // reads the three buffers alike.  g = 0: (u,s,t) = (i,j,k); g = 1: (j,i,k);
@@ -923,6 +926,7 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
           s1.mapA = 0; s1.mapB = 2; s1.Kpad = pP.Kpad;   // P(u,f,x,z) Q(f,t,s,y)
           s2.mapA = 5; s2.mapB = 3; s2.Kpad = pTx.Kpad;  // -t2(m,u,z,x) R(s,t,m,y)
           s3.mapA = 5; s3.mapB = 4; s3.Kpad = pTx.Kpad;  // -t2(m,u,y,x) R(t,s,m,z)
+          s2.bk = s3.bk = rbk;
           for (int g = 0; g < 3; g++) {
             const int64_t X = U[kRoles[g][0]], Yb = U[kRoles[g][1]], Z = U[kRoles[g][2]];
             ps.cg[g] = g * nb * nb * nb * o3p;
