@@ -75,13 +75,16 @@ void device_finite(scess::Ctx &ctx, const double *x, int64_t n, const char *what
   if (h) throw Error(SCESS_ERR_INVALID, std::string("non-finite value in ") + what);
 }
 
-// eri (nmo^4) on the device, from the host eri or from DF factors (FP64 build).
+// eri (nmo^4) on the device, from the host eri or from DF factors: an FP64
+// build, or for mixed-precision solves a tensor-core build (split FP16 hi/lo
+// products, ~2e-7 relative per element, 2 naux nmo^4 FLOPs in milliseconds
+// instead of seconds at the FP64 rate).
 double ms_since(std::chrono::steady_clock::time_point t0) {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
 scess::DTensor device_eri(scess::Ctx &ctx, const double *eri, const double *B, int64_t naux,
-                          int64_t N) {
+                          int64_t N, bool mixed_build = false) {
   auto t0 = std::chrono::steady_clock::now();
   scess::DTensor d({N, N, N, N});
   ctx.timer.host("eri_alloc", ms_since(t0));
@@ -97,8 +100,11 @@ scess::DTensor device_eri(scess::Ctx &ctx, const double *eri, const double *B, i
     scess::upload(ctx, dB.p(), B, naux * N * N);
     device_finite(ctx, dB.p(), naux * N * N, "B");
     // eri(p,q,r,s) = (pr|qs) = sum_Q B(Q,p,r) B(Q,q,s)
-    scess::einsum(ctx, "Qpr,Qqs->pqrs", 1.0, dB.v, dB.v, 0.0, d.v, scess::Backend::FP64);
+    t0 = std::chrono::steady_clock::now();
+    scess::einsum(ctx, "Qpr,Qqs->pqrs", 1.0, dB.v, dB.v, 0.0, d.v,
+                  mixed_build ? scess::Backend::TENSOR : scess::Backend::FP64);
     ctx.sync();
+    ctx.timer.host("eri_from_B", ms_since(t0));
   }
   return d;
 }
@@ -116,7 +122,7 @@ scess::RccsdState *make_state(scess::Ctx &c, const double *eri, const double *B,
   const int64_t v = nmo - nocc;
   if (f12_residual) host_finite(f12_residual, nocc * nocc * v * v, "f12_residual");
   if (f12_energy) host_finite(f12_energy, nocc * nocc * v * v, "f12_energy");
-  scess::DTensor d_eri = device_eri(c, eri, B, naux, nmo);
+  scess::DTensor d_eri = device_eri(c, eri, B, naux, nmo, o.precision == SCESS_PRECISION_MIXED);
   scess::SolveInput in;
   in.eps_host = eps;
   in.f12_residual = f12_residual;
@@ -152,7 +158,7 @@ int solve_common(scess_ctx *ctx, const double *eri, const double *B, int64_t nau
     ctl.cancel = c.cancel;
     ctl.user = c.user;
     ctl.time_limit_s = o.time_limit_s;
-    scess::DTensor d_eri = device_eri(c, eri, B, naux, nmo);
+    scess::DTensor d_eri = device_eri(c, eri, B, naux, nmo, o.precision == SCESS_PRECISION_MIXED);
     ctl.poll();
     scess::SolveInput in;
     in.eps_host = eps;

@@ -69,6 +69,17 @@ def test_solve_df_equals_eri_path(gctx):
     assert abs(a.E_CCSD - b.E_CCSD) < 1e-11
 
 
+def test_solve_df_mixed_builds_eri_on_tensor_cores(gctx):
+    """Mixed DF solve: the nmo^4 eri is contracted from B on the tensor cores
+    (~2e-7 relative per integral); the energy stays within 1 uEh of the FP64
+    eri-path solve."""
+    w = make_workload(8, 40, seed=5)
+    a = gctx.solve(w.eri(), w.eps, 8)
+    b = gctx.solve(None, w.eps, 8, B=w.B, precision='mixed')
+    assert b.converged
+    assert abs(a.E_CCSD - b.E_CCSD) < 1e-6
+
+
 def test_f12_coupling_matches_oracle(gctx):
     o, v = 5, 19
     w = make_workload(o, v, seed=3)
