@@ -73,7 +73,8 @@ def test_solve_df_mixed_builds_eri_on_tensor_cores(gctx):
     """Mixed DF solve: the nmo^4 eri is contracted from B on the tensor cores
     (~2e-7 relative per integral); the energy stays within 1 uEh of the FP64
     eri-path solve."""
-    w = make_workload(8, 40, seed=5)
+    from scess_gb300.synthetic import convergent_sigma
+    w = make_workload(8, 40, seed=5, sigma=convergent_sigma(8, 40))
     a = gctx.solve(w.eri(), w.eps, 8)
     b = gctx.solve(None, w.eps, 8, B=w.B, precision='mixed')
     assert b.converged
