@@ -273,6 +273,21 @@ int scess_transform_tei(scess_ctx *ctx, const double *tei, int64_t nao, const do
                         const double *D, int64_t nd, int32_t chem_to_phys, int32_t precision,
                         double *out);
 
+/* CCSD-F12b coupling of the conventional doubles to the fixed-amplitude
+ * geminals, CCSD_F12b.cpp:83-94 (the part of CCSD_F12b that feeds
+ * SolveRCCSD_DIIS).  All tensors are over the nmo OBS MOs, occupied first,
+ * physicists' notation, column-major: eri <pq|rs>, f12 <pq|f12|rs>,
+ * f12_repulsion <pq|r12^-1 f12|rs> (nmo^4 each), and C the MP2-F12/3C
+ * intermediate C_kl^ab (nocc^2 nvirt^2).  With
+ *   V(k,l,a,b) = f12_repulsion(k,l,a,b) - sum_rs eri(a,b,r,s) f12(k,l,r,s)
+ * and F(X)(i,j,a,b) = 3/8 X(i,j,a,b) + 1/8 X(j,i,a,b) (ContractFixedAmplitudes),
+ * residual_out = F(C + V) and energy_out = F(C) (nocc^2 nvirt^2 each): the
+ * f12_residual and f12_energy arguments of scess_rccsd_solve.  precision:
+ * FP64 (table GEMM), or MIXED (the rs contraction on tensor cores). */
+int scess_f12b_coupling(scess_ctx *ctx, const double *eri, const double *f12,
+                        const double *f12_repulsion, const double *C, int64_t nmo, int64_t nocc,
+                        int32_t precision, double *residual_out, double *energy_out);
+
 /* scess_einsum's FP64 contraction for callers that cannot allocate device
  * memory.  No counterpart in the reference.  Some host programs own every byte
  * of the GPU: a framework whose caching allocator has reserved the device's

@@ -17,3 +17,4 @@ from .rccsd import (  # noqa: F401
     solve_rccsd_diis, RCCSDWfn, full_piv_lu_solve, ccsd_flops,
 )
 from .rccsd_t import rccsd_triples_correction, triples_flops  # noqa: F401
+from .f12 import f12b_coupling, contract_fixed_amplitudes  # noqa: F401

@@ -121,6 +121,8 @@ EXPORTS = {
                                              C.POINTER(C.c_double), _dp, _dp, _dp]),
     'scess_transform_tei': (C.c_int, [C.c_void_p, _dp, C.c_int64, _dp, C.c_int64, _dp, C.c_int64,
                                       _dp, C.c_int64, _dp, C.c_int64, C.c_int32, C.c_int32, _dp]),
+    'scess_f12b_coupling': (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, C.c_int64, C.c_int64,
+                                      C.c_int32, _dp, _dp]),
     'scess_einsum_static': (C.c_int, [C.c_char_p, C.c_double, C.c_void_p, C.c_int32, _i64p,
                                       C.c_void_p, C.c_int32, _i64p, C.c_double, C.c_void_p,
                                       C.c_int32, _i64p, C.c_void_p]),
@@ -420,6 +422,24 @@ class Context:
                                           _ptr(out))
         self._check(st, 'scess_transform_tei')
         return out
+
+    def f12b_coupling(self, eri, f12, f12_repulsion, C, nocc, precision='fp64'):
+        """The CCSD-F12b coupling of CCSD_F12b.cpp:83-94: V_klab = <kl|r12^-1 f12|ab>
+        - sum_rs <ab|rs><kl|f12|rs>, then RCCSD_F12Coupling(residual = F(C + V),
+        energy = F(C)) with F(X) = 3/8 X + 1/8 X^(i<->j).  eri, f12 and f12_repulsion
+        are nmo^4 (physicists' notation), C is (o, o, v, v)."""
+        e = _f64(eri)
+        N = e.shape[0]
+        o, v = int(nocc), N - int(nocc)
+        f = _f64(f12, (N, N, N, N))
+        r = _f64(f12_repulsion, (N, N, N, N))
+        c = _f64(C, (o, o, v, v))
+        res = np.zeros((o, o, v, v), order='F')
+        en = np.zeros((o, o, v, v), order='F')
+        st = self.lib.scess_f12b_coupling(self.h, _ptr(e), _ptr(f), _ptr(r), _ptr(c), N, o,
+                                          PRECISION[precision], _ptr(res), _ptr(en))
+        self._check(st, 'scess_f12b_coupling')
+        return RCCSD_F12Coupling(residual=res, energy=en)
 
     # -- Lambda equations and the one-particle density ---------------------------------------
     def lambda_solve(self, eri, eps, nocc, t1, t2, precision='fp64', **opts):

@@ -1,5 +1,6 @@
 // C ABI of the engine (include/scess_cc.h): argument checks, host<->device
 // transfers and exception-to-status translation around the C++ drivers.
+#include <vector>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -799,6 +800,66 @@ int scess_transform_tei(scess_ctx *ctx, const double *tei, int64_t nao, const do
     } else {
       scess::download(c, out, x.p(), na * nb * nc * nd);
     }
+    if (precision == SCESS_PRECISION_MIXED) c.tensor_cores().check_error();
+  });
+}
+
+int scess_f12b_coupling(scess_ctx *ctx, const double *eri, const double *f12,
+                        const double *f12_repulsion, const double *C, int64_t nmo, int64_t nocc,
+                        int32_t precision, double *residual_out, double *energy_out) {
+  return guard(ctx, [&](scess::Ctx &c) {
+    check_shape(nmo, nocc);
+    need(eri, "eri");
+    need(f12, "f12");
+    need(f12_repulsion, "f12_repulsion");
+    need(C, "C");
+    need(residual_out, "residual_out");
+    need(energy_out, "energy_out");
+    if (precision != SCESS_PRECISION_FP64 && precision != SCESS_PRECISION_MIXED)
+      throw Error(SCESS_ERR_INVALID, "bad precision");
+    const scess::Backend be =
+        precision == SCESS_PRECISION_MIXED ? scess::Backend::TENSOR : scess::Backend::FP64;
+    const int64_t N = nmo, o = nocc, v = N - o, N2 = N * N, N3 = N2 * N;
+    // Host slices (Slice<> of CCSD_F12b.cpp:85-87): f12(k,l,r,s) and
+    // f12_repulsion(k,l,a,b); the eri block (a,b,r,s) is a view of the uploaded eri.
+    std::vector<double> f12_klrs((size_t)(o * o * N2)), rep_klab((size_t)(o * o * v * v));
+    for (int64_t s_ = 0; s_ < N; s_++)
+      for (int64_t r = 0; r < N; r++)
+        for (int64_t l = 0; l < o; l++)
+          for (int64_t k = 0; k < o; k++)
+            f12_klrs[(size_t)(k + o * (l + o * (r + N * s_)))] = f12[k + N * l + N2 * r + N3 * s_];
+    for (int64_t b = 0; b < v; b++)
+      for (int64_t a = 0; a < v; a++)
+        for (int64_t l = 0; l < o; l++)
+          for (int64_t k = 0; k < o; k++)
+            rep_klab[(size_t)(k + o * (l + o * (a + v * b)))] =
+                f12_repulsion[k + N * l + N2 * (o + a) + N3 * (o + b)];
+    host_finite(f12_klrs.data(), (int64_t)f12_klrs.size(), "f12");
+    host_finite(rep_klab.data(), (int64_t)rep_klab.size(), "f12_repulsion");
+    host_finite(C, o * o * v * v, "C");
+    scess::DTensor d_eri = device_eri(c, eri, nullptr, 0, N);
+    scess::DTensor dF({o, o, N, N}), V({o, o, v, v}), dC({o, o, v, v});
+    scess::upload(c, dF.p(), f12_klrs.data(), o * o * N2);
+    scess::upload(c, V.p(), rep_klab.data(), o * o * v * v);
+    scess::upload(c, dC.p(), C, o * o * v * v);
+    scess::TV eri_abrs;  // eri(o+a, o+b, r, s)
+    eri_abrs.p = d_eri.p() + o + o * N;
+    eri_abrs.nd = 4;
+    const int64_t ee[4] = {v, v, N, N}, es[4] = {1, N, N2, N3};
+    std::memcpy(eri_abrs.ext, ee, sizeof(ee));
+    std::memcpy(eri_abrs.str, es, sizeof(es));
+    // V_klab -= abrs,klrs->klab                                                 :85-87
+    scess::einsum(c, "abrs,klrs->klab", -1.0, eri_abrs, dF.v, 1.0, V.v, be);
+    // residual = F(C + V), energy = F(C), F(X) = 3/8 X + 1/8 X^(i<->j)    :31-35, :90-91
+    scess::DTensor X({o, o, v, v}), E({o, o, v, v});
+    scess::permute(c, "ijab->ijab", 1.0, V.v, 0.0, X.v);
+    scess::permute(c, "ijab->ijab", 1.0, dC.v, 1.0, X.v);
+    scess::permute(c, "ijab->ijab", 0.375, dC.v, 0.0, E.v);
+    scess::permute(c, "jiab->ijab", 0.125, dC.v, 1.0, E.v);
+    scess::permute(c, "ijab->ijab", 0.375, X.v, 0.0, V.v);
+    scess::permute(c, "jiab->ijab", 0.125, X.v, 1.0, V.v);
+    scess::download(c, residual_out, V.p(), o * o * v * v);
+    scess::download(c, energy_out, E.p(), o * o * v * v);
     if (precision == SCESS_PRECISION_MIXED) c.tensor_cores().check_error();
   });
 }
