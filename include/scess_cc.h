@@ -288,6 +288,22 @@ int scess_f12b_coupling(scess_ctx *ctx, const double *eri, const double *f12,
                         const double *f12_repulsion, const double *C, int64_t nmo, int64_t nocc,
                         int32_t precision, double *residual_out, double *energy_out);
 
+/* Closed-shell MP2 correlation energy, MP2_RHF_ClosedShell (RHF.cpp:306-345):
+ * E = -sum_ijab (ia|jb) [2 (ia|jb) - (ib|ja)] / (e_a + e_b - e_i - e_j) from
+ * the CHEMISTS'-notation MO tensor mo_eri(p,q,r,s) = (pq|rs) (nmo^4,
+ * column-major, occupied first) and the orbital energies eps (nmo).  FP64. */
+int scess_mp2_energy(scess_ctx *ctx, const double *mo_eri, const double *eps, int64_t nmo,
+                     int64_t nocc, double *e_mp2);
+
+/* MP2 from AO integrals, MP2_RHF_ClosedShellAO (RHF.cpp:267-304): ao_eri is
+ * (mu nu|kap lam) (nao^4), C the MO coefficients (nao x nmo, occupied first),
+ * eps (nmo); (a i|b j) is formed with scess_transform_tei's quarter transforms
+ * (C_virt, C_occ, C_virt, C_occ) and summed as the reference does.
+ * precision: FP64, or MIXED for the transform (the sum is FP64). */
+int scess_mp2_energy_ao(scess_ctx *ctx, const double *ao_eri, const double *C, const double *eps,
+                        int64_t nao, int64_t nmo, int64_t nocc, int32_t precision,
+                        double *e_mp2);
+
 /* scess_einsum's FP64 contraction for callers that cannot allocate device
  * memory.  No counterpart in the reference.  Some host programs own every byte
  * of the GPU: a framework whose caching allocator has reserved the device's

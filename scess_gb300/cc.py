@@ -123,6 +123,9 @@ EXPORTS = {
                                       _dp, C.c_int64, _dp, C.c_int64, C.c_int32, C.c_int32, _dp]),
     'scess_f12b_coupling': (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, C.c_int64, C.c_int64,
                                       C.c_int32, _dp, _dp]),
+    'scess_mp2_energy': (C.c_int, [C.c_void_p, _dp, _dp, C.c_int64, C.c_int64, _dp]),
+    'scess_mp2_energy_ao': (C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_int64, C.c_int64, C.c_int64,
+                                      C.c_int32, _dp]),
     'scess_einsum_static': (C.c_int, [C.c_char_p, C.c_double, C.c_void_p, C.c_int32, _i64p,
                                       C.c_void_p, C.c_int32, _i64p, C.c_double, C.c_void_p,
                                       C.c_int32, _i64p, C.c_void_p]),
@@ -422,6 +425,30 @@ class Context:
                                           _ptr(out))
         self._check(st, 'scess_transform_tei')
         return out
+
+    def mp2_energy(self, mo_chem, eps, nocc):
+        """MP2_RHF_ClosedShell (RHF.cpp:306-345) from chemists' MO integrals (pq|rs)."""
+        g = _f64(mo_chem)
+        N = g.shape[0]
+        e = _f64(eps, (N,))
+        out = C.c_double()
+        st = self.lib.scess_mp2_energy(self.h, _ptr(g), _ptr(e), N, int(nocc), C.byref(out))
+        self._check(st, 'scess_mp2_energy')
+        return out.value
+
+    def mp2_energy_ao(self, ao_chem, C_mo, eps, nocc, precision='fp64'):
+        """MP2_RHF_ClosedShellAO (RHF.cpp:267-304) from AO integrals (mu nu|kap lam) and
+        MO coefficients C (nao x nmo, occupied first)."""
+        g = _f64(ao_chem)
+        n = g.shape[0]
+        cm = _f64(C_mo)
+        nmo = cm.shape[1]
+        e = _f64(eps, (nmo,))
+        out = C.c_double()
+        st = self.lib.scess_mp2_energy_ao(self.h, _ptr(g), _ptr(cm), _ptr(e), n, nmo, int(nocc),
+                                          PRECISION[precision], C.byref(out))
+        self._check(st, 'scess_mp2_energy_ao')
+        return out.value
 
     def f12b_coupling(self, eri, f12, f12_repulsion, C, nocc, precision='fp64'):
         """The CCSD-F12b coupling of CCSD_F12b.cpp:83-94: V_klab = <kl|r12^-1 f12|ab>

@@ -864,4 +864,72 @@ int scess_f12b_coupling(scess_ctx *ctx, const double *eri, const double *f12,
   });
 }
 
+int scess_mp2_energy(scess_ctx *ctx, const double *mo_eri, const double *eps, int64_t nmo,
+                     int64_t nocc, double *e_mp2) {
+  return guard(ctx, [&](scess::Ctx &c) {
+    check_shape(nmo, nocc);
+    need(mo_eri, "mo_eri");
+    need(eps, "eps");
+    need(e_mp2, "e_mp2");
+    host_finite(eps, nmo, "eps");
+    const int64_t N = nmo, o = nocc, v = N - o, N2 = N * N;
+    scess::DTensor g = device_eri(c, mo_eri, nullptr, 0, N);
+    scess::DTensor de({N});
+    scess::upload(c, de.p(), eps, N);
+    // (ia|jb) = g(i, o+a, j, o+b)                                          RHF.cpp:334
+    scess::mp2_energy(o, v, g.p() + o * N + o * N2 * N, 1, N, N2, N2 * N, de.p(), c.partials,
+                      c.dscalars, c.stream);
+    SCESS_CUDA(cudaMemcpyAsync(c.hscalars, c.dscalars, sizeof(double), cudaMemcpyDeviceToHost,
+                               c.stream));
+    c.sync();
+    *e_mp2 = c.hscalars[0];
+  });
+}
+
+int scess_mp2_energy_ao(scess_ctx *ctx, const double *ao_eri, const double *C, const double *eps,
+                        int64_t nao, int64_t nmo, int64_t nocc, int32_t precision,
+                        double *e_mp2) {
+  return guard(ctx, [&](scess::Ctx &c) {
+    check_shape(nmo, nocc);
+    need(ao_eri, "ao_eri");
+    need(C, "C");
+    need(eps, "eps");
+    need(e_mp2, "e_mp2");
+    if (nao <= 0) throw Error(SCESS_ERR_INVALID, "bad dimensions");
+    if (precision != SCESS_PRECISION_FP64 && precision != SCESS_PRECISION_MIXED)
+      throw Error(SCESS_ERR_INVALID, "bad precision");
+    host_finite(eps, nmo, "eps");
+    const scess::Backend be =
+        precision == SCESS_PRECISION_MIXED ? scess::Backend::TENSOR : scess::Backend::FP64;
+    const int64_t n = nao, o = nocc, v = nmo - nocc;
+    scess::DTensor dC({n, nmo});
+    scess::upload(c, dC.p(), C, n * nmo);
+    device_finite(c, dC.p(), n * nmo, "C");
+    const scess::TV Cocc = scess::cm(dC.p(), {n, o}), Cvirt = scess::cm(dC.p() + n * o, {n, v});
+    // (a i|b j) = TransformTEI(aoERI, C_virt, C_occ, C_virt, C_occ), the last
+    // index first                                                            RHF.cpp:282-283
+    scess::DTensor x({n, n, n, n});
+    scess::upload(c, x.p(), ao_eri, n * n * n * n);
+    device_finite(c, x.p(), n * n * n * n, "ao_eri");
+    scess::DTensor y({n, n, n, o});
+    scess::einsum(c, "mnkl,ls->mnks", 1.0, x.v, Cocc, 0.0, y.v, be);
+    x = scess::DTensor({n, n, v, o});
+    scess::einsum(c, "mnks,kr->mnrs", 1.0, y.v, Cvirt, 0.0, x.v, be);
+    y = scess::DTensor({n, o, v, o});
+    scess::einsum(c, "mnrs,nq->mqrs", 1.0, x.v, Cocc, 0.0, y.v, be);
+    x = scess::DTensor({v, o, v, o});
+    scess::einsum(c, "mqrs,mp->pqrs", 1.0, y.v, Cvirt, 0.0, x.v, be);
+    scess::DTensor de({nmo});
+    scess::upload(c, de.p(), eps, nmo);
+    // (ia|jb) = aibj(a, i, b, j)                                            RHF.cpp:292
+    scess::mp2_energy(o, v, x.p(), v, 1, v * o * v, v * o, de.p(), c.partials, c.dscalars,
+                      c.stream);
+    SCESS_CUDA(cudaMemcpyAsync(c.hscalars, c.dscalars, sizeof(double), cudaMemcpyDeviceToHost,
+                               c.stream));
+    c.sync();
+    *e_mp2 = c.hscalars[0];
+    if (precision == SCESS_PRECISION_MIXED) c.tensor_cores().check_error();
+  });
+}
+
 }  // extern "C"

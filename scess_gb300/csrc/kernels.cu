@@ -347,6 +347,24 @@ __global__ void tau_energy_partial_kernel(int64_t o, int64_t v, const double *__
   if (threadIdx.x == 0) partials[blockIdx.x] = s;
 }
 
+// MP2 (RHF.cpp:289-296, 324-340): x = (ia|jb) = g[i si + a sa + j sj + b sb],
+// y = (ib|ja) (a and b swapped), eps occupied first.
+__global__ void mp2_partial_kernel(int64_t o, int64_t v, const double *__restrict__ g, int64_t si,
+                                   int64_t sa, int64_t sj, int64_t sb,
+                                   const double *__restrict__ eps, double *__restrict__ partials) {
+  const int64_t n = o * v * o * v;
+  double s = 0.0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e % o, a = (e / o) % v, j = (e / (o * v)) % o, b = e / (o * v * o);
+    const double x = g[i * si + a * sa + j * sj + b * sb];
+    const double y = g[i * si + b * sa + j * sj + a * sb];
+    s -= x * (2.0 * x - y) / (eps[o + a] + eps[o + b] - eps[i] - eps[j]);
+  }
+  s = block_sum(s);
+  if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
 __global__ void lincomb_kernel(int64_t n, int nv, const double *const *__restrict__ vecs,
                                const double *__restrict__ coef, double *__restrict__ out) {
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
@@ -415,6 +433,15 @@ void linear_combination(int64_t n, int nv, const double *const *vecs, const doub
 void tau_energy(int64_t o, int64_t v, const double *L, const double *t1, const double *t2,
                 double *partials, double *result, cudaStream_t stream) {
   tau_energy_partial_kernel<<<kDotBlocks, 256, 0, stream>>>(o, v, L, t1, t2, partials);
+  SCESS_CHECK_LAUNCH();
+  sum_partials_kernel<<<1, 1024, 0, stream>>>(kDotBlocks, partials, result);
+  SCESS_CHECK_LAUNCH();
+}
+
+void mp2_energy(int64_t o, int64_t v, const double *g, int64_t si, int64_t sa, int64_t sj,
+                int64_t sb, const double *eps, double *partials, double *result,
+                cudaStream_t stream) {
+  mp2_partial_kernel<<<kDotBlocks, 256, 0, stream>>>(o, v, g, si, sa, sj, sb, eps, partials);
   SCESS_CHECK_LAUNCH();
   sum_partials_kernel<<<1, 1024, 0, stream>>>(kDotBlocks, partials, result);
   SCESS_CHECK_LAUNCH();

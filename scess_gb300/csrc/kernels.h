@@ -68,6 +68,12 @@ void linear_combination(int64_t n, int nv, const double *const *vecs, const doub
 // result[0] = sum L(i,j,a,b) * (t2 + t1 t1)(i,j,a,b)  (CorrelationEnergy) deterministic
 void tau_energy(int64_t o, int64_t v, const double *L, const double *t1, const double *t2,
                 double *partials, double *result, cudaStream_t stream);
+// result[0] = E_MP2 = -sum (ia|jb) [2 (ia|jb) - (ib|ja)] / (e_a + e_b - e_i - e_j), with
+// (ia|jb) = g[i si + a sa + j sj + b sb] and (ib|ja) the same with a, b swapped;
+// deterministic (RHF.cpp:289-296, 324-340)
+void mp2_energy(int64_t o, int64_t v, const double *g, int64_t si, int64_t sa, int64_t sj,
+                int64_t sb, const double *eps, double *partials, double *result,
+                cudaStream_t stream);
 // any non-finite value in x -> flag[0] = 1
 void check_finite(int64_t n, const double *x, int *flag, cudaStream_t stream);
 

@@ -10,11 +10,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 # Known-answer energies of the reference's regression tests, src/SCESS/Tests.cpp:34-75
 # (value, tolerance used there; checks at :570-577, :594-607, :684-704).
 PINS = {
-    'h2_sto3g': {'E_RHF': (-1.1175058851, 1e-8), 'E_CCSD': (-0.0193419373, 1e-8)},
-    'h2o_sto3g': {'E_RHF': (-74.9629832288, 1e-6), 'E_CCSD': (-0.0494026324, 1e-7),
-                  'E_T': (-0.0000673499, 1e-8)},
-    'h2o_ccpvdz': {'E_RHF': (-76.0267859418, 1e-8), 'E_CCSD': (-0.2133077024, 1e-7),
-                   'E_T': (-0.0030574132, 1e-7)},
+    'h2_sto3g': {'E_RHF': (-1.1175058851, 1e-8), 'E_MP2': (-0.0125038087, 1e-8),
+                 'E_CCSD': (-0.0193419373, 1e-8)},
+    'h2o_sto3g': {'E_RHF': (-74.9629832288, 1e-6), 'E_MP2': (-0.0355225667, 1e-7),
+                  'E_CCSD': (-0.0494026324, 1e-7), 'E_T': (-0.0000673499, 1e-8)},
+    'h2o_ccpvdz': {'E_RHF': (-76.0267859418, 1e-8), 'E_MP2': (-0.2039840885, 1e-8),
+                   'E_CCSD': (-0.2133077024, 1e-7), 'E_T': (-0.0030574132, 1e-7)},
 }
 
 
