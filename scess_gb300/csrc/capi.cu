@@ -1,5 +1,6 @@
 // C ABI of the engine (include/scess_cc.h): argument checks, host<->device
 // transfers and exception-to-status translation around the C++ drivers.
+#include <memory>
 #include <vector>
 #include <chrono>
 #include <cmath>
@@ -76,38 +77,32 @@ void device_finite(scess::Ctx &ctx, const double *x, int64_t n, const char *what
   if (h) throw Error(SCESS_ERR_INVALID, std::string("non-finite value in ") + what);
 }
 
-// eri (nmo^4) on the device, from the host eri or from DF factors: an FP64
-// build, or for mixed-precision solves a tensor-core build (split FP16 hi/lo
-// products, ~2e-7 relative per element, 2 naux nmo^4 FLOPs in milliseconds
-// instead of seconds at the FP64 rate).
 double ms_since(std::chrono::steady_clock::time_point t0) {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
-scess::DTensor device_eri(scess::Ctx &ctx, const double *eri, const double *B, int64_t naux,
-                          int64_t N, bool mixed_build = false) {
+// eri (nmo^4) on the device from the host eri, checked finite.  DF inputs never
+// come here: their states contract the integral blocks they read from B.
+scess::DTensor device_eri(scess::Ctx &ctx, const double *eri, int64_t N) {
   auto t0 = std::chrono::steady_clock::now();
   scess::DTensor d({N, N, N, N});
   ctx.timer.host("eri_alloc", ms_since(t0));
-  if (eri) {
-    t0 = std::chrono::steady_clock::now();
-    scess::upload(ctx, d.p(), eri, N * N * N * N);
-    ctx.timer.host("eri_upload", ms_since(t0));
-    t0 = std::chrono::steady_clock::now();
-    device_finite(ctx, d.p(), N * N * N * N, "eri");
-    ctx.timer.host("eri_check", ms_since(t0));
-  } else {
-    scess::DTensor dB({naux, N, N});
-    scess::upload(ctx, dB.p(), B, naux * N * N);
-    device_finite(ctx, dB.p(), naux * N * N, "B");
-    // eri(p,q,r,s) = (pr|qs) = sum_Q B(Q,p,r) B(Q,q,s)
-    t0 = std::chrono::steady_clock::now();
-    scess::einsum(ctx, "Qpr,Qqs->pqrs", 1.0, dB.v, dB.v, 0.0, d.v,
-                  mixed_build ? scess::Backend::TENSOR : scess::Backend::FP64);
-    ctx.sync();
-    ctx.timer.host("eri_from_B", ms_since(t0));
-  }
+  t0 = std::chrono::steady_clock::now();
+  scess::upload(ctx, d.p(), eri, N * N * N * N);
+  ctx.timer.host("eri_upload", ms_since(t0));
+  t0 = std::chrono::steady_clock::now();
+  device_finite(ctx, d.p(), N * N * N * N, "eri");
+  ctx.timer.host("eri_check", ms_since(t0));
   return d;
+}
+
+// DF factors B (naux x nmo x nmo) on the device, checked finite.
+scess::DTensor device_B(scess::Ctx &ctx, const double *B, int64_t naux, int64_t N) {
+  if (naux <= 0) throw Error(SCESS_ERR_INVALID, "bad naux");
+  scess::DTensor dB({naux, N, N});
+  scess::upload(ctx, dB.p(), B, naux * N * N);
+  device_finite(ctx, dB.p(), naux * N * N, "B");
+  return dB;
 }
 
 scess::RccsdState *make_state(scess::Ctx &c, const double *eri, const double *B, int64_t naux,
@@ -123,13 +118,22 @@ scess::RccsdState *make_state(scess::Ctx &c, const double *eri, const double *B,
   const int64_t v = nmo - nocc;
   if (f12_residual) host_finite(f12_residual, nocc * nocc * v * v, "f12_residual");
   if (f12_energy) host_finite(f12_energy, nocc * nocc * v * v, "f12_energy");
-  scess::DTensor d_eri = device_eri(c, eri, B, naux, nmo, o.precision == SCESS_PRECISION_MIXED);
   scess::SolveInput in;
   in.eps_host = eps;
   in.f12_residual = f12_residual;
   in.f12_energy = f12_energy;
+  scess::RccsdState *st = nullptr;
+  if (B) {  // DF state: the integral blocks are contracted from B, no nmo^4 eri
+    scess::DTensor dB = device_B(c, B, naux, nmo);
+    const auto t0 = std::chrono::steady_clock::now();
+    st = new scess::RccsdState(c, std::move(dB), naux, nmo, nocc, in, o);
+    c.sync();
+    c.timer.host("state_build", ms_since(t0));
+    return st;
+  }
+  scess::DTensor d_eri = device_eri(c, eri, nmo);
   const auto t0 = std::chrono::steady_clock::now();
-  auto *st = new scess::RccsdState(c, std::move(d_eri), nmo, nocc, in, o);
+  st = new scess::RccsdState(c, std::move(d_eri), nmo, nocc, in, o);
   c.sync();
   c.timer.host("state_build", ms_since(t0));
   return st;
@@ -159,13 +163,17 @@ int solve_common(scess_ctx *ctx, const double *eri, const double *B, int64_t nau
     ctl.cancel = c.cancel;
     ctl.user = c.user;
     ctl.time_limit_s = o.time_limit_s;
-    scess::DTensor d_eri = device_eri(c, eri, B, naux, nmo, o.precision == SCESS_PRECISION_MIXED);
-    ctl.poll();
     scess::SolveInput in;
     in.eps_host = eps;
     in.f12_residual = f12_residual;
     in.f12_energy = f12_energy;
-    scess::RccsdState st(c, std::move(d_eri), nmo, nocc, in, o);
+    std::unique_ptr<scess::RccsdState> stp;
+    if (B)  // DF: the integral blocks are contracted from B, no nmo^4 eri
+      stp.reset(new scess::RccsdState(c, device_B(c, B, naux, nmo), naux, nmo, nocc, in, o));
+    else
+      stp.reset(new scess::RccsdState(c, device_eri(c, eri, nmo), nmo, nocc, in, o));
+    ctl.poll();
+    scess::RccsdState &st = *stp;
     if (o.resume) st.set_amplitudes(t1_out, t2_out);
     else st.mp2_guess();
     scess::rccsd_solve(c, st, ctl, t1_out, t2_out, result);
@@ -285,7 +293,7 @@ static int triples_common(scess_ctx *ctx, const double *eri, const double *B, in
     // the device; the nmo^4 eri is not built
     scess::DTensor d_eri, dB;
     if (eri) {
-      d_eri = device_eri(c, eri, nullptr, 0, nmo);
+      d_eri = device_eri(c, eri, nmo);
     } else {
       dB = scess::DTensor({naux, nmo, nmo});
       scess::upload(c, dB.p(), B, naux * nmo * nmo);
@@ -485,8 +493,10 @@ int scess_rccsd_state_triples(scess_rccsd_state *state, int32_t precision, doubl
     SCESS_CUDA(cudaEventCreate(&b));
     SCESS_CUDA(cudaEventRecord(a, c.stream));
     auto *st = state->impl;
+    // a DF state's (T) contracts its integral slices from B
     *e_t = scess::rccsd_triples(c, st->d_eri(), st->nmo(), st->nocc(), st->d_eps(), st->d_t1(),
-                                st->d_t2(), precision == SCESS_PRECISION_MIXED, ctl);
+                                st->d_t2(), precision == SCESS_PRECISION_MIXED, ctl, nullptr,
+                                st->d_B(), st->naux());
     SCESS_CUDA(cudaEventRecord(b, c.stream));
     SCESS_CUDA(cudaEventSynchronize(b));
     float ms = 0.0f;
@@ -551,7 +561,7 @@ int scess_rccsd_residual(scess_ctx *ctx, const double *eri, int64_t nmo, int64_t
     need(r1_out, "r1_out");
     need(r2_out, "r2_out");
     const int64_t o = nocc, v = nmo - nocc, n1 = o * v, n2 = o * o * v * v;
-    scess::DTensor d_eri = device_eri(c, eri, nullptr, 0, nmo);
+    scess::DTensor d_eri = device_eri(c, eri, nmo);
     scess::RccsdBlocks blocks;
     blocks.build(c, d_eri.p(), nmo, nocc);
     scess::DTensor amp({n1 + n2}), R({n1 + n2}), drv;
@@ -667,7 +677,7 @@ int scess_rccsd_lambda(scess_ctx *ctx, const double *eri, const double *eps, int
     ctl.cancel = c.cancel;
     ctl.user = c.user;
     ctl.time_limit_s = o.time_limit_s;
-    scess::DTensor d_eri = device_eri(c, eri, nullptr, 0, nmo);
+    scess::DTensor d_eri = device_eri(c, eri, nmo);
     scess::DTensor amp({n1 + n2}), lam({n1 + n2});
     scess::upload(c, amp.p(), t1, n1);
     scess::upload(c, amp.p() + n1, t2, n2);
@@ -699,7 +709,7 @@ int scess_rccsd_rdm1(scess_ctx *ctx, const double *eri, const double *eps, int64
     need(l2, "l2");
     need(dm1_out, "dm1_out");
     const int64_t oc = nocc, v = nmo - nocc, n1 = oc * v, n2 = oc * oc * v * v;
-    scess::DTensor d_eri = device_eri(c, eri, nullptr, 0, nmo);
+    scess::DTensor d_eri = device_eri(c, eri, nmo);
     scess::DTensor amp({n1 + n2}), lam({n1 + n2}), dm({nmo, nmo});
     scess::upload(c, amp.p(), t1, n1);
     scess::upload(c, amp.p() + n1, t2, n2);
@@ -837,7 +847,7 @@ int scess_f12b_coupling(scess_ctx *ctx, const double *eri, const double *f12,
     host_finite(f12_klrs.data(), (int64_t)f12_klrs.size(), "f12");
     host_finite(rep_klab.data(), (int64_t)rep_klab.size(), "f12_repulsion");
     host_finite(C, o * o * v * v, "C");
-    scess::DTensor d_eri = device_eri(c, eri, nullptr, 0, N);
+    scess::DTensor d_eri = device_eri(c, eri, N);
     scess::DTensor dF({o, o, N, N}), V({o, o, v, v}), dC({o, o, v, v});
     scess::upload(c, dF.p(), f12_klrs.data(), o * o * N2);
     scess::upload(c, V.p(), rep_klab.data(), o * o * v * v);
@@ -873,7 +883,7 @@ int scess_mp2_energy(scess_ctx *ctx, const double *mo_eri, const double *eps, in
     need(e_mp2, "e_mp2");
     host_finite(eps, nmo, "eps");
     const int64_t N = nmo, o = nocc, v = N - o, N2 = N * N;
-    scess::DTensor g = device_eri(c, mo_eri, nullptr, 0, N);
+    scess::DTensor g = device_eri(c, mo_eri, N);
     scess::DTensor de({N});
     scess::upload(c, de.p(), eps, N);
     // (ia|jb) = g(i, o+a, j, o+b)                                          RHF.cpp:334

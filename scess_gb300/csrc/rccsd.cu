@@ -53,6 +53,64 @@ void RccsdBlocks::build(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t nocc
   vvvv = view(e, o * (N1 + N2 + N3 + N4), {v, v, v, v}, {N1, N2, N3, N4});
   // oovv_phys(i,j,a,b) = <ij|ab>                                                    :66
   oovv_phys = view(e, o * N3 + o * N4, {o, o, v, v}, {N1, N2, N3, N4});
+  build_l(ctx);
+}
+
+void RccsdBlocks::build_df(Ctx &ctx, const double *d_B, int64_t naux, int64_t nmo, int64_t nocc,
+                           Backend be) {
+  o = nocc;
+  v = nmo - nocc;
+  N = nmo;
+  regions.clear();
+  regions.reserve(7);
+  // <pq|rs> = (pr|qs) = sum_Q B(Q,p,r) B(Q,q,s) over the index ranges of one
+  // region, stored (p, q, r, s) column-major
+  auto region = [&](int64_t p0, int64_t np, int64_t q0, int64_t nq, int64_t r0, int64_t nr,
+                    int64_t s0, int64_t ns) -> double * {
+    auto bview = [&](int64_t a0, int64_t na, int64_t b0, int64_t nb) {
+      TV t;
+      t.p = const_cast<double *>(d_B) + naux * a0 + naux * N * b0;
+      t.nd = 3;
+      const int64_t e3[3] = {naux, na, nb}, s3[3] = {1, naux, naux * N};
+      std::memcpy(t.ext, e3, sizeof(e3));
+      std::memcpy(t.str, s3, sizeof(s3));
+      return t;
+    };
+    regions.emplace_back(DTensor({np, nq, nr, ns}));
+    einsum(ctx, "Qpr,Qqs->pqrs", 1.0, bview(p0, np, r0, nr), bview(q0, nq, s0, ns), 0.0,
+           regions.back().v, be);
+    return regions.back().p();
+  };
+  auto tv = [](double *p, std::initializer_list<int64_t> ext, std::initializer_list<int64_t> str) {
+    TV t;
+    t.p = p;
+    t.nd = (int)ext.size();
+    int d = 0;
+    for (int64_t e : ext) t.ext[d++] = e;
+    d = 0;
+    for (int64_t x : str) t.str[d++] = x;
+    return t;
+  };
+  const int64_t o2 = o * o, ov = o * v;
+  // <kl|cd>: ovov(k,c,l,d) and oovv_phys(i,j,a,b)                               :55, :66
+  double *r_oovv = region(0, o, 0, o, o, v, o, v);
+  ovov = tv(r_oovv, {o, v, o, v}, {1, o2, o, o2 * v});
+  oovv_phys = tv(r_oovv, {o, o, v, v}, {1, o, o2, o2 * v});
+  // <ka|ic>: oovv(k,i,a,c)                                                        :57
+  oovv = tv(region(0, o, o, v, 0, o, o, v), {o, o, v, v}, {1, ov, o, o2 * v});
+  // <ka|ci>: ovvo(k,c,a,i)                                                        :59
+  ovvo = tv(region(0, o, o, v, o, v, 0, o), {o, v, v, o}, {1, ov, o, ov * v});
+  // <ka|dc>: ovvv(k,d,a,c)                                                        :61
+  ovvv = tv(region(0, o, o, v, o, v, o, v), {o, v, v, v}, {1, ov, o, ov * v});
+  // <lk|ci>: ovoo(l,c,k,i)                                                        :63
+  ovoo = tv(region(0, o, 0, o, o, v, 0, o), {o, v, o, o}, {1, o2, o, o2 * v});
+  // <kl|ij>, <ab|cd>                                                           :64-65
+  oooo = tv(region(0, o, 0, o, 0, o, 0, o), {o, o, o, o}, {1, o, o2, o2 * o});
+  vvvv = tv(region(o, v, o, v, o, v, o, v), {v, v, v, v}, {1, v, v * v, v * v * v});
+  build_l(ctx);
+}
+
+void RccsdBlocks::build_l(Ctx &ctx) {
   // L_oovv = 2 <ij|ab> - <ij|ba>                                                   :68-69
   L_oovv = DTensor({o, o, v, v});
   permute(ctx, "ijab->ijab", 2.0, oovv_phys, 0.0, L_oovv.v);
@@ -279,6 +337,21 @@ RccsdState::RccsdState(Ctx &ctx, DTensor &&eri, int64_t nmo, int64_t nocc, const
                        const scess_rccsd_options &opts)
     : ctx_(ctx), eri_(std::move(eri)), opts_(opts) {
   B_.build(ctx, eri_.p(), nmo, nocc);
+  init(in, opts);
+}
+
+RccsdState::RccsdState(Ctx &ctx, DTensor &&B, int64_t naux, int64_t nmo, int64_t nocc,
+                       const SolveInput &in, const scess_rccsd_options &opts)
+    : ctx_(ctx), dfB_(std::move(B)), naux_(naux), opts_(opts) {
+  // mixed solves contract the regions on the tensor cores (~3e-7 relative per
+  // integral), FP64 solves exactly
+  B_.build_df(ctx, dfB_.p(), naux, nmo, nocc,
+              opts.precision == SCESS_PRECISION_MIXED ? Backend::TENSOR : Backend::FP64);
+  init(in, opts);
+}
+
+void RccsdState::init(const SolveInput &in, const scess_rccsd_options &opts) {
+  Ctx &ctx = ctx_;
   const int64_t o = B_.o, v = B_.v, N = B_.N;
   n1_ = o * v;
   n2_ = o * o * v * v;

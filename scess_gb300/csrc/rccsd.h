@@ -13,7 +13,16 @@ struct RccsdBlocks {
   int64_t o = 0, v = 0, N = 0;
   TV ovov, oovv, ovvo, ovvv, ovoo, oooo, vvvv, oovv_phys;
   DTensor L_oovv, L_ovov;
+  std::vector<DTensor> regions;  // DF build: the eri regions the views point into
+  // views into the device eri (nmo^4)
   void build(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t nocc);
+  // from DF factors B (naux x nmo x nmo): only the seven regions of <pq|rs> the
+  // views need are contracted (no nmo^4 tensor); be: FP64 or the tensor cores
+  void build_df(Ctx &ctx, const double *d_B, int64_t naux, int64_t nmo, int64_t nocc,
+                Backend be);
+
+ private:
+  void build_l(Ctx &ctx);
 };
 
 // Device work arrays of one residual evaluation.
@@ -45,6 +54,9 @@ class RccsdState {
  public:
   RccsdState(Ctx &ctx, DTensor &&eri, int64_t nmo, int64_t nocc, const SolveInput &in,
              const scess_rccsd_options &opts);
+  // DF state: B (naux x nmo x nmo) on the device; no nmo^4 eri is formed
+  RccsdState(Ctx &ctx, DTensor &&B, int64_t naux, int64_t nmo, int64_t nocc,
+             const SolveInput &in, const scess_rccsd_options &opts);
   ~RccsdState();
   void mp2_guess();
   void set_amplitudes(const double *t1, const double *t2);
@@ -58,7 +70,9 @@ class RccsdState {
   bool has_f12() const { return have_f12_; }
   float last_device_ms() const { return last_device_ms_; }
   const RccsdBlocks &blocks() const { return B_; }
-  const double *d_eri() const { return eri_.p(); }
+  const double *d_eri() const { return eri_.p(); }  // null for a DF state
+  const double *d_B() const { return dfB_.p(); }     // null unless a DF state
+  int64_t naux() const { return naux_; }
   const double *d_eps() const { return eps_.p(); }
   const double *d_t1() const { return amp_.p(); }
   const double *d_t2() const { return amp_.p() + n1_; }
@@ -67,8 +81,11 @@ class RccsdState {
 
  private:
   void reset_history();
+  void init(const SolveInput &in, const scess_rccsd_options &opts);
   Ctx &ctx_;
   DTensor eri_;
+  DTensor dfB_;
+  int64_t naux_ = 0;
   RccsdBlocks B_;
   scess_rccsd_options opts_;
   int64_t n1_ = 0, n2_ = 0, n_ = 0;

@@ -69,16 +69,42 @@ def test_solve_df_equals_eri_path(gctx):
     assert abs(a.E_CCSD - b.E_CCSD) < 1e-11
 
 
-def test_solve_df_mixed_builds_eri_on_tensor_cores(gctx):
-    """Mixed DF solve: the nmo^4 eri is contracted from B on the tensor cores
-    (~2e-7 relative per integral); the energy stays within 1 uEh of the FP64
-    eri-path solve."""
-    from scess_gb300.synthetic import convergent_sigma
+def test_solve_df_mixed_builds_blocks_on_tensor_cores(gctx):
+    """Mixed DF solve: the integral blocks are contracted from B on the tensor
+    cores (~3e-7 relative per integral); the energy stays within 1 uEh of the
+    FP64 eri-path solve."""
     w = make_workload(8, 40, seed=5, sigma=convergent_sigma(8, 40))
     a = gctx.solve(w.eri(), w.eps, 8)
     b = gctx.solve(None, w.eps, 8, B=w.B, precision='mixed')
     assert b.converged
     assert abs(a.E_CCSD - b.E_CCSD) < 1e-6
+
+
+@pytest.mark.parametrize('o,v', [(5, 19), (9, 44)])
+def test_df_state_matches_eri_state(gctx, o, v):
+    """A DF state contracts only the seven integral regions CCSD reads from B
+    (no nmo^4 eri is allocated) and its (T) forms its slices from B: energies,
+    amplitudes and E_(T) equal the eri state's."""
+    w = make_workload(o, v, seed=4, sigma=convergent_sigma(o, v))
+    sa = gctx.state(w.eri(), w.eps, o, max_iterations=200)
+    gctx.profile(True)
+    sb = gctx.state(None, w.eps, o, B=w.B, max_iterations=200)
+    rep = gctx.profile_report()
+    gctx.profile(False)
+    assert 'host:state_build' in rep
+    assert not any('eri_alloc' in k or 'eri_upload' in k for k in rep)
+    ra, rb = sa.iterate(200)[0], sb.iterate(200)[0]
+    assert ra.converged and rb.converged
+    assert abs(ra.E_CCSD - rb.E_CCSD) < 1e-10
+    t1a, t2a = sa.amplitudes()
+    t1b, t2b = sb.amplitudes()
+    assert rel_err(t2b, t2a) < 1e-8
+    ea, eb = sa.triples()[0], sb.triples()[0]
+    assert abs(ea - eb) < 1e-11
+    em = sb.triples(precision='mixed')[0]
+    assert abs(em - ea) < 1e-6  # the mixed-precision bar: 1 uEh
+    sa.close()
+    sb.close()
 
 
 def test_f12_coupling_matches_oracle(gctx):
