@@ -131,8 +131,9 @@ int scess_rccsd_solve(scess_ctx *ctx, const double *eri, const double *eps, int6
                       const scess_rccsd_options *opts, double *t1_out, double *t2_out,
                       scess_rccsd_result *result);
 
-/* Same as scess_rccsd_solve, from DF factors B (naux x nmo x nmo): the integral
- * blocks are built on the GPU and the nmo^4 eri never crosses the bus. */
+/* Same as scess_rccsd_solve, from DF factors B (naux x nmo x nmo): only the
+ * regions of <pq|rs> the integral blocks read are contracted from B on the GPU
+ * (on the tensor cores for SCESS_PRECISION_MIXED); no nmo^4 eri is formed. */
 int scess_rccsd_solve_df(scess_ctx *ctx, const double *B, int64_t naux, const double *eps,
                          int64_t nmo, int64_t nocc, const double *f12_residual,
                          const double *f12_energy, const scess_rccsd_options *opts,
@@ -163,6 +164,8 @@ typedef struct scess_rccsd_state scess_rccsd_state;
 int scess_rccsd_state_create(scess_ctx *ctx, const double *eri, const double *eps, int64_t nmo,
                              int64_t nocc, const double *f12_residual, const double *f12_energy,
                              const scess_rccsd_options *opts, scess_rccsd_state **out);
+/* DF state: keeps B and the integral regions contracted from it (no nmo^4
+ * eri); scess_rccsd_state_triples on it forms the (T) slices from B. */
 int scess_rccsd_state_create_df(scess_ctx *ctx, const double *B, int64_t naux, const double *eps,
                                 int64_t nmo, int64_t nocc, const double *f12_residual,
                                 const double *f12_energy, const scess_rccsd_options *opts,
