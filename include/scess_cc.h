@@ -307,6 +307,33 @@ int scess_mp2_energy_ao(scess_ctx *ctx, const double *ao_eri, const double *C, c
                         int64_t nao, int64_t nmo, int64_t nocc, int32_t precision,
                         double *e_mp2);
 
+/* ---- Spin-orbital cross-check solvers (CC.h:45-85).  The reference keeps
+ * them to test the closed-shell solvers; they hold (2 nmo)^4 integrals and,
+ * for (T), three o^3 v^3 spin-orbital tensors (o = 2 nocc, v = 2 nvirt).
+ *
+ * Spin-orbital CCSD (CCSD.cpp:21-106) or, with diis != 0, CCSD_DIIS
+ * (CCSD-DIIS.cpp:17-198) from the CHEMISTS' MO integrals mo_eri(p,q,r,s) =
+ * (pq|rs) (nmo^4, column-major, occupied first) and the canonical orbital
+ * energies eps (nmo): <pq||rs> over 2 nmo spin orbitals (p = 2 x spatial +
+ * spin; AntisymmetriseIntegrateOutSpinClosedShell, IntegralTransforms.cpp:
+ * 135-162), t2 guess <ij||ab> / D_ijab, energy convergence 1e-6 within 50
+ * iterations, DIIS over 6 vectors from iteration 3.  With triples != 0 and a
+ * converged solve, result->E_T is the triples correction of CCSD_T
+ * (CCSD_T.cpp:18-66).  t1_out (o x v) and t2_out (o x o x v x v) receive the
+ * final amplitudes; g_out ((2 nmo)^4, may be NULL) the antisymmetrised
+ * integrals (CCSD_Wfn::mints).  result: E_CCSD (0 unless converged, as the
+ * reference's empty CCSD_Wfn), E_T, converged, iterations, last_dE; the
+ * remaining fields are zero. */
+int scess_ccsd_so_solve(scess_ctx *ctx, const double *mo_eri, const double *eps, int64_t nmo,
+                        int64_t nocc, int32_t diis, int32_t triples, double *t1_out,
+                        double *t2_out, double *g_out, scess_rccsd_result *result);
+
+/* CalculateTriplesCorrection (CCSD_T.cpp:89-229) from the antisymmetrised
+ * spin-orbital integrals g ((2 nmo)^4, as scess_ccsd_so_solve's g_out), the
+ * spatial orbital energies eps (nmo) and spin-orbital t1, t2.  FP64. */
+int scess_ccsd_so_triples(scess_ctx *ctx, const double *g, const double *eps, int64_t nmo,
+                          int64_t nocc, const double *t1, const double *t2, double *e_t);
+
 /* scess_einsum's FP64 contraction for callers that cannot allocate device
  * memory.  No counterpart in the reference.  Some host programs own every byte
  * of the GPU: a framework whose caching allocator has reserved the device's

@@ -19,3 +19,7 @@ from .rccsd import (  # noqa: F401
 from .rccsd_t import rccsd_triples_correction, triples_flops  # noqa: F401
 from .f12 import f12b_coupling, contract_fixed_amplitudes  # noqa: F401
 from .mp2 import mp2_energy, mp2_energy_ao  # noqa: F401
+from .ccsd_so import (  # noqa: F401
+    antisymmetrise_spin, ccsd as ccsd_spin_orbital, ccsd_t as ccsd_t_spin_orbital,
+    triples_correction as spin_triples_correction,
+)

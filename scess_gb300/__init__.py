@@ -8,4 +8,5 @@ package exposes its C ABI through :mod:`scess_gb300.cc`, whose
 from .cc import (  # noqa: F401
     Context, RCCSD_Wfn, RCCSD_F12Coupling, ScessError, SolveRCCSD_DIIS,
     RCCSD_TriplesCorrection, load_library, EXPORTS, LIB_PATH,
+    CCSD_Wfn, CCSD, CCSD_DIIS, CCSD_T, CalculateTriplesCorrection,
 )

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, 'csrc')
 BUILD = os.path.join(HERE, '_build')
 LIB = os.path.join(HERE, 'libscess_cc.so')
 SOURCES = ['kernels.cu', 'engine.cu', 'gemm_tc.cu', 'rccsd.cu', 'triples.cu', 'adjoint.cu',
-           'capi.cu', 'einsum_static.cu']
+           'capi.cu', 'einsum_static.cu', 'ccsd_so.cu']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 
 

@@ -124,6 +124,10 @@ EXPORTS = {
     'scess_f12b_coupling': (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, C.c_int64, C.c_int64,
                                       C.c_int32, _dp, _dp]),
     'scess_mp2_energy': (C.c_int, [C.c_void_p, _dp, _dp, C.c_int64, C.c_int64, _dp]),
+    'scess_ccsd_so_solve': (C.c_int, [C.c_void_p, _dp, _dp, C.c_int64, C.c_int64, C.c_int32,
+                                      C.c_int32, _dp, _dp, _dp, C.POINTER(Result)]),
+    'scess_ccsd_so_triples': (C.c_int, [C.c_void_p, _dp, _dp, C.c_int64, C.c_int64, _dp, _dp,
+                                        C.POINTER(C.c_double)]),
     'scess_mp2_energy_ao': (C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_int64, C.c_int64, C.c_int64,
                                       C.c_int32, _dp]),
     'scess_einsum_static': (C.c_int, [C.c_char_p, C.c_double, C.c_void_p, C.c_int32, _i64p,
@@ -174,6 +178,19 @@ class RCCSD_Wfn:
     iterations: int = 0
     mixed_iterations: int = 0
     history: np.ndarray | None = field(default=None, repr=False)
+
+
+@dataclass
+class CCSD_Wfn:
+    """CCSD_Wfn, CC.h:28-35: the spin-orbital solvers' result (spin orbital
+    p = 2 x spatial + spin, occupied first)."""
+    E_CCSD: float = 0.0
+    E_T: float = 0.0
+    t1: np.ndarray | None = None
+    t2: np.ndarray | None = None
+    mints: np.ndarray | None = field(default=None, repr=False)
+    converged: bool = False
+    iterations: int = 0
 
 
 @dataclass
@@ -450,6 +467,37 @@ class Context:
         self._check(st, 'scess_mp2_energy_ao')
         return out.value
 
+    def ccsd_so(self, mo_chem, eps, nocc, diis=True, triples=False, keep_ints=False) -> CCSD_Wfn:
+        """Spin-orbital CCSD (CCSD.cpp:21-106), CCSD_DIIS (CCSD-DIIS.cpp:17-198) or, with
+        triples, CCSD_T (CCSD_T.cpp:18-66) from chemists' MO integrals (pq|rs)."""
+        g = _f64(mo_chem)
+        N = g.shape[0]
+        e = _f64(eps, (N,))
+        o, v = 2 * int(nocc), 2 * (N - int(nocc))
+        t1 = np.zeros((o, v), order='F')
+        t2 = np.zeros((o, o, v, v), order='F')
+        gs = np.zeros((2 * N,) * 4, order='F') if keep_ints else None
+        res = Result()
+        st = self.lib.scess_ccsd_so_solve(self.h, _ptr(g), _ptr(e), N, int(nocc), int(bool(diis)),
+                                          int(bool(triples)), _ptr(t1), _ptr(t2), _ptr(gs),
+                                          C.byref(res))
+        self._check(st, 'scess_ccsd_so_solve')
+        return CCSD_Wfn(E_CCSD=res.E_CCSD, E_T=res.E_T, t1=t1, t2=t2, mints=gs,
+                        converged=bool(res.converged), iterations=res.iterations)
+
+    def ccsd_so_triples(self, g, eps, nocc, t1, t2) -> float:
+        """CalculateTriplesCorrection (CCSD_T.cpp:89-229) from <pq||rs> ((2 nmo)^4)."""
+        e = _f64(eps)
+        N = e.shape[0]
+        o, v = 2 * int(nocc), 2 * (N - int(nocc))
+        gf = _f64(g, (2 * N,) * 4)
+        out = C.c_double()
+        st = self.lib.scess_ccsd_so_triples(self.h, _ptr(gf), _ptr(e), N, int(nocc),
+                                            _ptr(_f64(t1, (o, v))), _ptr(_f64(t2, (o, o, v, v))),
+                                            C.byref(out))
+        self._check(st, 'scess_ccsd_so_triples')
+        return out.value
+
     def f12b_coupling(self, eri, f12, f12_repulsion, C, nocc, precision='fp64'):
         """The CCSD-F12b coupling of CCSD_F12b.cpp:83-94: V_klab = <kl|r12^-1 f12|ab>
         - sum_rs <ab|rs><kl|f12|rs>, then RCCSD_F12Coupling(residual = F(C + V),
@@ -624,3 +672,26 @@ def RCCSD_TriplesCorrection(eri, orbitalEnergies, nOcc, t1, t2, thread=None,
     """CC::RCCSD_TriplesCorrection (CC.h:154-158) on the GPU."""
     return default_context().triples(eri, orbitalEnergies, nOcc, t1, t2, precision=precision,
                                      thread=thread)
+
+
+def CCSD(mo_chem, orbitalEnergies, nOcc) -> CCSD_Wfn:
+    """CC::CCSD (CC.h:53-62) on the GPU, from the MO integrals TransformTEI gives."""
+    return default_context().ccsd_so(mo_chem, orbitalEnergies, nOcc, diis=False)
+
+
+def CCSD_DIIS(mo_chem, orbitalEnergies, nOcc) -> CCSD_Wfn:
+    """CC::CCSD_DIIS (CC.h:64-72) on the GPU; ``mints`` holds <pq||rs>."""
+    return default_context().ccsd_so(mo_chem, orbitalEnergies, nOcc, diis=True, keep_ints=True)
+
+
+def CCSD_T(mo_chem, orbitalEnergies, nOcc) -> CCSD_Wfn:
+    """CC::CCSD_T (CC.h:74-76) on the GPU."""
+    return default_context().ccsd_so(mo_chem, orbitalEnergies, nOcc, diis=True, triples=True,
+                                     keep_ints=True)
+
+
+def CalculateTriplesCorrection(ccsd: CCSD_Wfn, F, eri, nOcc, nVirt) -> float:
+    """CC::CalculateTriplesCorrection (CC.h:78-81): F the spin-orbital Fock matrix
+    (diagonal), eri = <pq||rs>, nOcc / nVirt spin-orbital counts."""
+    eps = np.diag(np.asarray(F))[::2]
+    return default_context().ccsd_so_triples(eri, eps, int(nOcc) // 2, ccsd.t1, ccsd.t2)

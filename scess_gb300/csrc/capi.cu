@@ -8,6 +8,7 @@
 #include <new>
 
 #include "adjoint.h"
+#include "ccsd_so.h"
 #include "gemm_tc.h"
 #include "rccsd.h"
 #include "triples.h"
@@ -939,6 +940,67 @@ int scess_mp2_energy_ao(scess_ctx *ctx, const double *ao_eri, const double *C, c
     c.sync();
     *e_mp2 = c.hscalars[0];
     if (precision == SCESS_PRECISION_MIXED) c.tensor_cores().check_error();
+  });
+}
+
+int scess_ccsd_so_solve(scess_ctx *ctx, const double *mo_eri, const double *eps, int64_t nmo,
+                        int64_t nocc, int32_t diis, int32_t triples, double *t1_out,
+                        double *t2_out, double *g_out, scess_rccsd_result *result) {
+  return guard(ctx, [&](scess::Ctx &c) {
+    check_shape(nmo, nocc);
+    need(mo_eri, "mo_eri");
+    need(eps, "eps");
+    need(t1_out, "t1_out");
+    need(t2_out, "t2_out");
+    need(result, "result");
+    host_finite(eps, nmo, "eps");
+    const int64_t N = 2 * nmo, o = 2 * nocc, v = N - o;
+    scess::Control ctl;
+    ctl.cancel = c.cancel;
+    ctl.user = c.user;
+    scess::DTensor g({N, N, N, N});
+    {
+      scess::DTensor chem = device_eri(c, mo_eri, nmo);
+      scess::so_antisymmetrise(c, chem.p(), nmo, g.p());
+    }
+    scess::DTensor de({nmo}), t1({o, v}), t2({o, o, v, v});
+    scess::upload(c, de.p(), eps, nmo);
+    const scess::SoResult r =
+        scess::so_ccsd(c, g.p(), de.p(), nmo, nocc, diis != 0, triples != 0, ctl, t1.p(), t2.p());
+    scess::download(c, t1_out, t1.p(), o * v);
+    scess::download(c, t2_out, t2.p(), o * o * v * v);
+    if (g_out) scess::download(c, g_out, g.p(), N * N * N * N);
+    *result = scess_rccsd_result{};
+    result->E_CCSD = r.E_CCSD;
+    result->E_T = r.E_T;
+    result->converged = r.converged ? 1 : 0;
+    result->iterations = r.iterations;
+    result->last_dE = r.last_dE;
+  });
+}
+
+int scess_ccsd_so_triples(scess_ctx *ctx, const double *g, const double *eps, int64_t nmo,
+                          int64_t nocc, const double *t1, const double *t2, double *e_t) {
+  return guard(ctx, [&](scess::Ctx &c) {
+    check_shape(nmo, nocc);
+    need(g, "g");
+    need(eps, "eps");
+    need(t1, "t1");
+    need(t2, "t2");
+    need(e_t, "e_t");
+    host_finite(eps, nmo, "eps");
+    const int64_t N = 2 * nmo, o = 2 * nocc, v = N - o;
+    scess::Control ctl;
+    ctl.cancel = c.cancel;
+    ctl.user = c.user;
+    scess::DTensor dg = device_eri(c, g, N);
+    scess::DTensor de({nmo}), d1({o, v}), d2({o, o, v, v});
+    scess::upload(c, de.p(), eps, nmo);
+    scess::upload(c, d1.p(), t1, o * v);
+    scess::upload(c, d2.p(), t2, o * o * v * v);
+    device_finite(c, d1.p(), o * v, "t1");
+    device_finite(c, d2.p(), o * o * v * v, "t2");
+    *e_t = scess::so_triples(c, dg.p(), de.p(), nmo, nocc, d1.p(), d2.p(), ctl);
   });
 }
 
