@@ -44,6 +44,46 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *tm, in
       : "memory");
 }
 
+// Two-SM (cluster pair) forms.  The pair's even CTA issues the MMAs; its
+// shared-memory barriers count both CTAs' copies and both CTAs' drains.
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t cluster_id_x() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t nclusters_x() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// Address of the same shared-memory object in the pair's rank-0 CTA.
+__device__ __forceinline__ uint32_t leader_addr(const void *p) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, 0;" : "=r"(r) : "r"(smem_u32(p)));
+  return r;
+}
+// TMA load into this CTA's shared memory whose completion is counted on a
+// barrier of either CTA of the pair (cluster address).
+__device__ __forceinline__ void tma_load_2d_pair(void *dst, const CUtensorMap *tm, int x, int y,
+                                                 uint32_t bar_cluster) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes [%0], "
+      "[%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"((uint64_t)tm), "r"(x), "r"(y), "r"(bar_cluster)
+      : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar_cluster) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar_cluster) : "memory");
+}
+
 __device__ __forceinline__ void tc_fence_before() {
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
 }
@@ -87,6 +127,33 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64
 __device__ __forceinline__ void mma_commit(uint64_t *bar) {
   asm volatile(
       "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+// M = 256 over the pair: A rows 0-127 from this CTA's shared memory, 128-255
+// from the peer's at the same offset; B columns split likewise (N/2 each); D
+// rows 0-127 in this SM's TMEM, 128-255 in the peer's.
+__device__ __forceinline__ void mma2_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                          uint32_t idesc, uint32_t accum) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum));
+}
+// Arrive on the barrier at this offset in both CTAs of the pair once the
+// issued MMAs have completed.
+__device__ __forceinline__ void mma2_commit_both(uint64_t *bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+          smem_u32(bar)),
+      "h"((uint16_t)3)
+      : "memory");
+}
+__device__ __forceinline__ void mma2_commit(uint64_t *bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
           smem_u32(bar))
       : "memory");
 }
@@ -185,20 +252,26 @@ constexpr int V2_BN = 128;  // tile width of the einsum launches
 //             168 registers a thread, so the warpgroups rebalance with
 //             setmaxnreg: 56 for warps 0-3, 224 for the epilogue (3 x 168 =
 //             56 + 2 x 224 per scheduler).
+//   PAIR:     BN = 256, BK = 64 on a cluster pair (M = 256 per unit, 128 rows
+//             a CTA): each CTA stages its A rows and half of the B columns,
+//             64 KiB a stage, 3 stages.
 // Every epilogue thread holds 128 columns of one row.
-template <int BN, int BK_>
+template <int BN, int BK_, bool PAIR = false>
 struct TcShape {
   static_assert((BN == 128 && BK_ == 64) || (BN == 256 && (BK_ == 64 || BK_ == 32)), "shape");
+  static_assert(!PAIR || (BN == 256 && BK_ == 64), "pair shape");
   static constexpr int BK = BK_;                   // K per stage (16-bit elements)
   static constexpr int SWZ = 2 * BK;               // row bytes = swizzle span
-  static constexpr int STAGES = BN == 128 ? 3 : (BK == 64 ? 2 : 4);
+  static constexpr int STAGES = PAIR ? 3 : (BN == 128 ? 3 : (BK == 64 ? 2 : 4));
+  static constexpr int BM = PAIR ? 2 * TC_BM : TC_BM;  // rows of a unit
+  static constexpr int BNL = PAIR ? BN / 2 : BN;       // B rows staged by one CTA
   static constexpr int NBUF = 512 / BN;
   static constexpr int EPI0 = BN == 256 ? 4 : 2;   // first epilogue warp
   static constexpr int NEPI = BN / 32;              // epilogue warps
   static constexpr int THREADS = 32 * (EPI0 + NEPI);
   static constexpr int CH = BN == 256 ? 16 : 32;    // columns per staged chunk
   static constexpr uint32_t A_BYTES = (uint32_t)TC_BM * BK * 2;
-  static constexpr uint32_t B_BYTES = (uint32_t)BN * BK * 2;
+  static constexpr uint32_t B_BYTES = (uint32_t)BNL * BK * 2;
   static constexpr uint32_t STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
   static constexpr uint32_t TMEM_COLS = 512;
   // 1 KiB alignment slack in front, the barriers behind the stages, and 1 KiB
@@ -233,10 +306,17 @@ __device__ __forceinline__ void seg_of(const TcArgs &a, int kb, int &s, int &lkb
 // per-element rounding error, still K-independent).
 // A problem's K range may span several segments with different operands
 // (up to 4), each optionally negated through the instruction descriptor.
-template <int BN, int BK>
-__global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
+// the MMA of the kernel's form (one CTA, or the pair)
+#define MMA_(...)                         \
+  do {                                    \
+    if constexpr (PAIR) mma2_bf16(__VA_ARGS__); \
+    else mma_bf16(__VA_ARGS__);           \
+  } while (0)
+
+template <int BN, int BK, bool PAIR = false>
+__global__ void __launch_bounds__(TcShape<BN, BK, PAIR>::THREADS, 1)
     tc_gemm_kernel(const __grid_constant__ TcMaps maps, TcOut out, TcArgs a) {
-  using SH = TcShape<BN, BK>;
+  using SH = TcShape<BN, BK, PAIR>;
   constexpr int STAGES = SH::STAGES, NBUF = SH::NBUF, HC = 128;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -267,6 +347,10 @@ __global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
   const int tiles = a.tiles_m * a.tiles_n;
   const int nprob = a.gstart[a.ng];
   const int units = tiles * nprob * a.splits;
+  // work distribution: per CTA, or per cluster pair (rank 0 issues the MMAs)
+  const int rank = PAIR ? (int)cluster_rank() : 0;
+  const int wid = PAIR ? (int)cluster_id_x() : (int)blockIdx.x;
+  const int nwork = PAIR ? (int)nclusters_x() : (int)gridDim.x;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; s++) {
@@ -275,7 +359,7 @@ __global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
     }
     for (int b = 0; b < NBUF; b++) {
       mbar_init(&tfull[b], 1);
-      mbar_init(&tempty[b], SH::NEPI);  // one arrival per epilogue warp
+      mbar_init(&tempty[b], SH::NEPI * (PAIR ? 2 : 1));  // one arrival per epilogue warp (of the pair)
     }
     mbar_init(done, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -292,14 +376,24 @@ __global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
     s_shift_ok = (f == 0.5 && e > -400 && e < 400) ? 1 : 0;
   }
   if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                     smem_u32(tmem_slot)),
-                 "r"(SH::TMEM_COLS)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    if constexpr (PAIR) {  // one warp of each CTA of the pair, collectively
+      asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                       smem_u32(tmem_slot)),
+                   "r"(SH::TMEM_COLS)
+                   : "memory");
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+    } else {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                       smem_u32(tmem_slot)),
+                   "r"(SH::TMEM_COLS)
+                   : "memory");
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
   }
   tc_fence_before();
   __syncthreads();
+  // the peer's barriers are initialised before any copy or arrival targets them
+  if constexpr (PAIR) cluster_sync_all();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
@@ -308,12 +402,12 @@ __global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
   // tiles per problem (a full one and a narrower remainder) every CTA gets
   // both kinds in turn instead of always the same one.
   auto unit_at = [&](int it) -> int {
-    int b = (int)blockIdx.x;
+    int b = wid;
     if (it & 1) {
       const int p = b ^ 1;
-      if (p < (int)gridDim.x) b = p;
+      if (p < nwork) b = p;
     }
-    return it * (int)gridDim.x + b;
+    return it * nwork + b;
   };
   // unit -> (tile m, tile n, problem y, z, g, K-block range)
   auto unit_coords = [&](int u, int &tm, int &tn, int &py, int &pz, int &pg, int &kb0, int &kb1) {
@@ -359,50 +453,78 @@ __global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
       int last[STAGES];
       for (int s = 0; s < STAGES; s++) last[s] = -1;
       bool ok = true;
-      for (int it = 0; it * (int)gridDim.x < units && ok; it++) {
+      for (int it = 0; it * nwork < units && ok; it++) {
         const int u = unit_at(it);
         if (u >= units) continue;
         int tm, tn, py, pz, pg, kb0, kb1;
         unit_coords(u, tm, tn, py, pz, pg, kb0, kb1);
+        // pair: this CTA stages A rows 128 rank.. of the unit and B columns from
+        // rank x (half the MMA width) on
+        int boff = 0;
+        if constexpr (PAIR) boff = rank * (min(BN, (a.N - tn * BN + 31) & ~31) / 2);
         for (int kb = kb0; kb < kb1; kb++, g++) {
           int sg, lkb;
           seg_of(a, kb, sg, lkb);
           const TcSegArgs &S = a.seg[sg];
-          const int ya = (int)(S.rowA0[pg] + py * S.rowAy[pg] + pz * S.rowAz[pg]) + tm * TC_BM;
-          const int yb = (int)(S.rowB0[pg] + py * S.rowBy[pg] + pz * S.rowBz[pg]) + tn * BN;
+          const int ya = (int)(S.rowA0[pg] + py * S.rowAy[pg] + pz * S.rowAz[pg]) + tm * SH::BM +
+                         rank * TC_BM;
+          const int yb = (int)(S.rowB0[pg] + py * S.rowBy[pg] + pz * S.rowBz[pg]) + tn * BN + boff;
           const int s = g % STAGES;
           const uint32_t ph = (uint32_t)(g / STAGES) & 1u;
           if (!mbar_wait(&empty[s], ph ^ 1u, a.err, ERR_EMPTY_WAIT)) { ok = false; break; }
           uint8_t *st = smem + s * SH::STAGE_BYTES;
           const CUtensorMap *mA = &maps.m[S.mapA], *mB = &maps.m[S.mapB];
           // a 32-wide block of a segment in a 64-wide kernel fills half a stage
-          mbar_expect_tx(&full[s], S.bk == SH::BK ? bytes : bytes / 2);
+          const uint32_t sb = S.bk == SH::BK ? bytes : bytes / 2;
           const int x = lkb * S.bk;
-          tma_load_2d(st, mA, x, ya, &full[s]);                                  // A hi
-          tma_load_2d(st + SH::A_BYTES, mB, x, yb, &full[s]);                    // B hi
-          if (a.split3) {
-            tma_load_2d(st + SH::A_BYTES + SH::B_BYTES, mA, S.kpad + x, ya, &full[s]);  // A lo
-            tma_load_2d(st + 2 * SH::A_BYTES + SH::B_BYTES, mB, S.kpad + x, yb, &full[s]);  // B lo
+          if constexpr (PAIR) {
+            // both CTAs' copies complete on the rank-0 CTA's barrier
+            const uint32_t fb = leader_addr(&full[s]);
+            if (rank == 0) mbar_expect_tx(&full[s], 2 * sb);
+            tma_load_2d_pair(st, mA, x, ya, fb);                                    // A hi
+            tma_load_2d_pair(st + SH::A_BYTES, mB, x, yb, fb);                      // B hi
+            if (a.split3) {
+              tma_load_2d_pair(st + SH::A_BYTES + SH::B_BYTES, mA, S.kpad + x, ya, fb);      // A lo
+              tma_load_2d_pair(st + 2 * SH::A_BYTES + SH::B_BYTES, mB, S.kpad + x, yb, fb);  // B lo
+            }
+          } else {
+            mbar_expect_tx(&full[s], sb);
+            tma_load_2d(st, mA, x, ya, &full[s]);                                  // A hi
+            tma_load_2d(st + SH::A_BYTES, mB, x, yb, &full[s]);                    // B hi
+            if (a.split3) {
+              tma_load_2d(st + SH::A_BYTES + SH::B_BYTES, mA, S.kpad + x, ya, &full[s]);  // A lo
+              tma_load_2d(st + 2 * SH::A_BYTES + SH::B_BYTES, mB, S.kpad + x, yb, &full[s]);  // B lo
+            }
           }
           last[s] = g;
         }
       }
-      for (int s = 0; s < STAGES; s++)
-        if (last[s] >= 0) mbar_drain(&full[s], (uint32_t)(last[s] / STAGES) & 1u);
+      // (pair: the rank-0 barriers also count the peer's copies; the peer
+      // leaves only after the cluster barrier at the end, i.e. after this
+      // drain, and after an error it first gives its last copies ~50 us)
+      if (!PAIR || rank == 0) {
+        for (int s = 0; s < STAGES; s++)
+          if (last[s] >= 0) mbar_drain(&full[s], (uint32_t)(last[s] / STAGES) & 1u);
+      } else if (!ok) {
+        const long long t0 = clock64();
+        while (clock64() - t0 < 100000) {
+        }
+      }
     }
   } else if (warp == 1) {
-    if (lane == 0) {
+    if (lane == 0 && (!PAIR || rank == 0)) {  // (pair: the rank-0 CTA issues for both)
       int g = 0, c = 0;
       bool ok = true;
-      for (int it = 0; it * (int)gridDim.x < units && ok; it++) {
+      for (int it = 0; it * nwork < units && ok; it++) {
         const int u = unit_at(it);
         if (u >= units) continue;
         int tm, tn, py, pz, pg, kb0, kb1;
         unit_coords(u, tm, tn, py, pz, pg, kb0, kb1);
         // MMA width: the tile's valid columns rounded up to 16 (M = 128 takes any
-        // N = 16..256 in steps of 16; the MMA time scales with N)
-        const int nvalid = min(BN, (a.N - tn * BN + 15) & ~15);
-        const uint32_t idesc = idesc_f16kind(TC_BM, nvalid, a.f16 ? 0u : 1u);
+        // N = 16..256 in steps of 16; the MMA time scales with N); pair: to 32,
+        // so that each CTA's half of B is a whole number of 16-row groups
+        const int nvalid = PAIR ? min(BN, (a.N - tn * BN + 31) & ~31) : min(BN, (a.N - tn * BN + 15) & ~15);
+        const uint32_t idesc = idesc_f16kind(SH::BM, nvalid, a.f16 ? 0u : 1u);
         for (int kb = kb0; kb < kb1; kb++, g++) {
           int sg, lkb;
           seg_of(a, kb, sg, lkb);
@@ -427,36 +549,40 @@ __global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
             if (a.split3) {
 #pragma unroll
               for (int k = 0; k < 2; k++, acc = 1)
-                mma_bf16(d, sw_desc<64>(alo + 32 * k), sw_desc<64>(bhi + 32 * k), id, acc);
+                MMA_(d, sw_desc<64>(alo + 32 * k), sw_desc<64>(bhi + 32 * k), id, acc);
 #pragma unroll
               for (int k = 0; k < 2; k++)
-                mma_bf16(d, sw_desc<64>(ahi + 32 * k), sw_desc<64>(blo + 32 * k), id, 1u);
+                MMA_(d, sw_desc<64>(ahi + 32 * k), sw_desc<64>(blo + 32 * k), id, 1u);
             }
 #pragma unroll
             for (int k = 0; k < 2; k++, acc = 1)
-              mma_bf16(d, sw_desc<64>(ahi + 32 * k), sw_desc<64>(bhi + 32 * k), id, acc);
+              MMA_(d, sw_desc<64>(ahi + 32 * k), sw_desc<64>(bhi + 32 * k), id, acc);
           } else {
             if (a.split3) {
 #pragma unroll
               for (int k = 0; k < SH::BK / 16; k++, acc = 1)
-                mma_bf16(d, sw_desc<SH::SWZ>(alo + 32 * k), sw_desc<SH::SWZ>(bhi + 32 * k), id, acc);
+                MMA_(d, sw_desc<SH::SWZ>(alo + 32 * k), sw_desc<SH::SWZ>(bhi + 32 * k), id, acc);
 #pragma unroll
               for (int k = 0; k < SH::BK / 16; k++)
-                mma_bf16(d, sw_desc<SH::SWZ>(ahi + 32 * k), sw_desc<SH::SWZ>(blo + 32 * k), id, 1u);
+                MMA_(d, sw_desc<SH::SWZ>(ahi + 32 * k), sw_desc<SH::SWZ>(blo + 32 * k), id, 1u);
             }
 #pragma unroll
             for (int k = 0; k < SH::BK / 16; k++, acc = 1)
-              mma_bf16(d, sw_desc<SH::SWZ>(ahi + 32 * k), sw_desc<SH::SWZ>(bhi + 32 * k), id, acc);
+              MMA_(d, sw_desc<SH::SWZ>(ahi + 32 * k), sw_desc<SH::SWZ>(bhi + 32 * k), id, acc);
           }
-          mma_commit(&empty[s]);
-          if (last) {
-            mma_commit(&tfull[b]);
-            c++;
+          if constexpr (PAIR) {
+            mma2_commit_both(&empty[s]);
+            if (last) mma2_commit_both(&tfull[b]);
+          } else {
+            mma_commit(&empty[s]);
+            if (last) mma_commit(&tfull[b]);
           }
+          if (last) c++;
         }
       }
       // every MMA issued above has completed once `done` fires
-      mma_commit(done);
+      if constexpr (PAIR) mma2_commit(done);
+      else mma_commit(done);
       mbar_drain(done, 0);
     }
   }
@@ -470,12 +596,12 @@ __global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
     int64_t *colH = colOff + HC * h;
     int c = 0;
     bool ok = true;
-    for (int it = 0; it * (int)gridDim.x < units && ok; it++) {
+    for (int it = 0; it * nwork < units && ok; it++) {
       const int u = unit_at(it);
       if (u >= units) continue;
       int tm, tn, py, pz, pg, kb0, kb1;
       unit_coords(u, tm, tn, py, pz, pg, kb0, kb1);
-      const int m = tm * TC_BM + row;
+      const int m = tm * SH::BM + rank * TC_BM + row;
       const int n0 = tn * BN + HC * h;
       asm volatile("bar.sync %0, 128;" ::"r"(bar) : "memory");  // previous unit's colOff reads done
       if (!a.partial) {
@@ -508,7 +634,10 @@ __global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
         }
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[b])) : "memory");
+        if (lane == 0) {
+          if constexpr (PAIR) mbar_arrive_cluster(leader_addr(&tempty[b]));  // the MMA issuer's barrier
+          else asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[b])) : "memory");
+        }
       }
       asm volatile("bar.sync %0, 128;" ::"r"(bar) : "memory");  // colOff of this unit written
       if (!ok || errv) break;
@@ -668,13 +797,22 @@ __global__ void __launch_bounds__(TcShape<BN, BK>::THREADS, 1)
   }
   tc_fence_before();
   __syncthreads();
+  // pair: neither CTA leaves (or frees TMEM) while the other's copies, MMAs or
+  // arrivals may still target it
+  if constexpr (PAIR) cluster_sync_all();
   if (warp == 1) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                 "r"(SH::TMEM_COLS)
-                 : "memory");
+    if constexpr (PAIR)
+      asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                   "r"(SH::TMEM_COLS)
+                   : "memory");
+    else
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                   "r"(SH::TMEM_COLS)
+                   : "memory");
   }
 }
+#undef MMA_
 
 __global__ void tc_reduce_kernel(TcOut out, int64_t M, int64_t N, int splits,
                                  const float *__restrict__ partial) {
@@ -951,7 +1089,8 @@ int TcEngine::k_block(int bn) {
 void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &out, int nseg,
                             int splits, float *partial, unsigned *err, cudaStream_t stream) {
   static std::once_flag once;
-  static bool wide_ok = false;
+  static bool wide_ok = false, pair_ok = false;
+  static int pair_clusters = 0;  // co-resident pairs of the pair kernel
   std::call_once(once, [] {
     cudaFuncSetAttribute(tc_gemm_kernel<128, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)TcShape<128, 64>::SMEM_BYTES);
@@ -961,11 +1100,33 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
                          (int)TcShape<256, 32>::SMEM_BYTES);
     // The 256-wide kernels' setmaxnreg split assumes they are launched with
     // exactly kLaunchRegs256 registers a thread (3 x 168 = 56 + 2 x 224 per scheduler).
-    cudaFuncAttributes fa, fb;
+    cudaFuncAttributes fa, fb, fc;
     wide_ok = cudaFuncGetAttributes(&fa, tc_gemm_kernel<256, 64>) == cudaSuccess &&
               fa.numRegs == kLaunchRegs256 &&
               cudaFuncGetAttributes(&fb, tc_gemm_kernel<256, 32>) == cudaSuccess &&
               fb.numRegs == kLaunchRegs256;
+    using SP = TcShape<256, 64, true>;
+    if (cudaFuncSetAttribute(tc_gemm_kernel<256, 64, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)SP::SMEM_BYTES) == cudaSuccess &&
+        cudaFuncGetAttributes(&fc, tc_gemm_kernel<256, 64, true>) == cudaSuccess &&
+        fc.numRegs == kLaunchRegs256) {
+      cudaLaunchConfig_t cfg = {};
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = 2;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.gridDim = dim3(2 * (kNumSMs / 2));
+      cfg.blockDim = dim3(SP::THREADS);
+      cfg.dynamicSmemBytes = SP::SMEM_BYTES;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int n = 0;
+      if (cudaOccupancyMaxActiveClusters(&n, tc_gemm_kernel<256, 64, true>, &cfg) == cudaSuccess && n > 0) {
+        pair_clusters = n;
+        pair_ok = true;
+      }
+    }
     cudaGetLastError();
   });
   const int bn = ps.bn == 256 ? 256 : 128;
@@ -973,6 +1134,10 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
   // the maps' boxes were made for this K block (a mismatch would overrun the stages)
   const int bk = TcEngine::k_block(bn);
   if (ps.bk != bk) throw Error(SCESS_ERR_INVALID, "tc_gemm: maps built for another K block");
+  const bool pair = ps.pair;
+  if (pair && (bn != 256 || bk != 64)) throw Error(SCESS_ERR_INVALID, "tc_gemm: pair needs the 256 x 64 kernel");
+  if (pair && !pair_ok) throw Error(SCESS_ERR_UNSUPPORTED, "tc_gemm: cluster-pair kernel unavailable");
+  const int bm = pair ? 2 * TC_BM : TC_BM;  // rows of a work unit
   if (ps.M <= 0 || ps.N <= 0 || ps.ny <= 0 || ps.nz <= 0 || ps.ng <= 0) return;
   if (ps.ng > 3) throw Error(SCESS_ERR_INVALID, "tc_gemm: groups");
   if (nseg != 1 && nseg != 3) throw Error(SCESS_ERR_INVALID, "tc_gemm: nseg");
@@ -982,7 +1147,7 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
   std::memset(&a, 0, sizeof(a));
   a.M = (int)ps.M;
   a.N = (int)ps.N;
-  a.tiles_m = (int)ceil_div(ps.M, TC_BM);
+  a.tiles_m = (int)ceil_div(ps.M, bm);
   a.tiles_n = (int)ceil_div(ps.N, bn);
   a.ny = ps.ny;
   a.nz = ps.nz;
@@ -1000,7 +1165,7 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
       throw Error(SCESS_ERR_INVALID, "tc_gemm: segment K not a multiple of its K block");
     for (int q = 0; q < ps.ng; q++) {
       const int64_t maxA = g.rowA0[q] + (int64_t)(ps.ny - 1) * g.rowAy[q] +
-                           (int64_t)(ps.nz - 1) * g.rowAz[q] + a.tiles_m * TC_BM;
+                           (int64_t)(ps.nz - 1) * g.rowAz[q] + a.tiles_m * bm;
       const int64_t maxB = g.rowB0[q] + (int64_t)(ps.ny - 1) * g.rowBy[q] +
                            (int64_t)(ps.nz - 1) * g.rowBz[q] + a.tiles_n * bn;
       if (maxA > INT32_MAX || maxB > INT32_MAX || g.rowA0[q] < 0 || g.rowB0[q] < 0 ||
@@ -1064,7 +1229,24 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
   const int64_t units = (int64_t)a.tiles_m * a.tiles_n * a.gstart[ps.ng] * splits;
   if (units > INT32_MAX) throw Error(SCESS_ERR_INVALID, "tc_gemm: too many work units");
   const unsigned grid = (unsigned)std::min<int64_t>(units, kNumSMs);
-  if (bn == 256)
+  if (pair) {
+    // one persistent pair per co-resident cluster slot
+    using SP = TcShape<256, 64, true>;
+    const int64_t ncl = std::min<int64_t>(units, pair_clusters);
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 2;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3((unsigned)(2 * ncl));
+    cfg.blockDim = dim3(SP::THREADS);
+    cfg.dynamicSmemBytes = SP::SMEM_BYTES;
+    cfg.stream = stream;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    SCESS_CUDA(cudaLaunchKernelEx(&cfg, tc_gemm_kernel<256, 64, true>, maps, out, a));
+  } else if (bn == 256)
     if (bk == 32)
       tc_gemm_kernel<256, 32><<<grid, TcShape<256, 32>::THREADS, TcShape<256, 32>::SMEM_BYTES, stream>>>(
           maps, out, a);

@@ -84,6 +84,10 @@ struct TcProblemSet {
   // k_block(bn)-wide boxes: map_of(p, rows, k_block(bn)), and bk must say so.
   int bn = 128;
   int bk = 64;
+  // bn = 256, bk = 64 only: run each 256 x 256 unit on a cluster pair of SMs
+  // (tcgen05 cta_group::2, M = 256); the B-side maps then have 128-row boxes
+  // (each CTA stages half of the unit's B columns) and so do the A-side maps
+  bool pair = false;
   // per-group output tables (null: the TcOut tables)
   const int64_t *rowC[3] = {nullptr, nullptr, nullptr};
   const int64_t *colC[3] = {nullptr, nullptr, nullptr};

@@ -804,6 +804,11 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   int tbn = 256;
   if (const char *env = std::getenv("SCESS_T_BN")) tbn = std::atoi(env) == 128 ? 128 : 256;
   const int tbk = TcEngine::k_block(tbn);
+  // 256 x 256 units on cluster pairs of SMs (each SM stages half of B): the
+  // default of the 256 x 64 kernel; SCESS_T_PAIR=0 keeps one SM per 128 x 256 unit
+  bool tpair = tbn == 256 && tbk == 64;
+  if (const char *env = std::getenv("SCESS_T_PAIR")) tpair = tpair && std::atoi(env) != 0;
+  const int bbox = tpair ? 128 : tbn;  // B rows staged per CTA
   // K block of the t2.R segments (K = o): 32 in the 64-wide kernel when o <= 32
   // (half-filled stages instead of mostly-padding 64-wide ones)
   const int rbk = (tbk == 64 && o <= 32) ? 32 : tbk;
@@ -848,10 +853,10 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
     // shared-memory traffic per FLOP (SCESS_T_BN=128 selects the narrow tiles).
     // Boxes as wide as the kernel's K block.
     mP = TcEngine::map_of(pP, 128, tbk);
-    mQ = TcEngine::map_of(pQ, tbn, tbk);
-    mQ2 = TcEngine::map_of(pQ2, tbn, tbk);
-    mR = TcEngine::map_of(pR, tbn, rbk);
-    mR2 = TcEngine::map_of(pR2, tbn, rbk);
+    mQ = TcEngine::map_of(pQ, bbox, tbk);
+    mQ2 = TcEngine::map_of(pQ2, bbox, tbk);
+    mR = TcEngine::map_of(pR, bbox, rbk);
+    mR2 = TcEngine::map_of(pR2, bbox, rbk);
     mTx = TcEngine::map_of(pTx, 128, rbk);
     // W_g[(y_l nb + z_l) nb + x_l][i + o j + o2p k]: every group stores its
     // (u, s, t) in the (i, j, k) order of the triple, so that the energy kernel
@@ -917,6 +922,7 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
           }
           ps.bn = tbn;
           ps.bk = tbk;
+          ps.pair = tpair;
           ps.cy = nb * nb * o3p;
           ps.cz = nb * o3p;
           const int kRoles[3][3] = {{0, 1, 2}, {1, 0, 2}, {2, 0, 1}};  // (x, y, z) of group g
