@@ -80,8 +80,12 @@ __device__ __forceinline__ void tma_load_2d_pair(void *dst, const CUtensorMap *t
       "l"((uint64_t)tm), "r"(x), "r"(y), "r"(bar_cluster)
       : "memory");
 }
+// Arrival on a barrier of either CTA of the pair.  Release at CTA scope: it
+// only has to follow this thread's completed TMEM loads (tcgen05.wait::ld);
+// a cluster-scope release would also wait for the thread's earlier global
+// stores to be acknowledged.
 __device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar_cluster) {
-  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar_cluster) : "memory");
+  asm volatile("mbarrier.arrive.release.cta.shared::cluster.b64 _, [%0];" ::"r"(bar_cluster) : "memory");
 }
 
 __device__ __forceinline__ void tc_fence_before() {
@@ -163,6 +167,18 @@ __device__ __forceinline__ void mma2_commit(uint64_t *bar) {
 __device__ __forceinline__ void tmem_ld16_async(uint32_t taddr, uint32_t *r) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+// 16x256b shape, 4 repetitions: thread t gets TMEM lanes base + t/4 (r[4j],
+// r[4j+1]) and base + 8 + t/4 (r[4j+2], r[4j+3]), columns 8j + 2 (t % 4) and
+// the next, j = 0..3 (the accumulator fragment of an m16n8 tile per repetition).
+__device__ __forceinline__ void tmem_ld16x256b_x4_async(uint32_t taddr, uint32_t *r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.16x256b.x4.b32 "
       "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
         "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
@@ -612,35 +628,101 @@ __global__ void __launch_bounds__(TcShape<BN, BK, PAIR>::THREADS, 1)
       // issued now, used after the K loop: their latency hides behind the MMAs
       const int64_t *rowT = a.rowCg[pg] ? a.rowCg[pg] : out.rowC;
       const int64_t rowOff = (!a.partial && m < a.M) ? rowT[m] : 0;
+      // Units whose output runs along pairs of columns (the (T) groups stored by
+      // column in aligned quads): TMEM is drained in the 16x256b shape, so that
+      // each thread holds column pairs of rows 32 q + 8 s + lane / 4 (s = 0..3)
+      // and stores them straight from registers (no staging through shared memory).
+      const bool pc = BN == 256 && a.stvec[pg] && out.fp32 && out.beta == 0.0 && !a.partial;
       const unsigned errv = *(volatile unsigned *)a.err;
       float acc[HC];
 #pragma unroll
       for (int j = 0; j < HC; j++) acc[j] = 0.0f;
-      for (int kb = kb0; kb < kb1; kb += a.kbd, c++) {
-        const int b = c % NBUF;
-        const uint32_t bph = (uint32_t)(c / NBUF) & 1u;
-        if (!mbar_wait(&tfull[b], bph, a.err, ERR_ACCUM_WAIT)) { ok = false; break; }
-        tc_fence_after();
-        const uint32_t t0 = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * BN + HC * h);
+      // (two copies of the drain loop, one per TMEM load shape: one loop with
+      // both shapes keeps the accumulators in local memory)
+      if (pc) {
+        for (int kb = kb0; kb < kb1; kb += a.kbd, c++) {
+          const int b = c % NBUF;
+          const uint32_t bph = (uint32_t)(c / NBUF) & 1u;
+          if (!mbar_wait(&tfull[b], bph, a.err, ERR_ACCUM_WAIT)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t t0 = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * BN + HC * h);
+          // acc[64 L + 4 j + e]: lane 32 q + 16 L + 8 (e / 2) + lane / 4,
+          // column 8 j + 2 (lane % 4) + e % 2 of the half
 #pragma unroll
-        for (int j = 0; j < HC; j += 16 * SCESS_TC_LDB) {
-          uint32_t r[16 * SCESS_TC_LDB];
+          for (int L = 0; L < 2; L++)
 #pragma unroll
-          for (int hh = 0; hh < SCESS_TC_LDB; hh++) tmem_ld16_async(t0 + (uint32_t)(j + 16 * hh), r + 16 * hh);
+            for (int p4 = 0; p4 < 4; p4++) {
+              uint32_t r[16];
+              tmem_ld16x256b_x4_async(t0 + ((uint32_t)(16 * L) << 16) + (uint32_t)(32 * p4), r);
+              tmem_wait16(r);
 #pragma unroll
-          for (int hh = 0; hh < SCESS_TC_LDB; hh++) tmem_wait16(r + 16 * hh);
-#pragma unroll
-          for (int i = 0; i < 16 * SCESS_TC_LDB; i++) acc[j + i] += __uint_as_float(r[i]);
+              for (int i = 0; i < 16; i++) acc[64 * L + 16 * p4 + i] += __uint_as_float(r[i]);
+            }
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) {
+            if constexpr (PAIR) mbar_arrive_cluster(leader_addr(&tempty[b]));  // the MMA issuer's barrier
+            else asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[b])) : "memory");
+          }
         }
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) {
-          if constexpr (PAIR) mbar_arrive_cluster(leader_addr(&tempty[b]));  // the MMA issuer's barrier
-          else asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[b])) : "memory");
+      } else {
+        for (int kb = kb0; kb < kb1; kb += a.kbd, c++) {
+          const int b = c % NBUF;
+          const uint32_t bph = (uint32_t)(c / NBUF) & 1u;
+          if (!mbar_wait(&tfull[b], bph, a.err, ERR_ACCUM_WAIT)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t t0 = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * BN + HC * h);
+#pragma unroll
+          for (int j = 0; j < HC; j += 16 * SCESS_TC_LDB) {
+            uint32_t r[16 * SCESS_TC_LDB];
+#pragma unroll
+            for (int hh = 0; hh < SCESS_TC_LDB; hh++) tmem_ld16_async(t0 + (uint32_t)(j + 16 * hh), r + 16 * hh);
+#pragma unroll
+            for (int hh = 0; hh < SCESS_TC_LDB; hh++) tmem_wait16(r + 16 * hh);
+#pragma unroll
+            for (int i = 0; i < 16 * SCESS_TC_LDB; i++) acc[j + i] += __uint_as_float(r[i]);
+          }
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) {
+            if constexpr (PAIR) mbar_arrive_cluster(leader_addr(&tempty[b]));  // the MMA issuer's barrier
+            else asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[b])) : "memory");
+          }
         }
       }
       asm volatile("bar.sync %0, 128;" ::"r"(bar) : "memory");  // colOff of this unit written
       if (!ok || errv) break;
+      if (pc) {
+        float *C = (float *)out.C;
+        const float fa = s_falpha;
+        const int cq = 2 * (lane & 3);
+        // the warp's 32 row offsets, read back in the 16x256b row order
+        rowOffS[h][row] = m < a.M ? rowOff : -1;
+        __syncwarp();
+        int64_t ro4[4];
+#pragma unroll
+        for (int s4 = 0; s4 < 4; s4++) ro4[s4] = rowOffS[h][32 * q + 8 * s4 + (lane >> 2)];
+#pragma unroll
+        for (int j = 0; j < HC / 8; j++) {
+          const int64_t co0 = colH[8 * j + cq], co1 = colH[8 * j + cq + 1];
+#pragma unroll
+          for (int s4 = 0; s4 < 4; s4++) {
+            const int64_t ro = ro4[s4];
+            const float v0 = fa * acc[64 * (s4 >> 1) + 4 * j + 2 * (s4 & 1)];
+            const float v1 = fa * acc[64 * (s4 >> 1) + 4 * j + 2 * (s4 & 1) + 1];
+            if (ro < 0) continue;
+            float *d = C + ro + co0;
+            if (co0 >= 0 && co1 == co0 + 1 && ((uintptr_t)d & 7) == 0) {
+              *reinterpret_cast<float2 *>(d) = make_float2(v0, v1);
+            } else {
+              if (co0 >= 0) C[ro + co0] = v0;
+              if (co1 >= 0) C[ro + co1] = v1;
+            }
+          }
+        }
+        __syncwarp();  // rowOffS read before the next unit rewrites it
+        continue;
+      }
       if (a.stcol[pg] && out.fp32 && out.beta == 0.0 && !a.partial) {
         // Tile staged through shared memory CH columns at a time, then each warp
         // stores its 32 rows with the lanes along the columns: for outputs whose
