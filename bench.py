@@ -46,7 +46,7 @@ CPU_SAMPLE = ('one full FP64 CCSD iteration of the NumPy oracle (MP2 guess, BLAS
 # DRAM bytes (read + write) of one grouped (T) GEMM launch at o=20, nb=12,
 # measured with ncu: the three W buffers (166 MB) are written once, 112 MB of
 # them reach DRAM, operands are read mostly from L2.
-TRIPLES_LAUNCH_TRAFFIC = 140.8e6
+TRIPLES_LAUNCH_TRAFFIC = 136.7e6
 
 
 def peaks():
@@ -443,7 +443,8 @@ def main():
                 'traffic': TRIPLES_LAUNCH_TRAFFIC if (o, v) == (20, 180) else None,
                 'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of one '
                                   'off-diagonal grouped (T) launch at o=20 v=96, which has the same '
-                                  'launch shape (nb=12, 1728 work units of 128 x 256) as o=20 v=180',
+                                  'launch shape (nb=12, 864 work units of 256 x 256 on cluster pairs) '
+                                  'as o=20 v=180',
                 'top_kernel_by_time': top}
     # "phase:" timers enclose kernel timers: shown, but not part of the shares
     kern = {k: v for k, v in prof.items() if not k.startswith('phase:')}
