@@ -304,6 +304,16 @@ def triples_only(args, wl, config, ctx_factory, lib, bf16_peak, peak_kind, torch
         'kernel_timers': prof, 'gpu_launches': launches, 'clocks': clocks}))
 
 
+def max_over_ranks(value, world, device='cuda'):
+    """The largest of the ranks' values (every rank gets it); world == 1: value."""
+    if world <= 1:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def rank_info():
     return (int(os.environ.get('RANK', 0)), int(os.environ.get('WORLD_SIZE', 1)),
             int(os.environ.get('LOCAL_RANK', 0)))
@@ -421,10 +431,7 @@ def main():
     ctx.profile(False)
     clocks = clk.stop()
     step_s = (float(np.mean(it_ms)) + float(np.mean(t_ms))) / 1e3
-    if world > 1:
-        tt = torch.tensor([step_s], device='cuda')
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        step_s = float(tt.item())
+    step_s = max_over_ranks(step_s, world)
     hist_mixed = st.hist.reshape(-1, 3)
     n_iter_mixed = args.warmup + args.steps
     t1m, t2m = st.amplitudes()
