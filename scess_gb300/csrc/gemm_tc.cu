@@ -1168,11 +1168,18 @@ int TcEngine::k_block(int bn) {
   return bn == 256 ? bk256 : 64;
 }
 
-void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &out, int nseg,
-                            int splits, float *partial, unsigned *err, cudaStream_t stream) {
+namespace {
+
+// One-time kernel attributes and capabilities of this device: the 256-wide
+// kernels' register count (their setmaxnreg split assumes kLaunchRegs256) and
+// how many cluster pairs of the pair kernel are co-resident.
+struct KernelSetup {
+  bool wide_ok = false, pair_ok = false;
+  int pair_clusters = 0;
+};
+const KernelSetup &kernel_setup() {
+  static KernelSetup k;
   static std::once_flag once;
-  static bool wide_ok = false, pair_ok = false;
-  static int pair_clusters = 0;  // co-resident pairs of the pair kernel
   std::call_once(once, [] {
     cudaFuncSetAttribute(tc_gemm_kernel<128, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)TcShape<128, 64>::SMEM_BYTES);
@@ -1183,7 +1190,7 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
     // The 256-wide kernels' setmaxnreg split assumes they are launched with
     // exactly kLaunchRegs256 registers a thread (3 x 168 = 56 + 2 x 224 per scheduler).
     cudaFuncAttributes fa, fb, fc;
-    wide_ok = cudaFuncGetAttributes(&fa, tc_gemm_kernel<256, 64>) == cudaSuccess &&
+    k.wide_ok = cudaFuncGetAttributes(&fa, tc_gemm_kernel<256, 64>) == cudaSuccess &&
               fa.numRegs == kLaunchRegs256 &&
               cudaFuncGetAttributes(&fb, tc_gemm_kernel<256, 32>) == cudaSuccess &&
               fb.numRegs == kLaunchRegs256;
@@ -1205,12 +1212,24 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
       cfg.numAttrs = 1;
       int n = 0;
       if (cudaOccupancyMaxActiveClusters(&n, tc_gemm_kernel<256, 64, true>, &cfg) == cudaSuccess && n > 0) {
-        pair_clusters = n;
-        pair_ok = true;
+        k.pair_clusters = n;
+        k.pair_ok = true;
       }
     }
     cudaGetLastError();
   });
+  return k;
+}
+
+}  // namespace
+
+bool TcEngine::pair_available() { return kernel_setup().pair_ok; }
+
+void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &out, int nseg,
+                            int splits, float *partial, unsigned *err, cudaStream_t stream) {
+  const KernelSetup &ks = kernel_setup();
+  const bool wide_ok = ks.wide_ok, pair_ok = ks.pair_ok;
+  const int pair_clusters = ks.pair_clusters;
   const int bn = ps.bn == 256 ? 256 : 128;
   if (bn == 256 && !wide_ok) throw Error(SCESS_ERR_UNSUPPORTED, "tc_gemm: 256-wide kernel unavailable");
   // the maps' boxes were made for this K block (a mismatch would overrun the stages)

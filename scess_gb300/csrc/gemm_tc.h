@@ -140,6 +140,9 @@ class TcEngine {
   static CUtensorMap map_of(const Packed &p, int box_rows, int bk = 64);
   // K block (16-bit values per stage row) of the kernel with tile width bn.
   static int k_block(int bn);
+  // whether this device runs the cluster-pair form of the 256 x 64 kernel
+  // (TcProblemSet::pair)
+  static bool pair_available();
   // TcOut scale pointers of a product of two packed operands.
   static void set_scales(TcOut &out, const Packed &A, const Packed &B) {
     out.scaleA = A.scale();

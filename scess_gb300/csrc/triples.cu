@@ -806,7 +806,7 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   const int tbk = TcEngine::k_block(tbn);
   // 256 x 256 units on cluster pairs of SMs (each SM stages half of B): the
   // default of the 256 x 64 kernel; SCESS_T_PAIR=0 keeps one SM per 128 x 256 unit
-  bool tpair = tbn == 256 && tbk == 64;
+  bool tpair = tbn == 256 && tbk == 64 && TcEngine::pair_available();
   if (const char *env = std::getenv("SCESS_T_PAIR")) tpair = tpair && std::atoi(env) != 0;
   const int bbox = tpair ? 128 : tbn;  // B rows staged per CTA
   // K block of the t2.R segments (K = o): 32 in the 64-wide kernel when o <= 32
