@@ -356,10 +356,14 @@ def main():
         if rank != 0:
             return
         N = o + v
-        # eri on the host without a GPU: (pr|qs) from the DF factors
-        Bm = wl.B.reshape(wl.naux, N * N)
-        chem = (Bm.T @ Bm).reshape(N, N, N, N)
-        eri = np.ascontiguousarray(chem.transpose(0, 2, 1, 3))
+        # eri on the host without a GPU: (pr|qs) from the DF factors, in row
+        # blocks (one 40000 x 40000 BLAS call has crashed some BLAS builds)
+        Bm = np.ascontiguousarray(wl.B.reshape(wl.naux, N * N))
+        chem = np.empty((N * N, N * N))
+        rb = 2048
+        for i0 in range(0, N * N, rb):
+            chem[i0:i0 + rb] = Bm[:, i0:i0 + rb].T @ Bm
+        eri = np.ascontiguousarray(chem.reshape(N, N, N, N).transpose(0, 2, 1, 3))
         del chem
         ints = oracle.make_integral_blocks(eri, o)
         for _ in range(min(args.warmup, 1)):
