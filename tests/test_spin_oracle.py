@@ -90,3 +90,17 @@ def test_spin_and_closed_shell_restatements_agree_on_synthetic_integrals():
     assert abs(s.E_T - et) < 2e-6 * max(1.0, abs(et))
     # closed-shell t1 is the alpha block of the spin-orbital t1
     assert np.allclose(s.t1[0::2, 0::2], r.t1, atol=1e-5)
+
+
+def test_committed_ccpvdz_spin_values_reproduce():
+    """tests/golden/spin_pins.json (used by the GPU test) is what the
+    restatement gives now (make_spin_pins.py)."""
+    import json
+    import os
+    from tests.golden import HERE
+    pin = json.load(open(os.path.join(HERE, 'spin_pins.json')))['h2o_ccpvdz']
+    d = load('h2o_ccpvdz')
+    w = oracle.ccsd_t_spin_orbital(_chem(d), d['eps'], d['nocc'])
+    assert w.converged and w.iterations == pin['iterations']
+    assert abs(w.E_CCSD - pin['E_CCSD']) < 1e-12
+    assert abs(w.E_T - pin['E_T']) < 1e-14
