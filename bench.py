@@ -3,22 +3,34 @@
 Metric (lower is better): seconds for one CCSD iteration (residual, Jacobi
 update, DIIS, energy) plus the full (T) correction, mixed-precision form, at
 o=20, v=180 on seeded synthetic DF integrals (the convergent variant of the
-generator; see scess_gb300/synthetic.py), inputs resident in HBM.  Beside it:
+generator; see scess_gb300/synthetic.py), inputs resident in HBM.  The timed
+state never leaves the mixed phase (its switch to FP64 refinement is
+disabled), so every timed step is the same work: one mixed iteration and one
+mixed (T); the loop checks that the mixed iteration count advanced by one.
 
-* the FP64 GPU path on the same workload (the drop-in form) and the ratio;
-* the energy differences mixed - FP64 on identical inputs;
-* ``e2e``: the same step through the public C ABI from pinned host buffers
+Beside it:
+
+* ``fp64``: the FP64 GPU path on the same workload (the drop-in form), one
+  iteration and one (T), and the energy differences mixed - FP64;
+* ``converged``: the drop-in calls themselves, SolveRCCSD_DIIS to convergence
+  (scess_rccsd_solve) followed by RCCSD_TriplesCorrection
+  (scess_rccsd_triples), once in the mixed form (mixed iterations, then FP64
+  refinement) and once in FP64, host buffers in and out: seconds, iteration
+  counts and the differences of E_CCSD, E_(T) and their sum;
+* ``e2e``: the timed step through the public C ABI from pinned host buffers
   (state create = nmo^4 eri upload + block build + MP2 guess, one iteration,
-  (T), amplitudes back), timed on the host around synchronous calls;
-* ``roofline`` of the dominant kernel (tcgen05 GEMM) from the library's
-  per-launch CUDA-event timers over the timed steps;
-* ``cpu_baseline``: the FP64 NumPy oracle on this host (one full CCSD
-  iteration + (T) extrapolated from the costliest leading-virtual slices).
+  (T), amplitudes back), median over the e2e steps;
+* ``roofline`` of the dominant kernel (the grouped (T) tcgen05 GEMM) from the
+  library's per-launch CUDA-event timers over the timed steps;
+* ``cpu_baseline``: the FP64 oracle on this host (one full NumPy CCSD
+  iteration + (T) of the C restatement, extrapolated from its costliest
+  leading-virtual slices).
 
-``--impl reference`` times only the CPU oracle on the same workload and prints
-the same JSON line with ``"impl": "reference"``.  Run ``python bench.py`` for
-the defaults (N=1).  Under torchrun every rank runs an independent replica
-(the path does not shard in this build: replicas only) and rank 0 prints.
+``--impl reference`` times only that CPU oracle on the same workload (each
+step the same bounded sample) and prints the same JSON line with
+``"impl": "reference"``.  Run ``python bench.py`` for the defaults (N=1).
+Under torchrun every rank runs an independent replica (the path does not
+shard in this build: replicas only) and rank 0 prints.
 """
 from __future__ import annotations
 
@@ -37,16 +49,21 @@ sys.path.insert(0, ROOT)
 
 METRIC = 'CCSD iter + (T) seconds, mixed vs FP64 GPU at <=1uEh; % tensor-pipe peak'
 UNIT = 's'
+CPU_TSLICES = 2  # costliest leading virtuals of the (T) sample (both CPU legs)
 CPU_SAMPLE = ('one full FP64 CCSD iteration of the NumPy oracle (MP2 guess, BLAS einsums) + '
-              '(T) of the C+OpenMP restatement of RCCSD_TriplesCorrection: its repack timed once '
-              'plus the 3 costliest leading virtuals scaled by the triple count (a full (T) at '
-              'o=10, v=90 lands within 16% of this estimate)')
+              '(T) of the C+OpenMP restatement of RCCSD_TriplesCorrection: its repack timed '
+              f'once plus the {CPU_TSLICES} costliest leading virtuals scaled by the triple count '
+              '(a full (T) at o=10, v=90 lands within 16% of this estimate); the eri is '
+              'column-major, as the C restatement reads it, so no step copies it')
 
 
 # DRAM bytes (read + write) of one grouped (T) GEMM launch at o=20, nb=12,
 # measured with ncu: the three W buffers (166 MB) are written once, 112 MB of
 # them reach DRAM, operands are read mostly from L2.
 TRIPLES_LAUNCH_TRAFFIC = 136.7e6
+TRIPLES_TRAFFIC_SOURCE = ('ncu dram__bytes_read.sum + dram__bytes_write.sum of one off-diagonal '
+                          'grouped (T) launch at o=20 v=96, which has the same launch shape '
+                          '(nb=12, 864 work units of 256 x 256 on cluster pairs) as o=20 v=180')
 
 
 def peaks():
@@ -139,7 +156,24 @@ def fp64_peak_tflops(torch):
     return 2.0 * n ** 3 / best / 1e12
 
 
-def cpu_oracle_step(eri, eps, o, ints=None, tslices=3):
+def build_eri_host_colmajor(w):
+    """eri(p,q,r,s) = (pr|qs) as a column-major N^4 array built on the host.
+
+    Formed one s slice at a time (an N^2 x naux by naux x N product each), so
+    that neither a full chemists' copy nor a layout conversion is needed: the
+    slice s of the column-major array is X[r,q,p] = (rp|sq) = chem[(r,p),(s,q)].
+    """
+    N = w.nmo
+    Bm = np.ascontiguousarray(w.B.reshape(w.naux, N * N))
+    flat = np.empty(N ** 4)
+    X = flat.reshape(N, N, N, N)  # C-order [s, r, q, p] == column-major (p, q, r, s)
+    for s in range(N):
+        blk = Bm.T @ Bm[:, s * N:(s + 1) * N]         # [(r, p), q]
+        X[s] = blk.reshape(N, N, N).transpose(0, 2, 1)
+    return flat.reshape((N, N, N, N), order='F')
+
+
+def cpu_oracle_step(eri, eps, o, ints=None, tslices=CPU_TSLICES):
     """One FP64 CPU CCSD iteration + (T) on a bounded sample, in seconds.
 
     CCSD: one full UpdateAmplitudes + energy of the NumPy oracle (BLAS-backed
@@ -319,6 +353,68 @@ def rank_info():
             int(os.environ.get('LOCAL_RANK', 0)))
 
 
+def reference_arm(args, wl, config):
+    """The reference's CPU implementation of the path (the FP64 oracle: NumPy
+    CCSD iteration + C/OpenMP (T) restatement) on this host's cores, each step
+    the same bounded sample as the cpu_baseline leg."""
+    o = args.o
+    eri = build_eri_host_colmajor(wl)
+    import oracle
+    ints = oracle.make_integral_blocks(eri, o)
+    warm = min(args.warmup, 1)
+    for _ in range(warm):
+        cpu_oracle_step(eri, wl.eps, o, ints=ints)
+    times = []
+    det = None
+    for _ in range(args.steps):
+        t, det = cpu_oracle_step(eri, wl.eps, o, ints=ints)
+        times.append(t)
+    val = float(np.median(times))
+    print(json.dumps({
+        'impl': 'reference', 'metric': METRIC, 'value': val, 'unit': UNIT, 'n_gpus': args.gpus,
+        'steps': args.steps, 'warmup': warm, 'ms_per_step': val * 1e3,
+        'higher_is_better': False, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+        'data': 'synthetic', 'config': config,
+        'cpu_baseline': {'value': val, 'unit': UNIT, 'cores': os.cpu_count(), 'kind': 'port',
+                         'sample': CPU_SAMPLE, 'details': det,
+                         'step_times_s': times, 'statistic': 'median over the steps'},
+        'e2e': {'value': val, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+    }))
+
+
+def converged_solves(ctx, eri_h, wl, o, torch):
+    """The drop-in calls to convergence, mixed then FP64: scess_rccsd_solve
+    (SolveRCCSD_DIIS) followed by scess_rccsd_triples (RCCSD_TriplesCorrection),
+    host eri in, amplitudes and energies out, timed on the host."""
+    out = {}
+    amps = {}
+    for prec in ('mixed', 'fp64'):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        w = ctx.solve(eri_h, wl.eps, o, precision=prec)
+        t1 = time.perf_counter()
+        et = ctx.triples(eri_h, wl.eps, o, w.t1, w.t2, precision=prec) if w.converged else None
+        t2 = time.perf_counter()
+        amps[prec] = (w.t1, w.t2)
+        out[prec] = {'seconds': t2 - t0, 'solve_s': t1 - t0, 'triples_s': t2 - t1,
+                     'converged': bool(w.converged), 'iterations': int(w.iterations),
+                     'mixed_iterations': int(w.mixed_iterations),
+                     'fp64_iterations': int(w.iterations - w.mixed_iterations),
+                     'E_CCSD': w.E_CCSD, 'E_T': et}
+    m, f = out['mixed'], out['fp64']
+    ok = m['converged'] and f['converged']
+    res = {'call': 'scess_rccsd_solve (eri from pinned host, MP2 guess, DIIS(8), dE < 1e-10 and '
+                   'rms < 1e-8) + scess_rccsd_triples (eri, t1, t2 from host), per precision',
+           'mixed': m, 'fp64': f,
+           'speedup_mixed_vs_fp64': f['seconds'] / m['seconds'] if ok else None}
+    if ok:
+        res['dE_CCSD'] = abs(m['E_CCSD'] - f['E_CCSD'])
+        res['dE_T'] = abs(m['E_T'] - f['E_T'])
+        res['dE_corr'] = abs(m['E_CCSD'] + m['E_T'] - f['E_CCSD'] - f['E_T'])
+        res['max_abs_dt2'] = float(np.max(np.abs(amps['mixed'][1] - amps['fp64'][1])))
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -329,9 +425,11 @@ def main():
     ap.add_argument('--v', type=int, default=180)
     ap.add_argument('--seed', type=int, default=0)
     ap.add_argument('--fp64-steps', type=int, default=1)
-    ap.add_argument('--e2e-steps', type=int, default=4)
+    ap.add_argument('--e2e-steps', type=int, default=5)
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-fp64', action='store_true')
+    ap.add_argument('--no-converged', action='store_true',
+                    help='skip the converged mixed and FP64 solves + (T)')
     ap.add_argument('--transform', action='store_true',
                     help='AO->MO transform of nmo^4 integrals (TransformTEI), mixed vs FP64')
     ap.add_argument('--triples-only', action='store_true',
@@ -353,36 +451,8 @@ def main():
               'parallelism': 'replicas' if world > 1 else 'single GPU'}
 
     if args.impl == 'reference':
-        if rank != 0:
-            return
-        N = o + v
-        # eri on the host without a GPU: (pr|qs) from the DF factors, in row
-        # blocks (one 40000 x 40000 BLAS call has crashed some BLAS builds)
-        Bm = np.ascontiguousarray(wl.B.reshape(wl.naux, N * N))
-        chem = np.empty((N * N, N * N))
-        rb = 2048
-        for i0 in range(0, N * N, rb):
-            chem[i0:i0 + rb] = Bm[:, i0:i0 + rb].T @ Bm
-        eri = np.ascontiguousarray(chem.reshape(N, N, N, N).transpose(0, 2, 1, 3))
-        del chem
-        ints = oracle.make_integral_blocks(eri, o)
-        for _ in range(min(args.warmup, 1)):
-            cpu_oracle_step(eri, wl.eps, o, ints=ints)
-        times = []
-        det = None
-        for _ in range(args.steps):
-            t, det = cpu_oracle_step(eri, wl.eps, o, ints=ints)
-            times.append(t)
-        val = float(np.mean(times))
-        print(json.dumps({
-            'impl': 'reference', 'metric': METRIC, 'value': val, 'unit': UNIT, 'n_gpus': args.gpus,
-            'steps': args.steps, 'warmup': min(args.warmup, 1), 'ms_per_step': val * 1e3,
-            'higher_is_better': False, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
-            'data': 'synthetic', 'config': config,
-            'cpu_baseline': {'value': val, 'unit': UNIT, 'cores': os.cpu_count(), 'kind': 'port',
-                             'sample': CPU_SAMPLE, 'details': det},
-            'e2e': {'value': val, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
-        }))
+        if rank == 0:
+            reference_arm(args, wl, config)
         return
 
     import torch
@@ -408,7 +478,10 @@ def main():
     ctx = s.Context(local)
 
     # ---- mixed form, inputs resident ----------------------------------------------------
-    st = ctx.state(eri_h, wl.eps, o, precision='mixed', max_iterations=1000)
+    # mixed_energy_switch = 0: the state never moves to its FP64 refinement phase,
+    # so every step below is one mixed iteration and one mixed (T)
+    st = ctx.state(eri_h, wl.eps, o, precision='mixed', max_iterations=1000,
+                   mixed_energy_switch=0.0)
     for _ in range(args.warmup):
         st.iterate(1)
         st.triples('mixed')
@@ -421,10 +494,15 @@ def main():
     ctx.profile(True)
     n0 = lib.scess_launch_count()
     it_ms, t_ms, ets = [], [], []
+    mixed_before = args.warmup
     wall0 = time.perf_counter()
     for _ in range(args.steps):
         r, ms1 = st.iterate(1)
         et, ms2 = st.triples('mixed')
+        if r.mixed_iterations != mixed_before + 1 or r.iterations != r.mixed_iterations:
+            raise RuntimeError(f'timed step was not one mixed iteration: {r.mixed_iterations} '
+                               f'mixed, {r.iterations} total after {mixed_before}')
+        mixed_before = r.mixed_iterations
         it_ms.append(ms1)
         t_ms.append(ms2)
         ets.append(et)
@@ -438,7 +516,6 @@ def main():
     step_s = max_over_ranks(step_s, world)
     hist_mixed = st.hist.reshape(-1, 3)
     n_iter_mixed = args.warmup + args.steps
-    t1m, t2m = st.amplitudes()
 
     # ---- roofline of the dominant kernel ----------------------------------------------------
     # The grouped (T) GEMM (one launch per block triple).  Algorithmic FLOPs are the
@@ -465,10 +542,7 @@ def main():
                 'launches': tc['launches'], 'avg_launch_ms': avg_ms,
                 'algorithmic_flops_per_launch': per_launch_alg,
                 'traffic': TRIPLES_LAUNCH_TRAFFIC if (o, v) == (20, 180) else None,
-                'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of one '
-                                  'off-diagonal grouped (T) launch at o=20 v=96, which has the same '
-                                  'launch shape (nb=12, 864 work units of 256 x 256 on cluster pairs) '
-                                  'as o=20 v=180',
+                'traffic_source': TRIPLES_TRAFFIC_SOURCE,
                 'top_kernel_by_time': top}
     # "phase:" timers enclose kernel timers: shown, but not part of the shares
     kern = {k: v for k, v in prof.items() if not k.startswith('phase:')}
@@ -498,6 +572,9 @@ def main():
         del sf
     st.close()
     del st
+
+    # ---- the drop-in calls to convergence, mixed vs FP64 --------------------------------------
+    converged = None if args.no_converged else converged_solves(ctx, eri_h, wl, o, torch)
 
     # ---- e2e through the public API from pinned host buffers ----------------------------------
     # host->device bandwidth of the pinned input right before the e2e steps (torch copy)
@@ -540,12 +617,14 @@ def main():
         ctx.profile(False)
         e2e_profile = {k: round(v['ms'], 3) for k, v in rep.items()
                        if k.startswith('host:') or v['ms'] > 1.0}
-    e2e = {'value': float(np.min(e2e_times)) if e2e_times else None, 'unit': UNIT,
+    med = int(np.argsort(e2e_times)[len(e2e_times) // 2]) if e2e_times else None
+    e2e = {'value': float(np.median(e2e_times)) if e2e_times else None, 'unit': UNIT,
+           'statistic': f'median of {len(e2e_times)} steps',
            'h2d_bytes_per_step': int(8 * (N ** 4 + N)),
            'd2h_bytes_per_step': int(8 * (o * v + o * o * v * v) + 64),
            'path': 'scess_rccsd_state_create (eri from pinned host) + state_iterate(1) + '
                    'state_triples(MIXED) + state_amplitudes + destroy',
-           'phases': e2e_phases[int(np.argmin(e2e_times))] if e2e_times else None,
+           'phases_of_median': e2e_phases[med] if e2e_times else None,
            'all_times': e2e_times, 'profiled_ms': e2e_profile,
            'pinned_h2d_gbps_torch_probe': h2d_probe}
 
@@ -561,11 +640,13 @@ def main():
                 'warmup': args.warmup, 'ms_per_step': step_s * 1e3, 'higher_is_better': False,
                 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f16x2-split (FP32 acc) + f64',
                 'data': 'synthetic', 'config': config,
+                'step': 'one mixed CCSD iteration + one mixed (T) on a state held in its mixed phase',
                 'breakdown_ms': {'ccsd_iter': float(np.mean(it_ms)), 'triples': float(np.mean(t_ms)),
                                  'wall_per_step': wall * 1e3},
                 'E_T_mixed': ets[-1], 'E_ccsd_iter_mixed': float(hist_mixed[n_iter_mixed - 1, 0]),
-                'fp64': fp64, 'roofline': roofline, 'kernel_share': share, 'kernel_timers': prof,
-                'cpu_baseline': cpu, 'e2e': e2e, 'gpu_launches': launches // max(args.steps, 1),
+                'fp64': fp64, 'converged': converged, 'roofline': roofline, 'kernel_share': share,
+                'kernel_timers': prof, 'cpu_baseline': cpu, 'e2e': e2e,
+                'gpu_launches': launches // max(args.steps, 1),
                 'gpu_launches_total': launches, 'clocks': clocks}
         print(json.dumps(line))
     if world > 1:

@@ -45,9 +45,10 @@ extern "C" {
 #define SCESS_ERR_TOO_LARGE 7   /* scess_einsum_static: beyond its fixed scratch */
 
 /* Arithmetic of the contractions. FP64 is the drop-in path (matches the
- * reference to <= 1e-9 Eh); MIXED runs the contractions on BF16 tensor cores
+ * reference to <= 1e-9 Eh); MIXED runs the contractions on FP16 tensor cores
  * (tcgen05, split hi+lo operands, FP32 accumulation) with FP64 denominators,
- * DIIS and energies, followed by FP64 refinement sweeps. */
+ * DIIS and energies, followed by a refinement that ends in FP64 iterations
+ * (see refine_sweeps). */
 #define SCESS_PRECISION_FP64 0
 #define SCESS_PRECISION_MIXED 1
 
@@ -69,12 +70,17 @@ typedef struct {
   int32_t diis_start;           /* 2     */
   int32_t max_diis_vectors;     /* 8     */
   int32_t precision;            /* SCESS_PRECISION_FP64 */
-  /* MIXED only: after the mixed iterations meet the thresholds, this many
-   * further iterations run in FP64 (0 = none). Convergence is re-checked in
-   * FP64 and the returned energy comes from an FP64 iteration. */
+  /* MIXED only: the least number of FP64 iterations of the refinement (at
+   * least 1).  The refinement starts with one FP64 iteration (the base: its
+   * residual R0 and intermediates at its amplitudes T0 are kept), continues
+   * with refined iterations whose residual R0 + dR(T0, T - T0) runs on the
+   * tensor cores with every product carrying a factor of the size of T - T0
+   * (so its rounding error shrinks with T - T0), and ends with an FP64
+   * iteration that must meet the convergence criteria (else it becomes the
+   * new base).  The returned energy comes from that FP64 iteration. */
   int32_t refine_sweeps;        /* 2 */
   /* MIXED only: the mixed phase ends once dE < mixed_energy_switch and
-   * rms(dt) < mixed_amplitude_switch; the FP64 phase then starts from the
+   * rms(dt) < mixed_amplitude_switch; the refinement then starts from the
    * mixed amplitudes with a fresh DIIS subspace. */
   double mixed_energy_switch;     /* 1e-8 */
   double mixed_amplitude_switch;  /* 1e-6 */
@@ -99,9 +105,10 @@ typedef struct {
   double E_T;             /* set by scess_rccsd_triples only                  */
   int32_t converged;
   int32_t iterations;     /* total iterations run (mixed + FP64)              */
-  int32_t mixed_iterations;
+  int32_t mixed_iterations; /* iterations whose residual ran on the tensor cores */
   double last_dE;
   double last_rms;
+  int32_t fp64_iterations;  /* iterations with an FP64 residual               */
 } scess_rccsd_result;
 
 const char *scess_status_string(int status);
@@ -114,6 +121,28 @@ void scess_ctx_destroy(scess_ctx *ctx);
 /* Message of the last failing call on this context ("" if none). */
 const char *scess_ctx_last_error(const scess_ctx *ctx);
 int scess_ctx_set_callbacks(scess_ctx *ctx, scess_cancel_fn cancel, scess_log_fn log, void *user);
+
+/* Device-memory cap of a context (no counterpart in the reference, which runs
+ * on host memory).  For a GPU shared with other work: the device memory this
+ * context's calls hold (their live buffers and the context's cache of released
+ * blocks) stays within `bytes`; an allocation beyond it first empties the
+ * cache, then fails with SCESS_ERR_OOM as a full device would, and the context
+ * stays usable.  0 removes the cap.  scess_ctx_memory_held reports the bytes
+ * currently held (-1 for a bad context). */
+int scess_ctx_set_memory_limit(scess_ctx *ctx, int64_t bytes);
+int64_t scess_ctx_memory_held(const scess_ctx *ctx);
+
+/* Diagnostics of the tensor-core kernels' failure path (no counterpart in the
+ * reference).  Every pipeline wait inside those kernels is bounded; this arms
+ * the NEXT tensor-core launch of the context with a bound of `wait_cycles` GPU
+ * clock cycles (2^16 .. 2^40; production launches use ~2^32) and makes its
+ * copy thread leave the first operand stage unfilled, so that the MMA
+ * thread's wait on it runs out.  The kernel then records the expiry, lets the
+ * copies it did issue land, frees its tensor memory and returns; the call that
+ * made the launch fails with SCESS_ERR_CUDA ("tensor-core pipeline wait
+ * expired"), and later calls on the context run normally.  Nothing faults,
+ * traps or hangs. */
+int scess_ctx_arm_wait_expiry(scess_ctx *ctx, int64_t wait_cycles);
 
 void scess_rccsd_default_options(scess_rccsd_options *opts);
 
@@ -197,6 +226,13 @@ int scess_ctx_profile_report(scess_ctx *ctx, char *buf, int64_t buflen);
 int scess_rccsd_residual(scess_ctx *ctx, const double *eri, int64_t nmo, int64_t nocc,
                          const double *t1, const double *t2, const double *t2_driver,
                          int32_t precision, double *r1_out, double *r2_out);
+/* Same from DF factors B (naux x nmo x nmo): the forward half of the pair
+ * whose reverse is scess_rccsd_residual_vjp_df; the eri
+ * <pq|rs> = sum_Q B(Q,p,r) B(Q,q,s) is formed on the GPU in FP64. */
+int scess_rccsd_residual_df(scess_ctx *ctx, const double *B, int64_t naux, int64_t nmo,
+                            int64_t nocc, const double *t1, const double *t2,
+                            const double *t2_driver, int32_t precision, double *r1_out,
+                            double *r2_out);
 
 /* Vector-Jacobian product of the residual numerators R(t1, t2; eri) of
  * scess_rccsd_residual (UpdateAmplitudes, RCCSD.cpp:101-233; the reference has
@@ -216,19 +252,22 @@ int scess_rccsd_residual_vjp_df(scess_ctx *ctx, const double *B, int64_t naux, i
                                 double *g_t1, double *g_t2, double *g_B);
 
 /* Vector-Jacobian product of E_(T) (RCCSD_TriplesCorrection, RCCSD_T.cpp:17-168;
- * the reference has no derivative code), FP64: for a cotangent g_e, writes
+ * the reference has no derivative code): for a cotangent g_e, writes
  * g_e dE_T/dt1 (o*v), g_e dE_T/dt2 (o^2 v^2) and, when g_eri is not NULL,
  * g_e dE_T/deri (nmo^4, eri layout; nonzero only on the (ov|vv), (oo|vo) and
  * (ov|ov) blocks E_T reads).  e_t (may be NULL) receives E_T.  The forward
- * W is recomputed block by block, so the memory use is that of the FP64 (T). */
+ * W is recomputed block by block, so the memory use is that of the FP64 (T).
+ * precision: SCESS_PRECISION_FP64 (FP64 table GEMMs), or MIXED (the forward
+ * and transposed GEMMs on the tensor cores: split operands, FP32
+ * accumulation; the element-wise gradient of the energy stays FP64). */
 int scess_rccsd_triples_vjp(scess_ctx *ctx, const double *eri, const double *eps, int64_t nmo,
-                            int64_t nocc, const double *t1, const double *t2, double g_e,
-                            double *e_t, double *g_t1, double *g_t2, double *g_eri);
+                            int64_t nocc, const double *t1, const double *t2, int32_t precision,
+                            double g_e, double *e_t, double *g_t1, double *g_t2, double *g_eri);
 /* Same from DF factors; g_B (naux x nmo x nmo, may be NULL) = g_e dE_T/dB. */
 int scess_rccsd_triples_vjp_df(scess_ctx *ctx, const double *B, int64_t naux, const double *eps,
                                int64_t nmo, int64_t nocc, const double *t1, const double *t2,
-                               double g_e, double *e_t, double *g_t1, double *g_t2,
-                               double *g_B);
+                               int32_t precision, double g_e, double *e_t, double *g_t1,
+                               double *g_t2, double *g_B);
 
 /* CCSD Lambda (left-hand) equations at converged t1/t2 (no counterpart in the
  * reference).  Omega(t; f) is the closed-shell residual with the Fock terms that
@@ -358,9 +397,11 @@ int scess_ccsd_so_triples(scess_ctx *ctx, const double *g, const double *eps, in
  * order them on one stream.  No part of it needs to start at zero: a call
  * writes all the scratch it reads before reading it.  The first call on a
  * device looks up the array's device address on that device (the CUDA runtime
- * loads the library's device code there); make that first call before any
- * stream capture.  Returns SCESS_ERR_INVALID for a bad spec, extents or null
- * pointers, SCESS_ERR_CUDA for a failed launch. */
+ * loads the library's device code there), and so does the first call after
+ * the device's CUDA context has changed (a cudaDeviceReset); make those calls
+ * before any stream capture.  Returns SCESS_ERR_INVALID for a bad spec,
+ * extents or null pointers, or when A, B or C is not device (or managed)
+ * memory of the current device, SCESS_ERR_CUDA for a failed launch. */
 int scess_einsum_static(const char *spec, double alpha, const double *A, int32_t a_nd,
                         const int64_t *a_ext, const double *B, int32_t b_nd,
                         const int64_t *b_ext, double beta, double *C, int32_t c_nd,

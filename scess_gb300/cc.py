@@ -64,7 +64,7 @@ class Result(C.Structure):
     _fields_ = [('E_CCSD', C.c_double), ('E_F12_Coupling', C.c_double), ('E_T', C.c_double),
                 ('converged', C.c_int32), ('iterations', C.c_int32),
                 ('mixed_iterations', C.c_int32), ('last_dE', C.c_double),
-                ('last_rms', C.c_double)]
+                ('last_rms', C.c_double), ('fp64_iterations', C.c_int32)]
 
 
 CANCEL_FN = C.CFUNCTYPE(C.c_int, C.c_void_p)
@@ -79,6 +79,9 @@ EXPORTS = {
     'scess_ctx_destroy': (None, [C.c_void_p]),
     'scess_ctx_last_error': (C.c_char_p, [C.c_void_p]),
     'scess_ctx_set_callbacks': (C.c_int, [C.c_void_p, CANCEL_FN, LOG_FN, C.c_void_p]),
+    'scess_ctx_set_memory_limit': (C.c_int, [C.c_void_p, C.c_int64]),
+    'scess_ctx_memory_held': (C.c_int64, [C.c_void_p]),
+    'scess_ctx_arm_wait_expiry': (C.c_int, [C.c_void_p, C.c_int64]),
     'scess_rccsd_default_options': (None, [C.POINTER(Options)]),
     'scess_rccsd_solve': (C.c_int, [C.c_void_p, _dp, _dp, C.c_int64, C.c_int64, _dp, _dp,
                                     C.POINTER(Options), _dp, _dp, C.POINTER(Result)]),
@@ -104,6 +107,8 @@ EXPORTS = {
     'scess_ctx_profile_report': (C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),
     'scess_rccsd_residual': (C.c_int, [C.c_void_p, _dp, C.c_int64, C.c_int64, _dp, _dp, _dp,
                                        C.c_int32, _dp, _dp]),
+    'scess_rccsd_residual_df': (C.c_int, [C.c_void_p, _dp, C.c_int64, C.c_int64, C.c_int64, _dp,
+                                          _dp, _dp, C.c_int32, _dp, _dp]),
     'scess_rccsd_residual_vjp': (C.c_int, [C.c_void_p, _dp, C.c_int64, C.c_int64, _dp, _dp, _dp,
                                            _dp, C.c_int32, _dp, _dp, _dp]),
     'scess_rccsd_residual_vjp_df': (C.c_int, [C.c_void_p, _dp, C.c_int64, C.c_int64, C.c_int64,
@@ -115,9 +120,10 @@ EXPORTS = {
     'scess_einsum': (C.c_int, [C.c_void_p, C.c_char_p, C.c_double, _dp, C.c_int32, _i64p, _dp,
                                C.c_int32, _i64p, C.c_double, _dp, C.c_int32, _i64p, C.c_int32]),
     'scess_rccsd_triples_vjp': (C.c_int, [C.c_void_p, _dp, _dp, C.c_int64, C.c_int64, _dp, _dp,
-                                          C.c_double, C.POINTER(C.c_double), _dp, _dp, _dp]),
+                                          C.c_int32, C.c_double, C.POINTER(C.c_double), _dp, _dp,
+                                          _dp]),
     'scess_rccsd_triples_vjp_df': (C.c_int, [C.c_void_p, _dp, C.c_int64, _dp, C.c_int64,
-                                             C.c_int64, _dp, _dp, C.c_double,
+                                             C.c_int64, _dp, _dp, C.c_int32, C.c_double,
                                              C.POINTER(C.c_double), _dp, _dp, _dp]),
     'scess_transform_tei': (C.c_int, [C.c_void_p, _dp, C.c_int64, _dp, C.c_int64, _dp, C.c_int64,
                                       _dp, C.c_int64, _dp, C.c_int64, C.c_int32, C.c_int32, _dp]),
@@ -249,6 +255,20 @@ class Context:
             msg = self.lib.scess_ctx_last_error(self.h).decode()
             raise ScessError(st, f'{what}: {msg}')
 
+    # -- device memory and diagnostics -------------------------------------------------------
+    def set_memory_limit(self, nbytes: int):
+        """Caps the device memory this context's calls hold (0: no cap)."""
+        self._check(self.lib.scess_ctx_set_memory_limit(self.h, int(nbytes)),
+                    'scess_ctx_set_memory_limit')
+
+    def memory_held(self) -> int:
+        return int(self.lib.scess_ctx_memory_held(self.h))
+
+    def arm_wait_expiry(self, wait_cycles: int = 1 << 20):
+        """The next tensor-core launch runs out its bounded pipeline wait."""
+        self._check(self.lib.scess_ctx_arm_wait_expiry(self.h, int(wait_cycles)),
+                    'scess_ctx_arm_wait_expiry')
+
     # -- options ---------------------------------------------------------------------------
     def default_options(self) -> Options:
         o = Options()
@@ -358,17 +378,27 @@ class Context:
         return json.loads(buf.value.decode())
 
     # -- one residual -------------------------------------------------------------------------
-    def residual(self, eri, nocc, t1, t2, t2_driver=None, precision: str = 'fp64'):
-        """(t1new, t2new) numerators of UpdateAmplitudes (before the division)."""
-        ef = _f64(eri)
-        N = ef.shape[0]
+    def residual(self, eri, nocc, t1, t2, t2_driver=None, precision: str = 'fp64', B=None):
+        """(t1new, t2new) numerators of UpdateAmplitudes (before the division), from
+        the eri or, with B, from DF factors (scess_rccsd_residual_df)."""
+        if B is not None:
+            Bf = _f64(B)
+            N = Bf.shape[1]
+        else:
+            ef = _f64(eri)
+            N = ef.shape[0]
         o, v = int(nocc), N - int(nocc)
         t1f, t2f = _f64(t1, (o, v)), _f64(t2, (o, o, v, v))
         drv = None if t2_driver is None else _f64(t2_driver, (o, o, v, v))
         r1 = np.zeros((o, v), order='F')
         r2 = np.zeros((o, o, v, v), order='F')
-        st = self.lib.scess_rccsd_residual(self.h, _ptr(ef), N, o, _ptr(t1f), _ptr(t2f),
-                                           _ptr(drv), PRECISION[precision], _ptr(r1), _ptr(r2))
+        if B is not None:
+            st = self.lib.scess_rccsd_residual_df(self.h, _ptr(Bf), Bf.shape[0], N, o, _ptr(t1f),
+                                                  _ptr(t2f), _ptr(drv), PRECISION[precision],
+                                                  _ptr(r1), _ptr(r2))
+        else:
+            st = self.lib.scess_rccsd_residual(self.h, _ptr(ef), N, o, _ptr(t1f), _ptr(t2f),
+                                               _ptr(drv), PRECISION[precision], _ptr(r1), _ptr(r2))
         self._check(st, 'scess_rccsd_residual')
         return r1, r2
 
@@ -402,8 +432,9 @@ class Context:
         return gt1, gt2, gI
 
     def triples_vjp(self, eri=None, eps=None, nocc=None, t1=None, t2=None, g_e=1.0, B=None,
-                    want_integrals=False):
-        """(E_T, g_t1, g_t2, g_eri or g_B): g_e times the gradient of E_(T) (FP64)."""
+                    want_integrals=False, precision='fp64'):
+        """(E_T, g_t1, g_t2, g_eri or g_B): g_e times the gradient of E_(T)
+        (FP64, or MIXED: its GEMMs on the tensor cores)."""
         eps = _f64(eps)
         N = eps.shape[0]
         o, v = int(nocc), N - int(nocc)
@@ -415,14 +446,15 @@ class Context:
             Bf = _f64(B)
             gI = np.zeros(Bf.shape, order='F') if want_integrals else None
             st = self.lib.scess_rccsd_triples_vjp_df(self.h, _ptr(Bf), Bf.shape[0], _ptr(eps), N, o,
-                                                     _ptr(t1f), _ptr(t2f), float(g_e), C.byref(et),
-                                                     _ptr(gt1), _ptr(gt2), _ptr(gI))
+                                                     _ptr(t1f), _ptr(t2f), PRECISION[precision],
+                                                     float(g_e), C.byref(et), _ptr(gt1),
+                                                     _ptr(gt2), _ptr(gI))
         else:
             ef = _f64(eri, (N, N, N, N))
             gI = np.zeros((N, N, N, N), order='F') if want_integrals else None
             st = self.lib.scess_rccsd_triples_vjp(self.h, _ptr(ef), _ptr(eps), N, o, _ptr(t1f),
-                                                  _ptr(t2f), float(g_e), C.byref(et), _ptr(gt1),
-                                                  _ptr(gt2), _ptr(gI))
+                                                  _ptr(t2f), PRECISION[precision], float(g_e),
+                                                  C.byref(et), _ptr(gt1), _ptr(gt2), _ptr(gI))
         self._check(st, 'scess_rccsd_triples_vjp')
         return et.value, gt1, gt2, gI
 

@@ -234,6 +234,21 @@ void scess_ctx_destroy(scess_ctx *ctx) {
 
 const char *scess_ctx_last_error(const scess_ctx *ctx) { return ctx ? ctx->err.c_str() : ""; }
 
+int scess_ctx_set_memory_limit(scess_ctx *ctx, int64_t bytes) {
+  if (!ctx || !ctx->impl || bytes < 0) return SCESS_ERR_INVALID;
+  ctx->impl->mem_limit = (size_t)bytes;
+  return SCESS_OK;
+}
+
+int64_t scess_ctx_memory_held(const scess_ctx *ctx) {
+  return (ctx && ctx->impl) ? (int64_t)ctx->impl->mem_held : -1;
+}
+
+int scess_ctx_arm_wait_expiry(scess_ctx *ctx, int64_t wait_cycles) {
+  if (wait_cycles < (int64_t(1) << 16) || wait_cycles > (int64_t(1) << 40)) return SCESS_ERR_INVALID;
+  return guard(ctx, [&](scess::Ctx &c) { c.tensor_cores().arm_wait_expiry(wait_cycles); });
+}
+
 int scess_ctx_set_callbacks(scess_ctx *ctx, scess_cancel_fn cancel, scess_log_fn log, void *user) {
   if (!ctx || !ctx->impl) return SCESS_ERR_INVALID;
   ctx->impl->cancel = cancel;
@@ -328,10 +343,12 @@ int scess_rccsd_triples_df(scess_ctx *ctx, const double *B, int64_t naux, const 
 
 static int triples_vjp_common(scess_ctx *ctx, const double *eri, const double *B, int64_t naux,
                               const double *eps, int64_t nmo, int64_t nocc, const double *t1,
-                              const double *t2, double g_e, double *e_t, double *g_t1,
-                              double *g_t2, double *g_eri, double *g_B) {
+                              const double *t2, int32_t precision, double g_e, double *e_t,
+                              double *g_t1, double *g_t2, double *g_eri, double *g_B) {
   return guard(ctx, [&](scess::Ctx &c) {
     check_shape(nmo, nocc);
+    if (precision != SCESS_PRECISION_FP64 && precision != SCESS_PRECISION_MIXED)
+      throw Error(SCESS_ERR_INVALID, "bad precision");
     need(eps, "eps");
     need(t1, "t1");
     need(t2, "t2");
@@ -374,7 +391,8 @@ static int triples_vjp_common(scess_ctx *ctx, const double *eri, const double *B
     ctl.poll();
     const double et = scess::rccsd_triples_vjp(c, d_eri.p(), nmo, nocc, d_eps.p(), d_t1.p(),
                                                d_t2.p(), g_e, ctl, gt1.p(), gt2.p(),
-                                               need_eri ? geri.p() : nullptr);
+                                               need_eri ? geri.p() : nullptr,
+                                               precision == SCESS_PRECISION_MIXED);
     if (e_t) *e_t = et;
     scess::download(c, g_t1, gt1.p(), n1);
     scess::download(c, g_t2, gt2.p(), n2);
@@ -392,20 +410,20 @@ static int triples_vjp_common(scess_ctx *ctx, const double *eri, const double *B
 }
 
 int scess_rccsd_triples_vjp(scess_ctx *ctx, const double *eri, const double *eps, int64_t nmo,
-                            int64_t nocc, const double *t1, const double *t2, double g_e,
-                            double *e_t, double *g_t1, double *g_t2, double *g_eri) {
+                            int64_t nocc, const double *t1, const double *t2, int32_t precision,
+                            double g_e, double *e_t, double *g_t1, double *g_t2, double *g_eri) {
   if (!eri) return SCESS_ERR_INVALID;
-  return triples_vjp_common(ctx, eri, nullptr, 0, eps, nmo, nocc, t1, t2, g_e, e_t, g_t1, g_t2,
-                            g_eri, nullptr);
+  return triples_vjp_common(ctx, eri, nullptr, 0, eps, nmo, nocc, t1, t2, precision, g_e, e_t,
+                            g_t1, g_t2, g_eri, nullptr);
 }
 
 int scess_rccsd_triples_vjp_df(scess_ctx *ctx, const double *B, int64_t naux, const double *eps,
                                int64_t nmo, int64_t nocc, const double *t1, const double *t2,
-                               double g_e, double *e_t, double *g_t1, double *g_t2,
-                               double *g_B) {
+                               int32_t precision, double g_e, double *e_t, double *g_t1,
+                               double *g_t2, double *g_B) {
   if (!B || naux <= 0) return SCESS_ERR_INVALID;
-  return triples_vjp_common(ctx, nullptr, B, naux, eps, nmo, nocc, t1, t2, g_e, e_t, g_t1, g_t2,
-                            nullptr, g_B);
+  return triples_vjp_common(ctx, nullptr, B, naux, eps, nmo, nocc, t1, t2, precision, g_e, e_t,
+                            g_t1, g_t2, nullptr, g_B);
 }
 
 static int state_create(scess_ctx *ctx, const double *eri, const double *B, int64_t naux,
@@ -551,18 +569,26 @@ int scess_ctx_profile_report(scess_ctx *ctx, char *buf, int64_t buflen) {
   });
 }
 
-int scess_rccsd_residual(scess_ctx *ctx, const double *eri, int64_t nmo, int64_t nocc,
-                         const double *t1, const double *t2, const double *t2_driver,
-                         int32_t precision, double *r1_out, double *r2_out) {
-  if (!eri) return SCESS_ERR_INVALID;
+static int residual_common(scess_ctx *ctx, const double *eri, const double *B, int64_t naux,
+                           int64_t nmo, int64_t nocc, const double *t1, const double *t2,
+                           const double *t2_driver, int32_t precision, double *r1_out,
+                           double *r2_out) {
   return guard(ctx, [&](scess::Ctx &c) {
     check_shape(nmo, nocc);
     need(t1, "t1");
     need(t2, "t2");
     need(r1_out, "r1_out");
     need(r2_out, "r2_out");
-    const int64_t o = nocc, v = nmo - nocc, n1 = o * v, n2 = o * o * v * v;
-    scess::DTensor d_eri = device_eri(c, eri, nmo);
+    const int64_t o = nocc, v = nmo - nocc, n1 = o * v, n2 = o * o * v * v, N = nmo;
+    scess::DTensor d_eri;
+    if (eri) {
+      d_eri = device_eri(c, eri, nmo);
+    } else {
+      // eri(p,q,r,s) = sum_Q B(Q,p,r) B(Q,q,s) in FP64, as the DF adjoint forms it
+      scess::DTensor dB = device_B(c, B, naux, nmo);
+      d_eri = scess::DTensor({N, N, N, N});
+      scess::einsum(c, "Qpr,Qqs->pqrs", 1.0, dB.v, dB.v, 0.0, d_eri.v, scess::Backend::FP64);
+    }
     scess::RccsdBlocks blocks;
     blocks.build(c, d_eri.p(), nmo, nocc);
     scess::DTensor amp({n1 + n2}), R({n1 + n2}), drv;
@@ -581,6 +607,23 @@ int scess_rccsd_residual(scess_ctx *ctx, const double *eri, int64_t nmo, int64_t
     scess::download(c, r2_out, R.p() + n1, n2);
     if (mixed) c.tensor_cores().check_error();
   });
+}
+
+int scess_rccsd_residual(scess_ctx *ctx, const double *eri, int64_t nmo, int64_t nocc,
+                         const double *t1, const double *t2, const double *t2_driver,
+                         int32_t precision, double *r1_out, double *r2_out) {
+  if (!eri) return SCESS_ERR_INVALID;
+  return residual_common(ctx, eri, nullptr, 0, nmo, nocc, t1, t2, t2_driver, precision, r1_out,
+                         r2_out);
+}
+
+int scess_rccsd_residual_df(scess_ctx *ctx, const double *B, int64_t naux, int64_t nmo,
+                            int64_t nocc, const double *t1, const double *t2,
+                            const double *t2_driver, int32_t precision, double *r1_out,
+                            double *r2_out) {
+  if (!B || naux <= 0) return SCESS_ERR_INVALID;
+  return residual_common(ctx, nullptr, B, naux, nmo, nocc, t1, t2, t2_driver, precision, r1_out,
+                         r2_out);
 }
 
 static int residual_vjp_common(scess_ctx *ctx, const double *eri, const double *B, int64_t naux,

@@ -5,8 +5,11 @@
 // partial sums) lives in one file-scope __device__ array of a fixed size.
 // Host code never passes the array's name to a kernel: on the host that name is
 // a stand-in, not a device address.  The device address is looked up with
-// cudaGetSymbolAddress once per device, with that device current, and the
-// looked-up pointer is what the kernels receive.
+// cudaGetSymbolAddress once per device and CUDA context, with that device
+// current, and the looked-up pointer is what the kernels receive.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <cstring>
 #include <mutex>
 
@@ -24,21 +27,69 @@ static __device__ __align__(256) unsigned char g_einsum_scratch[kScratchBytes];
 
 std::mutex g_addr_mu;
 void *g_addr[kMaxDevices];
+unsigned long long g_addr_ctx[kMaxDevices];  // context id the address belongs to
 
-// Device address of g_einsum_scratch on the current device (looked up once).
+// Unique id of the calling thread's current CUDA context (cuCtxGetId; ids are
+// never reused within a process), 0 if the driver cannot tell.  After a
+// cudaDeviceReset the device's next primary context has a new id, and the
+// library's device code, with this array, is loaded into it anew.
+unsigned long long current_context_id() {
+  static PFN_cuCtxGetCurrent_v4000 get_current = nullptr;
+  static PFN_cuCtxGetId_v12000 get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void *p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(p);
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<PFN_cuCtxGetId_v12000>(p);
+    cudaGetLastError();
+  });
+  CUcontext cx = nullptr;
+  unsigned long long id = 0;
+  if (get_current && get_id && get_current(&cx) == CUDA_SUCCESS && cx &&
+      get_id(cx, &id) == CUDA_SUCCESS)
+    return id;
+  return 0;
+}
+
+// Device address of g_einsum_scratch on the current device, looked up once per
+// device and context (again when the context has changed, e.g. after a
+// cudaDeviceReset).
 int scratch_address(int dev, void **out) {
   std::lock_guard<std::mutex> lock(g_addr_mu);
-  if (!g_addr[dev]) {
+  const unsigned long long cid = current_context_id();
+  if (!g_addr[dev] || cid == 0 || g_addr_ctx[dev] != cid) {
     void *p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_einsum_scratch);
     if (e != cudaSuccess || !p) {
       cudaGetLastError();
+      g_addr[dev] = nullptr;
       return SCESS_ERR_CUDA;
     }
     g_addr[dev] = p;
+    g_addr_ctx[dev] = cid;
   }
   *out = g_addr[dev];
   return SCESS_OK;
+}
+
+// Whether p is memory of device dev that kernels can read and write (device or
+// managed memory).  cudaPointerGetAttributes allocates nothing.
+bool on_device(const void *p, int dev) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (at.type == cudaMemoryTypeManaged) return true;
+  return at.type == cudaMemoryTypeDevice && at.device == dev;
 }
 
 // Index group of the contraction (M: free labels of A, N: free labels of B,
@@ -183,6 +234,8 @@ extern "C" int scess_einsum_static(const char *spec, double alpha, const double 
     return SCESS_ERR_CUDA;
   }
   if (dev < 0 || dev >= kMaxDevices) return SCESS_ERR_UNSUPPORTED;
+  // host memory, or another GPU's, would fault in the kernels: refuse it here
+  if (!on_device(A, dev) || !on_device(B, dev) || !on_device(C, dev)) return SCESS_ERR_INVALID;
   void *base = nullptr;
   const int st = scratch_address(dev, &base);
   if (st != SCESS_OK) return st;

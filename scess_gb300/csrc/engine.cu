@@ -1,6 +1,7 @@
 // Host engine: device memory, context, einsum compiler (spec -> offset-table GEMM).
 #include <algorithm>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstring>
 
 #include "engine.h"
@@ -15,6 +16,20 @@ thread_local Ctx *t_ctx = nullptr;
 }
 
 Ctx *current_ctx() { return t_ctx; }
+
+int64_t tune_value(const char *key, int64_t def) {
+  const char *env = std::getenv("SCESS_TUNE");
+  if (!env) return def;
+  const size_t kl = std::strlen(key);
+  for (const char *p = env; *p;) {
+    const char *end = std::strchr(p, ',');
+    if (!end) end = p + std::strlen(p);
+    if ((size_t)(end - p) > kl && std::strncmp(p, key, kl) == 0 && p[kl] == '=')
+      return std::strtoll(p + kl + 1, nullptr, 10);
+    p = *end ? end + 1 : end;
+  }
+  return def;
+}
 CurrentCtx::CurrentCtx(Ctx *c) : prev(t_ctx) { t_ctx = c; }
 CurrentCtx::~CurrentCtx() { t_ctx = prev; }
 
@@ -34,29 +49,47 @@ bool BlockCache::give(void *p, size_t bytes) {
   return true;
 }
 
-void BlockCache::flush() {
+size_t BlockCache::flush() {
   for (auto &kv : free_) cudaFree(kv.second);
   free_.clear();
+  const size_t t = total_;
   total_ = 0;
+  return t;
 }
+
+namespace {
+// Frees the context's cached blocks (after its queued work) and stops counting them.
+void flush_cache(Ctx *c) {
+  cudaStreamSynchronize(c->stream);
+  const size_t freed = c->blocks.flush();
+  c->mem_held -= std::min(freed, c->mem_held);
+}
+}  // namespace
 
 void DevMem::alloc(size_t bytes) {
   release();
   if (bytes == 0) return;
   Ctx *c = current_ctx();
   if (c && bytes >= BlockCache::kMinBytes) {
-    if (void *p = c->blocks.take(bytes)) {
+    if (void *p = c->blocks.take(bytes)) {  // (cached bytes are already counted as held)
       p_ = p;
       bytes_ = bytes;
       owner_ = c;
       return;
     }
   }
+  if (c && c->mem_limit) {
+    if (c->mem_held + bytes > c->mem_limit && c->blocks.bytes() > 0) flush_cache(c);
+    if (c->mem_held + bytes > c->mem_limit)
+      throw Error(SCESS_ERR_OOM, "device memory limit of the context reached: " +
+                                     std::to_string(c->mem_held) + " B held + " +
+                                     std::to_string(bytes) + " B requested > " +
+                                     std::to_string(c->mem_limit) + " B");
+  }
   cudaError_t e = cudaMalloc(&p_, bytes);
   if (e == cudaErrorMemoryAllocation && c && c->blocks.bytes() > 0) {
     cudaGetLastError();
-    cudaStreamSynchronize(c->stream);
-    c->blocks.flush();
+    flush_cache(c);
     e = cudaMalloc(&p_, bytes);
   }
   if (e != cudaSuccess) {
@@ -67,12 +100,20 @@ void DevMem::alloc(size_t bytes) {
   }
   bytes_ = bytes;
   owner_ = c;
+  if (c) c->mem_held += bytes;
 }
 
 void DevMem::release() {
   if (p_) {
     Ctx *c = current_ctx();
-    if (!(c && owner_ == c && c->blocks.give(p_, bytes_))) cudaFree(p_);
+    if (c && owner_ == c) {
+      if (!c->blocks.give(p_, bytes_)) {
+        cudaFree(p_);
+        c->mem_held -= std::min(bytes_, c->mem_held);
+      }
+    } else {
+      cudaFree(p_);
+    }
   }
   p_ = nullptr;
   bytes_ = 0;

@@ -26,13 +26,26 @@ class BlockCache {
   static constexpr size_t kMaxCached = size_t(96) << 30;
   void *take(size_t bytes);
   bool give(void *p, size_t bytes);  // false: the caller frees it
-  void flush();
+  size_t flush();  // frees every cached block; returns the bytes freed
   size_t bytes() const { return total_; }
 
  private:
   std::multimap<size_t, void *> free_;
   size_t total_ = 0;
 };
+
+// Internal tuning switches, for tests and tuning runs only: the environment
+// variable SCESS_TUNE holds "key=value" pairs separated by commas, read at
+// every call.  Keys: t_nb (virtual block size of (T), both forms; default: the
+// size chosen from o and v), t_kbd (K blocks of 64 per TMEM drain in the
+// mixed (T) launch: 1, 2 or 4) and t_wbuf (W buffers of the mixed (T): 3 or 1).
+// Returns `def` for an unset key.
+int64_t tune_value(const char *key, int64_t def);
+// TMEM drain cadence of the mixed (T) launch (K blocks of 64 per drain).
+constexpr int kTriplesKbd = 4;
+// W buffers of the mixed (T): 3 (one per group, plain stores) or 1 (the groups
+// add into one with L2 reductions).
+constexpr int kTriplesWBuffers = 3;
 
 // The context whose API call runs on this thread (null outside calls).
 Ctx *current_ctx();
@@ -210,6 +223,10 @@ struct Ctx {
   KernelTimer timer;
   Tape *tape = nullptr;  // recording target while an adjoint forward pass runs
   BlockCache blocks;     // released large device blocks (see BlockCache)
+  // Device memory held by this context's calls (live blocks and the block
+  // cache) and its cap (0 = none): an allocation beyond the cap fails with
+  // SCESS_ERR_OOM as if the device were full (scess_ctx_set_memory_limit).
+  size_t mem_held = 0, mem_limit = 0;
 
   explicit Ctx(int dev);
   ~Ctx();

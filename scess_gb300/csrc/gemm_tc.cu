@@ -95,6 +95,17 @@ __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
+// Fire-and-forget FP32 reductions into global memory (L2 atomics), 2 or 4
+// consecutive floats at an 8- or 16-byte aligned address.
+__device__ __forceinline__ void red_add_v2(float *p, float a, float b) {
+  asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(a), "f"(b) : "memory");
+}
+__device__ __forceinline__ void red_add_v4(float *p, float a, float b, float c, float d) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(a), "f"(b), "f"(c),
+               "f"(d)
+               : "memory");
+}
+
 // Shared-memory matrix descriptor of a K-major operand whose rows are SWZ
 // bytes (one swizzle span: 128 or 64): 8-row core-matrix groups 8 x SWZ bytes
 // apart (SBO), descriptor version 1 (sm_100 family), layout type 2
@@ -226,7 +237,7 @@ struct TcArgs {
   int split3;        // three hi/lo products (else hi*hi only)
   int kbd;           // K blocks accumulated in one TMEM buffer per drain (1 or 2)
   TcSegArgs seg[4];
-  int64_t cy, cz;    // output offset of problem (y, z, g): y * cy + z * cz + cg[g]
+  int64_t cy[3], cz[3];  // output offset of problem (y, z, g): y * cy[g] + z * cz[g] + cg[g]
   int64_t cg[3];
   const int64_t *rowCg[3], *colCg[3];  // per-group output tables (null: TcOut's)
   int tri[3];                          // group g keeps only the problems with y >= z (ny == nz)
@@ -236,6 +247,8 @@ struct TcArgs {
   float *partial;    // split-K partials (nullptr: direct epilogue)
   int64_t part_stride;
   unsigned *err;
+  long long wait_cycles;  // bound of every pipeline wait (clock64 cycles)
+  int withhold_first;     // diagnostics: the producer never fills its first stage
 };
 
 // Persistent tcgen05 GEMM over work units (problem, 128 x 128 output tile, K range).
@@ -487,7 +500,10 @@ __global__ void __launch_bounds__(TcShape<BN, BK, PAIR>::THREADS, 1)
           const int yb = (int)(S.rowB0[pg] + py * S.rowBy[pg] + pz * S.rowBz[pg]) + tn * BN + boff;
           const int s = g % STAGES;
           const uint32_t ph = (uint32_t)(g / STAGES) & 1u;
-          if (!mbar_wait(&empty[s], ph ^ 1u, a.err, ERR_EMPTY_WAIT)) { ok = false; break; }
+          if (!mbar_wait(&empty[s], ph ^ 1u, a.err, ERR_EMPTY_WAIT, a.wait_cycles)) { ok = false; break; }
+          // diagnostics: the first stage is taken but never filled, so that the
+          // MMA thread's bounded wait on it runs out (nothing is in flight there)
+          if (a.withhold_first && g == 0) continue;
           uint8_t *st = smem + s * SH::STAGE_BYTES;
           const CUtensorMap *mA = &maps.m[S.mapA], *mB = &maps.m[S.mapB];
           // a 32-wide block of a segment in a 64-wide kernel fills half a stage
@@ -551,8 +567,8 @@ __global__ void __launch_bounds__(TcShape<BN, BK, PAIR>::THREADS, 1)
           const uint32_t bph = (uint32_t)(c / NBUF) & 1u;
           const bool first = (kb - kb0) % a.kbd == 0;
           const bool last = (kb - kb0) % a.kbd == a.kbd - 1 || kb == kb1 - 1;
-          if (first && !mbar_wait(&tempty[b], bph ^ 1u, a.err, ERR_EMPTY_WAIT)) { ok = false; break; }
-          if (!mbar_wait(&full[s], ph, a.err, ERR_FULL_WAIT)) { ok = false; break; }
+          if (first && !mbar_wait(&tempty[b], bph ^ 1u, a.err, ERR_EMPTY_WAIT, a.wait_cycles)) { ok = false; break; }
+          if (!mbar_wait(&full[s], ph, a.err, ERR_FULL_WAIT, a.wait_cycles)) { ok = false; break; }
           tc_fence_after();
           const uint32_t st = smem_u32(smem + s * SH::STAGE_BYTES);
           const uint32_t ahi = st, bhi = st + SH::A_BYTES;
@@ -623,7 +639,7 @@ __global__ void __launch_bounds__(TcShape<BN, BK, PAIR>::THREADS, 1)
       if (!a.partial) {
         const int nn = n0 + et;
         const int64_t *colT = a.colCg[pg] ? a.colCg[pg] : out.colC;
-        colH[et] = nn < a.N ? out.baseC + py * a.cy + pz * a.cz + a.cg[pg] + colT[nn] : -1;
+        colH[et] = nn < a.N ? out.baseC + py * a.cy[pg] + pz * a.cz[pg] + a.cg[pg] + colT[nn] : -1;
       }
       // issued now, used after the K loop: their latency hides behind the MMAs
       const int64_t *rowT = a.rowCg[pg] ? a.rowCg[pg] : out.rowC;
@@ -632,7 +648,9 @@ __global__ void __launch_bounds__(TcShape<BN, BK, PAIR>::THREADS, 1)
       // column in aligned quads): TMEM is drained in the 16x256b shape, so that
       // each thread holds column pairs of rows 32 q + 8 s + lane / 4 (s = 0..3)
       // and stores them straight from registers (no staging through shared memory).
-      const bool pc = BN == 256 && a.stvec[pg] && out.fp32 && out.beta == 0.0 && !a.partial;
+      // beta = 1: the unit adds into C with L2 reductions instead of storing
+      const bool accum = out.beta == 1.0;
+      const bool pc = BN == 256 && a.stvec[pg] && out.fp32 && (out.beta == 0.0 || accum) && !a.partial;
       const unsigned errv = *(volatile unsigned *)a.err;
       float acc[HC];
 #pragma unroll
@@ -643,7 +661,7 @@ __global__ void __launch_bounds__(TcShape<BN, BK, PAIR>::THREADS, 1)
         for (int kb = kb0; kb < kb1; kb += a.kbd, c++) {
           const int b = c % NBUF;
           const uint32_t bph = (uint32_t)(c / NBUF) & 1u;
-          if (!mbar_wait(&tfull[b], bph, a.err, ERR_ACCUM_WAIT)) { ok = false; break; }
+          if (!mbar_wait(&tfull[b], bph, a.err, ERR_ACCUM_WAIT, a.wait_cycles)) { ok = false; break; }
           tc_fence_after();
           const uint32_t t0 = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * BN + HC * h);
           // acc[64 L + 4 j + e]: lane 32 q + 16 L + 8 (e / 2) + lane / 4,
@@ -669,7 +687,7 @@ __global__ void __launch_bounds__(TcShape<BN, BK, PAIR>::THREADS, 1)
         for (int kb = kb0; kb < kb1; kb += a.kbd, c++) {
           const int b = c % NBUF;
           const uint32_t bph = (uint32_t)(c / NBUF) & 1u;
-          if (!mbar_wait(&tfull[b], bph, a.err, ERR_ACCUM_WAIT)) { ok = false; break; }
+          if (!mbar_wait(&tfull[b], bph, a.err, ERR_ACCUM_WAIT, a.wait_cycles)) { ok = false; break; }
           tc_fence_after();
           const uint32_t t0 = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * BN + HC * h);
 #pragma unroll
@@ -713,7 +731,11 @@ __global__ void __launch_bounds__(TcShape<BN, BK, PAIR>::THREADS, 1)
             if (ro < 0) continue;
             float *d = C + ro + co0;
             if (co0 >= 0 && co1 == co0 + 1 && ((uintptr_t)d & 7) == 0) {
-              *reinterpret_cast<float2 *>(d) = make_float2(v0, v1);
+              if (accum) red_add_v2(d, v0, v1);
+              else *reinterpret_cast<float2 *>(d) = make_float2(v0, v1);
+            } else if (accum) {
+              if (co0 >= 0) atomicAdd(C + ro + co0, v0);
+              if (co1 >= 0) atomicAdd(C + ro + co1, v1);
             } else {
               if (co0 >= 0) C[ro + co0] = v0;
               if (co1 >= 0) C[ro + co1] = v1;
@@ -723,7 +745,7 @@ __global__ void __launch_bounds__(TcShape<BN, BK, PAIR>::THREADS, 1)
         __syncwarp();  // rowOffS read before the next unit rewrites it
         continue;
       }
-      if (a.stcol[pg] && out.fp32 && out.beta == 0.0 && !a.partial) {
+      if (a.stcol[pg] && out.fp32 && (out.beta == 0.0 || accum) && !a.partial) {
         // Tile staged through shared memory CH columns at a time, then each warp
         // stores its 32 rows with the lanes along the columns: for outputs whose
         // unit-stride index is a column index this writes contiguous runs.
@@ -754,8 +776,14 @@ __global__ void __launch_bounds__(TcShape<BN, BK, PAIR>::THREADS, 1)
                 const float v2 = stage[h][4 * cq + 2][r], v3 = stage[h][4 * cq + 3][r];
                 float *d = C + ro + co;
                 if (((uintptr_t)d & 15) == 0) {
-                  *reinterpret_cast<float4 *>(d) = make_float4(v0, v1, v2, v3);
-                } else {  // (not expected: the host asks for quads only when aligned)
+                  if (accum) red_add_v4(d, v0, v1, v2, v3);
+                  else *reinterpret_cast<float4 *>(d) = make_float4(v0, v1, v2, v3);
+                } else if (accum) {  // (not expected: the host asks for quads only when aligned)
+                  atomicAdd(d, v0);
+                  atomicAdd(d + 1, v1);
+                  atomicAdd(d + 2, v2);
+                  atomicAdd(d + 3, v3);
+                } else {
                   d[0] = v0;
                   d[1] = v1;
                   d[2] = v2;
@@ -773,7 +801,10 @@ __global__ void __launch_bounds__(TcShape<BN, BK, PAIR>::THREADS, 1)
             for (int rr = 0; rr < 32; rr += RSTEP) {
               const int r = 32 * q + rr + rsub;
               const int64_t ro = rowOffS[h][r];
-              if (ro >= 0 && co >= 0) C[ro + co] = stage[h][cl][r];
+              if (ro >= 0 && co >= 0) {
+                if (accum) atomicAdd(C + ro + co, stage[h][cl][r]);
+                else C[ro + co] = stage[h][cl][r];
+              }
             }
           }
         }
@@ -791,9 +822,10 @@ __global__ void __launch_bounds__(TcShape<BN, BK, PAIR>::THREADS, 1)
         continue;
       }
       const double alpha = s_alpha;
-      // beta == 1: fire-and-forget reductions (each element receives exactly one
-      // per launch, so the result is deterministic); beta == 0: plain stores;
-      // otherwise a batched read-modify-write.
+      // beta == 1: fire-and-forget reductions (deterministic when each element
+      // receives one per launch, as in every einsum launch; the (T) launch adds
+      // its three groups into one W, in whatever order they arrive); beta == 0:
+      // plain stores; otherwise a batched read-modify-write.
       if (out.fp32) {
         float *C = (float *)out.C;
         const float fa = s_falpha, fb = (float)out.beta;
@@ -1158,15 +1190,9 @@ CUtensorMap TcEngine::map_of(const Packed &p, int box_rows, int bk) {
   return make_map(p.p(), p.rows_pad, p.Kpad, box_rows, bk, p.fmt);
 }
 
-// K block of the 256-wide kernel: 64 (2 stages), or 32 (4 stages) with
-// SCESS_TC_BK256=32.
-int TcEngine::k_block(int bn) {
-  static const int bk256 = [] {
-    const char *e = std::getenv("SCESS_TC_BK256");
-    return (e && std::atoi(e) == 32) ? 32 : 64;
-  }();
-  return bn == 256 ? bk256 : 64;
-}
+// K block of the kernels: 64 (128-byte rows, SWIZZLE_128B).  (A 256-wide
+// kernel with 32-wide blocks in 4 stages measured 5 % slower.)
+int TcEngine::k_block(int) { return 64; }
 
 namespace {
 
@@ -1185,15 +1211,11 @@ const KernelSetup &kernel_setup() {
                          (int)TcShape<128, 64>::SMEM_BYTES);
     cudaFuncSetAttribute(tc_gemm_kernel<256, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)TcShape<256, 64>::SMEM_BYTES);
-    cudaFuncSetAttribute(tc_gemm_kernel<256, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)TcShape<256, 32>::SMEM_BYTES);
     // The 256-wide kernels' setmaxnreg split assumes they are launched with
     // exactly kLaunchRegs256 registers a thread (3 x 168 = 56 + 2 x 224 per scheduler).
-    cudaFuncAttributes fa, fb, fc;
+    cudaFuncAttributes fa, fc;
     k.wide_ok = cudaFuncGetAttributes(&fa, tc_gemm_kernel<256, 64>) == cudaSuccess &&
-              fa.numRegs == kLaunchRegs256 &&
-              cudaFuncGetAttributes(&fb, tc_gemm_kernel<256, 32>) == cudaSuccess &&
-              fb.numRegs == kLaunchRegs256;
+              fa.numRegs == kLaunchRegs256;
     using SP = TcShape<256, 64, true>;
     if (cudaFuncSetAttribute(tc_gemm_kernel<256, 64, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)SP::SMEM_BYTES) == cudaSuccess &&
@@ -1226,7 +1248,8 @@ const KernelSetup &kernel_setup() {
 bool TcEngine::pair_available() { return kernel_setup().pair_ok; }
 
 void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &out, int nseg,
-                            int splits, float *partial, unsigned *err, cudaStream_t stream) {
+                            int splits, float *partial, unsigned *err, cudaStream_t stream,
+                            const TcWaitDiag &diag) {
   const KernelSetup &ks = kernel_setup();
   const bool wide_ok = ks.wide_ok, pair_ok = ks.pair_ok;
   const int pair_clusters = ks.pair_clusters;
@@ -1300,9 +1323,9 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
   a.f16 = fmt == TcFormat::FP16 ? 1 : 0;
   a.split3 = nseg == 3 ? 1 : 0;
   a.kbd = (ps.kbd == 2 || ps.kbd == 4) ? ps.kbd : 1;
-  a.cy = ps.cy;
-  a.cz = ps.cz;
   for (int q = 0; q < 3; q++) {
+    a.cy[q] = ps.cy[q];
+    a.cz[q] = ps.cz[q];
     a.cg[q] = ps.cg[q];
     a.rowCg[q] = ps.rowC[q];
     a.colCg[q] = ps.colC[q];
@@ -1312,6 +1335,8 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
   a.partial = splits > 1 ? partial : nullptr;
   a.part_stride = ps.M * ps.N;
   a.err = err;
+  a.wait_cycles = diag.wait_cycles;
+  a.withhold_first = diag.withhold_first ? 1 : 0;
   if (splits > 1 && !partial) throw Error(SCESS_ERR_INVALID, "tc_gemm: split-K needs partials");
   TcMaps maps;
   for (int i = 0; i < 6; i++) maps.m[i] = ps.maps[std::min(i, ps.nmaps - 1)];
@@ -1348,12 +1373,8 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
     cfg.numAttrs = 1;
     SCESS_CUDA(cudaLaunchKernelEx(&cfg, tc_gemm_kernel<256, 64, true>, maps, out, a));
   } else if (bn == 256)
-    if (bk == 32)
-      tc_gemm_kernel<256, 32><<<grid, TcShape<256, 32>::THREADS, TcShape<256, 32>::SMEM_BYTES, stream>>>(
-          maps, out, a);
-    else
-      tc_gemm_kernel<256, 64><<<grid, TcShape<256, 64>::THREADS, TcShape<256, 64>::SMEM_BYTES, stream>>>(
-          maps, out, a);
+    tc_gemm_kernel<256, 64><<<grid, TcShape<256, 64>::THREADS, TcShape<256, 64>::SMEM_BYTES, stream>>>(
+        maps, out, a);
   else
     tc_gemm_kernel<128, 64><<<grid, TcShape<128, 64>::THREADS, TcShape<128, 64>::SMEM_BYTES, stream>>>(
         maps, out, a);
@@ -1369,7 +1390,7 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
 void tc_gemm_launch_maps(const CUtensorMap &ma, const CUtensorMap &mb, int64_t Kpad, int64_t rowA0,
                          int64_t M, int64_t rowB0, int64_t N, int bn, TcFormat fmt,
                          const TcOut &out, int nseg, int splits, float *partial, unsigned *err,
-                         cudaStream_t stream) {
+                         cudaStream_t stream, const TcWaitDiag &diag) {
   (void)bn;
   TcProblemSet ps;
   ps.maps[0] = ma;
@@ -1383,7 +1404,7 @@ void tc_gemm_launch_maps(const CUtensorMap &ma, const CUtensorMap &mb, int64_t K
   ps.seg[0].Kpad = Kpad;
   ps.seg[0].rowA0[0] = rowA0;
   ps.seg[0].rowB0[0] = rowB0;
-  tc_gemm_launch_grouped(ps, fmt, out, nseg, splits, partial, err, stream);
+  tc_gemm_launch_grouped(ps, fmt, out, nseg, splits, partial, err, stream, diag);
 }
 
 void TcEngine::gemm_maps(const CUtensorMap &ma, const CUtensorMap &mb, int64_t Kpad, int64_t Kreal,
@@ -1391,15 +1412,20 @@ void TcEngine::gemm_maps(const CUtensorMap &ma, const CUtensorMap &mb, int64_t K
                          int nseg, cudaStream_t stream) {
   TimedScope ts(ctx_.timer, "tc_gemm", 2.0 * M * N * Kreal, 0.0, stream ? stream : ctx_.stream);
   tc_gemm_launch_maps(ma, mb, Kpad, rowA0, M, rowB0, N, tile_n(N), fmt_, out, nseg, 1, nullptr,
-                      err_.as<unsigned>(), stream ? stream : ctx_.stream);
+                      err_.as<unsigned>(), stream ? stream : ctx_.stream, take_diag());
+}
+
+TcWaitDiag TcEngine::take_diag() {
+  TcWaitDiag d = diag_;
+  diag_ = TcWaitDiag();  // one launch only
+  return d;
 }
 
 // ---------------------------------------------------------------------------------------------
 
 TcEngine::TcEngine(Ctx &ctx) : ctx_(ctx) {
-  // SCESS_TC_FORMAT=bf16 selects the unscaled BF16 split (default: scaled FP16).
-  const char *f = std::getenv("SCESS_TC_FORMAT");
-  if (f && std::strcmp(f, "bf16") == 0) fmt_ = TcFormat::BF16;
+  // operands in the scaled FP16 split (the unscaled BF16 split is 32x coarser)
+  fmt_ = TcFormat::FP16;
   err_.alloc(sizeof(unsigned) * 4);
   SCESS_CUDA(cudaMemsetAsync(err_.as<void>(), 0, sizeof(unsigned) * 4, ctx_.stream));
 }
@@ -1410,7 +1436,7 @@ void TcEngine::gemm_grouped(const TcProblemSet &ps, const TcOut &out, double flo
                             const char *name, cudaStream_t stream) {
   TimedScope ts(ctx_.timer, name, flops, 0.0, stream ? stream : ctx_.stream);
   tc_gemm_launch_grouped(ps, fmt_, out, 3, 1, nullptr, err_.as<unsigned>(),
-                         stream ? stream : ctx_.stream);
+                         stream ? stream : ctx_.stream, take_diag());
 }
 
 // GB300's FP64 units run the table GEMM at ~1 TFLOP/s for large tiles and at a
@@ -1578,7 +1604,7 @@ void TcEngine::gemm(const Packed &A, int64_t rowA0, int64_t M, const Packed &B, 
   const int bn = tile_n(N);
   const CUtensorMap ma = map_of(A, TC_BM), mb = map_of(B, bn);
   tc_gemm_launch_maps(ma, mb, A.Kpad, rowA0, M, rowB0, N, bn, fmt_, o, nseg, splits, partial,
-                      err_.as<unsigned>(), ctx_.stream);
+                      err_.as<unsigned>(), ctx_.stream, take_diag());
 }
 
 void TcEngine::clear_cache(const void *owner) {
@@ -1597,6 +1623,22 @@ void TcEngine::check_error() {
     SCESS_CUDA(cudaMemsetAsync(err_.as<void>(), 0, sizeof(unsigned), ctx_.stream));
     throw Error(SCESS_ERR_CUDA, "tensor-core pipeline wait expired (code " + std::to_string(h) + ")");
   }
+}
+
+void TcEngine::table_gemm(const TableGemm &g, const char *name) {
+  const std::string tname = std::string("tc_gemm[") + name + "]";
+  timer_name_ = tname.c_str();
+  pack(g.A + g.baseA, g.rowA, g.M, g.kA, g.K, false, TC_BM, tmpA_);
+  pack(g.B + g.baseB, g.colB, g.N, g.kB, g.K, false, TC_BM, tmpB_);
+  TcOut o;
+  o.C = g.C + g.baseC;
+  o.fp32 = 0;
+  o.rowC = g.rowC;
+  o.colC = g.colC;
+  o.alpha = g.alpha;
+  o.beta = g.beta;
+  gemm(tmpA_, 0, g.M, tmpB_, 0, g.N, o, 3);
+  timer_name_ = nullptr;
 }
 
 void TcEngine::contract(const EinsumPlan &pl, double alpha, const double *A, const double *B,

@@ -53,8 +53,8 @@ struct TcOut {
 // multiplies rows rowA0[g] + y rowAy[g] + z rowAz[g] (+ m) of maps[mapA] with
 // rows rowB0[g] + y rowBy[g] + z rowBz[g] (+ n) of maps[mapB] over Kpad
 // columns, negated when `negate`.  Problem (y, z, g) writes at offset
-// y cy + z cz + cg[g] (plus the tables).  All segments' operand pairs must
-// carry the same scale product (the epilogue unscales once).
+// y cy[g] + z cz[g] + cg[g] (plus the tables).  All segments' operand pairs
+// must carry the same scale product (the epilogue unscales once).
 struct TcSegment {
   int mapA = 0, mapB = 1;
   int64_t Kpad = 0;
@@ -72,7 +72,7 @@ struct TcProblemSet {
   int ny = 1, nz = 1, ng = 1;
   int nseg = 1;
   TcSegment seg[4];
-  int64_t cy = 0, cz = 0;
+  int64_t cy[3] = {0, 0, 0}, cz[3] = {0, 0, 0};
   int64_t cg[3] = {0, 0, 0};
   // K blocks per TMEM drain: 1, 2 or 4 (fewer drains, more products
   // accumulated in TMEM between drains).  A K block is k_block(bn) wide.
@@ -92,11 +92,20 @@ struct TcProblemSet {
   const int64_t *rowC[3] = {nullptr, nullptr, nullptr};
   const int64_t *colC[3] = {nullptr, nullptr, nullptr};
   // group g writes along columns (lanes over columns, through shared memory):
-  // for FP32 outputs with beta = 0 whose unit-stride index is a column index
+  // for FP32 outputs with beta = 0 (stores) or beta = 1 (reductions into C)
+  // whose unit-stride index is a column index
   bool store_by_column[3] = {false, false, false};
   // ... and every aligned quad of columns (4 c .. 4 c + 3) goes to 4 contiguous
   // floats at a 16-byte aligned address (vector stores)
   bool store_quads[3] = {false, false, false};
+};
+
+// Bounds of the kernels' pipeline waits.  The defaults are the production
+// ones; the diagnostics entry point arms a short bound and a withheld first
+// stage for one launch, to exercise the expiry path.
+struct TcWaitDiag {
+  long long wait_cycles = 1ll << 32;
+  bool withhold_first = false;
 };
 
 class TcEngine {
@@ -105,6 +114,11 @@ class TcEngine {
   ~TcEngine();
   // Large enough to pay for packing and a tensor-core launch.
   static bool worth_it(const EinsumPlan &pl);
+  // The FP64 engine's table GEMM (TableGemm: C[baseC + rowC[m] + colC[n]] =
+  // alpha sum_k A[baseA + rowA[m] + kA[k]] B[baseB + colB[n] + kB[k]] + beta C)
+  // on the tensor cores: both operands packed through their tables, split
+  // hi/lo, FP32 accumulation; `name` labels the kernel timer.
+  void table_gemm(const TableGemm &g, const char *name);
   // einsum through the plan's offset tables (see einsum()).
   void contract(const EinsumPlan &pl, double alpha, const double *A, const double *B, double beta,
                 double *C, bool constA, bool constB);
@@ -158,6 +172,12 @@ class TcEngine {
                  int nseg = 3, cudaStream_t stream = nullptr);
   // Device error word set by bounded waits inside the kernels (0 = fine).
   void check_error();
+  // The next launch bounds its waits by wait_cycles and withholds its first
+  // operand stage (its MMA thread's wait then runs out).
+  void arm_wait_expiry(long long wait_cycles) {
+    diag_.wait_cycles = wait_cycles;
+    diag_.withhold_first = true;
+  }
   // Cached packings of constant operands are keyed by device pointer and
   // tagged with the owner that keeps those pointers alive: a resident
   // RccsdState (its address) or 0 for a single C-ABI call.  clear_cache(owner)
@@ -174,14 +194,17 @@ class TcEngine {
   Packed tmpA_, tmpB_;
   DevMem partial_;
   DevMem err_;
+  TcWaitDiag diag_;
+  TcWaitDiag take_diag();
 };
 
 // Raw launchers.
 void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &out, int nseg,
-                            int splits, float *partial, unsigned *err, cudaStream_t stream);
+                            int splits, float *partial, unsigned *err, cudaStream_t stream,
+                            const TcWaitDiag &diag = TcWaitDiag());
 void tc_gemm_launch_maps(const CUtensorMap &ma, const CUtensorMap &mb, int64_t Kpad, int64_t rowA0,
                          int64_t M, int64_t rowB0, int64_t N, int bn, TcFormat fmt,
                          const TcOut &out, int nseg, int splits, float *partial, unsigned *err,
-                         cudaStream_t stream);
+                         cudaStream_t stream, const TcWaitDiag &diag = TcWaitDiag());
 
 }  // namespace scess

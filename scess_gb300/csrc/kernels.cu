@@ -261,6 +261,20 @@ __global__ void tau_kernel(int64_t o, int64_t v, const double *__restrict__ t1,
   }
 }
 
+// dtau = tau(t1_0 + dt1, t2_0 + dt2) - tau(t1_0, t2_0)
+//      = dt2 + dt1(i,a) t1_1(j,b) + t1_0(i,a) dt1(j,b),  t1_1 = t1_0 + dt1
+__global__ void tau_delta_kernel(int64_t o, int64_t v, const double *__restrict__ t1_0,
+                                 const double *__restrict__ dt1, const double *__restrict__ dt2,
+                                 double *__restrict__ dtau) {
+  const int64_t n = o * o * v * v;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e % o, j = (e / o) % o, a = (e / (o * o)) % v, b = e / (o * o * v);
+    const int64_t ia = i + o * a, jb = j + o * b;
+    dtau[e] = dt2[e] + dt1[ia] * (t1_0[jb] + dt1[jb]) + t1_0[ia] * dt1[jb];
+  }
+}
+
 __global__ void denom_kernel(int64_t o, int64_t v, const double *__restrict__ eps,
                              const double *__restrict__ R1, const double *__restrict__ R2,
                              double *__restrict__ t1, double *__restrict__ t2) {
@@ -395,6 +409,12 @@ void permute_add(const PermDesc &d, double alpha, const double *X, double beta, 
 void make_tau(int64_t o, int64_t v, const double *t1, const double *t2, double s, double *tau,
               cudaStream_t stream) {
   tau_kernel<<<grid_for(o * o * v * v), 256, 0, stream>>>(o, v, t1, t2, s, tau);
+  SCESS_CHECK_LAUNCH();
+}
+
+void make_tau_delta(int64_t o, int64_t v, const double *t1_0, const double *dt1,
+                    const double *dt2, double *dtau, cudaStream_t stream) {
+  tau_delta_kernel<<<grid_for(o * o * v * v), 256, 0, stream>>>(o, v, t1_0, dt1, dt2, dtau);
   SCESS_CHECK_LAUNCH();
 }
 

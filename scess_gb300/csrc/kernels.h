@@ -49,6 +49,10 @@ void permute_add(const PermDesc &d, double alpha, const double *X, double beta, 
 // tau(i,j,a,b) = t2(i,j,a,b) + s * t1(i,a) t1(j,b)   (column major o,o,v,v)
 void make_tau(int64_t o, int64_t v, const double *t1, const double *t2, double s, double *tau,
               cudaStream_t stream);
+// dtau = tau(t1_0 + dt1, t2_0 + dt2) - tau(t1_0, t2_0), formed from the changes
+// (dt2 + dt1 (x) t1_1 + t1_0 (x) dt1), not as a difference of two taus
+void make_tau_delta(int64_t o, int64_t v, const double *t1_0, const double *dt1,
+                    const double *dt2, double *dtau, cudaStream_t stream);
 // x[i] = y[i] / d[i] style Jacobi update with on-the-fly denominators:
 // t1(i,a) = R1(i,a) / (e_i - e_a); t2(i,j,a,b) = R2 / (e_i + e_j - e_a - e_b).
 void divide_denominators(int64_t o, int64_t v, const double *eps, const double *R1,

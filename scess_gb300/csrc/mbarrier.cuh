@@ -1,7 +1,7 @@
-// mbarrier and bulk-copy helpers (inline PTX, sm_90+ forms used on sm_103a).
+// mbarrier helpers (inline PTX, sm_90+ forms used on sm_103a).
 //
 // Every wait is bounded: mbar_wait gives up after ~2^32 cycles (about 2 s at
-// 2 GHz) or when the error word is already set, records `code` in the error
+// 2 GHz; a launch may pass a shorter limit) or when the error word is already set, records `code` in the error
 // word and returns false, so that a kernel can stop, let its own copies land
 // (mbar_drain) and return instead of spinning forever.
 #pragma once
@@ -36,17 +36,17 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait: false (and the error word set) after ~2^32 cycles or when
-// another role of the CTA (or another CTA) already gave up.
+// Bounded wait: false (and the error word set) after `limit` cycles (~2^32 by
+// default) or when another role of the CTA (or another CTA) already gave up.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, unsigned *err,
-                                          unsigned code) {
+                                          unsigned code, long long limit = 1ll << 32) {
   if (mbar_try_wait(bar, parity)) return true;
   const long long t0 = clock64();
   for (unsigned spin = 1;; spin++) {
     if (mbar_try_wait(bar, parity)) return true;
     if ((spin & 1023u) == 0) {
       if (*(volatile unsigned *)err) return false;
-      if (clock64() - t0 > (1ll << 32)) {
+      if (clock64() - t0 > limit) {
         atomicCAS(err, 0u, code);
         return false;
       }
@@ -60,22 +60,6 @@ __device__ __forceinline__ void mbar_drain(uint64_t *bar, uint32_t parity) {
   const long long t0 = clock64();
   while (!mbar_try_wait(bar, parity))
     if (clock64() - t0 > (1ll << 32)) return;
-}
-
-// Orders this thread's earlier generic-proxy shared-memory accesses before its
-// later async-proxy (bulk copy) writes.
-__device__ __forceinline__ void fence_proxy_async_smem() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-// Contiguous global -> shared copy of `bytes` (multiple of 16; both addresses
-// 16-byte aligned) that completes `bytes` transactions on `bar`.
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_u32(dst)),
-      "l"((uint64_t)src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
 }
 
 }  // namespace scess

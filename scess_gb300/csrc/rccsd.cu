@@ -143,8 +143,9 @@ void RccsdWork::alloc(int64_t o, int64_t v, bool direct_vvvv) {
 }
 
 void rccsd_residual(Ctx &ctx, const RccsdBlocks &B, const double *amp, const double *t2driver,
-                    Backend be, RccsdWork &w, double *R) {
+                    Backend be, RccsdWork &w, double *R, ResidualList list) {
   const int64_t o = B.o, v = B.v;
+  const bool literal = list == ResidualList::AUTO ? be == Backend::FP64 : list == ResidualList::LITERAL;
   cudaStream_t s = ctx.stream;
   double *a = const_cast<double *>(amp);
   const TV t1 = cm(a, {o, v});
@@ -185,7 +186,7 @@ void rccsd_residual(Ctx &ctx, const RccsdBlocks &B, const double *amp, const dou
   E("kcli,klac->ia", 1.0, B.ovoo, tau, 1.0, R1, true);                               // :138
 
   // T2.  X collects every term the reference wraps in PlusTranspose.
-  if (be == Backend::FP64) {
+  if (literal) {
     E("kibc,ka->abic", -1.0, B.oovv, t1, 0.0, w.tmp_abic.v, true);                   // :144
     permute(ctx, "iacb->abic", 1.0, B.ovvv, 1.0, w.tmp_abic.v);                      // :145
     E("abic,jc->ijab", 1.0, w.tmp_abic.v, t1, 0.0, w.X.v);                           // :147
@@ -232,7 +233,7 @@ void rccsd_residual(Ctx &ctx, const RccsdBlocks &B, const double *amp, const dou
   E("lcki,la->akci", -1.0, w.tmp_lcki.v, t1, 1.0, w.Wvovo.v);                        // :210
 
   E("klij,klab->ijab", 1.0, w.Woooo.v, tau, 1.0, R2);                                // :214
-  if (be == Backend::FP64) {
+  if (literal) {
     permute(ctx, "abcd->abcd", 1.0, B.vvvv, 0.0, w.Wvvvv.v);                         // :178
     E("kdac,kb->abcd", -1.0, B.ovvv, t1, 1.0, w.Wvvvv.v, true);                      // :179
     E("kcbd,ka->abcd", -1.0, B.ovvv, t1, 1.0, w.Wvvvv.v, true);                      // :180
@@ -260,6 +261,103 @@ void rccsd_residual(Ctx &ctx, const RccsdBlocks &B, const double *amp, const dou
     op.v = v;
     ctx.tape->ops.push_back(op);
   }
+}
+
+// ---------------------------------------------------------------------------------------------
+
+void rccsd_residual_delta(Ctx &ctx, const RccsdBlocks &B, const double *amp0, const double *amp1,
+                          const double *damp, const RccsdWork &w0, Backend be, RccsdWork &w,
+                          double *tau1, double *dR) {
+  const int64_t o = B.o, v = B.v, n2 = o * o * v * v;
+  cudaStream_t s = ctx.stream;
+  double *a0 = const_cast<double *>(amp0), *a1 = const_cast<double *>(amp1);
+  double *da = const_cast<double *>(damp);
+  // base (T0), full (T1 = T0 + d) and change (d) of the amplitudes
+  const TV t1_0 = cm(a0, {o, v});
+  const TV t1_1 = cm(a1, {o, v}), t2_1 = cm(a1 + o * v, {o, o, v, v});
+  const TV dt1 = cm(da, {o, v}), dt2 = cm(da + o * v, {o, o, v, v});
+  const TV R1 = cm(dR, {o, v});
+  const TV R2 = cm(dR + o * v, {o, o, v, v});
+  auto E = [&](const char *spec, double alpha, const TV &A, const TV &Bt, double beta,
+               const TV &C, bool cA = false, bool cB = false) {
+    einsum(ctx, spec, alpha, A, Bt, beta, C, be, cA, cB);
+  };
+  // d(A B) = dA B1 + A0 dB for a product of two changing factors
+  auto E2 = [&](const char *spec, double alpha, const TV &dA, const TV &B1, const TV &A0,
+                const TV &dB, double beta, const TV &C) {
+    E(spec, alpha, dA, B1, beta, C);
+    E(spec, alpha, A0, dB, 1.0, C);
+  };
+  make_tau_delta(o, v, t1_0.p, dt1.p, dt2.p, w.tau.p(), s);
+  const TV dtau = w.tau.v;
+  SCESS_CUDA(cudaMemcpyAsync(tau1, w0.tau.p(), n2 * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  axpby(n2, 1.0, dtau.p, 1.0, tau1, s);
+  const TV tau_1 = cm(tau1, {o, o, v, v});
+
+  E("kcld,ilcd->ki", 1.0, B.L_ovov.v, dtau, 0.0, w.Foo.v, true);                     // :111
+  E("kcld,klad->ac", -1.0, B.L_ovov.v, dtau, 0.0, w.Fvv.v, true);                    // :113
+  E("kcld,ld->kc", 1.0, B.L_ovov.v, dt1, 0.0, w.Fov.v, true);                        // :115
+
+  E2("ac,ic->ia", 1.0, w.Fvv.v, t1_1, w0.Fvv.v, dt1, 0.0, R1);                       // :119
+  E2("ki,ka->ia", -1.0, w.Foo.v, t1_1, w0.Foo.v, dt1, 1.0, R1);                      // :121
+  E2("kc,kica->ia", 2.0, w.Fov.v, t2_1, w0.Fov.v, dt2, 1.0, R1);                     // :123
+  E2("kc,ikca->ia", -1.0, w.Fov.v, t2_1, w0.Fov.v, dt2, 1.0, R1);                    // :124
+  E2("kc,ic->ki", 1.0, w.Fov.v, t1_1, w0.Fov.v, dt1, 0.0, w.Fovt1.v);                // :127
+  E2("ki,ka->ia", 1.0, w.Fovt1.v, t1_1, w0.Fovt1.v, dt1, 1.0, R1);                   // :128
+  E("kcai,kc->ia", 2.0, B.ovvo, dt1, 1.0, R1, true);                                 // :131
+  E("kiac,kc->ia", -1.0, B.oovv, dt1, 1.0, R1, true);                                // :132
+  E("kdac,ikcd->ia", 2.0, B.ovvv, dtau, 1.0, R1, true);                              // :134
+  E("kcad,ikcd->ia", -1.0, B.ovvv, dtau, 1.0, R1, true);                             // :135
+  E("lcki,klac->ia", -2.0, B.ovoo, dtau, 1.0, R1, true);                             // :137
+  E("kcli,klac->ia", 1.0, B.ovoo, dtau, 1.0, R1, true);                              // :138
+
+  // T2 (reassociated list; the constant <ij|ab> and driver terms drop out)
+  E("kibc,jc->kibj", 1.0, B.oovv, dt1, 0.0, w.tmp_kibj.v, true);                     // :144-147
+  E("iacb,jc->ijab", 1.0, B.ovvv, dt1, 0.0, w.X.v, true);
+  E2("kibj,ka->ijab", -1.0, w.tmp_kibj.v, t1_1, w0.tmp_kibj.v, dt1, 1.0, w.X.v);
+  E("kcai,jc->akij", 1.0, B.ovvo, dt1, 0.0, w.tmp_akij.v, true);                     // :152-153
+  E2("akij,kb->ijab", -1.0, w.tmp_akij.v, t1_1, w0.tmp_akij.v, dt1, 1.0, w.X.v);     // :155
+  SCESS_CUDA(cudaMemsetAsync(R2.p, 0, n2 * sizeof(double), s));                      // :158-160
+
+  permute(ctx, "ki->ki", 1.0, w.Foo.v, 0.0, w.Loo.v);                                // :163
+  E("lcki,lc->ki", 2.0, B.ovoo, dt1, 1.0, w.Loo.v, true);                            // :164
+  E("kcli,lc->ki", -1.0, B.ovoo, dt1, 1.0, w.Loo.v, true);                           // :165
+  permute(ctx, "ac->ac", 1.0, w.Fvv.v, 0.0, w.Lvv.v);                                // :167
+  E("kdac,kd->ac", 2.0, B.ovvv, dt1, 1.0, w.Lvv.v, true);                            // :168
+  E("kcad,kd->ac", -1.0, B.ovvv, dt1, 1.0, w.Lvv.v, true);                           // :169
+
+  E("lcki,jc->klij", 1.0, B.ovoo, dt1, 0.0, w.Woooo.v, true);                        // :172-173
+  E("kclj,ic->klij", 1.0, B.ovoo, dt1, 1.0, w.Woooo.v, true);                        // :174
+  E("kcld,ijcd->klij", 1.0, B.ovov, dtau, 1.0, w.Woooo.v, true);                     // :175
+
+  E("kcad,id->akic", 1.0, B.ovvv, dt1, 0.0, w.Wvoov.v, true);                        // :183-185
+  E("kcli,la->akic", -1.0, B.ovoo, dt1, 1.0, w.Wvoov.v, true);                       // :186
+  E("ldkc,ilda->akic", -0.5, B.ovov, dt2, 1.0, w.Wvoov.v, true);                     // :188
+  E("lckd,ilad->akic", -0.5, B.ovov, dt2, 1.0, w.Wvoov.v, true);                     // :190
+  E("ldkc,ilad->akic", 1.0, B.ovov, dt2, 1.0, w.Wvoov.v, true);                      // :192
+  E("ldkc,id->lkci", 1.0, B.ovov, dt1, 0.0, w.tmp_lkci.v, true);                     // :195
+  E2("lkci,la->akic", -1.0, w.tmp_lkci.v, t1_1, w0.tmp_lkci.v, dt1, 1.0, w.Wvoov.v); // :196
+
+  E("kdac,id->akci", 1.0, B.ovvv, dt1, 0.0, w.Wvovo.v, true);                        // :200-202
+  E("lcki,la->akci", -1.0, B.ovoo, dt1, 1.0, w.Wvovo.v, true);                       // :203
+  E("lckd,ilda->akci", -0.5, B.ovov, dt2, 1.0, w.Wvovo.v, true);                     // :205
+  E("lckd,id->lcki", 1.0, B.ovov, dt1, 0.0, w.tmp_lcki.v, true);                     // :209
+  E2("lcki,la->akci", -1.0, w.tmp_lcki.v, t1_1, w0.tmp_lcki.v, dt1, 1.0, w.Wvovo.v); // :210
+
+  E2("klij,klab->ijab", 1.0, w.Woooo.v, tau_1, w0.Woooo.v, dtau, 1.0, R2);           // :214
+  // particle ladder with the T1 dressing folded in (as the reassociated list)
+  E("abcd,ijcd->ijab", 1.0, B.vvvv, dtau, 1.0, R2, true);                            // :216
+  E("kcbd,ijcd->kbij", 1.0, B.ovvv, dtau, 0.0, w.Yd.v, true);                        // :179-180
+  // d(t1 Yd) = dt1 Yd0 + t1_1 dYd
+  E("ka,kbij->ijab", -1.0, dt1, w0.Yd.v, 1.0, w.X.v);
+  E("ka,kbij->ijab", -1.0, t1_1, w.Yd.v, 1.0, w.X.v);
+  E2("ac,ijcb->ijab", 1.0, w.Lvv.v, t2_1, w0.Lvv.v, dt2, 1.0, w.X.v);                // :218
+  E2("ki,kjab->ijab", -1.0, w.Loo.v, t2_1, w0.Loo.v, dt2, 1.0, w.X.v);               // :220
+  E2("akic,kjcb->ijab", 2.0, w.Wvoov.v, t2_1, w0.Wvoov.v, dt2, 1.0, w.X.v);          // :223
+  E2("akci,kjcb->ijab", -1.0, w.Wvovo.v, t2_1, w0.Wvovo.v, dt2, 1.0, w.X.v);         // :225
+  E2("akic,kjbc->ijab", -1.0, w.Wvoov.v, t2_1, w0.Wvoov.v, dt2, 1.0, w.X.v);         // :228
+  E2("bkci,kjac->ijab", -1.0, w.Wvovo.v, t2_1, w0.Wvovo.v, dt2, 1.0, w.X.v);         // :231
+  plus_transpose(o, v, 1.0, w.X.p(), R2.p, s);                                       // :147-232
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -382,7 +480,7 @@ void RccsdState::init(const SolveInput &in, const scess_rccsd_options &opts) {
   coefd_.alloc((size_t)(maxv_ + 1) * sizeof(double));
   w_.alloc(o, v, !mixed_);
   have_wvvvv_ = !mixed_;
-  mixed_phase_ = mixed_;
+  phase_ = mixed_ ? Phase::MIXED : Phase::FP64;
   std::memset(&res_, 0, sizeof(res_));
   SCESS_CUDA(cudaEventCreate(&ev0_));
   SCESS_CUDA(cudaEventCreate(&ev1_));
@@ -422,7 +520,7 @@ void RccsdState::reset_history() {
   it_ = 0;
   phase_start_ = 0;
   fp64_iters_ = 0;
-  mixed_phase_ = mixed_;
+  phase_ = mixed_ ? Phase::MIXED : Phase::FP64;
   converged_ = false;
   std::memset(&res_, 0, sizeof(res_));
 }
@@ -446,12 +544,35 @@ bool RccsdState::iterate(int max_steps, const Control &ctl) {
   while (steps < max_steps && it_ < opts_.max_iterations && !converged_) {
     ctl.poll();                                                                       // :346
     SCESS_CUDA(cudaMemcpyAsync(prev_.p(), amp_.p(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    const Backend be = mixed_phase_ ? Backend::MIXED : Backend::FP64;
-    if (be == Backend::FP64 && !have_wvvvv_) {
-      w_.Wvvvv = DTensor({v, v, v, v});
-      have_wvvvv_ = true;
+    const Phase ph = phase_;
+    if (ph == Phase::MIXED) {
+      rccsd_residual(ctx_, B_, amp_.p(), drv_.p(), Backend::MIXED, w_, R_.p());       // :350
+    } else if (ph == Phase::FP64) {
+      if (!have_wvvvv_) {
+        w_.Wvvvv = DTensor({v, v, v, v});
+        have_wvvvv_ = true;
+      }
+      rccsd_residual(ctx_, B_, amp_.p(), drv_.p(), Backend::FP64, w_, R_.p());
+    } else if (ph == Phase::REFINED) {
+      // R = R0 + dR(T0, T - T0)
+      SCESS_CUDA(cudaMemcpyAsync(damp_.p(), amp_.p(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      axpby(n_, -1.0, amp0_.p(), 1.0, damp_.p(), s);
+      rccsd_residual_delta(ctx_, B_, amp0_.p(), amp_.p(), damp_.p(), w0_, Backend::MIXED, w_,
+                           tau1_.p(), R_.p());
+      axpby(n_, 1.0, R0_.p(), 1.0, R_.p(), s);
+    } else {  // BASE, CONFIRM: FP64, the reassociated list, intermediates kept in w0_
+      if (!amp0_.p()) {
+        w0_.alloc(o, v, false);
+        amp0_ = DTensor({n_});
+        R0_ = DTensor({n_});
+        damp_ = DTensor({n_});
+        tau1_ = DTensor({o, o, v, v});
+      }
+      rccsd_residual(ctx_, B_, amp_.p(), drv_.p(), Backend::FP64, w0_, R_.p(),
+                     ResidualList::REASSOCIATED);
+      SCESS_CUDA(cudaMemcpyAsync(amp0_.p(), amp_.p(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      SCESS_CUDA(cudaMemcpyAsync(R0_.p(), R_.p(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, s));
     }
-    rccsd_residual(ctx_, B_, amp_.p(), drv_.p(), be, w_, R_.p());                     // :350
     divide_denominators(o, v, eps_.p(), R_.p(), R_.p() + n1_, t1, t2, s);
 
     // AmplitudeDIIS::Extrapolate(updated, change)                                    :246-274
@@ -495,8 +616,10 @@ bool RccsdState::iterate(int max_steps, const Control &ctl) {
     const double rms = std::sqrt(errdot) / std::sqrt((double)n_);                     // :363
     E_last_ = E;
     if (!std::isfinite(E)) throw Error(SCESS_ERR_INVALID, "non-finite CCSD energy (diverging amplitudes)");
+    static const char *const kTag[] = {"", "   [mixed]", "   [fp64 base]", "   [refined]",
+                                       "   [fp64]"};
     ctx_.logf(1, "   CCSD(%d): E(corr) = %.12g      dE = %.12g      rms(dt) = %.12g%s", it_, E,
-              dE, rms, mixed_phase_ ? "   [mixed]" : "");
+              dE, rms, kTag[(int)ph]);
     if (opts_.history) {
       opts_.history[3 * it_ + 0] = E;
       opts_.history[3 * it_ + 1] = dE;
@@ -509,23 +632,44 @@ bool RccsdState::iterate(int max_steps, const Control &ctl) {
     }
     res_.last_dE = dE;
     res_.last_rms = rms;
-    if (!mixed_phase_) fp64_iters_++;
+    const bool fp64_it = ph == Phase::FP64 || ph == Phase::BASE || ph == Phase::CONFIRM;
+    if (fp64_it) fp64_iters_++;
+    else res_.mixed_iterations++;
     it_++;
     steps++;
     res_.iterations = it_;
-    if (mixed_phase_) {
-      res_.mixed_iterations = it_;
-      if (dE < opts_.mixed_energy_switch && rms < opts_.mixed_amplitude_switch) {
-        // FP64 refinement from the mixed amplitudes with a fresh DIIS subspace
-        mixed_phase_ = false;
-        phase_start_ = it_;
-        order_.clear();
-        gram_.clear();
-        ctx_.logf(1, "Mixed-precision phase done; FP64 refinement");
-      }
-    } else if (dE < opts_.energy_convergence && rms < opts_.amplitude_convergence &&  // :370
-               (!mixed_ || fp64_iters_ >= std::max(1, opts_.refine_sweeps))) {
-      converged_ = true;
+    res_.fp64_iterations = fp64_iters_;
+    const bool meets = dE < opts_.energy_convergence && rms < opts_.amplitude_convergence;  // :370
+    switch (ph) {
+      case Phase::FP64:
+        converged_ = meets;
+        break;
+      case Phase::MIXED:
+        if (dE < opts_.mixed_energy_switch && rms < opts_.mixed_amplitude_switch) {
+          // refinement from the mixed amplitudes with a fresh DIIS subspace
+          phase_ = Phase::BASE;
+          phase_start_ = it_;
+          order_.clear();
+          gram_.clear();
+          ctx_.logf(1, "Mixed-precision phase done; refinement from an FP64 base");
+        }
+        break;
+      case Phase::BASE:
+        phase_ = Phase::REFINED;
+        break;
+      case Phase::REFINED:
+        if (meets) phase_ = Phase::CONFIRM;
+        break;
+      case Phase::CONFIRM:
+        if (meets && fp64_iters_ >= std::max(1, opts_.refine_sweeps)) {
+          converged_ = true;
+        } else {
+          // this FP64 evaluation is the new base (its residual and
+          // intermediates at its input amplitudes are kept)
+          phase_ = Phase::REFINED;
+          ctx_.logf(1, "FP64 check not met; refining from it");
+        }
+        break;
     }
   }
   SCESS_CUDA(cudaEventRecord(ev1_, s));

@@ -38,8 +38,25 @@ struct RccsdWork {
 // reference's contraction list literally; Backend::MIXED evaluates the large
 // contractions on tensor cores and folds the T1 dressing of Wvvvv into the
 // ladder (vvvv tau plus two o^3v^3 contractions), so no v^4 tensor is formed.
+// list: the reference's literal contraction list (AUTO for the FP64 backend:
+// the drop-in path) or the reassociated one (AUTO for the tensor cores; also
+// the FP64 base evaluations of the refined mixed solve, which then write no
+// v^4 tensor).  Both compute the same function.
+enum class ResidualList { AUTO = 0, LITERAL = 1, REASSOCIATED = 2 };
 void rccsd_residual(Ctx &ctx, const RccsdBlocks &B, const double *amp, const double *t2driver,
-                    Backend be, RccsdWork &w, double *R);
+                    Backend be, RccsdWork &w, double *R, ResidualList list = ResidualList::AUTO);
+
+// Change of the residual numerators, dR = R(T0 + d) - R(T0), for the
+// reassociated list: w0 holds that list's intermediates at T0 (from
+// rccsd_residual with the reassociated list, FP64), amp1 = T0 + d and
+// damp = d.  Every product is expanded so that it has a factor of the size of
+// d (A1 B1 - A0 B0 = dA B1 + A0 dB), so the rounding error of the tensor-core
+// contractions scales with |d|, not with |T|: R0 + dR is then as accurate as
+// an FP64 evaluation while |d| stays small.  w receives the changes of the
+// intermediates; tau1 (o^2 v^2) is scratch.
+void rccsd_residual_delta(Ctx &ctx, const RccsdBlocks &B, const double *amp0, const double *amp1,
+                          const double *damp, const RccsdWork &w0, Backend be, RccsdWork &w,
+                          double *tau1, double *dR);
 
 struct SolveInput {
   const double *eps_host = nullptr;     // nmo
@@ -97,8 +114,19 @@ class RccsdState {
   std::deque<int> order_;  // DIIS slots, oldest first
   std::vector<std::vector<double>> gram_;
   double E_last_ = 0.0;
+  // Phases of a solve.  FP64: every iteration in FP64 (the drop-in path).  A
+  // MIXED solve: MIXED (tensor-core residuals) until its switch thresholds;
+  // BASE, one FP64 iteration whose residual R0 and intermediates at its input
+  // amplitudes T0 are kept; REFINED, iterations whose residual is
+  // R0 + dR(T0, T - T0) (rccsd_residual_delta, tensor cores) until the
+  // reference's criteria hold; CONFIRM, an FP64 iteration that must meet
+  // them too, else it becomes the new base and REFINED resumes.
+  enum class Phase { FP64, MIXED, BASE, REFINED, CONFIRM };
+  Phase phase_ = Phase::FP64;
+  RccsdWork w0_;                       // intermediates at the base amplitudes
+  DTensor amp0_, R0_, damp_, tau1_;    // base amplitudes and residual; change; scratch
   int it_ = 0, phase_start_ = 0, fp64_iters_ = 0;
-  bool mixed_phase_ = false, converged_ = false;
+  bool converged_ = false;
   scess_rccsd_result res_{};
   cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
   float last_device_ms_ = 0.0f;

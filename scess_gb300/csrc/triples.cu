@@ -14,11 +14,13 @@
 //
 // FP64 form: DFMA GEMMs straight from the padded FP64 repacks, FP64 W and
 // FP64 energy arithmetic.  MIXED form: the same 12 products regroup into three
-// sets of four K segments that each write their own FP32 buffer once (one
-// grouped tcgen05 launch per block triple, plain stores, no reductions); the
-// operands are packed once per call into FP16 hi/lo rows grouped by block, and
-// the energy kernel sums the three buffers in shared memory, working in FP32
-// per element with FP64 accumulation per triple.
+// sets of four K segments (one grouped tcgen05 launch per block triple) whose
+// epilogues add them into one FP32 W with L2 reductions, so that W (nb^3 o^3
+// floats, 55 MB at o = 20) stays in L2 between the launch and the energy
+// kernel; the operands are packed once per call into FP16 hi/lo rows grouped
+// by block.  The energy kernel reads W once, clears it for the next block
+// triple and works in FP32 per element with denominators formed from the FP64
+// orbital energies in double-float, compensated sums and FP64 per triple.
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -144,40 +146,100 @@ __global__ void to_f32_rows_kernel(const double *__restrict__ x, int64_t rows, i
   }
 }
 
-// Layout of the grouped W buffers and the FP32 copy of S the mixed energy
-// kernel reads: rows of o^2 (i, j) pairs are padded to o2p = o^2 rounded up to
-// a multiple of 4 floats, so that every k row and every o^3 block starts on a
-// 16-byte boundary.  W_g[((y_l nb + z_l) nb + x_l) o3p + i + o j + o2p k] with
+// Layout of the mixed form's W and of the FP32 copy of S its energy kernel
+// reads: rows of o^2 (i, j) pairs are padded to o2p = o^2 rounded up to a
+// multiple of 4 floats, so that every k row and every o^3 block starts on a
+// 16-byte boundary.  W[((a_l nb + b_l) nb + c_l) o3p + i + o j + o2p k] with
 // o3p = o o2p; S as [(a + v b) o2p + i + o j].
 __host__ __device__ inline int64_t pad4(int64_t n) { return (n + 3) & ~int64_t(3); }
 
-// Energy of one block triple from the three grouped W buffers of the
-// tensor-core form: W^{abc}_{ijk} = W0[b,c][a] + W1[a,c][b] + W2[a,b][c], each
-// block of o^3 floats in (i, j, k) order (buffer g holds [y_l][z_l][x_l][o^3]
-// for its roles (x, y, z)).  Threads own (i, j) pairs and walk k: one pass of
-// coalesced loads forms Y = W + V in shared memory, W is recovered as Y - V in
-// the energy loop.  Otherwise as triples_energy_kernel (FP32 per element, FP64
-// per thread sum).
-__global__ void __launch_bounds__(256) triples_energy3_kernel(
-    const float *__restrict__ W, int64_t o, int64_t v, int64_t nb, int64_t A, int64_t Bk,
-    int64_t C, const double *__restrict__ eps, const double *__restrict__ t1,
-    const float *__restrict__ S, double *__restrict__ energies) {
-  const int64_t al = blockIdx.x / (nb * nb), bl = (blockIdx.x / nb) % nb, cl = blockIdx.x % nb;
+// Double-float arithmetic in FP32: two_sum gives s + e == a + b exactly
+// (Knuth's TwoSum, six FP32 operations, no branch).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// Orbits of (i, j, k) under the six orderings, i <= j <= k, for the energy
+// kernel: entry = i | j << 8 | k << 16 | m << 24 with m = 0 (three distinct
+// indices: the six orderings are six elements), 1 (two equal: each element
+// counted twice), 2 (all equal: six times).
+std::vector<uint32_t> orbit_table(int64_t o) {
+  std::vector<uint32_t> t;
+  for (int64_t k = 0; k < o; k++)
+    for (int64_t j = 0; j <= k; j++)
+      for (int64_t i = 0; i <= j; i++) {
+        const uint32_t m = (i == k) ? 2u : ((i == j || j == k) ? 1u : 0u);
+        t.push_back((uint32_t)i | (uint32_t)j << 8 | (uint32_t)k << 16 | m << 24);
+      }
+  return t;
+}
+
+// Energy of one block triple in the mixed form.  W^{abc}_{ijk} is the sum of
+// the grouped launch's three products: NW = 3 buffers written by the groups
+// (W_0[b,c][a], W_1[a,c][b], W_2[a,b][c], as laid out by their tables), or
+// NW = 1 buffer the groups reduced into (W[a,b,c]), which this kernel clears
+// after reading so that it starts at zero for the next block triple.  Each
+// block is o^3 floats in (i, j, k) order, i + o j + o2p k.  One CTA per local
+// triple (a_l, b_l, c_l).
+//
+// Pass 1 (threads own (i, j) pairs and walk k, coalesced loads; the CTA's
+// blocks are first prefetched into L2 in bulk): W and Y = W + V into shared
+// memory, V_ijk = t1_ia (jb|kc) + t1_jb (ia|kc) + t1_kc (ia|jb) (GetV,
+// RCCSD_T.cpp:70-75).
+// Pass 2 (threads own orbits of (i, j, k)): r3 (:152-154) maps the even
+// orderings of an orbit to 3 Y + S_e - 2 S_o and the odd ones to
+// 3 Y + S_o - 2 S_e (S_e, S_o: sums of Y over the even / odd orderings), and
+// the denominator (:155) is the same for the whole orbit, so
+//   sum_orbit W r3(Y) / D = [3 sum W Y + W_e (S_e - 2 S_o) + W_o (S_o - 2 S_e)] / D
+// with W_e, W_o the sums of W over the even / odd orderings: one division per
+// orbit instead of six.  D comes from the FP64 orbital energies without FP64
+// arithmetic per orbit: every energy is split into FP32 hi + lo, the sum is
+// formed in double-float (two_sum) and rounded once.  The orbit sums are
+// compensated (Kahan), the sums over the warp double-float, the CTA's FP64.
+template <int NW>
+__global__ void __launch_bounds__(256) triples_energy_orbit_kernel(
+    float *__restrict__ W, int64_t o, int64_t v, int64_t nb, int64_t A, int64_t Bk, int64_t C,
+    const double *__restrict__ eps, const double *__restrict__ t1, const float *__restrict__ S,
+    const uint32_t *__restrict__ orbits, int norbits, double *__restrict__ energies) {
+  const int al = (int)(blockIdx.x / (nb * nb)), bl = (int)((blockIdx.x / nb) % nb),
+            cl = (int)(blockIdx.x % nb);
   const int64_t a = A * nb + al, b = Bk * nb + bl, c = C * nb + cl;
-  if (a >= v || b >= v || c >= v || b > a || c > b) return;
-  extern __shared__ __align__(16) unsigned char sm_raw[];
-  __shared__ double red[32];
   const int oo = (int)o, o2 = oo * oo;
-  const int64_t o2p = pad4(o2), o3p = oo * o2p;
-  // Y(i,j,k) at i + p1 j + p2 k with odd p1, p2 (conflict-free permuted reads)
+  const int o2p = (int)pad4(o2), o3p = oo * o2p;
+  const int64_t nb3o3 = nb * nb * nb * (int64_t)o3p;
+  const float *Wg[3];
+  if (NW == 3) {
+    Wg[0] = W + ((bl * nb + cl) * nb + al) * (int64_t)o3p;
+    Wg[1] = W + nb3o3 + ((al * nb + cl) * nb + bl) * (int64_t)o3p;
+    Wg[2] = W + 2 * nb3o3 + ((al * nb + bl) * nb + cl) * (int64_t)o3p;
+  } else {
+    Wg[0] = Wg[1] = Wg[2] = W + ((al * nb + bl) * nb + cl) * (int64_t)o3p;
+  }
+  const bool unique = a < v && b < v && c < v && b <= a && c <= b;
+  if (!unique) {
+    if (NW == 1) {  // its block received the launch's sums all the same: clear it
+      float4 *w4 = reinterpret_cast<float4 *>(const_cast<float *>(Wg[0]));
+      for (int e = threadIdx.x; e < o3p / 4; e += blockDim.x) w4[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    return;
+  }
+  if (threadIdx.x < NW) {  // the blocks of this triple into L2 while the tables load
+    const uint32_t bytes = (uint32_t)o3p * 4u;  // a multiple of 16; blocks 16-byte aligned
+    const float *pf = threadIdx.x == 0 ? Wg[0] : (threadIdx.x == 1 ? Wg[1] : Wg[2]);
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(pf), "r"(bytes) : "memory");
+  }
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  __shared__ float red_hi[32], red_lo[32];
+  __shared__ float s_ev[2];
+  // ek[k] = (e_k hi, e_k lo, t1_kc, 0); Y, Ws at i + p1 j + p2 k with odd p1, p2
   const int p1 = oo | 1, p2 = (p1 * oo) | 1;
-  float *Y = reinterpret_cast<float *>(sm_raw);
-  float *Sbc = Y + p2 * oo, *Sac = Sbc + o2, *Sab = Sac + o2;
-  float *ta = Sab + o2, *tb = ta + oo, *tc = tb + oo, *eo = tc + oo;
-  const int64_t nb3o3 = nb * nb * nb * o3p;
-  const float *W0 = W + ((bl * nb + cl) * nb + al) * o3p;
-  const float *W1 = W + nb3o3 + ((al * nb + cl) * nb + bl) * o3p;
-  const float *W2 = W + 2 * nb3o3 + ((al * nb + bl) * nb + cl) * o3p;
+  float4 *ek = reinterpret_cast<float4 *>(sm_raw);
+  float *Y = reinterpret_cast<float *>(ek + oo);
+  float *Ws = Y + p2 * oo;
+  float *Sbc = Ws + p2 * oo, *Sac = Sbc + o2, *Sab = Sac + o2;
+  float *ta = Sab + o2, *tb = ta + oo;
   const float *S_bc = S + (b + v * c) * o2p, *S_ac = S + (a + v * c) * o2p, *S_ab = S + (a + v * b) * o2p;
   for (int e = threadIdx.x; e < o2; e += blockDim.x) {
     Sbc[e] = S_bc[e];
@@ -185,54 +247,97 @@ __global__ void __launch_bounds__(256) triples_energy3_kernel(
     Sab[e] = S_ab[e];
   }
   for (int i = threadIdx.x; i < oo; i += blockDim.x) {
+    const double e = eps[i];
+    const float h = (float)e;
+    ek[i] = make_float4(h, (float)(e - (double)h), (float)t1[i + o * c], 0.f);
     ta[i] = (float)t1[i + o * a];
     tb[i] = (float)t1[i + o * b];
-    tc[i] = (float)t1[i + o * c];
-    eo[i] = (float)eps[i];
+  }
+  if (threadIdx.x == 0) {
+    const double ev = eps[o + a] + eps[o + b] + eps[o + c];
+    const float h = (float)ev;
+    s_ev[0] = h;
+    s_ev[1] = (float)(ev - (double)h);
   }
   __syncthreads();
-  // Y = W0 + W1 + W2 + V;  V_ijk = t1_ia (jb|kc) + t1_jb (ia|kc) + t1_kc (ia|jb)
+  // pass 1: W and Y = W + V (loads only: a store into W between them would
+  // serialise them)
   for (int pr = threadIdx.x; pr < o2; pr += blockDim.x) {
     const int i = pr % oo, j = pr / oo;
     const float tai = ta[i], tbj = tb[j], sab = Sab[pr];
-    float *y = Y + i + p1 * j;
-#pragma unroll 8
+    const int yo = i + p1 * j;
+#pragma unroll 4
     for (int k = 0; k < oo; k++) {
-      const int64_t e = pr + o2p * k;
-      y[p2 * k] = (W0[e] + W1[e]) + W2[e] + tai * Sbc[j + oo * k] + tbj * Sac[i + oo * k] +
-                  tc[k] * sab;
+      const int e = pr + o2p * k;
+      float w = Wg[0][e];
+      if (NW == 3) w += Wg[1][e] + Wg[2][e];
+      Ws[yo + p2 * k] = w;
+      Y[yo + p2 * k] = w + (tai * Sbc[j + oo * k] + tbj * Sac[i + oo * k] + ek[k].z * sab);
     }
   }
   __syncthreads();
-  const float evirt = (float)(eps[o + a] + eps[o + b] + eps[o + c]);
-  double acc = 0.0;
-  for (int pr = threadIdx.x; pr < o2; pr += blockDim.x) {
-    const int i = pr % oo, j = pr / oo;
-    const float tai = ta[i], tbj = tb[j], sab = Sab[pr], eij = eo[i] + eo[j];
-    float part = 0.0f;
-#pragma unroll 2
-    for (int k = 0; k < oo; k++) {
-      const float y = Y[i + p1 * j + p2 * k];
-      // r3(Y) = 4 Y_ijk + Y_kij + Y_jki - 2 Y_kji - 2 Y_ikj - 2 Y_jik           :152-154
-      const float r3 = 4.0f * y + Y[k + p1 * i + p2 * j] + Y[j + p1 * k + p2 * i] -
-                       2.0f * (Y[k + p1 * j + p2 * i] + Y[i + p1 * k + p2 * j] + Y[j + p1 * i + p2 * k]);
-      const float wv = y - (tai * Sbc[j + oo * k] + tbj * Sac[i + oo * k] + tc[k] * sab);
-      const float d = (eij + eo[k]) - evirt;                                       // :155
-      part += __fdividef(wv * r3, d);                                               // :156
-    }
-    acc += (double)part;
+  if (NW == 1) {  // the block of W is read: clear it for the next block triple's reductions
+    float4 *w4 = reinterpret_cast<float4 *>(const_cast<float *>(Wg[0]));
+    for (int e = threadIdx.x; e < o3p / 4; e += blockDim.x) w4[e] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
-  for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+  // pass 2: orbits
+  const float evh = s_ev[0], evl = s_ev[1];
+  float sum = 0.0f, comp = 0.0f;
+  for (int q = threadIdx.x; q < norbits; q += blockDim.x) {
+    const uint32_t code = __ldg(orbits + q);
+    const int i = code & 255, j = (code >> 8) & 255, k = (code >> 16) & 255;
+    const int m = code >> 24;
+    // even orderings ijk, jki, kij; odd ikj, kji, jik
+    const int xe0 = i + p1 * j + p2 * k, xe1 = j + p1 * k + p2 * i, xe2 = k + p1 * i + p2 * j;
+    const int xo0 = i + p1 * k + p2 * j, xo1 = k + p1 * j + p2 * i, xo2 = j + p1 * i + p2 * k;
+    const float ye0 = Y[xe0], ye1 = Y[xe1], ye2 = Y[xe2], yo0 = Y[xo0], yo1 = Y[xo1], yo2 = Y[xo2];
+    const float we0 = Ws[xe0], we1 = Ws[xe1], we2 = Ws[xe2], wo0 = Ws[xo0], wo1 = Ws[xo1], wo2 = Ws[xo2];
+    const float Se = (ye0 + ye1) + ye2, So = (yo0 + yo1) + yo2;
+    const float We = (we0 + we1) + we2, Wo = (wo0 + wo1) + wo2;
+    float wy = we0 * ye0;
+    wy = fmaf(we1, ye1, wy);
+    wy = fmaf(we2, ye2, wy);
+    wy = fmaf(wo0, yo0, wy);
+    wy = fmaf(wo1, yo1, wy);
+    wy = fmaf(wo2, yo2, wy);
+    float num = fmaf(We, Se - 2.0f * So, 3.0f * wy);                               // :152-156
+    num = fmaf(Wo, So - 2.0f * Se, num);
+    // D = e_i + e_j + e_k - (e_a + e_b + e_c) in double-float, rounded once   :155
+    const float4 ei = ek[i], ej = ek[j], ekk = ek[k];
+    float s1, e1, s2, e2, s3, e3;
+    two_sum(ei.x, ej.x, s1, e1);
+    two_sum(s1, ekk.x, s2, e2);
+    two_sum(s2, -evh, s3, e3);
+    const float d = s3 + (((e1 + e2) + e3) + (((ei.y + ej.y) + ekk.y) - evl));
+    const float mult = m == 0 ? 1.0f : (m == 1 ? 0.5f : (1.0f / 6.0f));
+    const float term = __fdividef(num * mult, d) - comp;
+    const float t = sum + term;
+    comp = (t - sum) - term;
+    sum = t;
+  }
+  // warp sums in double-float, the CTA's in FP64
+  float acc_hi = sum, acc_lo = -comp;
+  for (int off = 16; off > 0; off >>= 1) {
+    const float oh = __shfl_down_sync(0xffffffffu, acc_hi, off);
+    const float ol = __shfl_down_sync(0xffffffffu, acc_lo, off);
+    float h, e;
+    two_sum(acc_hi, oh, h, e);
+    acc_hi = h;
+    acc_lo += e + ol;
+  }
   const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
-  if (lane == 0) red[wi] = acc;
+  if (lane == 0) {
+    red_hi[wi] = acc_hi;
+    red_lo[wi] = acc_lo;
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double sum = 0.0;
-    for (int q = 0; q < (int)(blockDim.x >> 5); q++) sum += red[q];
+    double total = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) total += (double)red_hi[q] + (double)red_lo[q];
     double deg = 1.0;                                                               // :135-139
     if (a == c) deg = 6.0;
     else if (a == b || b == c) deg = 2.0;
-    energies[triple_id(a, b, c)] = sum / deg;
+    energies[triple_id(a, b, c)] = total / deg;
   }
 }
 
@@ -336,10 +441,8 @@ struct DevTables {
 const int kPerm[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
 
 int choose_nb(int64_t o, int64_t v, size_t welem_bytes, size_t budget) {
-  if (const char *env = std::getenv("SCESS_T_NB")) {  // block size override (tests, tuning)
-    const int nb = std::atoi(env);
-    if (nb >= 1) return (int)std::min<int64_t>(nb, v);
-  }
+  const int64_t forced = tune_value("t_nb", 0);  // block size override (tests, tuning)
+  if (forced >= 1) return (int)std::min<int64_t>(forced, v);
   const double o3 = (double)o * o * o;
   int nb = (int)std::floor(std::cbrt((double)budget / (welem_bytes * o3)));
   nb = std::max(1, std::min<int>(nb, (int)v));
@@ -484,7 +587,9 @@ void TriplesSetup::build(Ctx &ctx, const double *d_eri, const double *d_t2, cons
 // The 12 FP64 GEMMs of block triple U = (A, B, C): W[(a_l,b_l,c_l)][i,j,k] =
 // sum over the six permutations of the raw P.Q - R.t2 product (GetW,
 // RCCSD_T.cpp:62-68), each added at its permuted position (Symmetrise :78-106).
-void w_block_fp64(Ctx &ctx, const TriplesSetup &T, const int64_t U[3], double *W, double *ws) {
+// tc: the same GEMMs on the tensor cores (TcEngine::table_gemm).
+void w_block_fp64(Ctx &ctx, const TriplesSetup &T, const int64_t U[3], double *W, double *ws,
+                  bool tc = false) {
   cudaStream_t s = ctx.stream;
   const int64_t o = T.o, v = T.v, nb = T.nb, vp = T.vp, o2 = o * o, o3 = o2 * o;
   for (int p = 0; p < 6; p++) {
@@ -511,7 +616,9 @@ void w_block_fp64(Ctx &ctx, const TriplesSetup &T, const int64_t U[3], double *W
     g.beta = p == 0 ? 0.0 : 1.0;
     g.aUnitM = 1;
     g.bUnitN = 0;
-    {
+    if (tc) {
+      ctx.tensor_cores().table_gemm(g, "triples_w");
+    } else {
       TimedScope ts(ctx.timer, "dgemm_table", 2.0 * g.M * g.N * g.K, 0.0, s);
       dgemm_table(g, ws, s);
     }
@@ -534,8 +641,12 @@ void w_block_fp64(Ctx &ctx, const TriplesSetup &T, const int64_t U[3], double *W
     h.beta = 1.0;
     h.aUnitM = r_swapped(pi) ? 0 : 1;
     h.bUnitN = 0;
-    TimedScope ts(ctx.timer, "dgemm_table", 2.0 * h.M * h.N * h.K, 0.0, s);
-    dgemm_table(h, ws, s);
+    if (tc) {
+      ctx.tensor_cores().table_gemm(h, "triples_w");
+    } else {
+      TimedScope ts(ctx.timer, "dgemm_table", 2.0 * h.M * h.N * h.K, 0.0, s);
+      dgemm_table(h, ws, s);
+    }
   }
 }
 
@@ -663,12 +774,18 @@ __global__ void __launch_bounds__(256) triples_grad_kernel(
 // Transposed GEMMs of w_block_fp64 for block triple U: with G = dE/dW,
 //   gP  += G Q,   gQ  += G^T P,   gR -= G' t2,   gt2 -= G'^T R
 // per permutation, G read through that permutation's W tables.
+// tc: the same GEMMs on the tensor cores (TcEngine::table_gemm).
 void g_block_fp64(Ctx &ctx, const TriplesSetup &T, const int64_t U[3], const double *G, double *gP,
-                  double *gQt, double *gRt, double *gT2p, bool integrals, double *ws) {
+                  double *gQt, double *gRt, double *gT2p, bool integrals, double *ws,
+                  bool tc = false) {
   cudaStream_t s = ctx.stream;
   const int64_t o = T.o, v = T.v, nb = T.nb, vp = T.vp, o2 = o * o, o3 = o2 * o;
   const size_t K0 = T.kOperand;
   auto run = [&](TableGemm &g) {
+    if (tc) {
+      ctx.tensor_cores().table_gemm(g, "triples_vjp");
+      return;
+    }
     TimedScope ts(ctx.timer, "dgemm_table", 2.0 * g.M * g.N * g.K, 0.0, s);
     dgemm_table(g, ws, s);
   };
@@ -718,18 +835,16 @@ void g_block_fp64(Ctx &ctx, const TriplesSetup &T, const int64_t U[3], const dou
 
 // Block size of the grouped tensor-core form: GEMM rows (u, x_l) = o nb fill
 // the 128-row tiles well, the padded virtual range vp = NB nb stays close to v,
-// and the three W buffers (3 nb^3 o^3 floats) stay within 256 MiB; ties go to
-// the larger block (fewer, larger launches).  SCESS_T_NB overrides it.
+// and W (nb^3 o^3 floats per buffer) stays within 64 MiB a buffer; ties go to
+// the larger block (fewer, larger launches).  The tuning key t_nb overrides it.
 int choose_nb_grouped(int64_t o, int64_t v) {
-  if (const char *env = std::getenv("SCESS_T_NB")) {
-    const int nb = std::atoi(env);
-    if (nb >= 1) return (int)std::min<int64_t>(nb, v);
-  }
+  const int64_t forced = tune_value("t_nb", 0);
+  if (forced >= 1) return (int)std::min<int64_t>(forced, v);
   int best = 1;
   double best_score = -1.0;
   const double o3 = (double)o * o * o;
   for (int nb = 1; nb <= std::min<int64_t>(v, 64); nb++) {
-    if (nb > 1 && 3.0 * nb * nb * nb * o3 * 4.0 > double(256 << 20)) break;
+    if (nb > 1 && (double)nb * nb * nb * o3 * 4.0 > double(64 << 20)) break;
     const double rows = (double)o * nb;
     const double effM = rows / (128.0 * std::ceil(rows / 128.0));
     const double vp = (double)ceil_div(v, nb) * nb;
@@ -772,42 +887,55 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   const int64_t ntrip = v * (v + 1) * (v + 2) / 6;
   DTensor energies({std::max<int64_t>(ntrip, 1)});
   SCESS_CUDA(cudaMemsetAsync(energies.p(), 0, energies.size() * sizeof(double), s));
-  // FP64: one W; MIXED: the three grouped buffers W0 | W1 | W2
-  // MIXED rows of (i, j) pairs padded to o2p floats (see pad4)
+  // FP64: W in FP64.  MIXED: W in FP32 with rows of (i, j) pairs padded to o2p
+  // floats (see pad4), either three buffers the groups store into (nw = 3) or
+  // one the groups add into with L2 reductions (nw = 1: zeroed here, cleared
+  // again by every energy launch after it has read it)
+  const int nw = (int)tune_value("t_wbuf", kTriplesWBuffers) == 1 ? 1 : 3;
   const int64_t o2p = pad4(o2), o3p = o * o2p;
-  const size_t wbytes = (size_t)nb * nb * nb * (mixed ? 3 * 4 * o3p : 8 * o3);
+  const size_t wbytes = (size_t)nb * nb * nb * (mixed ? 4 * nw * o3p : 8 * o3);
   DevMem W(wbytes);
+  if (mixed && nw == 1) SCESS_CUDA(cudaMemsetAsync(W.as<void>(), 0, wbytes, s));
   const int64_t p1 = o | 1, p2 = (p1 * o) | 1;
-  const size_t ysmem = (size_t)(p2 * o + 3 * o2 + 4 * o) * (mixed ? 4 : 8);
+  const size_t ysmem = mixed ? (size_t)(4 * o + 2 * p2 * o + 3 * o2 + 2 * o) * 4
+                             : (size_t)(p2 * o + 3 * o2 + 4 * o) * 8;
   if (ysmem > 200 * 1024) throw Error(SCESS_ERR_UNSUPPORTED, "(T): o^3 too large for one CTA");
+  if (o > 255) throw Error(SCESS_ERR_UNSUPPORTED, "(T): more than 255 occupied orbitals");
+  DevMem orbits;
+  int norbits = 0;
   if (mixed) {
-    SCESS_CUDA(cudaFuncSetAttribute(triples_energy3_kernel,
+    SCESS_CUDA(cudaFuncSetAttribute(nw == 1 ? triples_energy_orbit_kernel<1> : triples_energy_orbit_kernel<3>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ysmem));
+    const std::vector<uint32_t> ot = orbit_table(o);
+    norbits = (int)ot.size();
+    orbits.alloc(ot.size() * sizeof(uint32_t));
+    SCESS_CUDA(cudaMemcpyAsync(orbits.as<void>(), ot.data(), ot.size() * sizeof(uint32_t),
+                               cudaMemcpyHostToDevice, s));
+    ctx.sync();  // (ot is a host vector of this scope)
   } else {
     SCESS_CUDA(cudaFuncSetAttribute(triples_energy_kernel<double, double>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ysmem));
   }
 
-  // MIXED: the 12 GEMMs of a block triple regroup into three problems sets that
-  // write disjoint buffers.  Group g has the roles (x, y, z) = (a, b, c),
-  // (b, a, c), (c, a, b) and, for each (y_l, z_l), the GEMM
+  // MIXED: the 12 GEMMs of a block triple regroup into three problem sets.
+  // Group g has the roles (x, y, z) = (a, b, c), (b, a, c), (c, a, b) and, for
+  // each (y_l, z_l), the GEMM
   //   W_g[(u, x_l), (s, t)] =   sum_f P(u,f,x,y) Q(f,s,t,z) + sum_f P(u,f,x,z) Q(f,t,s,y)
   //                           - sum_m t2(m,u,z,x) R(s,t,m,y) - sum_m t2(m,u,y,x) R(t,s,m,z)
   // where u is x's occupied partner (i, j or k for x = a, b, c) and (s, t) the
   // other two occupied indices in order: the P.Q terms of the permutations
   // that put x's pair on the rows and the R.t2 terms whose t2 carries it (four
-  // K segments of one accumulation).  The operands are packed once per call
-  // into block-grouped FP16 hi/lo rows; the t2 rows are packed negated, and
-  // the A side (P, t2) and the B side (Q, R) each share one scale so that all
-  // segments carry the same scale product.
+  // K segments of one accumulation); W = W_0 + W_1 + W_2, each group adding
+  // its product into W at its (a, b, c, i, j, k) positions.  The operands are
+  // packed once per call into block-grouped FP16 hi/lo rows; the t2 rows are
+  // packed negated, and the A side (P, t2) and the B side (Q, R) each share one
+  // scale so that all segments carry the same scale product.
   Packed pP, pQ, pQ2, pR, pR2, pTx;
-  int tbn = 256;
-  if (const char *env = std::getenv("SCESS_T_BN")) tbn = std::atoi(env) == 128 ? 128 : 256;
+  const int tbn = 256;
   const int tbk = TcEngine::k_block(tbn);
-  // 256 x 256 units on cluster pairs of SMs (each SM stages half of B): the
-  // default of the 256 x 64 kernel; SCESS_T_PAIR=0 keeps one SM per 128 x 256 unit
-  bool tpair = tbn == 256 && tbk == 64 && TcEngine::pair_available();
-  if (const char *env = std::getenv("SCESS_T_PAIR")) tpair = tpair && std::atoi(env) != 0;
+  // 256 x 256 units on cluster pairs of SMs (each SM stages half of B) where
+  // the device runs the pair kernel, else one SM per 128 x 256 unit
+  const bool tpair = TcEngine::pair_available();
   const int bbox = tpair ? 128 : tbn;  // B rows staged per CTA
   // K block of the t2.R segments (K = o): 32 in the 64-wide kernel when o <= 32
   // (half-filled stages instead of mostly-padding 64-wide ones)
@@ -858,13 +986,19 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
     mR = TcEngine::map_of(pR, bbox, rbk);
     mR2 = TcEngine::map_of(pR2, bbox, rbk);
     mTx = TcEngine::map_of(pTx, 128, rbk);
-    // W_g[(y_l nb + z_l) nb + x_l][i + o j + o2p k]: every group stores its
-    // (u, s, t) in the (i, j, k) order of the triple, so that the energy kernel
-    // reads the three buffers alike.  g = 0: (u,s,t) = (i,j,k); g = 1: (j,i,k);
-    // g = 2: (k,i,j).  Rows (u, x_l), columns (s, t).
-    gdt.build(ctx, {table({{o, 1}, {nb, o3p}}), table({{o, o}, {o, o2p}}),
-               table({{o, o}, {nb, o3p}}), table({{o, 1}, {o, o2p}}),
-               table({{o, o2p}, {nb, o3p}}), table({{o, 1}, {o, o}})});
+    // Every group writes its (u, s, t) at the triple's (i, j, k), i + o j + o2p k.
+    // Rows (u, x_l), columns (s, t): g = 0 (x = a): (u,s,t) = (i,j,k);
+    // g = 1 (x = b): (j,i,k); g = 2 (x = c): (k,i,j).  nw = 3: buffer g holds
+    // W_g[(y_l nb + z_l) nb + x_l]; nw = 1: W[(a_l nb + b_l) nb + c_l], the
+    // (y_l, z_l) strides being the problem offsets cy, cz.
+    if (nw == 3)
+      gdt.build(ctx, {table({{o, 1}, {nb, o3p}}), table({{o, o}, {o, o2p}}),
+                 table({{o, o}, {nb, o3p}}), table({{o, 1}, {o, o2p}}),
+                 table({{o, o2p}, {nb, o3p}}), table({{o, 1}, {o, o}})});
+    else
+      gdt.build(ctx, {table({{o, 1}, {nb, nb * nb * o3p}}), table({{o, o}, {o, o2p}}),
+                 table({{o, o}, {nb, nb * o3p}}), table({{o, 1}, {o, o2p}}),
+                 table({{o, o2p}, {nb, o3p}}), table({{o, 1}, {o, o}})});
     Sf.alloc((size_t)o2p * v * v * sizeof(float));
     to_f32_rows_kernel<<<(unsigned)std::min<int64_t>(ceil_div(o2p * v * v, 256), 16 * kNumSMs), 256, 0, s>>>(
         T.S.p(), v * v, o2, o2p, Sf.as<float>());
@@ -911,20 +1045,23 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
           // TMEM drains per tile.  The FP32 accumulation inside the tensor
           // core truncates, so the error of E_T grows with the products
           // accumulated between drains: measured 1.7e-7 / 4.6e-7 / 1.1e-6
-          // relative to FP64 with a drain per 64 / 128 / 256 K.  One per 256 K
-          // (two per tile at this K) lets a tile's stores overlap the whole
-          // next tile's MMAs (each TMEM buffer then holds half a tile).
-          // SCESS_T_KBD sets the K blocks (of 64) per drain: 1, 2 or 4.
-          ps.kbd = 256 / TcEngine::k_block(tbn);
-          if (const char *env = std::getenv("SCESS_T_KBD")) {
-            const int kb = std::atoi(env);
-            if (kb == 1 || kb == 2 || kb == 4) ps.kbd = kb;
-          }
+          // relative to FP64 with a drain per 64 / 128 / 256 K.
+          ps.kbd = (int)tune_value("t_kbd", kTriplesKbd);
+          if (ps.kbd != 1 && ps.kbd != 2 && ps.kbd != 4) ps.kbd = kTriplesKbd;
           ps.bn = tbn;
           ps.bk = tbk;
           ps.pair = tpair;
-          ps.cy = nb * nb * o3p;
-          ps.cz = nb * o3p;
+          // problem offsets of (y_l, z_l): nw = 3, in the group's own buffer;
+          // nw = 1, in W with g = 0 (y, z) = (b, c), g = 1 (a, c), g = 2 (a, b)
+          for (int g = 0; g < 3; g++) {
+            ps.cy[g] = nb * nb * o3p;
+            ps.cz[g] = nb * o3p;
+          }
+          if (nw == 1) {
+            ps.cy[0] = nb * o3p;      ps.cz[0] = o3p;
+            ps.cy[1] = nb * nb * o3p; ps.cz[1] = o3p;
+            ps.cy[2] = nb * nb * o3p; ps.cz[2] = nb * o3p;
+          }
           const int kRoles[3][3] = {{0, 1, 2}, {1, 0, 2}, {2, 0, 1}};  // (x, y, z) of group g
           const int64_t rp = o * nb * nb, rq = o2 * nb;                 // block strides of the packs
           TcSegment &s0 = ps.seg[0], &s1 = ps.seg[1], &s2 = ps.seg[2], &s3 = ps.seg[3];
@@ -935,7 +1072,7 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
           s2.bk = s3.bk = rbk;
           for (int g = 0; g < 3; g++) {
             const int64_t X = U[kRoles[g][0]], Yb = U[kRoles[g][1]], Z = U[kRoles[g][2]];
-            ps.cg[g] = g * nb * nb * nb * o3p;
+            ps.cg[g] = nw == 3 ? g * nb * nb * nb * o3p : 0;
             s0.rowA0[g] = rp * (Yb + NB * X); s0.rowAy[g] = o * nb;
             s0.rowB0[g] = rq * Z;             s0.rowBz[g] = o2;
             s1.rowA0[g] = rp * (Z + NB * X);  s1.rowAz[g] = o * nb;
@@ -959,14 +1096,14 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
             ps.store_quads[g] = g > 0 && o % 4 == 0;
           }
           out.alpha = 1.0;
-          out.beta = 0.0;
+          out.beta = nw == 1 ? 1.0 : 0.0;  // nw = 1: W += each group's product (L2 reductions)
           TcEngine::set_scales(out, pP, pQ);
           // In a diagonal block triple a group's problems with y_l < z_l feed no
           // unique triple a >= b >= c: g0 (y, z) = (b, c) when B = C, g1 (a, c)
           // when A = C, g2 (a, b) when A = B.
-          ps.tri[0] = tbn == 256 && Bk == C;
-          ps.tri[1] = tbn == 256 && A == C;
-          ps.tri[2] = tbn == 256 && A == Bk;
+          ps.tri[0] = Bk == C;
+          ps.tri[1] = A == C;
+          ps.tri[2] = A == Bk;
           double nprob = 0.0;
           for (int g = 0; g < 3; g++) nprob += ps.tri[g] ? nb * (nb + 1) / 2.0 : (double)nb * nb;
           const double flops = nprob * 2.0 * (double)Mg * Ng * (2.0 * v + 2.0 * o);
@@ -975,10 +1112,16 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
           w_block_fp64(ctx, T, U, W.d(), ws);
         }
         const unsigned nblk = (unsigned)(nb * nb * nb);
-        TimedScope ts(ctx.timer, "triples_energy", 0.0, (double)nblk * o3 * (mixed ? 3 * 4 : 8), s);
-        if (mixed)
-          triples_energy3_kernel<<<nblk, e3threads, ysmem, s>>>(
-              W.as<float>(), o, v, nb, A, Bk, C, d_eps, d_t1, Sf.as<float>(), energies.p());
+        TimedScope ts(ctx.timer, "triples_energy", 0.0,
+                      (double)nblk * o3 * (mixed ? (nw == 1 ? 2 : 3) * 4 : 8), s);
+        if (mixed && nw == 1)
+          triples_energy_orbit_kernel<1><<<nblk, e3threads, ysmem, s>>>(
+              W.as<float>(), o, v, nb, A, Bk, C, d_eps, d_t1, Sf.as<float>(),
+              orbits.as<uint32_t>(), norbits, energies.p());
+        else if (mixed)
+          triples_energy_orbit_kernel<3><<<nblk, e3threads, ysmem, s>>>(
+              W.as<float>(), o, v, nb, A, Bk, C, d_eps, d_t1, Sf.as<float>(),
+              orbits.as<uint32_t>(), norbits, energies.p());
         else
           triples_energy_kernel<double, double><<<nblk, 256, ysmem, s>>>(
               W.d(), o, v, nb, A, Bk, C, d_eps, d_t1, T.S.p(), energies.p());
@@ -999,7 +1142,8 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
 
 double rccsd_triples_vjp(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o,
                          const double *d_eps, const double *d_t1, const double *d_t2, double gE,
-                         const Control &ctl, double *d_gt1, double *d_gt2, double *d_geri) {
+                         const Control &ctl, double *d_gt1, double *d_gt2, double *d_geri,
+                         bool mixed) {
   const int64_t v = nmo - o, N = nmo;
   cudaStream_t s = ctx.stream;
   const int nb = choose_nb(o, v, 8, size_t(64) << 20);  // W and G, nb^3 o^3 FP64 each
@@ -1053,7 +1197,7 @@ double rccsd_triples_vjp(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o,
       for (int64_t C = 0; C <= Bk; C++) {
         if ((blocks_done & 15) == 0) ctl.poll();
         const int64_t U[3] = {A, Bk, C};
-        w_block_fp64(ctx, T, U, W.d(), ws);
+        w_block_fp64(ctx, T, U, W.d(), ws, mixed);
         {
           TimedScope ts(ctx.timer, "triples_grad", 0.0, 0.0, s);
           triples_grad_kernel<<<(unsigned)(nb * nb * nb), 256, gsmem, s>>>(
@@ -1062,12 +1206,13 @@ double rccsd_triples_vjp(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o,
           SCESS_CHECK_LAUNCH();
         }
         g_block_fp64(ctx, T, U, G.d(), integrals ? gP.p() : nullptr, gQt.p(),
-                     integrals ? gRt.p() : nullptr, gT2p.p(), integrals, ws);
+                     integrals ? gRt.p() : nullptr, gT2p.p(), integrals, ws, mixed);
         blocks_done++;
       }
   sum_energies_kernel<<<1, 1024, 0, s>>>(ntrip, energies.p(), ctx.dscalars);
   SCESS_CHECK_LAUNCH();
   SCESS_CUDA(cudaMemcpyAsync(ctx.hscalars, ctx.dscalars, sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (mixed) ctx.tensor_cores().check_error();
 
   // back through the repacks (RCCSD_T.cpp:30-56) into t2 and eri
   const TV g_t2 = cm(d_gt2, {o, o, v, v});

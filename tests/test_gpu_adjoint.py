@@ -86,3 +86,39 @@ def test_vjp_mixed_close_to_fp64(gctx):
     sym = lambda x: 0.5 * (x + x.transpose(1, 0, 3, 2))  # noqa: E731
     assert rel_err(m1, f1) < 1e-5
     assert rel_err(sym(m2), sym(f2)) < 1e-5
+
+
+def test_vjp_central_differences_64_directions_at_o10_v90(gctx):
+    """The residual VJP at the adjoint workload's size (o=10, v=90, nmo=100,
+    naux=300): 64 seeded directions over (t1, t2, B), each block scaled to the
+    rms of what it perturbs, against central differences (step 1e-5) of the
+    FP64 forward from B.  FP64 adjoint: <= 1e-6 relative per direction; the
+    tensor-core adjoint (FP32 accumulation, split operands) is held to its
+    contraction accuracy, <= 1e-5."""
+    o, v = 10, 90
+    w, t1, t2, g1, g2 = _point(o, v)
+    # on the closed-shell subspace t2(ijab) = t2(jiba), where the tensor-core
+    # forward (its Wvvvv dressing uses tau(ijcd) = tau(jidc)) is the same function
+    sym = lambda x: 0.5 * (x + x.transpose(1, 0, 3, 2))  # noqa: E731
+    t2, g2 = sym(t2), sym(g2)
+    B = w.B
+    f64 = gctx.residual_vjp(None, o, t1, t2, g1, g2, B=B, want_integrals=True)
+    mix = gctx.residual_vjp(None, o, t1, t2, g1, g2, B=B, want_integrals=True, precision='mixed')
+    rng = np.random.default_rng(23)
+    h = 1e-5
+    scale = [np.sqrt(np.mean(x ** 2)) for x in (t1, t2, B)]
+    worst = {'fp64': 0.0, 'mixed': 0.0}
+    for _ in range(64):
+        d1, d2, dB = (s * rng.standard_normal(x.shape) for s, x in zip(scale, (t1, t2, B)))
+        d2 = sym(d2)
+        dB = 0.5 * (dB + dB.transpose(0, 2, 1))  # B stays symmetric in (p, q)
+
+        def f(s):
+            r1, r2 = gctx.residual(None, o, t1 + s * d1, t2 + s * d2, B=B + s * dB)
+            return float((r1 * g1).sum() + (r2 * g2).sum())
+        fd = (f(h) - f(-h)) / (2 * h)
+        for name, (gt1, gt2, gB) in (('fp64', f64), ('mixed', mix)):
+            an = float((gt1 * d1).sum() + (gt2 * d2).sum() + (gB * dB).sum())
+            worst[name] = max(worst[name], abs(fd - an) / max(abs(an), 1e-30))
+    assert worst['fp64'] <= 1e-6, worst
+    assert worst['mixed'] <= 1e-5, worst

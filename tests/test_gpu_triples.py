@@ -48,7 +48,7 @@ def test_triples_df_native_multiblock(gctx, monkeypatch, precision, tol):
     """DF input, integrals contracted from B without the nmo^4 eri, several
     block triples with padded virtuals; against the eri route in FP64."""
     from scess_gb300.synthetic import convergent_sigma
-    monkeypatch.setenv('SCESS_T_NB', '7')
+    monkeypatch.setenv('SCESS_TUNE', 't_nb=7')
     o, v = 6, 40
     w = make_workload(o, v, seed=4, with_amplitudes=True, sigma=convergent_sigma(o, v))
     ref = gctx.triples(w.eri(), w.eps, o, w.t1, w.t2, precision='fp64')
@@ -62,7 +62,7 @@ def test_triples_mixed_block_layouts(gctx, monkeypatch, o, v, nb):
     """Several block triples with padded virtuals; odd o (scalar reads of the
     grouped W buffers, padded S rows) and o % 4 == 0 (4-row vector reads)."""
     from scess_gb300.synthetic import convergent_sigma
-    monkeypatch.setenv('SCESS_T_NB', str(nb))
+    monkeypatch.setenv('SCESS_TUNE', f't_nb={nb}')
     w = make_workload(o, v, seed=6, with_amplitudes=True, sigma=convergent_sigma(o, v))
     eri = w.eri()
     em = gctx.triples(eri, w.eps, o, w.t1, w.t2, precision='mixed')

@@ -20,7 +20,7 @@ def _point(o, v, seed=3):
 @pytest.mark.parametrize('o,v,nb,g_e', [(3, 8, None, 1.0), (4, 13, 4, 1.0), (5, 18, 5, -2.5)])
 def test_triples_vjp_matches_autograd(gctx, monkeypatch, o, v, nb, g_e):
     if nb:
-        monkeypatch.setenv('SCESS_T_NB', str(nb))
+        monkeypatch.setenv('SCESS_TUNE', f't_nb={nb}')
     w = _point(o, v)
     eri = w.eri()
     e_ref, r1, r2, re = autodiff.triples_vjp(eri, w.eps, o, w.t1, w.t2)
@@ -32,7 +32,7 @@ def test_triples_vjp_matches_autograd(gctx, monkeypatch, o, v, nb, g_e):
 
 
 def test_triples_vjp_central_differences_64_directions(gctx, monkeypatch):
-    monkeypatch.setenv('SCESS_T_NB', '4')
+    monkeypatch.setenv('SCESS_TUNE', 't_nb=4')
     o, v = 4, 14
     w = _point(o, v, seed=5)
     eri, t1, t2 = w.eri(), w.t1, w.t2
@@ -54,7 +54,7 @@ def test_triples_vjp_central_differences_64_directions(gctx, monkeypatch):
 
 
 def test_triples_vjp_df_factors_match_autograd(gctx, monkeypatch):
-    monkeypatch.setenv('SCESS_T_NB', '4')
+    monkeypatch.setenv('SCESS_TUNE', 't_nb=4')
     o, v = 3, 10
     w = _point(o, v, seed=9)
     B = torch.tensor(w.B, dtype=torch.float64, requires_grad=True)
@@ -77,3 +77,49 @@ def test_triples_vjp_energy_matches_forward(gctx):
     eri = w.eri()
     e, *_ = gctx.triples_vjp(eri, w.eps, o, w.t1, w.t2)
     assert abs(e - gctx.triples(eri, w.eps, o, w.t1, w.t2, precision='fp64')) <= 1e-12 * abs(e)
+
+
+def test_triples_vjp_central_differences_64_directions_at_o10_v90(gctx):
+    """The (T) VJP at the adjoint workload's size (o=10, v=90, DF factors,
+    denominator-scaled amplitudes): 64 seeded directions over (t1, t2, B), each
+    block scaled to the rms of what it perturbs, against central differences
+    (step 1e-5) of the GPU's FP64 (T) from B: <= 1e-6 relative per direction for
+    the FP64 adjoint, <= 1e-5 for the tensor-core adjoint (FP32 accumulation)."""
+    o, v = 10, 90
+    w = _point(o, v, seed=4)
+    t1, t2, B = w.t1, w.t2, w.B
+    grads = {p: gctx.triples_vjp(eps=w.eps, nocc=o, t1=t1, t2=t2, B=B, want_integrals=True,
+                                 precision=p)[1:] for p in ('fp64', 'mixed')}
+    rng = np.random.default_rng(29)
+    h = 1e-5
+    worst = {'fp64': 0.0, 'mixed': 0.0}
+    scale = [np.sqrt(np.mean(x ** 2)) for x in (t1, t2, B)]
+    for _ in range(64):
+        d1, d2, dB = (s * rng.standard_normal(x.shape) for s, x in zip(scale, (t1, t2, B)))
+        dB = 0.5 * (dB + dB.transpose(0, 2, 1))
+
+        def f(s):
+            return gctx.triples(None, w.eps, o, t1 + s * d1, t2 + s * d2, B=B + s * dB,
+                                precision='fp64')
+        fd = (f(h) - f(-h)) / (2 * h)
+        for p, (g1, g2, gB) in grads.items():
+            an = float((g1 * d1).sum() + (g2 * d2).sum() + (gB * dB).sum())
+            worst[p] = max(worst[p], abs(fd - an) / max(abs(an), 1e-30))
+    # FP64 adjoint: 1e-6; the tensor-core adjoint (FP32 accumulation): 1e-5
+    assert worst['fp64'] <= 1e-6, worst
+    assert worst['mixed'] <= 1e-5, worst
+
+
+def test_triples_vjp_mixed_matches_fp64(gctx, monkeypatch):
+    """The tensor-core (T) VJP against the FP64 one over several blocks."""
+    monkeypatch.setenv('SCESS_TUNE', 't_nb=4')
+    o, v = 5, 18
+    w = _point(o, v, seed=6)
+    eri = w.eri()
+    ef, f1, f2, fe = gctx.triples_vjp(eri, w.eps, o, w.t1, w.t2, want_integrals=True)
+    em, m1, m2, me = gctx.triples_vjp(eri, w.eps, o, w.t1, w.t2, want_integrals=True,
+                                      precision='mixed')
+    assert abs(em - ef) <= 1e-6 * abs(ef)
+    assert rel_err(m1, f1) < 1e-5
+    assert rel_err(m2, f2) < 1e-5
+    assert rel_err(me, fe) < 1e-5

@@ -39,7 +39,7 @@ def test_fixture_symmetry():
 
 
 def test_flop_formulas():
-    # SURVEY/BASELINE figures for the algorithmic work
+    # published algorithmic-work figures of the closed-shell path (FLOPs per CCSD iteration, per (T))
     assert abs(oracle.ccsd_flops(10, 90) / 2.91e10 - 1) < 5e-3
     assert abs(oracle.ccsd_flops(20, 180) / 1.735e12 - 1) < 5e-3
     assert abs(oracle.triples_flops(10, 90) / 1.51e11 - 1) < 5e-3

@@ -6,10 +6,10 @@ fixed arena at start-up and forbids allocations afterwards.  They pass their
 own device buffers; the library's only scratch is a fixed 16 MiB array shared
 by all calls.
 
-The GPU test compares it with scess_einsum (FP64), within the 1e-13 relative
-tolerance of the other FP64 contraction tests, over calls in a row that reuse
-the array (a split-K case, a different shape with beta != 0, the first case
-again).  The file is named so that pytest collects it last: a run that stops
+The GPU test compares it with scess_einsum (FP64) and with NumPy on the host,
+within the 1e-13 relative tolerance of the other FP64 contraction tests, over
+calls in a row that reuse the array (a split-K case, a different shape with
+beta != 0, the first case again).  The file is named so that pytest collects it last: a run that stops
 at the first failure has then already run every other test.
 """
 import numpy as np
@@ -36,9 +36,15 @@ def _rel_err(x, ref):
     return float(np.max(np.abs(x - ref)) / max(np.max(np.abs(ref)), 1e-300))
 
 
-def test_rejects_before_touching_the_gpu():
+@pytest.fixture(scope='module')
+def lib():
+    from scess_gb300 import build
+    build.build()
+    return cc.load_library()
+
+
+def test_rejects_before_touching_the_gpu(lib):
     """Too-large and malformed requests return at once (no CUDA call: runs on CPU too)."""
-    lib = cc.load_library()
     fake = 1 << 20  # never dereferenced: the checks come first
     # 'i,j->ij' with M + N + K = 1,100,000 + 1 + 1 > 1,048,576
     assert cc.einsum_static('i,j->ij', fake, [1_100_000], fake, [1], fake, [1_100_000, 1]) \
@@ -53,7 +59,7 @@ def test_rejects_before_touching_the_gpu():
 
 
 @pytest.mark.gpu
-def test_matches_scess_einsum_on_consecutive_calls():
+def test_matches_scess_einsum_on_consecutive_calls(lib):
     torch = pytest.importorskip('torch')
     import scess_gb300 as s
     ctx = s.Context(0)
@@ -74,10 +80,29 @@ def test_matches_scess_einsum_on_consecutive_calls():
         torch.cuda.synchronize()
         out = dev[2].cpu().numpy().reshape(sc, order='F')
         assert _rel_err(out, ref) < 1e-13, spec
+        # and against the host: the same kernels behind both entry points could
+        # share a fault
+        host = alpha * np.einsum(spec, A, B) + beta * C0
+        assert _rel_err(out, host) < 1e-13, spec
 
 
 @pytest.mark.gpu
-def test_too_large_leaves_output_untouched():
+def test_rejects_buffers_that_are_not_device_memory(lib):
+    """A host buffer would fault in the kernels: the entry point refuses it
+    before queueing work and leaves the device buffers untouched."""
+    torch = pytest.importorskip('torch')
+    a = np.ones((4, 5))
+    Bd = torch.ones(5 * 3, dtype=torch.float64, device='cuda:0')
+    Cd = torch.full((4 * 3,), 7.0, dtype=torch.float64, device='cuda:0')
+    st = cc.einsum_static('ij,jk->ik', a.ctypes.data, [4, 5], Bd.data_ptr(), [5, 3],
+                          Cd.data_ptr(), [4, 3])
+    assert st == cc.SCESS_ERR_INVALID
+    torch.cuda.synchronize()
+    assert bool((Cd == 7.0).all())
+
+
+@pytest.mark.gpu
+def test_too_large_leaves_output_untouched(lib):
     torch = pytest.importorskip('torch')
     n = 1_100_000
     A = torch.ones(n, dtype=torch.float64, device='cuda:0')
