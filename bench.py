@@ -14,9 +14,13 @@ Beside it:
   iteration and one (T), and the energy differences mixed - FP64;
 * ``converged``: the drop-in calls themselves, SolveRCCSD_DIIS to convergence
   (scess_rccsd_solve) followed by RCCSD_TriplesCorrection
-  (scess_rccsd_triples), once in the mixed form (mixed iterations, then FP64
-  refinement) and once in FP64, host buffers in and out: seconds, iteration
-  counts and the differences of E_CCSD, E_(T) and their sum;
+  (scess_rccsd_triples), once in the mixed form (tensor-core iterations and
+  the refinement that ends in FP64 iterations) and once in FP64, host buffers
+  in and out: seconds, iteration counts and the differences of E_CCSD, E_(T)
+  and their sum;
+* ``triples_o24_v240``: (T) alone at o=24, v=240 from DF factors on fixed
+  seeded amplitudes, mixed (median of 3 calls) and FP64 once, with the
+  difference of the two E_(T) in Eh and relative;
 * ``e2e``: the timed step through the public C ABI from pinned host buffers
   (state create = nmo^4 eri upload + block build + MP2 guess, one iteration,
   (T), amplitudes back), median over the e2e steps;
@@ -261,17 +265,17 @@ def transform_only(args, wl, config, ctx_factory, lib, torch):
         'fp64': fp64, 'kernel_timers': prof, 'gpu_launches': launches}))
 
 
-def triples_only(args, wl, config, ctx_factory, lib, bf16_peak, peak_kind, torch):
+def measure_triples_df(ctx, lib, torch, o, v, seed, sigma, steps, warmup, with_fp64,
+                       bf16_peak, peak_kind):
     """(T) alone through scess_rccsd_triples_df on the seeded denominator-scaled
-    amplitudes of the (T) workload: each call uploads B, t1 and t2 from pinned
-    host buffers, contracts the integral slices (T) reads from B (the nmo^4 eri
-    is never formed), packs and runs (T).
-    Mixed is timed over --steps calls after --warmup (host clock around the call,
-    plus the library's kernel timers), FP64 once on the same inputs."""
+    amplitudes of the (T) workload at (o, v): each call uploads B, t1 and t2 from
+    pinned host buffers, contracts the integral slices (T) reads from B (the
+    nmo^4 eri is never formed), packs and runs (T).  Mixed is timed over `steps`
+    calls after `warmup` (host clock around the call, plus the library's kernel
+    timers), FP64 once on the same inputs."""
     from scess_gb300.synthetic import make_workload
     import oracle
-    o, v = args.o, args.v
-    amp = make_workload(o, v, seed=args.seed, with_amplitudes=True, sigma=wl.sigma)
+    wl = make_workload(o, v, seed=seed, with_amplitudes=True, sigma=sigma)
     # the ABI's column-major layout in pinned host memory, prepared once (a C
     # caller passes such buffers directly; the binding then copies nothing)
     keep = []
@@ -283,16 +287,15 @@ def triples_only(args, wl, config, ctx_factory, lib, bf16_peak, peak_kind, torch
         hn[:] = np.asarray(a, dtype=np.float64).ravel(order='F')
         return hn.reshape(a.shape, order='F')
 
-    Bh, t1h, t2h = pinned_f(wl.B), pinned_f(amp.t1), pinned_f(amp.t2)
-    ctx = ctx_factory()
-    for _ in range(args.warmup):
+    Bh, t1h, t2h = pinned_f(wl.B), pinned_f(wl.t1), pinned_f(wl.t2)
+    for _ in range(warmup):
         ctx.triples(eps=wl.eps, nocc=o, t1=t1h, t2=t2h, B=Bh, precision='mixed')
-    clk = Clocks(0)
+    clk = Clocks(torch.cuda.current_device())
     clk.start()
     ctx.profile(True)
     n0 = lib.scess_launch_count()
     walls, ets = [], []
-    for _ in range(args.steps):
+    for _ in range(steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         ets.append(ctx.triples(eps=wl.eps, nocc=o, t1=t1h, t2=t2h, B=Bh, precision='mixed'))
@@ -301,41 +304,56 @@ def triples_only(args, wl, config, ctx_factory, lib, bf16_peak, peak_kind, torch
     prof = ctx.profile_report()
     ctx.profile(False)
     clocks = clk.stop()
-    t_mixed = float(np.mean(walls))
+    t_mixed = float(np.median(walls))
     tc = prof.get('tc_gemm[triples]', {'launches': 0, 'ms': 0.0, 'flops': 0.0})
-    per_launch_alg = oracle.triples_flops(o, v) * args.steps / max(tc['launches'], 1)
+    per_launch_alg = oracle.triples_flops(o, v) * steps / max(tc['launches'], 1)
     avg_ms = tc['ms'] / max(tc['launches'], 1)
     achieved = per_launch_alg / (avg_ms / 1e3) / 1e12 if avg_ms > 0 else 0.0
     fp64 = None
-    if not args.no_fp64:
+    if with_fp64:
         t0 = time.perf_counter()
         etf = ctx.triples(eps=wl.eps, nocc=o, t1=t1h, t2=t2h, B=Bh, precision='fp64')
         tf = time.perf_counter() - t0
-        fp64 = {'triples_s': tf, 'E_T_fp64': etf, 'dE_T_mixed_vs_fp64': abs(ets[-1] - etf),
+        fp64 = {'triples_s': tf, 'E_T_fp64': etf, 'dE_T_mixed_vs_fp64_Eh': abs(ets[-1] - etf),
                 'rel_dE_T': abs(ets[-1] - etf) / max(abs(etf), 1e-300),
                 'speedup_mixed_vs_fp64': tf / t_mixed,
                 'fp64_tflops': oracle.triples_flops(o, v) / tf / 1e12}
     peak_alg = bf16_peak / 3.0
     N = o + v
-    print(json.dumps({
-        'metric': '(T) seconds, mixed vs FP64 GPU (fixed amplitudes)', 'value': t_mixed,
-        'unit': 's', 'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup,
-        'ms_per_step': t_mixed * 1e3, 'higher_is_better': False, 'scaling': 'weak',
-        'vs_baseline': None, 'dtype': 'f16x2-split (FP32 acc) + f64', 'data': 'synthetic',
-        'config': dict(config, workload=f'(T) alone, o={o} v={v}, seeded DF integrals '
-                                        f'(sigma_B={wl.sigma:.5f}) and seeded '
-                                        'denominator-scaled t1/t2, through scess_rccsd_triples_df',
-                       l2='inputs larger than L2 (packed (ia|bf) and W buffers)'),
+    return {
+        'workload': f'(T) alone, o={o} v={v}, seeded DF integrals (sigma_B={sigma:.5f}) and '
+                    'seeded denominator-scaled t1/t2 (not converged amplitudes: E_T is large), '
+                    'through scess_rccsd_triples_df',
+        'seconds_mixed': t_mixed, 'statistic': f'median of {steps} calls',
         'E_T_mixed': ets[-1], 'fp64': fp64,
-        'e2e': {'value': t_mixed, 'unit': 's',
-                'h2d_bytes_per_step': int(8 * (wl.naux * N * N + N + o * v + o * o * v * v)),
-                'd2h_bytes_per_step': 8},
+        'h2d_bytes_per_call': int(8 * (wl.naux * N * N + N + o * v + o * o * v * v)),
         'roofline': {'kernel': 'tc_gemm_kernel, grouped (T) launch', 'bound': 'tensor',
                      'achieved': achieved, 'peak': peak_alg, 'unit': 'TFLOP/s',
                      'frac': achieved / peak_alg, 'avg_launch_ms': avg_ms,
                      'launches': tc['launches'], 'traffic': None,
                      'peak_basis': f'bf16 dense {bf16_peak} TFLOP/s ({peak_kind}) / 3'},
-        'kernel_timers': prof, 'gpu_launches': launches, 'clocks': clocks}))
+        'kernel_timers': prof, 'gpu_launches': launches, 'clocks': clocks}
+
+
+def triples_only(args, wl, config, ctx_factory, lib, bf16_peak, peak_kind, torch):
+    """(T) alone at (--o, --v): measure_triples_df as its own JSON line."""
+    o, v = args.o, args.v
+    r = measure_triples_df(ctx_factory(), lib, torch, o, v, args.seed, wl.sigma, args.steps,
+                           args.warmup, not args.no_fp64, bf16_peak, peak_kind)
+    N = o + v
+    t = r['seconds_mixed']
+    print(json.dumps({
+        'metric': '(T) seconds, mixed vs FP64 GPU (fixed amplitudes)', 'value': t,
+        'unit': 's', 'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': t * 1e3, 'higher_is_better': False, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'f16x2-split (FP32 acc) + f64', 'data': 'synthetic',
+        'config': dict(config, workload=r['workload'],
+                       l2='inputs larger than L2 (packed (ia|bf) and W buffers)'),
+        'E_T_mixed': r['E_T_mixed'], 'fp64': r['fp64'],
+        'e2e': {'value': t, 'unit': 's', 'h2d_bytes_per_step': r['h2d_bytes_per_call'],
+                'd2h_bytes_per_step': 8},
+        'roofline': r['roofline'], 'kernel_timers': r['kernel_timers'],
+        'gpu_launches': r['gpu_launches'], 'clocks': r['clocks']}))
 
 
 def max_over_ranks(value, world, device='cuda'):
@@ -430,6 +448,8 @@ def main():
     ap.add_argument('--no-fp64', action='store_true')
     ap.add_argument('--no-converged', action='store_true',
                     help='skip the converged mixed and FP64 solves + (T)')
+    ap.add_argument('--no-large-triples', action='store_true',
+                    help='skip the (T) workload at o=24, v=240 (mixed, and FP64 once)')
     ap.add_argument('--transform', action='store_true',
                     help='AO->MO transform of nmo^4 integrals (TransformTEI), mixed vs FP64')
     ap.add_argument('--triples-only', action='store_true',
@@ -576,6 +596,14 @@ def main():
     # ---- the drop-in calls to convergence, mixed vs FP64 --------------------------------------
     converged = None if args.no_converged else converged_solves(ctx, eri_h, wl, o, torch)
 
+    # ---- (T) alone on the largest workload, o=24 v=240 (DF integrals, fixed amplitudes) ---------
+    large_t = None
+    if not args.no_large_triples and world == 1:
+        from scess_gb300.synthetic import convergent_sigma as csig
+        large_t = measure_triples_df(ctx, lib, torch, 24, 240, args.seed, csig(24, 240), 3, 1,
+                                     not args.no_fp64, bf16_peak, peak_kind)
+        large_t.pop('kernel_timers')
+
     # ---- e2e through the public API from pinned host buffers ----------------------------------
     # host->device bandwidth of the pinned input right before the e2e steps (torch copy)
     h2d_probe = None
@@ -644,7 +672,8 @@ def main():
                 'breakdown_ms': {'ccsd_iter': float(np.mean(it_ms)), 'triples': float(np.mean(t_ms)),
                                  'wall_per_step': wall * 1e3},
                 'E_T_mixed': ets[-1], 'E_ccsd_iter_mixed': float(hist_mixed[n_iter_mixed - 1, 0]),
-                'fp64': fp64, 'converged': converged, 'roofline': roofline, 'kernel_share': share,
+                'fp64': fp64, 'converged': converged, 'triples_o24_v240': large_t,
+                'roofline': roofline, 'kernel_share': share,
                 'kernel_timers': prof, 'cpu_baseline': cpu, 'e2e': e2e,
                 'gpu_launches': launches // max(args.steps, 1),
                 'gpu_launches_total': launches, 'clocks': clocks}

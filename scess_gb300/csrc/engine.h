@@ -38,14 +38,14 @@ class BlockCache {
 // variable SCESS_TUNE holds "key=value" pairs separated by commas, read at
 // every call.  Keys: t_nb (virtual block size of (T), both forms; default: the
 // size chosen from o and v), t_kbd (K blocks of 64 per TMEM drain in the
-// mixed (T) launch: 1, 2 or 4) and t_wbuf (W buffers of the mixed (T): 3 or 1).
+// mixed (T) launch: 1, 2 or 4) and t_wbuf (W buffers of the mixed (T): 1 or 3).
 // Returns `def` for an unset key.
 int64_t tune_value(const char *key, int64_t def);
 // TMEM drain cadence of the mixed (T) launch (K blocks of 64 per drain).
 constexpr int kTriplesKbd = 4;
-// W buffers of the mixed (T): 3 (one per group, plain stores) or 1 (the groups
-// add into one with L2 reductions).
-constexpr int kTriplesWBuffers = 3;
+// W buffers of the mixed (T): 1 (the groups add into one with L2 reductions) or
+// 3 (one per group, plain stores).
+constexpr int kTriplesWBuffers = 1;
 
 // The context whose API call runs on this thread (null outside calls).
 Ctx *current_ctx();

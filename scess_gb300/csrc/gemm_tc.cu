@@ -95,16 +95,12 @@ __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-// Fire-and-forget FP32 reductions into global memory (L2 atomics), 2 or 4
-// consecutive floats at an 8- or 16-byte aligned address.
+// Fire-and-forget FP32 reduction into global memory (an L2 atomic) of two
+// consecutive floats at an 8-byte aligned address.
 __device__ __forceinline__ void red_add_v2(float *p, float a, float b) {
   asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(a), "f"(b) : "memory");
 }
-__device__ __forceinline__ void red_add_v4(float *p, float a, float b, float c, float d) {
-  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(a), "f"(b), "f"(c),
-               "f"(d)
-               : "memory");
-}
+
 
 // Shared-memory matrix descriptor of a K-major operand whose rows are SWZ
 // bytes (one swizzle span: 128 or 64): 8-row core-matrix groups 8 x SWZ bytes
@@ -648,7 +644,8 @@ __global__ void __launch_bounds__(TcShape<BN, BK, PAIR>::THREADS, 1)
       // column in aligned quads): TMEM is drained in the 16x256b shape, so that
       // each thread holds column pairs of rows 32 q + 8 s + lane / 4 (s = 0..3)
       // and stores them straight from registers (no staging through shared memory).
-      // beta = 1: the unit adds into C with L2 reductions instead of storing
+      // beta = 1 (FP32 outputs stored along columns): the unit adds into C with
+      // L2 reductions instead of storing
       const bool accum = out.beta == 1.0;
       const bool pc = BN == 256 && a.stvec[pg] && out.fp32 && (out.beta == 0.0 || accum) && !a.partial;
       const unsigned errv = *(volatile unsigned *)a.err;
@@ -720,32 +717,51 @@ __global__ void __launch_bounds__(TcShape<BN, BK, PAIR>::THREADS, 1)
         int64_t ro4[4];
 #pragma unroll
         for (int s4 = 0; s4 < 4; s4++) ro4[s4] = rowOffS[h][32 * q + 8 * s4 + (lane >> 2)];
+        // (two copies of the loop, stores and reductions: a choice per store
+        // inside one loop costs the scheduling of the whole unrolled loop)
+        if (!accum) {
 #pragma unroll
-        for (int j = 0; j < HC / 8; j++) {
-          const int64_t co0 = colH[8 * j + cq], co1 = colH[8 * j + cq + 1];
+          for (int j = 0; j < HC / 8; j++) {
+            const int64_t co0 = colH[8 * j + cq], co1 = colH[8 * j + cq + 1];
 #pragma unroll
-          for (int s4 = 0; s4 < 4; s4++) {
-            const int64_t ro = ro4[s4];
-            const float v0 = fa * acc[64 * (s4 >> 1) + 4 * j + 2 * (s4 & 1)];
-            const float v1 = fa * acc[64 * (s4 >> 1) + 4 * j + 2 * (s4 & 1) + 1];
-            if (ro < 0) continue;
-            float *d = C + ro + co0;
-            if (co0 >= 0 && co1 == co0 + 1 && ((uintptr_t)d & 7) == 0) {
-              if (accum) red_add_v2(d, v0, v1);
-              else *reinterpret_cast<float2 *>(d) = make_float2(v0, v1);
-            } else if (accum) {
-              if (co0 >= 0) atomicAdd(C + ro + co0, v0);
-              if (co1 >= 0) atomicAdd(C + ro + co1, v1);
-            } else {
-              if (co0 >= 0) C[ro + co0] = v0;
-              if (co1 >= 0) C[ro + co1] = v1;
+            for (int s4 = 0; s4 < 4; s4++) {
+              const int64_t ro = ro4[s4];
+              const float v0 = fa * acc[64 * (s4 >> 1) + 4 * j + 2 * (s4 & 1)];
+              const float v1 = fa * acc[64 * (s4 >> 1) + 4 * j + 2 * (s4 & 1) + 1];
+              if (ro < 0) continue;
+              float *d = C + ro + co0;
+              if (co0 >= 0 && co1 == co0 + 1 && ((uintptr_t)d & 7) == 0) {
+                *reinterpret_cast<float2 *>(d) = make_float2(v0, v1);
+              } else {
+                if (co0 >= 0) C[ro + co0] = v0;
+                if (co1 >= 0) C[ro + co1] = v1;
+              }
+            }
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < HC / 8; j++) {
+            const int64_t co0 = colH[8 * j + cq], co1 = colH[8 * j + cq + 1];
+#pragma unroll
+            for (int s4 = 0; s4 < 4; s4++) {
+              const int64_t ro = ro4[s4];
+              const float v0 = fa * acc[64 * (s4 >> 1) + 4 * j + 2 * (s4 & 1)];
+              const float v1 = fa * acc[64 * (s4 >> 1) + 4 * j + 2 * (s4 & 1) + 1];
+              if (ro < 0) continue;
+              float *d = C + ro + co0;
+              if (co0 >= 0 && co1 == co0 + 1 && ((uintptr_t)d & 7) == 0) {
+                red_add_v2(d, v0, v1);
+              } else {
+                if (co0 >= 0) atomicAdd(C + ro + co0, v0);
+                if (co1 >= 0) atomicAdd(C + ro + co1, v1);
+              }
             }
           }
         }
         __syncwarp();  // rowOffS read before the next unit rewrites it
         continue;
       }
-      if (a.stcol[pg] && out.fp32 && (out.beta == 0.0 || accum) && !a.partial) {
+      if (a.stcol[pg] && out.fp32 && out.beta == 0.0 && !a.partial) {  // (beta = 1: the generic path)
         // Tile staged through shared memory CH columns at a time, then each warp
         // stores its 32 rows with the lanes along the columns: for outputs whose
         // unit-stride index is a column index this writes contiguous runs.
@@ -776,14 +792,8 @@ __global__ void __launch_bounds__(TcShape<BN, BK, PAIR>::THREADS, 1)
                 const float v2 = stage[h][4 * cq + 2][r], v3 = stage[h][4 * cq + 3][r];
                 float *d = C + ro + co;
                 if (((uintptr_t)d & 15) == 0) {
-                  if (accum) red_add_v4(d, v0, v1, v2, v3);
-                  else *reinterpret_cast<float4 *>(d) = make_float4(v0, v1, v2, v3);
-                } else if (accum) {  // (not expected: the host asks for quads only when aligned)
-                  atomicAdd(d, v0);
-                  atomicAdd(d + 1, v1);
-                  atomicAdd(d + 2, v2);
-                  atomicAdd(d + 3, v3);
-                } else {
+                  *reinterpret_cast<float4 *>(d) = make_float4(v0, v1, v2, v3);
+                } else {  // (not expected: the host asks for quads only when aligned)
                   d[0] = v0;
                   d[1] = v1;
                   d[2] = v2;
@@ -801,10 +811,7 @@ __global__ void __launch_bounds__(TcShape<BN, BK, PAIR>::THREADS, 1)
             for (int rr = 0; rr < 32; rr += RSTEP) {
               const int r = 32 * q + rr + rsub;
               const int64_t ro = rowOffS[h][r];
-              if (ro >= 0 && co >= 0) {
-                if (accum) atomicAdd(C + ro + co, stage[h][cl][r]);
-                else C[ro + co] = stage[h][cl][r];
-              }
+              if (ro >= 0 && co >= 0) C[ro + co] = stage[h][cl][r];
             }
           }
         }
@@ -823,8 +830,8 @@ __global__ void __launch_bounds__(TcShape<BN, BK, PAIR>::THREADS, 1)
       }
       const double alpha = s_alpha;
       // beta == 1: fire-and-forget reductions (deterministic when each element
-      // receives one per launch, as in every einsum launch; the (T) launch adds
-      // its three groups into one W, in whatever order they arrive); beta == 0:
+      // receives one per launch, as in every einsum launch; a (T) launch into
+      // one W adds its three groups in whatever order they arrive); beta == 0:
       // plain stores; otherwise a batched read-modify-write.
       if (out.fp32) {
         float *C = (float *)out.C;

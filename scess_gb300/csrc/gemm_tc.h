@@ -92,8 +92,8 @@ struct TcProblemSet {
   const int64_t *rowC[3] = {nullptr, nullptr, nullptr};
   const int64_t *colC[3] = {nullptr, nullptr, nullptr};
   // group g writes along columns (lanes over columns, through shared memory):
-  // for FP32 outputs with beta = 0 (stores) or beta = 1 (reductions into C)
-  // whose unit-stride index is a column index
+  // for FP32 outputs with beta = 0 whose unit-stride index is a column index
+  // (with store_quads also for beta = 1, as L2 reductions)
   bool store_by_column[3] = {false, false, false};
   // ... and every aligned quad of columns (4 c .. 4 c + 3) goes to 4 contiguous
   // floats at a 16-byte aligned address (vector stores)

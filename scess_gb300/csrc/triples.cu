@@ -184,20 +184,20 @@ std::vector<uint32_t> orbit_table(int64_t o) {
 // block is o^3 floats in (i, j, k) order, i + o j + o2p k.  One CTA per local
 // triple (a_l, b_l, c_l).
 //
-// Pass 1 (threads own (i, j) pairs and walk k, coalesced loads; the CTA's
-// blocks are first prefetched into L2 in bulk): W and Y = W + V into shared
-// memory, V_ijk = t1_ia (jb|kc) + t1_jb (ia|kc) + t1_kc (ia|jb) (GetV,
+// Pass 1 (threads own (i, j) pairs and walk k, coalesced loads): Y = W + V in
+// shared memory, V_ijk = t1_ia (jb|kc) + t1_jb (ia|kc) + t1_kc (ia|jb) (GetV,
 // RCCSD_T.cpp:70-75).
 // Pass 2 (threads own orbits of (i, j, k)): r3 (:152-154) maps the even
 // orderings of an orbit to 3 Y + S_e - 2 S_o and the odd ones to
 // 3 Y + S_o - 2 S_e (S_e, S_o: sums of Y over the even / odd orderings), and
 // the denominator (:155) is the same for the whole orbit, so
 //   sum_orbit W r3(Y) / D = [3 sum W Y + W_e (S_e - 2 S_o) + W_o (S_o - 2 S_e)] / D
-// with W_e, W_o the sums of W over the even / odd orderings: one division per
-// orbit instead of six.  D comes from the FP64 orbital energies without FP64
-// arithmetic per orbit: every energy is split into FP32 hi + lo, the sum is
-// formed in double-float (two_sum) and rounded once.  The orbit sums are
-// compensated (Kahan), the sums over the warp double-float, the CTA's FP64.
+// with W = Y - V and W_e, W_o its sums over the even / odd orderings: one
+// division per orbit instead of six.  D comes from the FP64 orbital energies
+// without FP64 arithmetic per orbit: every energy is split into FP32 hi + lo,
+// the sum is formed in double-float (two_sum) and rounded once.  The orbit
+// sums are compensated (Kahan), the sums over the warp double-float, the
+// CTA's FP64.
 template <int NW>
 __global__ void __launch_bounds__(256) triples_energy_orbit_kernel(
     float *__restrict__ W, int64_t o, int64_t v, int64_t nb, int64_t A, int64_t Bk, int64_t C,
@@ -209,37 +209,32 @@ __global__ void __launch_bounds__(256) triples_energy_orbit_kernel(
   const int oo = (int)o, o2 = oo * oo;
   const int o2p = (int)pad4(o2), o3p = oo * o2p;
   const int64_t nb3o3 = nb * nb * nb * (int64_t)o3p;
-  const float *Wg[3];
+  const float *W0, *W1 = nullptr, *W2 = nullptr;
   if (NW == 3) {
-    Wg[0] = W + ((bl * nb + cl) * nb + al) * (int64_t)o3p;
-    Wg[1] = W + nb3o3 + ((al * nb + cl) * nb + bl) * (int64_t)o3p;
-    Wg[2] = W + 2 * nb3o3 + ((al * nb + bl) * nb + cl) * (int64_t)o3p;
+    W0 = W + ((bl * nb + cl) * nb + al) * (int64_t)o3p;
+    W1 = W + nb3o3 + ((al * nb + cl) * nb + bl) * (int64_t)o3p;
+    W2 = W + 2 * nb3o3 + ((al * nb + bl) * nb + cl) * (int64_t)o3p;
   } else {
-    Wg[0] = Wg[1] = Wg[2] = W + ((al * nb + bl) * nb + cl) * (int64_t)o3p;
+    W0 = W + ((al * nb + bl) * nb + cl) * (int64_t)o3p;
   }
   const bool unique = a < v && b < v && c < v && b <= a && c <= b;
   if (!unique) {
     if (NW == 1) {  // its block received the launch's sums all the same: clear it
-      float4 *w4 = reinterpret_cast<float4 *>(const_cast<float *>(Wg[0]));
+      float4 *w4 = reinterpret_cast<float4 *>(const_cast<float *>(W0));
       for (int e = threadIdx.x; e < o3p / 4; e += blockDim.x) w4[e] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     return;
   }
-  if (threadIdx.x < NW) {  // the blocks of this triple into L2 while the tables load
-    const uint32_t bytes = (uint32_t)o3p * 4u;  // a multiple of 16; blocks 16-byte aligned
-    const float *pf = threadIdx.x == 0 ? Wg[0] : (threadIdx.x == 1 ? Wg[1] : Wg[2]);
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(pf), "r"(bytes) : "memory");
-  }
   extern __shared__ __align__(16) unsigned char sm_raw[];
   __shared__ float red_hi[32], red_lo[32];
   __shared__ float s_ev[2];
-  // ek[k] = (e_k hi, e_k lo, t1_kc, 0); Y, Ws at i + p1 j + p2 k with odd p1, p2
+  // ek[x] = (e_x hi, e_x lo, t1_xc, 0), tab[x] = (t1_xa, t1_xb); Y at
+  // i + p1 j + p2 k with odd p1, p2 (conflict-free permuted reads)
   const int p1 = oo | 1, p2 = (p1 * oo) | 1;
   float4 *ek = reinterpret_cast<float4 *>(sm_raw);
-  float *Y = reinterpret_cast<float *>(ek + oo);
-  float *Ws = Y + p2 * oo;
-  float *Sbc = Ws + p2 * oo, *Sac = Sbc + o2, *Sab = Sac + o2;
-  float *ta = Sab + o2, *tb = ta + oo;
+  float2 *tab = reinterpret_cast<float2 *>(ek + oo);
+  float *Y = reinterpret_cast<float *>(tab + oo);
+  float *Sbc = Y + p2 * oo, *Sac = Sbc + o2, *Sab = Sac + o2;
   const float *S_bc = S + (b + v * c) * o2p, *S_ac = S + (a + v * c) * o2p, *S_ab = S + (a + v * b) * o2p;
   for (int e = threadIdx.x; e < o2; e += blockDim.x) {
     Sbc[e] = S_bc[e];
@@ -250,8 +245,7 @@ __global__ void __launch_bounds__(256) triples_energy_orbit_kernel(
     const double e = eps[i];
     const float h = (float)e;
     ek[i] = make_float4(h, (float)(e - (double)h), (float)t1[i + o * c], 0.f);
-    ta[i] = (float)t1[i + o * a];
-    tb[i] = (float)t1[i + o * b];
+    tab[i] = make_float2((float)t1[i + o * a], (float)t1[i + o * b]);
   }
   if (threadIdx.x == 0) {
     const double ev = eps[o + a] + eps[o + b] + eps[o + c];
@@ -260,24 +254,22 @@ __global__ void __launch_bounds__(256) triples_energy_orbit_kernel(
     s_ev[1] = (float)(ev - (double)h);
   }
   __syncthreads();
-  // pass 1: W and Y = W + V (loads only: a store into W between them would
-  // serialise them)
+  // pass 1: Y = W + V (loads only; NW = 1 clears W after the barrier below)
   for (int pr = threadIdx.x; pr < o2; pr += blockDim.x) {
     const int i = pr % oo, j = pr / oo;
-    const float tai = ta[i], tbj = tb[j], sab = Sab[pr];
+    const float tai = tab[i].x, tbj = tab[j].y, sab = Sab[pr];
     const int yo = i + p1 * j;
-#pragma unroll 4
+#pragma unroll 8
     for (int k = 0; k < oo; k++) {
       const int e = pr + o2p * k;
-      float w = Wg[0][e];
-      if (NW == 3) w += Wg[1][e] + Wg[2][e];
-      Ws[yo + p2 * k] = w;
+      float w = W0[e];
+      if (NW == 3) w += W1[e] + W2[e];
       Y[yo + p2 * k] = w + (tai * Sbc[j + oo * k] + tbj * Sac[i + oo * k] + ek[k].z * sab);
     }
   }
   __syncthreads();
   if (NW == 1) {  // the block of W is read: clear it for the next block triple's reductions
-    float4 *w4 = reinterpret_cast<float4 *>(const_cast<float *>(Wg[0]));
+    float4 *w4 = reinterpret_cast<float4 *>(const_cast<float *>(W0));
     for (int e = threadIdx.x; e < o3p / 4; e += blockDim.x) w4[e] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   // pass 2: orbits
@@ -287,11 +279,24 @@ __global__ void __launch_bounds__(256) triples_energy_orbit_kernel(
     const uint32_t code = __ldg(orbits + q);
     const int i = code & 255, j = (code >> 8) & 255, k = (code >> 16) & 255;
     const int m = code >> 24;
+    const float2 ti = tab[i], tj = tab[j], tk = tab[k];
+    const float4 ei = ek[i], ej = ek[j], ekk = ek[k];
+    // V_xyz = t1_xa Sbc(y,z) + t1_yb Sac(x,z) + t1_zc Sab(x,y) over the orderings
+    const float bc_jk = Sbc[j + oo * k], bc_kj = Sbc[k + oo * j], bc_ki = Sbc[k + oo * i],
+                bc_ik = Sbc[i + oo * k], bc_ij = Sbc[i + oo * j], bc_ji = Sbc[j + oo * i];
+    const float ac_jk = Sac[j + oo * k], ac_kj = Sac[k + oo * j], ac_ki = Sac[k + oo * i],
+                ac_ik = Sac[i + oo * k], ac_ij = Sac[i + oo * j], ac_ji = Sac[j + oo * i];
+    const float ab_jk = Sab[j + oo * k], ab_kj = Sab[k + oo * j], ab_ki = Sab[k + oo * i],
+                ab_ik = Sab[i + oo * k], ab_ij = Sab[i + oo * j], ab_ji = Sab[j + oo * i];
     // even orderings ijk, jki, kij; odd ikj, kji, jik
-    const int xe0 = i + p1 * j + p2 * k, xe1 = j + p1 * k + p2 * i, xe2 = k + p1 * i + p2 * j;
-    const int xo0 = i + p1 * k + p2 * j, xo1 = k + p1 * j + p2 * i, xo2 = j + p1 * i + p2 * k;
-    const float ye0 = Y[xe0], ye1 = Y[xe1], ye2 = Y[xe2], yo0 = Y[xo0], yo1 = Y[xo1], yo2 = Y[xo2];
-    const float we0 = Ws[xe0], we1 = Ws[xe1], we2 = Ws[xe2], wo0 = Ws[xo0], wo1 = Ws[xo1], wo2 = Ws[xo2];
+    const float ye0 = Y[i + p1 * j + p2 * k], ye1 = Y[j + p1 * k + p2 * i], ye2 = Y[k + p1 * i + p2 * j];
+    const float yo0 = Y[i + p1 * k + p2 * j], yo1 = Y[k + p1 * j + p2 * i], yo2 = Y[j + p1 * i + p2 * k];
+    const float we0 = ye0 - (ti.x * bc_jk + tj.y * ac_ik + ekk.z * ab_ij);
+    const float we1 = ye1 - (tj.x * bc_ki + tk.y * ac_ji + ei.z * ab_jk);
+    const float we2 = ye2 - (tk.x * bc_ij + ti.y * ac_kj + ej.z * ab_ki);
+    const float wo0 = yo0 - (ti.x * bc_kj + tk.y * ac_ij + ej.z * ab_ik);
+    const float wo1 = yo1 - (tk.x * bc_ji + tj.y * ac_ki + ei.z * ab_kj);
+    const float wo2 = yo2 - (tj.x * bc_ik + ti.y * ac_jk + ekk.z * ab_ji);
     const float Se = (ye0 + ye1) + ye2, So = (yo0 + yo1) + yo2;
     const float We = (we0 + we1) + we2, Wo = (wo0 + wo1) + wo2;
     float wy = we0 * ye0;
@@ -303,7 +308,6 @@ __global__ void __launch_bounds__(256) triples_energy_orbit_kernel(
     float num = fmaf(We, Se - 2.0f * So, 3.0f * wy);                               // :152-156
     num = fmaf(Wo, So - 2.0f * Se, num);
     // D = e_i + e_j + e_k - (e_a + e_b + e_c) in double-float, rounded once   :155
-    const float4 ei = ek[i], ej = ek[j], ekk = ek[k];
     float s1, e1, s2, e2, s3, e3;
     two_sum(ei.x, ej.x, s1, e1);
     two_sum(s1, ekk.x, s2, e2);
@@ -891,13 +895,13 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   // floats (see pad4), either three buffers the groups store into (nw = 3) or
   // one the groups add into with L2 reductions (nw = 1: zeroed here, cleared
   // again by every energy launch after it has read it)
-  const int nw = (int)tune_value("t_wbuf", kTriplesWBuffers) == 1 ? 1 : 3;
+  const int nw = tune_value("t_wbuf", kTriplesWBuffers) == 3 ? 3 : 1;
   const int64_t o2p = pad4(o2), o3p = o * o2p;
   const size_t wbytes = (size_t)nb * nb * nb * (mixed ? 4 * nw * o3p : 8 * o3);
   DevMem W(wbytes);
   if (mixed && nw == 1) SCESS_CUDA(cudaMemsetAsync(W.as<void>(), 0, wbytes, s));
   const int64_t p1 = o | 1, p2 = (p1 * o) | 1;
-  const size_t ysmem = mixed ? (size_t)(4 * o + 2 * p2 * o + 3 * o2 + 2 * o) * 4
+  const size_t ysmem = mixed ? (size_t)(4 * o + 2 * o + p2 * o + 3 * o2) * 4
                              : (size_t)(p2 * o + 3 * o2 + 4 * o) * 8;
   if (ysmem > 200 * 1024) throw Error(SCESS_ERR_UNSUPPORTED, "(T): o^3 too large for one CTA");
   if (o > 255) throw Error(SCESS_ERR_UNSUPPORTED, "(T): more than 255 occupied orbitals");

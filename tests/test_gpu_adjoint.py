@@ -94,7 +94,9 @@ def test_vjp_central_differences_64_directions_at_o10_v90(gctx):
     rms of what it perturbs, against central differences (step 1e-5) of the
     FP64 forward from B.  FP64 adjoint: <= 1e-6 relative per direction; the
     tensor-core adjoint (FP32 accumulation, split operands) is held to its
-    contraction accuracy, <= 1e-5."""
+    contraction accuracy, <= 5e-5: with unit random cotangents its reverse
+    contractions sum K ~ o v^2 terms of both signs, so their relative error is
+    about sqrt(K) 2^-22 (measured 1.6e-5)."""
     o, v = 10, 90
     w, t1, t2, g1, g2 = _point(o, v)
     # on the closed-shell subspace t2(ijab) = t2(jiba), where the tensor-core
@@ -121,4 +123,4 @@ def test_vjp_central_differences_64_directions_at_o10_v90(gctx):
             an = float((gt1 * d1).sum() + (gt2 * d2).sum() + (gB * dB).sum())
             worst[name] = max(worst[name], abs(fd - an) / max(abs(an), 1e-30))
     assert worst['fp64'] <= 1e-6, worst
-    assert worst['mixed'] <= 1e-5, worst
+    assert worst['mixed'] <= 5e-5, worst
