@@ -184,20 +184,22 @@ std::vector<uint32_t> orbit_table(int64_t o) {
 // block is o^3 floats in (i, j, k) order, i + o j + o2p k.  One CTA per local
 // triple (a_l, b_l, c_l).
 //
-// Pass 1 (threads own (i, j) pairs and walk k, coalesced loads): Y = W + V in
-// shared memory, V_ijk = t1_ia (jb|kc) + t1_jb (ia|kc) + t1_kc (ia|jb) (GetV,
-// RCCSD_T.cpp:70-75).
-// Pass 2 (threads own orbits of (i, j, k)): r3 (:152-154) maps the even
-// orderings of an orbit to 3 Y + S_e - 2 S_o and the odd ones to
-// 3 Y + S_o - 2 S_e (S_e, S_o: sums of Y over the even / odd orderings), and
-// the denominator (:155) is the same for the whole orbit, so
-//   sum_orbit W r3(Y) / D = [3 sum W Y + W_e (S_e - 2 S_o) + W_o (S_o - 2 S_e)] / D
-// with W = Y - V and W_e, W_o its sums over the even / odd orderings: one
-// division per orbit instead of six.  D comes from the FP64 orbital energies
-// without FP64 arithmetic per orbit: every energy is split into FP32 hi + lo,
-// the sum is formed in double-float (two_sum) and rounded once.  The orbit
-// sums are compensated (Kahan), the sums over the warp double-float, the
-// CTA's FP64.
+// Pass 1 (threads own (i, j) pairs and walk k; a pair's loads are all issued
+// before any is used): Y = W + V in shared memory, V_ijk = t1_ia (jb|kc) +
+// t1_jb (ia|kc) + t1_kc (ia|jb) (GetV, RCCSD_T.cpp:70-75).
+// Pass 2 (threads own orbits of (i, j, k)): r3 (:152-154) of an even ordering
+// of the orbit is 3 Y + (S_e - 2 S_o), of an odd one 3 Y + (S_o - 2 S_e)
+// (S_e, S_o: sums of Y over the even / odd orderings), and the denominator
+// (:155) is the same for the whole orbit:
+//   sum_orbit W r3(Y) / D = [sum_even W (3 Y + S_e - 2 S_o) + sum_odd W (3 Y + S_o - 2 S_e)] / D,
+// one division per orbit instead of six; r3 is formed per ordering before it
+// multiplies W (it is a small difference of similar Y values), and W = Y - V
+// with V recomputed from the (ia|jb) slices, so that shared memory holds only
+// Y and the slices.  D comes from the FP64 orbital energies without FP64
+// arithmetic per orbit: every energy is split into FP32 hi + lo, the sum is
+// formed in double-float (two_sum) and rounded once.  The orbit sums are
+// compensated (Kahan), the sums over the warp double-float, the CTA's FP64.
+constexpr int kEnergyMaxO = 32;  // pass 1 keeps a pair's o loads in registers
 template <int NW>
 __global__ void __launch_bounds__(256) triples_energy_orbit_kernel(
     float *__restrict__ W, int64_t o, int64_t v, int64_t nb, int64_t A, int64_t Bk, int64_t C,
@@ -229,17 +231,19 @@ __global__ void __launch_bounds__(256) triples_energy_orbit_kernel(
   __shared__ float red_hi[32], red_lo[32];
   __shared__ float s_ev[2];
   // ek[x] = (e_x hi, e_x lo, t1_xc, 0), tab[x] = (t1_xa, t1_xb); Y at
-  // i + p1 j + p2 k with odd p1, p2 (conflict-free permuted reads)
+  // i + p1 j + p2 k with odd p1, p2, the (ia|jb) slices at x + p1 y, so that
+  // reads along any one index are free of bank conflicts
   const int p1 = oo | 1, p2 = (p1 * oo) | 1;
   float4 *ek = reinterpret_cast<float4 *>(sm_raw);
   float2 *tab = reinterpret_cast<float2 *>(ek + oo);
   float *Y = reinterpret_cast<float *>(tab + oo);
-  float *Sbc = Y + p2 * oo, *Sac = Sbc + o2, *Sab = Sac + o2;
+  float *Sbc = Y + p2 * oo, *Sac = Sbc + p1 * oo, *Sab = Sac + p1 * oo;
   const float *S_bc = S + (b + v * c) * o2p, *S_ac = S + (a + v * c) * o2p, *S_ab = S + (a + v * b) * o2p;
   for (int e = threadIdx.x; e < o2; e += blockDim.x) {
-    Sbc[e] = S_bc[e];
-    Sac[e] = S_ac[e];
-    Sab[e] = S_ab[e];
+    const int x = e % oo, y = e / oo;
+    Sbc[x + p1 * y] = S_bc[e];
+    Sac[x + p1 * y] = S_ac[e];
+    Sab[x + p1 * y] = S_ab[e];
   }
   for (int i = threadIdx.x; i < oo; i += blockDim.x) {
     const double e = eps[i];
@@ -253,19 +257,31 @@ __global__ void __launch_bounds__(256) triples_energy_orbit_kernel(
     s_ev[0] = h;
     s_ev[1] = (float)(ev - (double)h);
   }
-  __syncthreads();
-  // pass 1: Y = W + V (loads only; NW = 1 clears W after the barrier below)
-  for (int pr = threadIdx.x; pr < o2; pr += blockDim.x) {
-    const int i = pr % oo, j = pr / oo;
-    const float tai = tab[i].x, tbj = tab[j].y, sab = Sab[pr];
-    const int yo = i + p1 * j;
-#pragma unroll 8
-    for (int k = 0; k < oo; k++) {
-      const int e = pr + o2p * k;
-      float w = W0[e];
-      if (NW == 3) w += W1[e] + W2[e];
-      Y[yo + p2 * k] = w + (tai * Sbc[j + oo * k] + tbj * Sac[i + oo * k] + ek[k].z * sab);
+  // pass 1: Y = W + V (loads only; NW = 1 clears W after the barrier below).
+  // A pair's o loads are all issued before any is used; the first pair's go
+  // out before the barrier that publishes the tables.
+  float wr[kEnergyMaxO];
+  auto load_pair = [&](int pr) {
+#pragma unroll
+    for (int k = 0; k < kEnergyMaxO; k++) {
+      if (k < oo) {
+        const int e = pr + o2p * k;
+        wr[k] = W0[e];
+        if (NW == 3) wr[k] += W1[e] + W2[e];
+      }
     }
+  };
+  if ((int)threadIdx.x < o2) load_pair(threadIdx.x);
+  __syncthreads();
+  for (int pr = threadIdx.x; pr < o2; pr += blockDim.x) {
+    if (pr != (int)threadIdx.x) load_pair(pr);
+    const int i = pr % oo, j = pr / oo;
+    const float tai = tab[i].x, tbj = tab[j].y, sab = Sab[i + p1 * j];
+    const int yo = i + p1 * j;
+#pragma unroll
+    for (int k = 0; k < kEnergyMaxO; k++)
+      if (k < oo)
+        Y[yo + p2 * k] = wr[k] + (tai * Sbc[j + p1 * k] + tbj * Sac[i + p1 * k] + ek[k].z * sab);
   }
   __syncthreads();
   if (NW == 1) {  // the block of W is read: clear it for the next block triple's reductions
@@ -281,16 +297,17 @@ __global__ void __launch_bounds__(256) triples_energy_orbit_kernel(
     const int m = code >> 24;
     const float2 ti = tab[i], tj = tab[j], tk = tab[k];
     const float4 ei = ek[i], ej = ek[j], ekk = ek[k];
+    const int pi = p1 * i, pj = p1 * j, pk = p1 * k, qi = p2 * i, qj = p2 * j, qk = p2 * k;
     // V_xyz = t1_xa Sbc(y,z) + t1_yb Sac(x,z) + t1_zc Sab(x,y) over the orderings
-    const float bc_jk = Sbc[j + oo * k], bc_kj = Sbc[k + oo * j], bc_ki = Sbc[k + oo * i],
-                bc_ik = Sbc[i + oo * k], bc_ij = Sbc[i + oo * j], bc_ji = Sbc[j + oo * i];
-    const float ac_jk = Sac[j + oo * k], ac_kj = Sac[k + oo * j], ac_ki = Sac[k + oo * i],
-                ac_ik = Sac[i + oo * k], ac_ij = Sac[i + oo * j], ac_ji = Sac[j + oo * i];
-    const float ab_jk = Sab[j + oo * k], ab_kj = Sab[k + oo * j], ab_ki = Sab[k + oo * i],
-                ab_ik = Sab[i + oo * k], ab_ij = Sab[i + oo * j], ab_ji = Sab[j + oo * i];
+    const float bc_jk = Sbc[j + pk], bc_kj = Sbc[k + pj], bc_ki = Sbc[k + pi],
+                bc_ik = Sbc[i + pk], bc_ij = Sbc[i + pj], bc_ji = Sbc[j + pi];
+    const float ac_jk = Sac[j + pk], ac_kj = Sac[k + pj], ac_ki = Sac[k + pi],
+                ac_ik = Sac[i + pk], ac_ij = Sac[i + pj], ac_ji = Sac[j + pi];
+    const float ab_jk = Sab[j + pk], ab_kj = Sab[k + pj], ab_ki = Sab[k + pi],
+                ab_ik = Sab[i + pk], ab_ij = Sab[i + pj], ab_ji = Sab[j + pi];
     // even orderings ijk, jki, kij; odd ikj, kji, jik
-    const float ye0 = Y[i + p1 * j + p2 * k], ye1 = Y[j + p1 * k + p2 * i], ye2 = Y[k + p1 * i + p2 * j];
-    const float yo0 = Y[i + p1 * k + p2 * j], yo1 = Y[k + p1 * j + p2 * i], yo2 = Y[j + p1 * i + p2 * k];
+    const float ye0 = Y[i + pj + qk], ye1 = Y[j + pk + qi], ye2 = Y[k + pi + qj];
+    const float yo0 = Y[i + pk + qj], yo1 = Y[k + pj + qi], yo2 = Y[j + pi + qk];
     const float we0 = ye0 - (ti.x * bc_jk + tj.y * ac_ik + ekk.z * ab_ij);
     const float we1 = ye1 - (tj.x * bc_ki + tk.y * ac_ji + ei.z * ab_jk);
     const float we2 = ye2 - (tk.x * bc_ij + ti.y * ac_kj + ej.z * ab_ki);
@@ -298,15 +315,13 @@ __global__ void __launch_bounds__(256) triples_energy_orbit_kernel(
     const float wo1 = yo1 - (tk.x * bc_ji + tj.y * ac_ki + ei.z * ab_kj);
     const float wo2 = yo2 - (tj.x * bc_ik + ti.y * ac_jk + ekk.z * ab_ji);
     const float Se = (ye0 + ye1) + ye2, So = (yo0 + yo1) + yo2;
-    const float We = (we0 + we1) + we2, Wo = (wo0 + wo1) + wo2;
-    float wy = we0 * ye0;
-    wy = fmaf(we1, ye1, wy);
-    wy = fmaf(we2, ye2, wy);
-    wy = fmaf(wo0, yo0, wy);
-    wy = fmaf(wo1, yo1, wy);
-    wy = fmaf(wo2, yo2, wy);
-    float num = fmaf(We, Se - 2.0f * So, 3.0f * wy);                               // :152-156
-    num = fmaf(Wo, So - 2.0f * Se, num);
+    const float ce = Se - 2.0f * So, co = So - 2.0f * Se;                          // :152-154
+    float num = we0 * fmaf(3.0f, ye0, ce);
+    num = fmaf(we1, fmaf(3.0f, ye1, ce), num);
+    num = fmaf(we2, fmaf(3.0f, ye2, ce), num);
+    num = fmaf(wo0, fmaf(3.0f, yo0, co), num);
+    num = fmaf(wo1, fmaf(3.0f, yo1, co), num);
+    num = fmaf(wo2, fmaf(3.0f, yo2, co), num);
     // D = e_i + e_j + e_k - (e_a + e_b + e_c) in double-float, rounded once   :155
     float s1, e1, s2, e2, s3, e3;
     two_sum(ei.x, ej.x, s1, e1);
@@ -314,7 +329,7 @@ __global__ void __launch_bounds__(256) triples_energy_orbit_kernel(
     two_sum(s2, -evh, s3, e3);
     const float d = s3 + (((e1 + e2) + e3) + (((ei.y + ej.y) + ekk.y) - evl));
     const float mult = m == 0 ? 1.0f : (m == 1 ? 0.5f : (1.0f / 6.0f));
-    const float term = __fdividef(num * mult, d) - comp;
+    const float term = __fdividef(num * mult, d) - comp;                           // :156
     const float t = sum + term;
     comp = (t - sum) - term;
     sum = t;
@@ -901,10 +916,12 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   DevMem W(wbytes);
   if (mixed && nw == 1) SCESS_CUDA(cudaMemsetAsync(W.as<void>(), 0, wbytes, s));
   const int64_t p1 = o | 1, p2 = (p1 * o) | 1;
-  const size_t ysmem = mixed ? (size_t)(4 * o + 2 * o + p2 * o + 3 * o2) * 4
+  const size_t ysmem = mixed ? (size_t)(4 * o + 2 * o + p2 * o + 3 * p1 * o) * 4
                              : (size_t)(p2 * o + 3 * o2 + 4 * o) * 8;
   if (ysmem > 200 * 1024) throw Error(SCESS_ERR_UNSUPPORTED, "(T): o^3 too large for one CTA");
   if (o > 255) throw Error(SCESS_ERR_UNSUPPORTED, "(T): more than 255 occupied orbitals");
+  if (mixed && o > kEnergyMaxO)
+    throw Error(SCESS_ERR_UNSUPPORTED, "(T), mixed form: more than 32 occupied orbitals");
   DevMem orbits;
   int norbits = 0;
   if (mixed) {
