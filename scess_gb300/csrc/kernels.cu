@@ -275,6 +275,80 @@ __global__ void tau_delta_kernel(int64_t o, int64_t v, const double *__restrict_
   }
 }
 
+// Pairs of the particle ladder's symmetric / antisymmetric form: upper pairs
+// p <= q of n labels at u(p, q) = q (q + 1) / 2 + p, strict pairs p < q at
+// s(p, q) = q (q - 1) / 2 + p; pu / ps list each pair's (p, q).
+__device__ __forceinline__ int64_t upair(int64_t p, int64_t q) { return q * (q + 1) / 2 + p; }
+__device__ __forceinline__ int64_t spair(int64_t p, int64_t q) { return q * (q - 1) / 2 + p; }
+
+// Vp(x, k) = V(a,b,c,d) + V(a,b,d,c) (c < d) or V(a,b,c,c) (c = d) for upper
+// pairs x = (a,b), k = (c,d); Vm(x, k) = V(a,b,c,d) - V(a,b,d,c) for strict
+// pairs.  V(a,b,c,d) = V[a s0 + b s1 + c s2 + d s3].
+__global__ void ladder_vpm_kernel(const double *__restrict__ V, int64_t s0, int64_t s1, int64_t s2,
+                                  int64_t s3, const int2 *__restrict__ pu, int64_t nu,
+                                  const int2 *__restrict__ ps, int64_t ns, double *__restrict__ Vp,
+                                  double *__restrict__ Vm) {
+  const int64_t total = nu * nu + ns * ns;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    if (e < nu * nu) {
+      const int2 ab = pu[e % nu], cd = pu[e / nu];
+      const int64_t base = ab.x * s0 + ab.y * s1;
+      const double v1 = V[base + cd.x * s2 + cd.y * s3];
+      Vp[e] = cd.x < cd.y ? v1 + V[base + cd.y * s2 + cd.x * s3] : v1;
+    } else {
+      const int64_t f = e - nu * nu;
+      const int2 ab = ps[f % ns], cd = ps[f / ns];
+      const int64_t base = ab.x * s0 + ab.y * s1;
+      Vm[f] = V[base + cd.x * s2 + cd.y * s3] - V[base + cd.y * s2 + cd.x * s3];
+    }
+  }
+}
+
+// Tp(y, k) = (tau(i,j,c,d) + tau(i,j,d,c)) / 2 over upper pairs y = (i,j),
+// k = (c,d); Tm(y, k) = (tau(i,j,c,d) - tau(i,j,d,c)) / 2 over strict pairs.
+__global__ void ladder_tpm_kernel(int64_t o, int64_t v, const double *__restrict__ tau,
+                                  const int2 *__restrict__ puo, int64_t nuo,
+                                  const int2 *__restrict__ pso, int64_t nso,
+                                  const int2 *__restrict__ puv, int64_t nuv,
+                                  const int2 *__restrict__ psv, int64_t nsv,
+                                  double *__restrict__ Tp, double *__restrict__ Tm) {
+  const int64_t total = nuo * nuv + nso * nsv, o2 = o * o, o2v = o2 * v;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    if (e < nuo * nuv) {
+      const int2 ij = puo[e % nuo], cd = puv[e / nuo];
+      const int64_t b = ij.x + o * ij.y;
+      Tp[e] = 0.5 * (tau[b + o2 * cd.x + o2v * cd.y] + tau[b + o2 * cd.y + o2v * cd.x]);
+    } else {
+      const int64_t f = e - nuo * nuv;
+      const int2 ij = pso[f % nso], cd = psv[f / nso];
+      const int64_t b = ij.x + o * ij.y;
+      Tm[f] = 0.5 * (tau[b + o2 * cd.x + o2v * cd.y] - tau[b + o2 * cd.y + o2v * cd.x]);
+    }
+  }
+}
+
+// R2(i,j,a,b) += Sp(u(i,j), u(a,b)) + sgn Sm(s(i,j), s(a,b)) with the pairs
+// sorted and sgn = +1 when (i < j) == (a < b), -1 otherwise (0 when i = j or
+// a = b): Sp is symmetric and Sm antisymmetric in each pair.  Sp is
+// nuo x nuv, Sm nso x nsv, both column-major.
+__global__ void ladder_unpack_kernel(int64_t o, int64_t v, const double *__restrict__ Sp,
+                                     const double *__restrict__ Sm, double *__restrict__ R2) {
+  const int64_t n = o * o * v * v, nuo = o * (o + 1) / 2, nso = o * (o - 1) / 2;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e % o, j = (e / o) % o, a = (e / (o * o)) % v, b = e / (o * o * v);
+    const int64_t i0 = i < j ? i : j, j0 = i < j ? j : i, a0 = a < b ? a : b, b0 = a < b ? b : a;
+    double s = Sp[upair(i0, j0) + nuo * upair(a0, b0)];
+    if (i != j && a != b) {
+      const double m = Sm[spair(i0, j0) + nso * spair(a0, b0)];
+      s += ((i < j) == (a < b)) ? m : -m;
+    }
+    R2[e] += s;
+  }
+}
+
 __global__ void denom_kernel(int64_t o, int64_t v, const double *__restrict__ eps,
                              const double *__restrict__ R1, const double *__restrict__ R2,
                              double *__restrict__ t1, double *__restrict__ t2) {
@@ -415,6 +489,28 @@ void make_tau(int64_t o, int64_t v, const double *t1, const double *t2, double s
 void make_tau_delta(int64_t o, int64_t v, const double *t1_0, const double *dt1,
                     const double *dt2, double *dtau, cudaStream_t stream) {
   tau_delta_kernel<<<grid_for(o * o * v * v), 256, 0, stream>>>(o, v, t1_0, dt1, dt2, dtau);
+  SCESS_CHECK_LAUNCH();
+}
+
+void ladder_vpm(const double *V, int64_t s0, int64_t s1, int64_t s2, int64_t s3, const int2 *pu,
+                int64_t nu, const int2 *ps, int64_t ns, double *Vp, double *Vm,
+                cudaStream_t stream) {
+  ladder_vpm_kernel<<<grid_for(nu * nu + ns * ns), 256, 0, stream>>>(V, s0, s1, s2, s3, pu, nu, ps,
+                                                                    ns, Vp, Vm);
+  SCESS_CHECK_LAUNCH();
+}
+
+void ladder_tpm(int64_t o, int64_t v, const double *tau, const int2 *puo, int64_t nuo,
+                const int2 *pso, int64_t nso, const int2 *puv, int64_t nuv, const int2 *psv,
+                int64_t nsv, double *Tp, double *Tm, cudaStream_t stream) {
+  ladder_tpm_kernel<<<grid_for(nuo * nuv + nso * nsv), 256, 0, stream>>>(
+      o, v, tau, puo, nuo, pso, nso, puv, nuv, psv, nsv, Tp, Tm);
+  SCESS_CHECK_LAUNCH();
+}
+
+void ladder_unpack(int64_t o, int64_t v, const double *Sp, const double *Sm, double *R2,
+                   cudaStream_t stream) {
+  ladder_unpack_kernel<<<grid_for(o * o * v * v), 256, 0, stream>>>(o, v, Sp, Sm, R2);
   SCESS_CHECK_LAUNCH();
 }
 

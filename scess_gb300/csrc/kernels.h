@@ -53,6 +53,21 @@ void make_tau(int64_t o, int64_t v, const double *t1, const double *t2, double s
 // (dt2 + dt1 (x) t1_1 + t1_0 (x) dt1), not as a difference of two taus
 void make_tau_delta(int64_t o, int64_t v, const double *t1_0, const double *dt1,
                     const double *dt2, double *dtau, cudaStream_t stream);
+// Particle ladder in its symmetric / antisymmetric form (pairs: upper p <= q
+// at q(q+1)/2 + p, strict p < q at q(q-1)/2 + p; pu / ps list each pair's
+// (p, q)).  ladder_vpm: Vp(x,k) = V(a,b,c,d) + V(a,b,d,c) (c < d) or V(a,b,c,c),
+// Vm(x,k) = V(a,b,c,d) - V(a,b,d,c), x = (a,b), k = (c,d), V through strides.
+// ladder_tpm: Tp / Tm = (tau(i,j,c,d) +/- tau(i,j,d,c)) / 2 over (i,j), (c,d).
+// ladder_unpack: R2(i,j,a,b) += Sp(ij, ab) +/- Sm(ij, ab) (symmetric /
+// antisymmetric in each pair), Sp = Tp Vp^T, Sm = Tm Vm^T.
+void ladder_vpm(const double *V, int64_t s0, int64_t s1, int64_t s2, int64_t s3, const int2 *pu,
+                int64_t nu, const int2 *ps, int64_t ns, double *Vp, double *Vm,
+                cudaStream_t stream);
+void ladder_tpm(int64_t o, int64_t v, const double *tau, const int2 *puo, int64_t nuo,
+                const int2 *pso, int64_t nso, const int2 *puv, int64_t nuv, const int2 *psv,
+                int64_t nsv, double *Tp, double *Tm, cudaStream_t stream);
+void ladder_unpack(int64_t o, int64_t v, const double *Sp, const double *Sm, double *R2,
+                   cudaStream_t stream);
 // x[i] = y[i] / d[i] style Jacobi update with on-the-fly denominators:
 // t1(i,a) = R1(i,a) / (e_i - e_a); t2(i,j,a,b) = R2 / (e_i + e_j - e_a - e_b).
 void divide_denominators(int64_t o, int64_t v, const double *eps, const double *R1,

@@ -121,6 +121,56 @@ void RccsdBlocks::build_l(Ctx &ctx) {
   permute(ctx, "kdlc->kcld", -1.0, ovov, 1.0, L_ovov.v);
 }
 
+void ladder_pm(Ctx &ctx, const RccsdBlocks &B, const TV &tau, double *R2, Backend be) {
+  const int64_t o = B.o, v = B.v;
+  cudaStream_t s = ctx.stream;
+  if (!B.ladder) {
+    auto L = std::make_unique<LadderPM>();
+    L->nuo = o * (o + 1) / 2;
+    L->nso = o * (o - 1) / 2;
+    L->nuv = v * (v + 1) / 2;
+    L->nsv = v * (v - 1) / 2;
+    std::vector<int2> pr;
+    auto add = [&](int64_t n, bool strict) {
+      for (int64_t q = 0; q < n; q++)
+        for (int64_t p = 0; p < (strict ? q : q + 1); p++) pr.push_back(make_int2((int)p, (int)q));
+    };
+    add(o, false);
+    add(o, true);
+    add(v, false);
+    add(v, true);
+    L->pairs.alloc(std::max<size_t>(pr.size(), 1) * sizeof(int2));
+    SCESS_CUDA(cudaMemcpyAsync(L->pairs.as<void>(), pr.data(), pr.size() * sizeof(int2),
+                               cudaMemcpyHostToDevice, s));
+    L->pu_o = L->pairs.as<int2>();
+    L->ps_o = L->pu_o + L->nuo;
+    L->pu_v = L->ps_o + L->nso;
+    L->ps_v = L->pu_v + L->nuv;
+    L->Vp = DTensor({L->nuv, L->nuv});
+    L->Vm = DTensor({std::max<int64_t>(L->nsv, 1), std::max<int64_t>(L->nsv, 1)});
+    ladder_vpm(B.vvvv.p, B.vvvv.str[0], B.vvvv.str[1], B.vvvv.str[2], B.vvvv.str[3], L->pu_v,
+               L->nuv, L->ps_v, L->nsv, L->Vp.p(), L->Vm.p(), s);
+    L->Tp = DTensor({L->nuo, L->nuv});
+    L->Tm = DTensor({std::max<int64_t>(L->nso, 1), std::max<int64_t>(L->nsv, 1)});
+    L->Sp = DTensor({L->nuo, L->nuv});
+    L->Sm = DTensor({std::max<int64_t>(L->nso, 1), std::max<int64_t>(L->nsv, 1)});
+    ctx.sync();  // (pr is a host vector of this scope)
+    B.ladder = std::move(L);
+  }
+  LadderPM &L = *B.ladder;
+  ladder_tpm(o, v, tau.p, L.pu_o, L.nuo, L.ps_o, L.nso, L.pu_v, L.nuv, L.ps_v, L.nsv, L.Tp.p(),
+             L.Tm.p(), s);
+  // S+(y, x) = sum_k T+(y, k) V+(x, k); the same for the strict pairs
+  einsum(ctx, "yk,xk->yx", 1.0, cm(L.Tp.p(), {L.nuo, L.nuv}), cm(L.Vp.p(), {L.nuv, L.nuv}), 0.0,
+         cm(L.Sp.p(), {L.nuo, L.nuv}), be, false, true);
+  if (L.nso > 0 && L.nsv > 0)
+    einsum(ctx, "yk,xk->yx", 1.0, cm(L.Tm.p(), {L.nso, L.nsv}), cm(L.Vm.p(), {L.nsv, L.nsv}), 0.0,
+           cm(L.Sm.p(), {L.nso, L.nsv}), be, false, true);
+  else
+    SCESS_CUDA(cudaMemsetAsync(L.Sm.p(), 0, L.Sm.size() * sizeof(double), s));
+  ladder_unpack(o, v, L.Sp.p(), L.Sm.p(), R2, s);
+}
+
 void RccsdWork::alloc(int64_t o, int64_t v, bool direct_vvvv) {
   tau = DTensor({o, o, v, v});
   Foo = DTensor({o, o});
@@ -241,7 +291,10 @@ void rccsd_residual(Ctx &ctx, const RccsdBlocks &B, const double *amp, const dou
   } else {
     // sum_cd Wvvvv tau = vvvv tau - PlusTranspose(sum_k t1(k,a) Y(k,b,i,j)),
     // Y(k,b,i,j) = sum_cd (kc|bd) tau(i,j,c,d), using tau(i,j,c,d) = tau(j,i,d,c).
-    E("abcd,ijcd->ijab", 1.0, B.vvvv, tau, 1.0, R2, true);                           // :216
+    // vvvv tau in its symmetric / antisymmetric form (a quarter of the FLOPs);
+    // the adjoint's recorded forward keeps the plain contraction.
+    if (ctx.tape) E("abcd,ijcd->ijab", 1.0, B.vvvv, tau, 1.0, R2, true);             // :216
+    else ladder_pm(ctx, B, tau, R2.p, be);
     E("kcbd,ijcd->kbij", 1.0, B.ovvv, tau, 0.0, w.Yd.v, true);                       // :179-180
     E("ka,kbij->ijab", -1.0, t1, w.Yd.v, 1.0, w.X.v);
   }
@@ -346,7 +399,7 @@ void rccsd_residual_delta(Ctx &ctx, const RccsdBlocks &B, const double *amp0, co
 
   E2("klij,klab->ijab", 1.0, w.Woooo.v, tau_1, w0.Woooo.v, dtau, 1.0, R2);           // :214
   // particle ladder with the T1 dressing folded in (as the reassociated list)
-  E("abcd,ijcd->ijab", 1.0, B.vvvv, dtau, 1.0, R2, true);                            // :216
+  ladder_pm(ctx, B, dtau, R2.p, be);                                                 // :216
   E("kcbd,ijcd->kbij", 1.0, B.ovvv, dtau, 0.0, w.Yd.v, true);                        // :179-180
   // d(t1 Yd) = dt1 Yd0 + t1_1 dYd
   E("ka,kbij->ijab", -1.0, dt1, w0.Yd.v, 1.0, w.X.v);

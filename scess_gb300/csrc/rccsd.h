@@ -1,11 +1,26 @@
 // Closed-shell CCSD on the GPU: integral blocks, residual, Jacobi update, DIIS.
 #pragma once
 #include <deque>
+#include <memory>
 #include <vector>
 
 #include "engine.h"
 
 namespace scess {
+
+// Particle ladder sum_cd <ab|cd> tau(i,j,c,d) in its symmetric /
+// antisymmetric form: with V+-(ab,cd) = V(a,b,c,d) +- V(a,b,d,c) over pairs
+// c <= d (c < d for -) and tau+- = (tau(i,j,c,d) +- tau(i,j,d,c)) / 2, the
+// ladder is S(ij,ab) + -S-(ij,ab), S+- = tau+- V+-^T over pairs i <= j, a <= b
+// (i < j, a < b for -): a quarter of the FLOPs of the plain contraction
+// (it uses V(a,b,c,d) = V(b,a,d,c) and tau(i,j,c,d) = tau(j,i,d,c)).
+struct LadderPM {
+  int64_t nuo = 0, nso = 0, nuv = 0, nsv = 0;
+  DevMem pairs;            // pu_o | ps_o | pu_v | ps_v as int2
+  DTensor Vp, Vm;          // nuv x nuv, nsv x nsv (built once from the vvvv view)
+  DTensor Tp, Tm, Sp, Sm;  // per call
+  const int2 *pu_o = nullptr, *ps_o = nullptr, *pu_v = nullptr, *ps_v = nullptr;
+};
 
 // Integral blocks of RCCSD.cpp:32-44 as strided views into the device eri
 // (no copies), plus the two materialised linear combinations.
@@ -14,6 +29,7 @@ struct RccsdBlocks {
   TV ovov, oovv, ovvo, ovvv, ovoo, oooo, vvvv, oovv_phys;
   DTensor L_oovv, L_ovov;
   std::vector<DTensor> regions;  // DF build: the eri regions the views point into
+  mutable std::unique_ptr<LadderPM> ladder;  // built on first use (ladder_pm)
   // views into the device eri (nmo^4)
   void build(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t nocc);
   // from DF factors B (naux x nmo x nmo): only the seven regions of <pq|rs> the
@@ -45,6 +61,11 @@ struct RccsdWork {
 enum class ResidualList { AUTO = 0, LITERAL = 1, REASSOCIATED = 2 };
 void rccsd_residual(Ctx &ctx, const RccsdBlocks &B, const double *amp, const double *t2driver,
                     Backend be, RccsdWork &w, double *R, ResidualList list = ResidualList::AUTO);
+
+// R2 += sum_cd <ab|cd> tau(i,j,c,d) through the symmetric / antisymmetric
+// form (LadderPM), on the backend be; the V+- operands are built from the
+// vvvv view on first use and kept with the blocks.
+void ladder_pm(Ctx &ctx, const RccsdBlocks &B, const TV &tau, double *R2, Backend be);
 
 // Change of the residual numerators, dR = R(T0 + d) - R(T0), for the
 // reassociated list: w0 holds that list's intermediates at T0 (from
