@@ -110,6 +110,24 @@ void RccsdBlocks::build_df(Ctx &ctx, const double *d_B, int64_t naux, int64_t nm
   build_l(ctx);
 }
 
+const TV &RccsdBlocks::l_ovvv(Ctx &ctx) const {
+  if (!L_ovvv.p()) {
+    L_ovvv = DTensor({o, v, v, v});
+    permute(ctx, "kdac->kdac", 2.0, ovvv, 0.0, L_ovvv.v);
+    permute(ctx, "kcad->kdac", -1.0, ovvv, 1.0, L_ovvv.v);
+  }
+  return L_ovvv.v;
+}
+
+const TV &RccsdBlocks::l_ovoo(Ctx &ctx) const {
+  if (!L_ovoo.p()) {
+    L_ovoo = DTensor({o, v, o, o});
+    permute(ctx, "lcki->lcki", 2.0, ovoo, 0.0, L_ovoo.v);
+    permute(ctx, "kcli->lcki", -1.0, ovoo, 1.0, L_ovoo.v);
+  }
+  return L_ovoo.v;
+}
+
 void RccsdBlocks::build_l(Ctx &ctx) {
   // L_oovv = 2 <ij|ab> - <ij|ba>                                                   :68-69
   L_oovv = DTensor({o, o, v, v});
@@ -230,10 +248,19 @@ void rccsd_residual(Ctx &ctx, const RccsdBlocks &B, const double *amp, const dou
   E("ki,ka->ia", 1.0, w.Fovt1.v, t1, 1.0, R1);                                       // :128
   E("kcai,kc->ia", 2.0, B.ovvo, t1, 1.0, R1, true);                                  // :131
   E("kiac,kc->ia", -1.0, B.oovv, t1, 1.0, R1, true);                                 // :132
-  E("kdac,ikcd->ia", 2.0, B.ovvv, tau, 1.0, R1, true);                               // :134
-  E("kcad,ikcd->ia", -1.0, B.ovvv, tau, 1.0, R1, true);                              // :135
-  E("lcki,klac->ia", -2.0, B.ovoo, tau, 1.0, R1, true);                              // :137
-  E("kcli,klac->ia", 1.0, B.ovoo, tau, 1.0, R1, true);                               // :138
+  // The reassociated list (not recorded for the adjoint, whose gradients flow
+  // back through views of the eri) contracts each pair of terms over the same
+  // index pattern once, with the combined integrals L_ovvv, L_ovoo.
+  const bool combined = !literal && !ctx.tape;
+  if (combined) {
+    E("kdac,ikcd->ia", 1.0, B.l_ovvv(ctx), tau, 1.0, R1, true);                      // :134-135
+    E("lcki,klac->ia", -1.0, B.l_ovoo(ctx), tau, 1.0, R1, true);                     // :137-138
+  } else {
+    E("kdac,ikcd->ia", 2.0, B.ovvv, tau, 1.0, R1, true);                             // :134
+    E("kcad,ikcd->ia", -1.0, B.ovvv, tau, 1.0, R1, true);                            // :135
+    E("lcki,klac->ia", -2.0, B.ovoo, tau, 1.0, R1, true);                            // :137
+    E("kcli,klac->ia", 1.0, B.ovoo, tau, 1.0, R1, true);                             // :138
+  }
 
   // T2.  X collects every term the reference wraps in PlusTranspose.
   if (literal) {
@@ -255,11 +282,19 @@ void rccsd_residual(Ctx &ctx, const RccsdBlocks &B, const double *amp, const dou
   if (t2driver) axpby(o * o * v * v, 1.0, t2driver, 1.0, R2.p, s);                   // :159-160
 
   permute(ctx, "ki->ki", 1.0, w.Foo.v, 0.0, w.Loo.v);                                // :163
-  E("lcki,lc->ki", 2.0, B.ovoo, t1, 1.0, w.Loo.v, true);                             // :164
-  E("kcli,lc->ki", -1.0, B.ovoo, t1, 1.0, w.Loo.v, true);                            // :165
+  if (combined) {
+    E("lcki,lc->ki", 1.0, B.l_ovoo(ctx), t1, 1.0, w.Loo.v, true);                    // :164-165
+  } else {
+    E("lcki,lc->ki", 2.0, B.ovoo, t1, 1.0, w.Loo.v, true);                           // :164
+    E("kcli,lc->ki", -1.0, B.ovoo, t1, 1.0, w.Loo.v, true);                          // :165
+  }
   permute(ctx, "ac->ac", 1.0, w.Fvv.v, 0.0, w.Lvv.v);                                // :167
-  E("kdac,kd->ac", 2.0, B.ovvv, t1, 1.0, w.Lvv.v, true);                             // :168
-  E("kcad,kd->ac", -1.0, B.ovvv, t1, 1.0, w.Lvv.v, true);                            // :169
+  if (combined) {
+    E("kdac,kd->ac", 1.0, B.l_ovvv(ctx), t1, 1.0, w.Lvv.v, true);                    // :168-169
+  } else {
+    E("kdac,kd->ac", 2.0, B.ovvv, t1, 1.0, w.Lvv.v, true);                           // :168
+    E("kcad,kd->ac", -1.0, B.ovvv, t1, 1.0, w.Lvv.v, true);                          // :169
+  }
 
   permute(ctx, "klij->klij", 1.0, B.oooo, 0.0, w.Woooo.v);                           // :172
   E("lcki,jc->klij", 1.0, B.ovoo, t1, 1.0, w.Woooo.v, true);                         // :173
@@ -359,10 +394,8 @@ void rccsd_residual_delta(Ctx &ctx, const RccsdBlocks &B, const double *amp0, co
   E2("ki,ka->ia", 1.0, w.Fovt1.v, t1_1, w0.Fovt1.v, dt1, 1.0, R1);                   // :128
   E("kcai,kc->ia", 2.0, B.ovvo, dt1, 1.0, R1, true);                                 // :131
   E("kiac,kc->ia", -1.0, B.oovv, dt1, 1.0, R1, true);                                // :132
-  E("kdac,ikcd->ia", 2.0, B.ovvv, dtau, 1.0, R1, true);                              // :134
-  E("kcad,ikcd->ia", -1.0, B.ovvv, dtau, 1.0, R1, true);                             // :135
-  E("lcki,klac->ia", -2.0, B.ovoo, dtau, 1.0, R1, true);                             // :137
-  E("kcli,klac->ia", 1.0, B.ovoo, dtau, 1.0, R1, true);                              // :138
+  E("kdac,ikcd->ia", 1.0, B.l_ovvv(ctx), dtau, 1.0, R1, true);                       // :134-135
+  E("lcki,klac->ia", -1.0, B.l_ovoo(ctx), dtau, 1.0, R1, true);                      // :137-138
 
   // T2 (reassociated list; the constant <ij|ab> and driver terms drop out)
   E("kibc,jc->kibj", 1.0, B.oovv, dt1, 0.0, w.tmp_kibj.v, true);                     // :144-147
@@ -373,11 +406,9 @@ void rccsd_residual_delta(Ctx &ctx, const RccsdBlocks &B, const double *amp0, co
   SCESS_CUDA(cudaMemsetAsync(R2.p, 0, n2 * sizeof(double), s));                      // :158-160
 
   permute(ctx, "ki->ki", 1.0, w.Foo.v, 0.0, w.Loo.v);                                // :163
-  E("lcki,lc->ki", 2.0, B.ovoo, dt1, 1.0, w.Loo.v, true);                            // :164
-  E("kcli,lc->ki", -1.0, B.ovoo, dt1, 1.0, w.Loo.v, true);                           // :165
+  E("lcki,lc->ki", 1.0, B.l_ovoo(ctx), dt1, 1.0, w.Loo.v, true);                     // :164-165
   permute(ctx, "ac->ac", 1.0, w.Fvv.v, 0.0, w.Lvv.v);                                // :167
-  E("kdac,kd->ac", 2.0, B.ovvv, dt1, 1.0, w.Lvv.v, true);                            // :168
-  E("kcad,kd->ac", -1.0, B.ovvv, dt1, 1.0, w.Lvv.v, true);                           // :169
+  E("kdac,kd->ac", 1.0, B.l_ovvv(ctx), dt1, 1.0, w.Lvv.v, true);                     // :168-169
 
   E("lcki,jc->klij", 1.0, B.ovoo, dt1, 0.0, w.Woooo.v, true);                        // :172-173
   E("kclj,ic->klij", 1.0, B.ovoo, dt1, 1.0, w.Woooo.v, true);                        // :174

@@ -30,6 +30,11 @@ struct RccsdBlocks {
   DTensor L_oovv, L_ovov;
   std::vector<DTensor> regions;  // DF build: the eri regions the views point into
   mutable std::unique_ptr<LadderPM> ladder;  // built on first use (ladder_pm)
+  // The reassociated list's combined integrals, built on first use:
+  // L_ovvv(k,d,a,c) = 2 (kd|ac) - (kc|ad), L_ovoo(l,c,k,i) = 2 (lc|ki) - (kc|li)
+  mutable DTensor L_ovvv, L_ovoo;
+  const TV &l_ovvv(Ctx &ctx) const;
+  const TV &l_ovoo(Ctx &ctx) const;
   // views into the device eri (nmo^4)
   void build(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t nocc);
   // from DF factors B (naux x nmo x nmo): only the seven regions of <pq|rs> the

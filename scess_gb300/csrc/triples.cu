@@ -153,6 +153,24 @@ __global__ void to_f32_rows_kernel(const double *__restrict__ x, int64_t rows, i
 // o3p = o o2p; S as [(a + v b) o2p + i + o j].
 __host__ __device__ inline int64_t pad4(int64_t n) { return (n + 3) & ~int64_t(3); }
 
+// FP32 tables of the mixed energy kernel, built once per (T) call: every
+// orbital energy as hi + lo (hi = the FP32 rounding of eps, lo = the FP32
+// rounding of the remainder) and t1 in FP32.
+__global__ void energy_tables_kernel(const double *__restrict__ eps, int64_t n,
+                                     const double *__restrict__ t1, int64_t nt1,
+                                     float2 *__restrict__ ehl, float *__restrict__ t1f) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n + nt1;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    if (e < n) {
+      const double x = eps[e];
+      const float h = (float)x;
+      ehl[e] = make_float2(h, (float)(x - (double)h));
+    } else {
+      t1f[e - n] = (float)t1[e - n];
+    }
+  }
+}
+
 // Double-float arithmetic in FP32: two_sum gives s + e == a + b exactly
 // (Knuth's TwoSum, six FP32 operations, no branch).
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
@@ -203,7 +221,7 @@ constexpr int kEnergyMaxO = 32;  // pass 1 keeps a pair's o loads in registers
 template <int NW>
 __global__ void __launch_bounds__(256) triples_energy_orbit_kernel(
     float *__restrict__ W, int64_t o, int64_t v, int64_t nb, int64_t A, int64_t Bk, int64_t C,
-    const double *__restrict__ eps, const double *__restrict__ t1, const float *__restrict__ S,
+    const float2 *__restrict__ ehl, const float *__restrict__ t1f, const float *__restrict__ S,
     const uint32_t *__restrict__ orbits, int norbits, double *__restrict__ energies) {
   const int al = (int)(blockIdx.x / (nb * nb)), bl = (int)((blockIdx.x / nb) % nb),
             cl = (int)(blockIdx.x % nb);
@@ -246,16 +264,19 @@ __global__ void __launch_bounds__(256) triples_energy_orbit_kernel(
     Sab[x + p1 * y] = S_ab[e];
   }
   for (int i = threadIdx.x; i < oo; i += blockDim.x) {
-    const double e = eps[i];
-    const float h = (float)e;
-    ek[i] = make_float4(h, (float)(e - (double)h), (float)t1[i + o * c], 0.f);
-    tab[i] = make_float2((float)t1[i + o * a], (float)t1[i + o * b]);
+    const float2 e = ehl[i];
+    ek[i] = make_float4(e.x, e.y, t1f[i + o * c], 0.f);
+    tab[i] = make_float2(t1f[i + o * a], t1f[i + o * b]);
   }
-  if (threadIdx.x == 0) {
-    const double ev = eps[o + a] + eps[o + b] + eps[o + c];
-    const float h = (float)ev;
-    s_ev[0] = h;
-    s_ev[1] = (float)(ev - (double)h);
+  if (threadIdx.x == 0) {  // e_a + e_b + e_c in double-float
+    const float2 ea = ehl[o + a], eb = ehl[o + b], ec = ehl[o + c];
+    float s1, e1, s2, e2;
+    two_sum(ea.x, eb.x, s1, e1);
+    two_sum(s1, ec.x, s2, e2);
+    const float lo = (e1 + e2) + ((ea.y + eb.y) + ec.y);
+    const float hi = s2 + lo;
+    s_ev[0] = hi;
+    s_ev[1] = lo - (hi - s2);
   }
   // pass 1: Y = W + V (loads only; NW = 1 clears W after the barrier below).
   // A pair's o loads are all issued before any is used; the first pair's go
@@ -963,7 +984,8 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
   const int rbk = (tbk == 64 && o <= 32) ? 32 : tbk;
   CUtensorMap mP{}, mQ{}, mQ2{}, mR{}, mR2{}, mTx{};
   DevTables gdt;  // W_g row / column tables
-  DevMem Sf;  // (ia|jb) as FP32 for the energy kernel (padded rows)
+  DevMem Sf;    // (ia|jb) as FP32 for the energy kernel (padded rows)
+  DevMem etab;  // eps as FP32 hi + lo (nmo float2), then t1 in FP32
   const int64_t Mg = o * nb, Ng = o2;
   const int64_t Mpq = o * nb * nb, Npq = o2 * nb, Mr = o2 * nb, Nr = o * nb * nb;  // FP64 GEMMs
   if (mixed) {
@@ -1021,6 +1043,10 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
                  table({{o, o}, {nb, nb * o3p}}), table({{o, 1}, {o, o2p}}),
                  table({{o, o2p}, {nb, o3p}}), table({{o, 1}, {o, o}})});
     Sf.alloc((size_t)o2p * v * v * sizeof(float));
+    etab.alloc((size_t)N * sizeof(float2) + (size_t)o * v * sizeof(float));
+    energy_tables_kernel<<<(unsigned)std::min<int64_t>(ceil_div(N + o * v, 256), 4 * kNumSMs), 256, 0, s>>>(
+        d_eps, N, d_t1, o * v, etab.as<float2>(), reinterpret_cast<float *>(etab.as<float2>() + N));
+    SCESS_CHECK_LAUNCH();
     to_f32_rows_kernel<<<(unsigned)std::min<int64_t>(ceil_div(o2p * v * v, 256), 16 * kNumSMs), 256, 0, s>>>(
         T.S.p(), v * v, o2, o2p, Sf.as<float>());
     SCESS_CHECK_LAUNCH();
@@ -1137,11 +1163,13 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
                       (double)nblk * o3 * (mixed ? (nw == 1 ? 2 : 3) * 4 : 8), s);
         if (mixed && nw == 1)
           triples_energy_orbit_kernel<1><<<nblk, e3threads, ysmem, s>>>(
-              W.as<float>(), o, v, nb, A, Bk, C, d_eps, d_t1, Sf.as<float>(),
+              W.as<float>(), o, v, nb, A, Bk, C, etab.as<float2>(),
+              reinterpret_cast<const float *>(etab.as<float2>() + N), Sf.as<float>(),
               orbits.as<uint32_t>(), norbits, energies.p());
         else if (mixed)
           triples_energy_orbit_kernel<3><<<nblk, e3threads, ysmem, s>>>(
-              W.as<float>(), o, v, nb, A, Bk, C, d_eps, d_t1, Sf.as<float>(),
+              W.as<float>(), o, v, nb, A, Bk, C, etab.as<float2>(),
+              reinterpret_cast<const float *>(etab.as<float2>() + N), Sf.as<float>(),
               orbits.as<uint32_t>(), norbits, energies.p());
         else
           triples_energy_kernel<double, double><<<nblk, 256, ysmem, s>>>(

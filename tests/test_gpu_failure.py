@@ -48,12 +48,14 @@ def test_memory_limit_gives_oom_and_the_context_recovers(gctx, small):
         gctx.set_memory_limit(0)
     got = gctx.solve(eri, w.eps, 5)
     assert got.converged and abs(got.E_CCSD - ref.E_CCSD) < 1e-9
-    # a cap the solve fits in
+    # a cap the solve fits in, above what the context already holds (its
+    # workspaces persist between calls)
+    cap = gctx.memory_held() + (1 << 30)
     try:
-        gctx.set_memory_limit(1 << 30)
+        gctx.set_memory_limit(cap)
         got = gctx.solve(eri, w.eps, 5, precision='mixed')
         assert got.converged and abs(got.E_CCSD - ref.E_CCSD) < 1e-6
-        assert gctx.memory_held() <= 1 << 30
+        assert gctx.memory_held() <= cap
     finally:
         gctx.set_memory_limit(0)
 
