@@ -97,8 +97,10 @@ __device__ __forceinline__ void tc_fence_after() {
 
 // Fire-and-forget FP32 reduction into global memory (an L2 atomic) of two
 // consecutive floats at an 8-byte aligned address.
-__device__ __forceinline__ void red_add_v2(float *p, float a, float b) {
-  asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(a), "f"(b) : "memory");
+__device__ __forceinline__ void red_add_v4(float *p, float a, float b, float c, float d) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(a), "f"(b), "f"(c),
+               "f"(d)
+               : "memory");
 }
 
 
@@ -739,21 +741,34 @@ __global__ void __launch_bounds__(TcShape<BN, BK, PAIR>::THREADS, 1)
             }
           }
         } else {
+          // Column quads: the lanes holding columns (c, c + 1) and (c + 2, c + 3)
+          // of rows r and r + 8 swap half their values, so that the even lane adds
+          // the quad of row r and the odd lane that of row r + 8, each with one
+          // 16-byte reduction.
+          const int odd = lane & 1;
+          const int cq4 = 4 * ((lane >> 1) & 1);
 #pragma unroll
           for (int j = 0; j < HC / 8; j++) {
-            const int64_t co0 = colH[8 * j + cq], co1 = colH[8 * j + cq + 1];
+            const int64_t co = colH[8 * j + cq4], co3 = colH[8 * j + cq4 + 3];
 #pragma unroll
-            for (int s4 = 0; s4 < 4; s4++) {
-              const int64_t ro = ro4[s4];
-              const float v0 = fa * acc[64 * (s4 >> 1) + 4 * j + 2 * (s4 & 1)];
-              const float v1 = fa * acc[64 * (s4 >> 1) + 4 * j + 2 * (s4 & 1) + 1];
-              if (ro < 0) continue;
-              float *d = C + ro + co0;
-              if (co0 >= 0 && co1 == co0 + 1 && ((uintptr_t)d & 7) == 0) {
-                red_add_v2(d, v0, v1);
-              } else {
-                if (co0 >= 0) atomicAdd(C + ro + co0, v0);
-                if (co1 >= 0) atomicAdd(C + ro + co1, v1);
+            for (int L = 0; L < 2; L++) {
+              const int b = 64 * L + 4 * j;
+              const float s0 = odd ? acc[b] : acc[b + 2], s1 = odd ? acc[b + 1] : acc[b + 3];
+              const float r0 = __shfl_xor_sync(0xffffffffu, s0, 1);
+              const float r1 = __shfl_xor_sync(0xffffffffu, s1, 1);
+              const float v0 = fa * (odd ? r0 : acc[b]), v1 = fa * (odd ? r1 : acc[b + 1]);
+              const float v2 = fa * (odd ? acc[b + 2] : r0), v3 = fa * (odd ? acc[b + 3] : r1);
+              const int64_t ro = odd ? ro4[2 * L + 1] : ro4[2 * L];
+              if (ro < 0 || co < 0) continue;
+              float *d = C + ro + co;
+              if (co3 == co + 3 && ((uintptr_t)d & 15) == 0) {
+                red_add_v4(d, v0, v1, v2, v3);
+              } else {  // (not expected: the host asks for quads only when aligned)
+                const int64_t c1 = colH[8 * j + cq4 + 1], c2 = colH[8 * j + cq4 + 2];
+                atomicAdd(C + ro + co, v0);
+                if (c1 >= 0) atomicAdd(C + ro + c1, v1);
+                if (c2 >= 0) atomicAdd(C + ro + c2, v2);
+                if (co3 >= 0) atomicAdd(C + ro + co3, v3);
               }
             }
           }
