@@ -64,10 +64,13 @@ CPU_SAMPLE = ('one full FP64 CCSD iteration of the NumPy oracle (MP2 guess, BLAS
 # DRAM bytes (read + write) of one grouped (T) GEMM launch at o=20, nb=12,
 # measured with ncu: the three W buffers (166 MB) are written once, 112 MB of
 # them reach DRAM, operands are read mostly from L2.
-TRIPLES_LAUNCH_TRAFFIC = 136.7e6
-TRIPLES_TRAFFIC_SOURCE = ('ncu dram__bytes_read.sum + dram__bytes_write.sum of one off-diagonal '
-                          'grouped (T) launch at o=20 v=96, which has the same launch shape '
-                          '(nb=12, 864 work units of 256 x 256 on cluster pairs) as o=20 v=180')
+TRIPLES_LAUNCH_TRAFFIC = 36.6e6
+TRIPLES_TRAFFIC_SOURCE = ('ncu dram__bytes_read.sum + dram__bytes_write.sum (30.7 MB + 5.9 MB) of one '
+                          'grouped (T) launch of `bench.py --triples-only --o 20 --v 180`, the same '
+                          'launches as this workload (nb=12, 864 work units of 256 x 256 on cluster '
+                          'pairs), application replay with --cache-control none: the L2 as the '
+                          'program leaves it, W (55 MB) resident between the GEMM and the energy '
+                          'kernel')
 
 
 def peaks():
