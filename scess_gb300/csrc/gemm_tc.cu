@@ -423,6 +423,9 @@ __global__ void __launch_bounds__(TcShape<BN, BK, PAIR>::THREADS, 1)
   if constexpr (PAIR) cluster_sync_all();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  // the stream's next kernel may be scheduled once every CTA is here (it waits
+  // for this grid's completion before it reads what this grid writes)
+  if (threadIdx.x == 0) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 
   // The CTA's it-th unit: round it of a round-robin over the grid whose odd
   // rounds swap neighbouring CTAs, so that with an even grid and two column
@@ -618,6 +621,9 @@ __global__ void __launch_bounds__(TcShape<BN, BK, PAIR>::THREADS, 1)
   }
   } else {  // epilogue warps
     if constexpr (BN == 256) asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(kEpiRegs256));
+    // a programmatic dependent launch (TcProblemSet::pdl) stores only after the
+    // previous grid is complete and its writes are visible (no-op otherwise)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     const int q = warp & 3;
     const int row = 32 * q + lane;
     const int h = (warp - SH::EPI0) >> 2;                 // column half (BN = 256)
@@ -1382,17 +1388,19 @@ void tc_gemm_launch_grouped(const TcProblemSet &ps, TcFormat fmt, const TcOut &o
     using SP = TcShape<256, 64, true>;
     const int64_t ncl = std::min<int64_t>(units, pair_clusters);
     cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute at[1];
+    cudaLaunchAttribute at[2];
     at[0].id = cudaLaunchAttributeClusterDimension;
     at[0].val.clusterDim.x = 2;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
+    at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[1].val.programmaticStreamSerializationAllowed = 1;
     cfg.gridDim = dim3((unsigned)(2 * ncl));
     cfg.blockDim = dim3(SP::THREADS);
     cfg.dynamicSmemBytes = SP::SMEM_BYTES;
     cfg.stream = stream;
     cfg.attrs = at;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = ps.pdl ? 2 : 1;
     SCESS_CUDA(cudaLaunchKernelEx(&cfg, tc_gemm_kernel<256, 64, true>, maps, out, a));
   } else if (bn == 256)
     tc_gemm_kernel<256, 64><<<grid, TcShape<256, 64>::THREADS, TcShape<256, 64>::SMEM_BYTES, stream>>>(

@@ -98,6 +98,12 @@ struct TcProblemSet {
   // ... and every aligned quad of columns (4 c .. 4 c + 3) goes to 4 contiguous
   // floats at a 16-byte aligned address (vector stores)
   bool store_quads[3] = {false, false, false};
+  // launch as a programmatic dependent of the stream's previous kernel (which
+  // must call griddepcontrol.launch_dependents): the prologue and the MMAs run
+  // while that kernel finishes, the epilogue waits for it before its first
+  // store.  Only for a launch whose operands and tables that kernel does not
+  // write (the (T) launches after the first, behind an energy kernel).
+  bool pdl = false;
 };
 
 // Bounds of the kernels' pipeline waits.  The defaults are the production

@@ -237,8 +237,14 @@ __global__ void __launch_bounds__(256) triples_energy_orbit_kernel(
   } else {
     W0 = W + ((al * nb + bl) * nb + cl) * (int64_t)o3p;
   }
+  // the next (T) launch may be scheduled once every CTA is here: it does not
+  // touch W before this grid is complete
+  if (threadIdx.x == 0) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   const bool unique = a < v && b < v && c < v && b <= a && c <= b;
   if (!unique) {
+    // launched as a programmatic dependent of the grouped GEMM: W is complete
+    // and visible only after this wait (no-op for an ordinary launch)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     if (NW == 1) {  // its block received the launch's sums all the same: clear it
       float4 *w4 = reinterpret_cast<float4 *>(const_cast<float *>(W0));
       for (int e = threadIdx.x; e < o3p / 4; e += blockDim.x) w4[e] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -278,6 +284,9 @@ __global__ void __launch_bounds__(256) triples_energy_orbit_kernel(
     s_ev[0] = hi;
     s_ev[1] = lo - (hi - s2);
   }
+  // the tables above come from the call's setup; W from the grouped GEMM just
+  // before, complete after this wait
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   // pass 1: Y = W + V (loads only; NW = 1 clears W after the barrier below).
   // A pair's o loads are all issued before any is used; the first pair's go
   // out before the barrier that publishes the tables.
@@ -1067,6 +1076,9 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
     ws = ctx.ensure_workspace(std::max(dgemm_table_workspace(probe), dgemm_table_workspace(probe2)));
   }
 
+  // MIXED: consecutive launches overlap (programmatic dependent launches);
+  // SCESS_TUNE t_pdl = 0 serialises them, for comparison
+  const bool pdl = tune_value("t_pdl", 1) != 0;
   int64_t blocks_done = 0;
   for (int64_t A = 0; A < NB; A++)
     for (int64_t Bk = 0; Bk <= A; Bk++)
@@ -1154,6 +1166,9 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
           double nprob = 0.0;
           for (int g = 0; g < 3; g++) nprob += ps.tri[g] ? nb * (nb + 1) / 2.0 : (double)nb * nb;
           const double flops = nprob * 2.0 * (double)Mg * Ng * (2.0 * v + 2.0 * o);
+          // behind the previous block triple's energy kernel, the launch starts
+          // its MMAs while that kernel finishes (W is stored to only after it)
+          ps.pdl = pdl && blocks_done > 0;
           tc.gemm_grouped(ps, out, flops, "tc_gemm[triples]");
         } else {
           w_block_fp64(ctx, T, U, W.d(), ws);
@@ -1161,17 +1176,27 @@ double rccsd_triples(Ctx &ctx, const double *d_eri, int64_t nmo, int64_t o, cons
         const unsigned nblk = (unsigned)(nb * nb * nb);
         TimedScope ts(ctx.timer, "triples_energy", 0.0,
                       (double)nblk * o3 * (mixed ? (nw == 1 ? 2 : 3) * 4 : 8), s);
-        if (mixed && nw == 1)
-          triples_energy_orbit_kernel<1><<<nblk, e3threads, ysmem, s>>>(
-              W.as<float>(), o, v, nb, A, Bk, C, etab.as<float2>(),
-              reinterpret_cast<const float *>(etab.as<float2>() + N), Sf.as<float>(),
-              orbits.as<uint32_t>(), norbits, energies.p());
-        else if (mixed)
-          triples_energy_orbit_kernel<3><<<nblk, e3threads, ysmem, s>>>(
-              W.as<float>(), o, v, nb, A, Bk, C, etab.as<float2>(),
-              reinterpret_cast<const float *>(etab.as<float2>() + N), Sf.as<float>(),
-              orbits.as<uint32_t>(), norbits, energies.p());
-        else
+        if (mixed) {
+          // a programmatic dependent of the grouped GEMM: its CTAs take the SMs
+          // that GEMM pairs leave and stage their tables while the last pairs
+          // finish; W is read after griddepcontrol.wait
+          cudaLaunchConfig_t cfg = {};
+          cudaLaunchAttribute at[1];
+          at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+          at[0].val.programmaticStreamSerializationAllowed = 1;
+          cfg.gridDim = dim3(nblk);
+          cfg.blockDim = dim3(e3threads);
+          cfg.dynamicSmemBytes = ysmem;
+          cfg.stream = s;
+          cfg.attrs = at;
+          cfg.numAttrs = pdl ? 1 : 0;
+          const float *t1f = reinterpret_cast<const float *>(etab.as<float2>() + N);
+          SCESS_CUDA(cudaLaunchKernelEx(&cfg, nw == 1 ? triples_energy_orbit_kernel<1> : triples_energy_orbit_kernel<3>,
+                                        W.as<float>(), (int64_t)o, (int64_t)v, (int64_t)nb, (int64_t)A,
+                                        (int64_t)Bk, (int64_t)C, (const float2 *)etab.as<float2>(), t1f,
+                                        (const float *)Sf.as<float>(), (const uint32_t *)orbits.as<uint32_t>(),
+                                        norbits, energies.p()));
+        } else
           triples_energy_kernel<double, double><<<nblk, 256, ysmem, s>>>(
               W.d(), o, v, nb, A, Bk, C, d_eps, d_t1, T.S.p(), energies.p());
         SCESS_CHECK_LAUNCH();
