@@ -295,18 +295,21 @@ def measure_triples_df(ctx, lib, torch, o, v, seed, sigma, steps, warmup, with_f
         ctx.triples(eps=wl.eps, nocc=o, t1=t1h, t2=t2h, B=Bh, precision='mixed')
     clk = Clocks(torch.cuda.current_device())
     clk.start()
-    ctx.profile(True)
     n0 = lib.scess_launch_count()
     walls, ets = [], []
-    for _ in range(steps):
+    for _ in range(steps):  # (no per-kernel timers: their events would serialise the launches)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         ets.append(ctx.triples(eps=wl.eps, nocc=o, t1=t1h, t2=t2h, B=Bh, precision='mixed'))
         walls.append(time.perf_counter() - t0)
     launches = int(lib.scess_launch_count() - n0)
+    clocks = clk.stop()
+    # the same calls again with the per-kernel CUDA-event timers (roofline, shares)
+    ctx.profile(True)
+    for _ in range(steps):
+        ctx.triples(eps=wl.eps, nocc=o, t1=t1h, t2=t2h, B=Bh, precision='mixed')
     prof = ctx.profile_report()
     ctx.profile(False)
-    clocks = clk.stop()
     t_mixed = float(np.median(walls))
     tc = prof.get('tc_gemm[triples]', {'launches': 0, 'ms': 0.0, 'flops': 0.0})
     per_launch_alg = oracle.triples_flops(o, v) * steps / max(tc['launches'], 1)
