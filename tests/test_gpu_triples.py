@@ -68,3 +68,24 @@ def test_triples_mixed_block_layouts(gctx, monkeypatch, o, v, nb):
     em = gctx.triples(eri, w.eps, o, w.t1, w.t2, precision='mixed')
     ref = gctx.triples(eri, w.eps, o, w.t1, w.t2, precision='fp64')
     assert abs(em - ref) <= 2e-6 * max(1.0, abs(ref))
+
+
+def test_overlapped_launches_equal_serialised(gctx, monkeypatch):
+    """The mixed (T) overlaps each block triple's grouped GEMM and energy
+    launches with their neighbours (programmatic dependent launches: the
+    energy kernel reads W, and the next GEMM adds into it, only after the
+    earlier grid is complete).  Serialised launches (t_pdl = 0) must give the
+    same energy up to the order in which the three groups' reductions land,
+    over many block triples."""
+    from scess_gb300.synthetic import convergent_sigma
+    o, v = 8, 60
+    w = make_workload(o, v, seed=6, with_amplitudes=True, sigma=convergent_sigma(o, v))
+    eri = w.eri()
+    ref = oracle.rccsd_triples_correction(eri, w.eps, o, w.t1, w.t2)
+    monkeypatch.setenv('SCESS_TUNE', 't_nb=5,t_pdl=1')    # 12 blocks: 364 block triples
+    over = [gctx.triples(eri, w.eps, o, w.t1, w.t2, precision='mixed') for _ in range(3)]
+    monkeypatch.setenv('SCESS_TUNE', 't_nb=5,t_pdl=0')
+    ser = gctx.triples(eri, w.eps, o, w.t1, w.t2, precision='mixed')
+    for e in over:
+        assert abs(e - ser) <= 1e-9 * abs(ser), (e, ser)
+    assert abs(ser - ref) <= 2e-6 * max(1.0, abs(ref))
