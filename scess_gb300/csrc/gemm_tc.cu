@@ -1524,7 +1524,17 @@ void TcEngine::pack(const double *src, const int64_t *rowOff, int64_t rows, cons
   uint16_t *dst = out.mem.as<uint16_t>();
   clear_pad_rows(dst, rows, rows_pad, Kpad, ctx_.stream);
   const int u = unitK ? 1 : 0;
-  if (fmt_ == TcFormat::FP16) {
+  const unsigned *hint = nullptr;
+  for (const MaxHint &h : hints_)
+    if (h.p == src) hint = hint_words_.as<unsigned>() + h.slot;
+  if (fmt_ == TcFormat::FP16 && hint) {  // the tensor's maximum, reduced once
+    if (aff)
+      pack_split_kernel<true, true><<<grid, 256, 0, ctx_.stream>>>(src, nullptr, rows, nullptr, K, u, dst,
+                                                                   Kpad, hint, scale, 0, rs, ks, rt);
+    else
+      pack_split_kernel<true, false><<<grid, 256, 0, ctx_.stream>>>(src, rowOff, rows, kOff, K, u, dst,
+                                                                    Kpad, hint, scale, 0, 0, 0, rt);
+  } else if (fmt_ == TcFormat::FP16) {
     SCESS_CUDA(cudaMemsetAsync(maxbits, 0, sizeof(unsigned), ctx_.stream));
     const int64_t n = rows * K;
     if (dense || (aff && ((rs == 1 && ks == rows) || (ks == 1 && rs == K)))) {  // the gather is src[0, n)
@@ -1557,6 +1567,25 @@ void TcEngine::pack(const double *src, const int64_t *rowOff, int64_t rows, cons
   }
   SCESS_CHECK_LAUNCH();
 }
+
+void TcEngine::add_max_hint(const double *p, int64_t n) {
+  constexpr int kSlots = 8;
+  if (fmt_ != TcFormat::FP16 || !p || n <= 0 || (int)hints_.size() >= kSlots) return;
+  if (!hint_words_.bytes()) {
+    ctx_.sync();
+    hint_words_.alloc(kSlots * sizeof(unsigned));
+  }
+  const int slot = (int)hints_.size();
+  unsigned *word = hint_words_.as<unsigned>() + slot;
+  TimedScope ts(ctx_.timer, "pack_max", 0.0, (double)n * 8, ctx_.stream);
+  SCESS_CUDA(cudaMemsetAsync(word, 0, sizeof(unsigned), ctx_.stream));
+  const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256 * 8), 8 * kNumSMs));
+  maxabs_flat_kernel<<<blocks, 256, 0, ctx_.stream>>>(p, n, word);
+  SCESS_CHECK_LAUNCH();
+  hints_.push_back({p, slot});
+}
+
+void TcEngine::clear_max_hints() { hints_.clear(); }
 
 void TcEngine::maxabs_into(const double *src, const int64_t *rowOff, int64_t rows,
                            const int64_t *kOff, int64_t K, bool unitK, unsigned *maxbits) {

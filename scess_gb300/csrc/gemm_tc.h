@@ -16,6 +16,7 @@
 #include <cuda_bf16.h>
 
 #include <map>
+#include <vector>
 #include <memory>
 #include <string>
 
@@ -191,6 +192,16 @@ class TcEngine {
   void set_cache_owner(const void *owner) { owner_ = owner; }
   void clear_cache(const void *owner);
 
+  // max|x| of a whole tensor, reduced once and shared by every pack whose
+  // gather starts at that tensor's base pointer (each reads a subset of it,
+  // so the shared maximum bounds its own; the FP16 scale is a power of two
+  // that keeps every packed value in range).  For operands a call packs
+  // several times in different orders (t2 and tau in a residual): one flat
+  // pass instead of one gathered pass per pack.  The caller keeps the tensor
+  // unchanged until clear_max_hints().
+  void add_max_hint(const double *p, int64_t n);
+  void clear_max_hints();
+
  private:
   Ctx &ctx_;
   TcFormat fmt_ = TcFormat::FP16;
@@ -198,6 +209,12 @@ class TcEngine {
   const void *owner_ = nullptr;
   const char *timer_name_ = nullptr;
   Packed tmpA_, tmpB_;
+  struct MaxHint {
+    const double *p;
+    int slot;
+  };
+  std::vector<MaxHint> hints_;
+  DevMem hint_words_;  // one max word per hint slot
   DevMem partial_;
   DevMem err_;
   TcWaitDiag diag_;

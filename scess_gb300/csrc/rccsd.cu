@@ -210,6 +210,23 @@ void RccsdWork::alloc(int64_t o, int64_t v, bool direct_vvvv) {
   if (direct_vvvv) Wvvvv = DTensor({v, v, v, v});
 }
 
+// Shared max|x| of tensors a residual packs several times (TcEngine max
+// hints), for the calls that run on the tensor cores; cleared on scope exit.
+struct MaxHints {
+  TcEngine *tc = nullptr;
+  MaxHints(Ctx &ctx, Backend be) {
+    if (be != Backend::FP64) tc = &ctx.tensor_cores();
+  }
+  void add(const double *p, int64_t n) {
+    if (tc) tc->add_max_hint(p, n);
+  }
+  ~MaxHints() {
+    if (tc) tc->clear_max_hints();
+  }
+  MaxHints(const MaxHints &) = delete;
+  MaxHints &operator=(const MaxHints &) = delete;
+};
+
 void rccsd_residual(Ctx &ctx, const RccsdBlocks &B, const double *amp, const double *t2driver,
                     Backend be, RccsdWork &w, double *R, ResidualList list) {
   const int64_t o = B.o, v = B.v;
@@ -226,6 +243,11 @@ void rccsd_residual(Ctx &ctx, const RccsdBlocks &B, const double *amp, const dou
   };
   make_tau(o, v, t1.p, t2.p, 1.0, w.tau.p(), s);                                     // :107
   const TV tau = w.tau.v;
+  // t2 and tau are packed for the tensor cores several times, in different
+  // orders: their maxima once each
+  MaxHints hints(ctx, be);
+  hints.add(t2.p, o * o * v * v);
+  hints.add(tau.p, o * o * v * v);
   if (ctx.tape) {
     TapeOp op;
     op.kind = TapeOp::TAU;
