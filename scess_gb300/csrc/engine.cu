@@ -497,6 +497,31 @@ void einsum(Ctx &ctx, const char *spec, double alpha, const TV &A, const TV &B, 
     ctx.tape->ops.push_back(op);
   }
   const EinsumPlan &pl = plan_einsum(ctx, spec, A, B, C);
+  // short K and one short free side: an HBM-bound contraction, on the CUDA
+  // cores in FP32 rather than packed for the tensor cores
+  if (be != Backend::FP64 && pl.K <= kSkinnyMaxK && std::min(pl.M, pl.N) <= kSkinnyMaxS &&
+      std::max(pl.M, pl.N) >= 4096 && !ctx.tape) {
+    const bool small_is_a = pl.M <= pl.N;
+    TableGemm g;
+    g.A = A.p;
+    g.B = B.p;
+    g.C = C.p;
+    g.rowA = pl.d_rowA;
+    g.kA = pl.d_kA;
+    g.colB = pl.d_colB;
+    g.kB = pl.d_kB;
+    g.rowC = pl.d_rowC;
+    g.colC = pl.d_colC;
+    g.M = pl.M;
+    g.N = pl.N;
+    g.K = pl.K;
+    g.alpha = alpha;
+    g.beta = beta;
+    const std::string tname = std::string("skinny[") + spec + "]";
+    TimedScope ts(ctx.timer, tname.c_str(), 2.0 * pl.M * pl.N * pl.K, 0.0, ctx.stream);
+    skinny_table(g, small_is_a, small_is_a ? pl.cUnitM : pl.cUnitN, ctx.stream);
+    return;
+  }
   if ((be == Backend::MIXED && TcEngine::worth_it(pl)) || be == Backend::TENSOR) {
     ctx.tensor_cores().contract(pl, alpha, A.p, B.p, beta, C.p, constA, constB);
     return;

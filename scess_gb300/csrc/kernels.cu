@@ -158,6 +158,150 @@ __global__ void dgemv_table_kernel(TableGemm g) {
 }
 }  // namespace
 
+namespace {
+// Tables of a skinny contraction seen from its small side (Sm, s indices) and
+// its long side (Lg, l indices); C(m, n) at C[cS[m] + cL[n]].
+struct SkinnyArgs {
+  const double *Sm, *Lg;
+  double *C;
+  const int64_t *sR, *sK, *lR, *lK, *cS, *cL;
+  int s, sp, K;  // sp: s rounded up to 4
+  int64_t l;
+  float alpha;
+  double beta;
+};
+
+__device__ __forceinline__ void skinny_out(double *p, float v, double beta) {
+  if (beta == 1.0) {
+    asm volatile("red.global.add.f64 [%0], %1;" ::"l"(p), "d"((double)v) : "memory");
+  } else if (beta == 0.0) {
+    *p = (double)v;
+  } else {
+    *p = fma(beta, *p, (double)v);
+  }
+}
+
+// Persistent: each block stages the small operand once (FP32, [k][m]) and its
+// warps walk tiles of 32 long indices, one per lane, with the lane's K long
+// values in registers; every shared load of four small-side values (a 16-byte
+// broadcast) feeds four FMAs.
+template <bool STAGE>
+__global__ void __launch_bounds__(256) skinny_kernel(SkinnyArgs a) {
+  extern __shared__ __align__(16) unsigned char sk_raw[];
+  float4 *sS4 = reinterpret_cast<float4 *>(sk_raw);                  // [K][sp / 4]
+  int64_t *cSs = reinterpret_cast<int64_t *>(sS4 + a.K * (a.sp / 4));  // [s]
+  int64_t *lKs = cSs + a.sp;                                         // [K]
+  float *stage = reinterpret_cast<float *>(lKs + kSkinnyMaxK);       // [8][32][33] (STAGE)
+  float *sS = reinterpret_cast<float *>(sS4);
+  for (int e = threadIdx.x; e < a.K * a.sp; e += blockDim.x) {
+    const int m = e % a.sp, k = e / a.sp;
+    sS[e] = m < a.s ? (float)a.Sm[a.sR[m] + a.sK[k]] : 0.0f;
+  }
+  for (int m = threadIdx.x; m < a.s; m += blockDim.x) cSs[m] = a.cS[m];
+  for (int k = threadIdx.x; k < a.K; k += blockDim.x) lKs[k] = a.lK[k];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t tiles = (a.l + 31) / 32;
+  for (int64_t t = (int64_t)blockIdx.x * 8 + w; t < tiles; t += (int64_t)gridDim.x * 8) {
+    const int64_t n = t * 32 + lane;
+    const bool ok = n < a.l;
+    const int64_t lr = ok ? a.lR[n] : 0, cl = ok ? a.cL[n] : 0;
+    float lv[kSkinnyMaxK];
+#pragma unroll
+    for (int k = 0; k < kSkinnyMaxK; k++) lv[k] = (ok && k < a.K) ? (float)a.Lg[lr + lKs[k]] : 0.0f;
+    if (!STAGE) {
+      for (int m4 = 0; m4 < a.sp / 4; m4++) {
+        float c0 = 0.f, c1 = 0.f, c2 = 0.f, c3 = 0.f;
+#pragma unroll
+        for (int k = 0; k < kSkinnyMaxK; k++) {
+          if (k < a.K) {
+            const float4 q = sS4[k * (a.sp / 4) + m4];
+            c0 = fmaf(q.x, lv[k], c0);
+            c1 = fmaf(q.y, lv[k], c1);
+            c2 = fmaf(q.z, lv[k], c2);
+            c3 = fmaf(q.w, lv[k], c3);
+          }
+        }
+        if (!ok) continue;
+        const int m = 4 * m4;
+        skinny_out(a.C + cSs[m] + cl, a.alpha * c0, a.beta);
+        if (m + 1 < a.s) skinny_out(a.C + cSs[m + 1] + cl, a.alpha * c1, a.beta);
+        if (m + 2 < a.s) skinny_out(a.C + cSs[m + 2] + cl, a.alpha * c2, a.beta);
+        if (m + 3 < a.s) skinny_out(a.C + cSs[m + 3] + cl, a.alpha * c3, a.beta);
+      }
+    } else {
+      float *st = stage + w * 32 * 33;
+      for (int m0 = 0; m0 < a.s; m0 += 32) {
+        // this lane's 32 results C(m0 .. m0 + 31, n) into its row of the stage
+#pragma unroll
+        for (int j4 = 0; j4 < 8; j4++) {
+          float c0 = 0.f, c1 = 0.f, c2 = 0.f, c3 = 0.f;
+          const int m4 = m0 / 4 + j4;
+          if (4 * m4 < a.sp) {
+#pragma unroll
+            for (int k = 0; k < kSkinnyMaxK; k++) {
+              if (k < a.K) {
+                const float4 q = sS4[k * (a.sp / 4) + m4];
+                c0 = fmaf(q.x, lv[k], c0);
+                c1 = fmaf(q.y, lv[k], c1);
+                c2 = fmaf(q.z, lv[k], c2);
+                c3 = fmaf(q.w, lv[k], c3);
+              }
+            }
+          }
+          st[lane * 33 + 4 * j4] = a.alpha * c0;
+          st[lane * 33 + 4 * j4 + 1] = a.alpha * c1;
+          st[lane * 33 + 4 * j4 + 2] = a.alpha * c2;
+          st[lane * 33 + 4 * j4 + 3] = a.alpha * c3;
+        }
+        __syncwarp();
+        // lanes along the small side: column n' of the tile, rows m0 + lane
+        const int m = m0 + lane;
+        for (int j = 0; j < 32; j++) {
+          const int64_t clj = __shfl_sync(0xffffffffu, cl, j);
+          if (t * 32 + j < a.l && m < a.s) skinny_out(a.C + cSs[m] + clj, st[j * 33 + lane], a.beta);
+        }
+        __syncwarp();
+      }
+    }
+  }
+}
+}  // namespace
+
+void skinny_table(const TableGemm &g, bool small_is_a, bool stage, cudaStream_t stream) {
+  SkinnyArgs a;
+  a.Sm = (small_is_a ? g.A + g.baseA : g.B + g.baseB);
+  a.Lg = (small_is_a ? g.B + g.baseB : g.A + g.baseA);
+  a.C = g.C + g.baseC;
+  a.sR = small_is_a ? g.rowA : g.colB;
+  a.sK = small_is_a ? g.kA : g.kB;
+  a.lR = small_is_a ? g.colB : g.rowA;
+  a.lK = small_is_a ? g.kB : g.kA;
+  a.cS = small_is_a ? g.rowC : g.colC;
+  a.cL = small_is_a ? g.colC : g.rowC;
+  const int64_t s = small_is_a ? g.M : g.N, l = small_is_a ? g.N : g.M;
+  if (s < 1 || s > kSkinnyMaxS || g.K < 1 || g.K > kSkinnyMaxK || l < 1)
+    throw Error(SCESS_ERR_INVALID, "skinny contraction out of range");
+  a.s = (int)s;
+  a.sp = (int)round_up(s, 4);
+  a.K = (int)g.K;
+  a.l = l;
+  a.alpha = (float)g.alpha;
+  a.beta = g.beta;
+  const size_t smem = (size_t)a.K * a.sp * sizeof(float) + (size_t)(a.sp + kSkinnyMaxK) * sizeof(int64_t) +
+                      (stage ? (size_t)8 * 32 * 33 * sizeof(float) : 0);
+  const int64_t tiles = ceil_div(l, 32);
+  const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(tiles, 8), 4 * kNumSMs));
+  if (stage) {
+    SCESS_CUDA(cudaFuncSetAttribute(skinny_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    skinny_kernel<true><<<blocks, 256, smem, stream>>>(a);
+  } else {
+    SCESS_CUDA(cudaFuncSetAttribute(skinny_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    skinny_kernel<false><<<blocks, 256, smem, stream>>>(a);
+  }
+  SCESS_CHECK_LAUNCH();
+}
+
 void dgemv_table(const TableGemm &g, cudaStream_t stream) {
   if (g.M <= 0) return;
   const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(g.M * 32, 256), 16 * kNumSMs);

@@ -22,6 +22,17 @@ struct TableGemm {
   int bUnitN = 0;  // B's cols are unit-stride
 };
 
+// The same contraction over a short K (<= kSkinnyMaxK) with one free side of at
+// most kSkinnyMaxS indices (the small side: A's rows when small_is_a, else
+// B's columns) and a long other side: HBM-bound, so it runs on the CUDA cores
+// in FP32 (operands rounded to FP32, products and the K sum in FP32; the
+// result is scaled by alpha in FP32 and added to beta * C in FP64: beta = 1
+// by L2 FP64 reductions, beta = 0 by stores, other beta read-modify-write).
+// stage: C's unit-stride index is on the small side (stores are then staged
+// through shared memory so that lanes run along it).
+constexpr int kSkinnyMaxK = 32, kSkinnyMaxS = 256;
+void skinny_table(const TableGemm &g, bool small_is_a, bool stage, cudaStream_t stream);
+
 // FP64 matrix-vector form of the same contraction (N == 1), one warp per row,
 // deterministic.  Used instead of dgemm_table when N == 1 (or M == 1, swapped).
 void dgemv_table(const TableGemm &g, cudaStream_t stream);

@@ -69,3 +69,27 @@ def test_fp64_einsum_deterministic(gctx):
     o1 = gctx.einsum('kdac,ikcd->ia', A, B, out_shape=(8, 40))
     o2 = gctx.einsum('kdac,ikcd->ia', A, B, out_shape=(8, 40))
     assert np.array_equal(o1, o2)
+
+
+SKINNY = [
+    # (spec, A shape, B shape): K <= 32 and one free side of at most 256, the
+    # other long: FP32 on the CUDA cores in the mixed form
+    ('ki,kjab->ijab', (20, 20), (20, 20, 30, 30)),     # small side A, C unit stride on it
+    ('lcki,la->akci', (20, 30, 20, 20), (20, 30)),     # small side B, C unit stride on it
+    ('ka,kbij->ijab', (20, 30), (20, 30, 20, 20)),     # small side A, C unit stride on the long side
+    ('kibj,ka->ijab', (12, 12, 40, 12), (12, 40)),
+    ('mk,kn->mn', (250, 7), (7, 5000)),
+]
+
+
+@pytest.mark.parametrize('spec,sa,sb', SKINNY)
+@pytest.mark.parametrize('alpha,beta', [(1.0, 1.0), (-2.0, 0.0), (0.5, 0.75)])
+def test_skinny_contractions(gctx, spec, sa, sb, alpha, beta):
+    # operands rounded to FP32, FP32 products and K sums: below 2e-6 of max|C|
+    A, B, ref = _operands(spec, sa, sb, seed=5)
+    C0 = np.random.default_rng(6).standard_normal(ref.shape)
+    out = gctx.einsum(spec, A, B, C_init=C0, alpha=alpha, beta=beta, precision='mixed')
+    assert rel_err(out, alpha * ref + beta * C0) < 2e-6
+    # the FP64 form of the same contraction is unaffected
+    out64 = gctx.einsum(spec, A, B, C_init=C0, alpha=alpha, beta=beta, precision='fp64')
+    assert rel_err(out64, alpha * ref + beta * C0) < 1e-13
