@@ -133,6 +133,9 @@ struct EinsumPlan {
   bool aDense = false, bDense = false;
   std::string key;
   std::string spec;
+  // content hashes of (rowA, kA) and (colB, kB), computed on first use: two
+  // plans that gather an operand through equal tables pack it identically
+  mutable uint64_t hashA = 0, hashB = 0;
 };
 class TcEngine;  // tensor-core (mixed precision) backend, gemm_tc.cu
 

@@ -1585,7 +1585,10 @@ void TcEngine::add_max_hint(const double *p, int64_t n) {
   hints_.push_back({p, slot});
 }
 
-void TcEngine::clear_max_hints() { hints_.clear(); }
+void TcEngine::clear_max_hints() {
+  hints_.clear();
+  reuse_.clear();
+}
 
 void TcEngine::maxabs_into(const double *src, const int64_t *rowOff, int64_t rows,
                            const int64_t *kOff, int64_t K, bool unitK, unsigned *maxbits) {
@@ -1718,12 +1721,42 @@ void TcEngine::contract(const EinsumPlan &pl, double alpha, const double *A, con
   const Hint hA{pl.aRowStride, pl.aKStride, pl.aRowP, pl.aRowE, pl.aDense};
   const Hint hB{pl.bColStride, pl.bKStride, pl.bColP, pl.bColE, pl.bDense};
   const Hint &hX = swap ? hB : hA, &hY = swap ? hA : hB;
+  auto table_hash = [](const std::vector<int64_t> &r, const std::vector<int64_t> &k) {
+    uint64_t x = 1469598103934665603ull;  // FNV-1a over sizes and entries
+    auto mix = [&](uint64_t v) {
+      for (int b = 0; b < 8; b++) {
+        x ^= (v >> (8 * b)) & 0xffu;
+        x *= 1099511628211ull;
+      }
+    };
+    mix(r.size());
+    for (int64_t e : r) mix((uint64_t)e);
+    mix(k.size());
+    for (int64_t e : k) mix((uint64_t)e);
+    return x | 1ull;  // (0 = not yet computed)
+  };
   auto get = [&](const double *src, const int64_t *rows, int64_t nrows, const int64_t *ks,
                  bool unitK, bool isConst, const char *tag, Packed &tmp,
                  const Hint &h) -> const Packed & {
     if (!isConst) {
-      pack(src, rows, nrows, ks, pl.K, unitK, TC_BM, tmp, h.rs, h.ks, h.P, h.E, h.dense);
-      return tmp;
+      bool hinted = false;
+      for (const MaxHint &mh : hints_) hinted = hinted || mh.p == src;
+      if (!hinted) {
+        pack(src, rows, nrows, ks, pl.K, unitK, TC_BM, tmp, h.rs, h.ks, h.P, h.E, h.dense);
+        return tmp;
+      }
+      const bool isA = rows == pl.d_rowA;
+      uint64_t &hs = isA ? pl.hashA : pl.hashB;
+      if (!hs) hs = isA ? table_hash(pl.rowA, pl.kA) : table_hash(pl.colB, pl.kB);
+      const std::string key = std::to_string((uintptr_t)src) + "|" + std::to_string(hs) + "|" +
+                              std::to_string(nrows) + "|" + std::to_string(pl.K) + (unitK ? "u" : "s");
+      auto it = reuse_.find(key);
+      if (it != reuse_.end()) return *it->second;
+      auto pk = std::make_unique<Packed>();
+      pack(src, rows, nrows, ks, pl.K, unitK, TC_BM, *pk, h.rs, h.ks, h.P, h.E, h.dense);
+      auto &ref = *pk;
+      reuse_[key] = std::move(pk);
+      return ref;
     }
     std::string key = pl.key + tag + std::to_string((uintptr_t)src);
     auto it = cache_.find(key);

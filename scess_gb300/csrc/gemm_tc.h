@@ -197,8 +197,9 @@ class TcEngine {
   // so the shared maximum bounds its own; the FP16 scale is a power of two
   // that keeps every packed value in range).  For operands a call packs
   // several times in different orders (t2 and tau in a residual): one flat
-  // pass instead of one gathered pass per pack.  The caller keeps the tensor
-  // unchanged until clear_max_hints().
+  // pass instead of one gathered pass per pack, and one pack for every
+  // einsum that gathers the tensor through equal tables.  The caller keeps
+  // the tensor unchanged until clear_max_hints().
   void add_max_hint(const double *p, int64_t n);
   void clear_max_hints();
 
@@ -214,6 +215,10 @@ class TcEngine {
     int slot;
   };
   std::vector<MaxHint> hints_;
+  // packs of hinted tensors, by source and gather: a second einsum that
+  // gathers the same tensor through equal tables reuses the first one's pack
+  // (dropped with the hints)
+  std::map<std::string, std::unique_ptr<Packed>> reuse_;
   DevMem hint_words_;  // one max word per hint slot
   DevMem partial_;
   DevMem err_;
