@@ -357,6 +357,9 @@ void rccsd_residual(Ctx &ctx, const RccsdBlocks &B, const double *amp, const dou
   }
   E("ac,ijcb->ijab", 1.0, w.Lvv.v, t2, 1.0, w.X.v);                                  // :218
   E("ki,kjab->ijab", -1.0, w.Loo.v, t2, 1.0, w.X.v);                                 // :220
+  // Wvoov and Wvovo are complete: each feeds two of the ring contractions below
+  hints.add(w.Wvoov.p(), o * o * v * v);
+  hints.add(w.Wvovo.p(), o * o * v * v);
   E("akic,kjcb->ijab", 2.0, w.Wvoov.v, t2, 1.0, w.X.v);                              // :223
   E("akci,kjcb->ijab", -1.0, w.Wvovo.v, t2, 1.0, w.X.v);                             // :225
   E("akic,kjbc->ijab", -1.0, w.Wvoov.v, t2, 1.0, w.X.v);                             // :228
@@ -403,6 +406,12 @@ void rccsd_residual_delta(Ctx &ctx, const RccsdBlocks &B, const double *amp0, co
   SCESS_CUDA(cudaMemcpyAsync(tau1, w0.tau.p(), n2 * sizeof(double), cudaMemcpyDeviceToDevice, s));
   axpby(n2, 1.0, dtau.p, 1.0, tau1, s);
   const TV tau_1 = cm(tau1, {o, o, v, v});
+  // the changes and the new amplitudes, each packed several times
+  MaxHints hints(ctx, be);
+  hints.add(dt2.p, n2);
+  hints.add(dtau.p, n2);
+  hints.add(t2_1.p, n2);
+  hints.add(tau_1.p, n2);
 
   E("kcld,ilcd->ki", 1.0, B.L_ovov.v, dtau, 0.0, w.Foo.v, true);                     // :111
   E("kcld,klad->ac", -1.0, B.L_ovov.v, dtau, 0.0, w.Fvv.v, true);                    // :113
