@@ -33,8 +33,8 @@ Beside it:
 ``--impl reference`` times only that CPU oracle on the same workload (each
 step the same bounded sample) and prints the same JSON line with
 ``"impl": "reference"``.  Run ``python bench.py`` for the defaults (N=1).
-Under torchrun every rank runs an independent replica (the path does not
-shard in this build: replicas only) and rank 0 prints.
+Under torchrun every rank runs an independent replica (one solve does not
+shard across GPUs: replicas only) and rank 0 prints.
 """
 from __future__ import annotations
 
