@@ -95,8 +95,8 @@ __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-// Fire-and-forget FP32 reduction into global memory (an L2 atomic) of two
-// consecutive floats at an 8-byte aligned address.
+// Fire-and-forget FP32 reduction into global memory (an L2 atomic) of four
+// consecutive floats at a 16-byte aligned address.
 __device__ __forceinline__ void red_add_v4(float *p, float a, float b, float c, float d) {
   asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(a), "f"(b), "f"(c),
                "f"(d)
